@@ -1,0 +1,239 @@
+/*
+ * pm_gb300.h — C ABI of the GB300-native PruneJuice pruning pipeline.
+ *
+ * The reference (tahsinreza/pattenmatching_sharedmemory) has no plugin or FFI
+ * API: its hot path is reached through the `patternmatching` CLI, the TOTEM
+ * file formats and the per-step C++ class contract
+ *   AlgoResults <Step>::compute(const graph_t&, MultipleLabelGlobalState*)
+ * driven by MultipleLabelCpu (src/patternmatching/multiple_label_cpu.h:32-53).
+ * Every entry point below replaces one piece of that contract; the citation
+ * in front of each names the reference interface it stands in for.  Plain
+ * pointers and sizes only; no C++ or torch types cross this boundary.
+ *
+ * Ownership: the caller owns every host buffer it passes in.  The library
+ * owns the device-resident CSR (pm_graph) and each query's device arena
+ * (pm_query) until the matching *_destroy call.
+ *
+ * Errors follow TOTEM's error_t convention (src/totem/totem_comdef.h:31-32):
+ * PM_SUCCESS = 0, PM_FAILURE = -1, plus distinct negative codes.  The last
+ * error message of the calling thread is available from pm_last_error().
+ *
+ * Threading: calls on distinct pm_query handles may run concurrently from
+ * different host threads; a single handle must not be used concurrently.
+ */
+#ifndef PM_GB300_H
+#define PM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (src/totem/totem_comdef.h:31-32 SUCCESS/FAILURE) ---- */
+typedef int32_t pm_status_t;
+#define PM_SUCCESS 0
+#define PM_FAILURE (-1)           /* generic failure, as TOTEM's FAILURE      */
+#define PM_E_INVALID_ARG (-2)     /* null pointer, bad size, bad enum         */
+#define PM_E_IO (-3)              /* file cannot be opened / read / written   */
+#define PM_E_FORMAT (-4)          /* malformed or truncated TOTEM file        */
+#define PM_E_PATTERN_TOO_LARGE (-5) /* template > 64 vertices or walk too long */
+#define PM_E_ADMISSION_DENIED (-6)  /* server memory budget exceeded          */
+#define PM_E_TIMEOUT (-7)           /* request deadline passed                */
+#define PM_E_DEVICE (-8)            /* CUDA error or device-side error status */
+#define PM_E_NO_DEVICE (-9)         /* no CUDA device / extension unusable    */
+#define PM_E_CANCELLED (-10)        /* request cancelled before it finished   */
+#define PM_E_OOM (-11)              /* host or device allocation failed       */
+#define PM_E_BUSY (-12)             /* server queue full, retry later         */
+
+/* Last error message of the calling host thread (never NULL). */
+const char* pm_last_error(void);
+
+/* Library version string. */
+const char* pm_version(void);
+
+/* ---- step kinds: MultipleLabelStep::Step (multiple_label_step.h:16-25) ---- */
+typedef enum {
+  PM_STEP_START = 0,
+  PM_STEP_END = 1,
+  PM_STEP_LCC0 = 2,
+  PM_STEP_LCC = 3,
+  PM_STEP_CC = 4,
+  PM_STEP_PC = 5,
+  PM_STEP_TDS = 6,
+  PM_STEP_ENUMERATION = 7
+} pm_step_kind;
+
+/* AlgoResults (src/patternmatching/algorithms/algo_results.h:9-20). */
+typedef struct {
+  uint64_t vertex_eliminated;
+  uint64_t edge_eliminated;
+  uint64_t match_eliminated;
+  uint64_t enumeration;
+} pm_algo_results;
+
+/* One row of the reference's results.totem
+ * (MultipleLabelCpu::logResults, multiple_label_cpu.cc:187-213). */
+typedef struct {
+  int32_t iteration;
+  int32_t step; /* pm_step_kind */
+  double step_ms;
+  double cumulative_ms;
+  pm_algo_results results;
+  uint64_t active_vertex;
+  uint64_t total_vertex;
+  uint64_t active_edge;
+  uint64_t total_edge;
+} pm_step_record;
+
+typedef struct pm_graph pm_graph;
+typedef struct pm_query pm_query;
+
+/* ---- graph (TOTEM graph_t + I/O) ------------------------------------- */
+
+/* graph_initialize(graph or .bin) + parseVertexFile(labels) + optional
+ * graph_store_binary(bin) — the load sequence of MultipleLabelCpu::allocate
+ * (multiple_label_cpu.cc:22-35), including its quirk that an existing
+ * bin_path is loaded instead of graph_path and labels_path.  bin_path and
+ * labels_path may be NULL or "".  The CSR is copied to device `device`. */
+pm_status_t pm_graph_load(const char* graph_path, const char* bin_path,
+                          const char* labels_path, int device, pm_graph** out);
+
+/* Builds a graph from caller-owned host CSR buffers (graph_t vertices /
+ * edges / values, totem_graph.h:137-180).  labels may be NULL (all 0). */
+pm_status_t pm_graph_from_csr(const uint64_t* offsets, const uint32_t* adj,
+                              const uint64_t* labels, uint32_t vertex_count,
+                              uint64_t edge_count, int device, pm_graph** out);
+
+/* graph_store_binary (totem_graph.cu:883-922), 32-bit edge-id layout when
+ * the edge count fits, else the EID=64 layout. */
+pm_status_t pm_graph_store_binary(const pm_graph* g, const char* path);
+
+pm_status_t pm_graph_info(const pm_graph* g, uint32_t* vertex_count,
+                          uint64_t* edge_count, uint64_t* device_bytes);
+void pm_graph_destroy(pm_graph* g);
+
+/* ---- query: one template over one resident graph ---------------------- */
+
+/* MultipleLabelCpu::allocate's pattern half (multiple_label_cpu.cc:37-104):
+ * loads pattern_dir/"pattern_edge[.totem]" and pattern_dir/"pattern_vertex_data",
+ * generates the local, cycle, path, template and enumeration constraints,
+ * allocates the per-query device state and initialises the step machine.
+ * pattern_dir is concatenated exactly as the reference does (it should end
+ * with '/').  load_pattern_labels mirrors the reference's rule that pattern
+ * labels are read only when a graph label file was given (:44-47). */
+pm_status_t pm_query_create(pm_graph* g, const char* pattern_dir,
+                            int load_pattern_labels, pm_query** out);
+
+/* Same from caller-owned template CSR buffers. */
+pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets,
+                                     const uint32_t* p_adj,
+                                     const uint64_t* p_labels,
+                                     uint32_t p_vertex_count,
+                                     uint64_t p_edge_count, pm_query** out);
+
+/* Number of cycle / path / template constraints
+ * (MultipleLabelStep::initStep{Cc,Pc,Tds}, multiple_label_step.cc:12-25). */
+pm_status_t pm_query_constraint_counts(const pm_query* q, int32_t* n_cycle,
+                                       int32_t* n_path, int32_t* n_template);
+
+/* The constraint dump the reference writes to log.totem (the print()
+ * methods of the generators), without timestamps.  Writes up to cap bytes
+ * (NUL-terminated) and the full size to *needed. */
+pm_status_t pm_query_dump_constraints(const pm_query* q, char* buf, size_t cap,
+                                      size_t* needed);
+
+/* One iteration of MultipleLabelCpu::runPatternMatching
+ * (multiple_label_cpu.cc:121-175): resets per-step state, runs the current
+ * step's compute on the GPU and advances MultipleLabelStep::getNextStep.
+ * *finished is set when the step machine reaches END. */
+pm_status_t pm_query_step(pm_query* q, pm_step_record* record, int* finished);
+
+/* The full run loop (≤1000 iterations) plus the final END row.  Writes up
+ * to cap records; *n_records receives the number of rows produced. */
+pm_status_t pm_query_run(pm_query* q, pm_step_record* records, int32_t cap,
+                         int32_t* n_records);
+
+/* Copies the pruned state back to caller-owned host buffers (any may be
+ * NULL): candidate role bitmask per vertex (bit p = pattern vertex p, the
+ * FixedBitmap<64> of multiple_label_common_cpu.h:49), active flag per CSR
+ * entry and per vertex. */
+pm_status_t pm_query_export(const pm_query* q, uint64_t* cand_masks,
+                            uint8_t* edge_active, uint8_t* vertex_active);
+
+/* Writes results.totem, graph_NNNN.totem and vertex_NNNN.totem exactly as
+ * MultipleLabelCpu::logResults / printActiveGraph / printActiveVertex do
+ * (multiple_label_cpu.cc:187-296, utils/logger.cc:90-136). */
+pm_status_t pm_query_write_outputs(const pm_query* q, const char* out_dir);
+
+/* Final exact match count (the ENUMERATION row), or 0 before it ran. */
+pm_status_t pm_query_match_count(const pm_query* q, uint64_t* count);
+
+/* Device bytes held by this query's state arena. */
+pm_status_t pm_query_device_bytes(const pm_query* q, uint64_t* bytes);
+
+/* Device bytes a query over graph g with a template of p_vertex_count
+ * vertices would hold (admission control). */
+pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count,
+                                    uint64_t* bytes);
+
+void pm_query_destroy(pm_query* q);
+
+/* ---- batched and served execution ------------------------------------- */
+
+/* Runs n_queries templates over one resident graph together: every query's
+ * pruning steps are launched as fused multi-query kernels on one stream
+ * (one launch per step kind covers every query currently in that step),
+ * each query keeps its own step machine, and results are identical to
+ * running each query alone.  Templates are given as concatenated CSR
+ * buffers: query i uses p_offsets[off_index[i] .. off_index[i]+n_i] etc.
+ * match_counts[i] receives query i's exact count; step_counts[i] the number
+ * of result rows query i produced (may be NULL). */
+pm_status_t pm_batch_run(pm_graph* g, int32_t n_queries,
+                         const uint32_t* p_vertex_counts,
+                         const uint64_t* p_offsets, const uint32_t* p_adj,
+                         const uint64_t* p_labels, uint64_t* match_counts,
+                         int32_t* step_counts);
+
+typedef struct pm_server pm_server;
+
+typedef struct {
+  uint64_t memory_budget_bytes; /* admission limit for per-query arenas   */
+  int32_t max_slots;            /* queries resident on the device at once */
+  int32_t max_queue;            /* pending requests before PM_E_BUSY      */
+} pm_server_config;
+
+typedef struct {
+  pm_status_t status;      /* PM_SUCCESS, PM_E_TIMEOUT, PM_E_CANCELLED ... */
+  uint64_t match_count;
+  uint64_t active_vertex;
+  uint64_t active_edge;
+  int32_t n_steps;
+  double submit_to_start_ms; /* queueing delay                             */
+  double submit_to_done_ms;  /* end-to-end latency                         */
+} pm_request_result;
+
+/* Continuous-batching server over one resident graph: requests are admitted
+ * as slots and memory free up, share fused multi-query launches with the
+ * requests already running, and leave as soon as their own step machine
+ * reaches END. */
+pm_status_t pm_server_create(pm_graph* g, const pm_server_config* cfg,
+                             pm_server** out);
+pm_status_t pm_server_submit(pm_server* s, const uint64_t* p_offsets,
+                             const uint32_t* p_adj, const uint64_t* p_labels,
+                             uint32_t p_vertex_count, double timeout_ms,
+                             uint64_t* ticket);
+/* Drives the server one scheduling round (admit, launch, retire). */
+pm_status_t pm_server_progress(pm_server* s, int32_t* n_running,
+                               int32_t* n_pending);
+/* *done = 1 and *out filled once the request finished (any status). */
+pm_status_t pm_server_poll(pm_server* s, uint64_t ticket, pm_request_result* out,
+                           int* done);
+pm_status_t pm_server_cancel(pm_server* s, uint64_t ticket);
+void pm_server_destroy(pm_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PM_GB300_H */

@@ -1,0 +1,45 @@
+/*
+ * pm_gb300_tools.h — helpers around the pm_gb300.h boundary that the
+ * reference has no counterpart for: seeded synthetic inputs (standing in for
+ * the reference's external datasets), zero-copy access to the host CSR of a
+ * pm_graph, and engine statistics.  Not needed by a drop-in caller.
+ */
+#ifndef PM_GB300_TOOLS_H
+#define PM_GB300_TOOLS_H
+
+#include "pm_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Undirected RMAT graph: 2^scale vertices, edge_factor * 2^scale sampled
+ * pairs with quadrant probabilities a, b, c (d = 1-a-b-c), symmetrised,
+ * self-loops and duplicate edges removed, adjacency sorted; vertex ids
+ * shuffled by a seeded permutation when permute != 0.  The graph is host-
+ * only until pm_graph_to_device (or a query) moves it to a device. */
+pm_status_t pm_graph_generate_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed,
+                                   int32_t permute, pm_graph** out);
+
+/* Vertex labels 0..n_labels-1: kind 0 = uniform, 1 = Zipf(zipf_s),
+ * 2 = correlated with degree rank.  Must precede device residency. */
+pm_status_t pm_graph_assign_labels(pm_graph* g, int32_t kind, uint32_t n_labels, double zipf_s, uint64_t seed);
+
+/* Library-owned host CSR of g (valid until pm_graph_destroy). */
+pm_status_t pm_graph_host_csr(const pm_graph* g, const uint64_t** offsets, const uint32_t** adj,
+                              const uint64_t** labels);
+
+/* Copies the CSR to device `device` (no-op when already there). */
+pm_status_t pm_graph_to_device(pm_graph* g, int32_t device);
+
+/* Writes the graph as TOTEM text and its labels as a vertex file. */
+pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const char* labels_path);
+
+/* Number of NLCC steps that needed the exact sequential emulation of the
+ * reference's alreadyMatched shortcut, and of memo-table overflow retries. */
+pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PM_GB300_TOOLS_H */

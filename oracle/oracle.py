@@ -1,0 +1,128 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper of oracle/pm_oracle.cc, the CPU restatement of the reference's
+pattern-matching pipeline.  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg import this module; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libpm_oracle.so"
+REF_BIN = HERE / "_ref" / "patternmatching"
+
+
+def build() -> Path:
+    """Compiles the restatement (g++, a few seconds)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "lib"], check=True)
+    return LIB_PATH
+
+
+class _Record(ctypes.Structure):
+    _fields_ = [("iteration", ctypes.c_int32), ("step", ctypes.c_int32), ("step_ms", ctypes.c_double),
+                ("cumulative_ms", ctypes.c_double), ("vertex_eliminated", ctypes.c_uint64),
+                ("edge_eliminated", ctypes.c_uint64), ("match_eliminated", ctypes.c_uint64),
+                ("enumeration", ctypes.c_uint64), ("active_vertex", ctypes.c_uint64),
+                ("total_vertex", ctypes.c_uint64), ("active_edge", ctypes.c_uint64), ("total_edge", ctypes.c_uint64)]
+
+
+STEP_NAMES = {0: "START", 1: "END", 2: "LCC0", 3: "LCC", 4: "CC", 5: "PC", 6: "TDS", 7: "ENUMERATION"}
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        lib = ctypes.CDLL(str(LIB_PATH))
+        P = ctypes.POINTER
+        lib.pmo_run.restype = ctypes.c_int
+        lib.pmo_run.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64), ctypes.c_uint32,
+                                ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int64, P(_Record),
+                                ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_uint64), P(ctypes.c_uint8),
+                                P(ctypes.c_uint8)]
+        lib.pmo_dump_constraints.restype = ctypes.c_int
+        lib.pmo_dump_constraints.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                             ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
+                                             P(ctypes.c_size_t)]
+        _lib = lib
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+class OracleResult:
+    def __init__(self, rows, cand, eact, vact):
+        self.rows = rows          # list of tuples without timing (see row_tuple)
+        self.timings = []         # per-row step ms
+        self.cand = cand
+        self.eact = eact
+        self.vact = vact
+
+    @property
+    def match_count(self) -> int:
+        for r in self.rows:
+            if r[0] == "ENUMERATION":
+                return r[8]
+        return 0
+
+
+def run(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, stop_before_enumeration: bool = False,
+        enum_vertex_limit: int = 0) -> OracleResult:
+    """Runs the restated pipeline; threads=1 is the canonical sequential order."""
+    lib = _load()
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ad = np.ascontiguousarray(adj, np.uint32)
+    lab = np.ascontiguousarray(labels, np.uint64)
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    V, E, k = len(off) - 1, len(ad), len(po) - 1
+    cap = 1100
+    recs = (_Record * cap)()
+    n = ctypes.c_int32()
+    cand = np.zeros(V, np.uint64)
+    eact = np.zeros(E, np.uint8)
+    vact = np.zeros(V, np.uint8)
+    st = lib.pmo_run(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), V, E,
+                     _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k, threads,
+                     int(stop_before_enumeration), enum_vertex_limit, recs, cap, ctypes.byref(n),
+                     _p(cand, ctypes.c_uint64), _p(eact, ctypes.c_uint8), _p(vact, ctypes.c_uint8))
+    if st != 0:
+        raise RuntimeError(f"oracle failed with status {st}")
+    rows = [row_tuple(recs[i]) for i in range(n.value)]
+    res = OracleResult(rows, cand, eact, vact)
+    res.timings = [recs[i].step_ms for i in range(n.value)]
+    return res
+
+
+def row_tuple(r) -> tuple:
+    return (STEP_NAMES[r.step], r.vertex_eliminated, r.active_vertex, r.total_vertex, r.edge_eliminated,
+            r.active_edge, r.total_edge, r.match_eliminated, r.enumeration)
+
+
+def dump_constraints(p_offsets, p_adj, p_labels) -> str:
+    lib = _load()
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    k = len(po) - 1
+    need = ctypes.c_size_t()
+    st = lib.pmo_dump_constraints(_p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k,
+                                  None, 0, ctypes.byref(need))
+    if st != 0:
+        raise RuntimeError(f"constraint compilation failed with status {st}")
+    buf = ctypes.create_string_buffer(need.value)
+    lib.pmo_dump_constraints(_p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k, buf,
+                             need.value, None)
+    return buf.value.decode()

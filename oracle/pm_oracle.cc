@@ -1,0 +1,630 @@
+// ORACLE — test infrastructure only.  A CPU restatement of the reference's
+// PruneJuice pipeline (tahsinreza/pattenmatching_sharedmemory,
+// src/patternmatching/multiple_label/), used by tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg as the checker.  The product never calls
+// it.  Pinned against the reference's own compiled CPU path (oracle/Makefile)
+// through the golden fixtures under tests/golden/.
+//
+// Semantics follow the reference file:line cited on each function.  With
+// threads == 1 the per-vertex loops run in ascending vertex order, which is
+// the canonical order of the reference's timing-dependent "alreadyMatched"
+// shortcut (multiple_label_cc_cpu.tpp:107, pc :107/:127, tds :165); with
+// threads > 1 the loops are OpenMP-parallel like the reference's, for timing.
+// Template constraints come from the product's template compiler
+// (constraints.cc), itself pinned against the reference's log.totem dumps.
+#include <omp.h>
+
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../pattenmatching_sharedmemory_gb300/csrc/constraints.h"
+
+using namespace pmgb;
+
+namespace {
+
+struct PairHashO {
+  size_t operator()(const std::pair<uint32_t, uint32_t>& x) const {
+    return std::hash<uint32_t>()(x.first) ^ std::hash<uint32_t>()(x.second);
+  }
+};
+using EdgeMemo = std::unordered_map<std::pair<uint32_t, uint32_t>, uint64_t, PairHashO>;
+
+inline std::pair<uint32_t, uint32_t> undirected(uint32_t a, uint32_t b) {
+  return a > b ? std::make_pair(a, b) : std::make_pair(b, a);
+}
+
+struct Results {
+  uint64_t vertex = 0, edge = 0, match = 0, enumeration = 0;
+  bool empty() const { return !vertex && !edge && !match && !enumeration; }
+};
+
+// MultipleLabelGlobalState<uint32_t> (multiple_label_common_cpu.h:24-59),
+// one flag byte per vertex / CSR entry, one 64-bit role set per vertex.
+struct State {
+  const uint64_t* off;
+  const uint32_t* adj;
+  const uint64_t* lab;
+  uint32_t V;
+  uint64_t E;
+  uint32_t k;
+  std::vector<uint8_t> active, modified, scheduled, edge_active;
+  std::vector<uint64_t> cand, matched, unmatch;
+  uint64_t active_vertices, active_edges;
+  bool parallel;
+  void mark_matched(uint32_t v, uint32_t p) {
+    if (parallel)
+      __atomic_fetch_or(&matched[v], uint64_t(1) << p, __ATOMIC_RELAXED);
+    else
+      matched[v] |= uint64_t(1) << p;
+  }
+  bool is_matched(uint32_t v, uint32_t p) const {
+    uint64_t w = parallel ? __atomic_load_n(&matched[v], __ATOMIC_RELAXED) : matched[v];
+    return w >> p & 1;
+  }
+  bool has(uint32_t v, uint32_t p) const { return cand[v] >> p & 1; }
+};
+
+// Second sweep shared by the CC, PC and TDS steps (multiple_label_cc_cpu.tpp:134-173,
+// pc :150-186, tds :203-241): apply the roles to unmatch, deactivate empty
+// vertices, and reschedule modified vertices and their neighbours.
+void apply_unmatch(State& s, Results& r) {
+  uint64_t ve = 0, me = 0;
+#pragma omp parallel for reduction(+ : ve, me) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    s.matched[v] = 0;
+    if (s.modified[v]) {
+      me += __builtin_popcountll(s.unmatch[v]);
+      s.cand[v] &= ~s.unmatch[v];
+      if (s.cand[v] == 0) {
+        s.active[v] = 0;
+        ++ve;
+      }
+      s.scheduled[v] = 1;
+      s.unmatch[v] = 0;
+    } else {
+      bool sched = false;
+      for (uint64_t e = s.off[v]; e < s.off[v + 1]; ++e) {
+        if (!s.edge_active[e]) continue;
+        if (!s.modified[s.adj[e]]) continue;
+        sched = true;
+        break;
+      }
+      s.scheduled[v] = sched;
+    }
+  }
+  s.active_vertices -= ve;
+  r.vertex = ve;
+  r.match = me;
+}
+
+// LCC0 (multiple_label_lcc0_cpu.tpp:15-87).
+Results step_lcc0(State& s, const QueryConstraints& qc) {
+  Results r;
+  uint64_t ve = 0, me = 0;
+#pragma omp parallel for reduction(+ : ve, me) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    for (uint32_t p = 0; p < s.k; ++p) {
+      if (!s.has(v, p)) continue;
+      if (s.lab[v] != qc.local[p].origin_label) {
+        ++me;
+        s.cand[v] &= ~(uint64_t(1) << p);
+      }
+    }
+    if (s.cand[v] == 0) {
+      s.active[v] = 0;
+      ++ve;
+    }
+  }
+  s.active_vertices -= ve;
+  r.vertex = ve;
+  r.match = me;
+  return r;
+}
+
+// LCC (multiple_label_lcc_cpu.tpp:20-151).
+Results step_lcc(State& s, const QueryConstraints& qc) {
+  Results r;
+  uint64_t ee = 0;
+#pragma omp parallel for reduction(+ : ee) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v] || !s.scheduled[v]) continue;
+    uint64_t nbr_set = 0;
+    for (uint32_t p = 0; p < s.k; ++p)
+      if (s.has(v, p)) nbr_set |= qc.local[p].neighbor_mask;
+    std::unordered_map<uint64_t, size_t> counts;
+    for (uint64_t e = s.off[v]; e < s.off[v + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w]) continue;
+      if ((s.cand[w] & nbr_set) == 0) {
+        ++ee;
+        s.edge_active[e] = 0;
+        s.modified[v] = 1;
+        continue;
+      }
+      ++counts[s.lab[w]];
+    }
+    bool changed = false;
+    for (uint32_t p = 0; p < s.k; ++p) {
+      if (!s.has(v, p)) continue;
+      const LocalConstraint& lc = qc.local[p];
+      if (s.lab[v] != lc.origin_label) {
+        s.unmatch[v] |= uint64_t(1) << p;
+        changed = true;
+        continue;
+      }
+      for (const auto& req : lc.required) {
+        auto it = counts.find(req.first);
+        size_t have = it == counts.end() ? 0 : it->second;
+        if (have < req.second) {
+          s.unmatch[v] |= uint64_t(1) << p;
+          changed = true;
+          break;
+        }
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  uint64_t ve = 0, me = 0;
+#pragma omp parallel for reduction(+ : ve, me) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    if (s.modified[v]) {
+      me += __builtin_popcountll(s.unmatch[v]);
+      s.cand[v] &= ~s.unmatch[v];
+      if (s.cand[v] == 0) {
+        s.active[v] = 0;
+        ++ve;
+      }
+      s.scheduled[v] = 1;
+      s.unmatch[v] = 0;
+    } else {
+      bool sched = false;
+      for (uint64_t e = s.off[v]; e < s.off[v + 1]; ++e) {
+        if (!s.edge_active[e]) continue;
+        if (!s.modified[s.adj[e]]) continue;
+        sched = true;
+        break;
+      }
+      s.scheduled[v] = sched;
+    }
+  }
+  s.active_vertices -= ve;
+  s.active_edges -= ee;
+  r.vertex = ve;
+  r.edge = ee;
+  r.match = me;
+  return r;
+}
+
+// CC walk (multiple_label_cc_cpu.tpp:13-70).  The memo is keyed by the
+// undirected edge; it is tested with the current cycle position and filled
+// with the next template vertex id, and never rolled back within one source.
+bool cc_walk(State& s, const CycleConstraint& c, EdgeMemo& memo, uint32_t source, uint32_t cur, size_t start,
+             size_t remaining) {
+  const size_t L = c.length();
+  if (remaining == 1) {
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w]) continue;
+      if (w == source) return true;
+    }
+    return false;
+  }
+  const size_t cur_pos = (start + L - remaining) % L;
+  const size_t next_pos = (start + L - (remaining - 1)) % L;
+  const uint32_t next_role = c.ids[next_pos];
+  for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+    if (!s.edge_active[e]) continue;
+    uint32_t w = s.adj[e];
+    if (!s.active[w]) continue;
+    if (!s.has(w, next_role)) continue;
+    auto key = undirected(cur, w);
+    auto it = memo.find(key);
+    if (it != memo.end() && (it->second >> cur_pos & 1)) continue;
+    memo[key] |= uint64_t(1) << next_role;
+    if (cc_walk(s, c, memo, source, w, start, remaining - 1)) {
+      s.mark_matched(w, next_role);
+      return true;
+    }
+  }
+  return false;
+}
+
+// CC step (multiple_label_cc_cpu.tpp:79-183).
+Results step_cc(State& s, const CycleConstraint& c) {
+  Results r;
+  EdgeMemo memo;
+#pragma omp parallel for private(memo) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    bool changed = false;
+    for (size_t pos = 0; pos < c.length(); ++pos) {
+      uint32_t role = c.ids[pos];
+      if (!s.has(v, role)) continue;
+      if (s.is_matched(v, role)) continue;
+      memo.clear();
+      if (!cc_walk(s, c, memo, v, v, pos, c.length())) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r);
+  return r;
+}
+
+// PC walk (multiple_label_pc_cpu.tpp:12-81).
+bool pc_walk(State& s, const PathConstraint& pc, bool reverse, EdgeMemo& memo, uint32_t source, uint32_t cur,
+             size_t remaining) {
+  const size_t L = pc.length();
+  const size_t cur_pos = reverse ? remaining : (L - remaining - 1);
+  const size_t next_pos = reverse ? remaining - 1 : (L - remaining);
+  const uint32_t next_role = pc.ids[next_pos];
+  if (remaining == 1) {
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w]) continue;
+      if (!s.has(w, next_role)) continue;
+      if (source != w) {
+        s.mark_matched(w, next_role);
+        return true;
+      }
+    }
+    return false;
+  }
+  for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+    if (!s.edge_active[e]) continue;
+    uint32_t w = s.adj[e];
+    if (!s.active[w]) continue;
+    if (!s.has(w, next_role)) continue;
+    auto key = undirected(cur, w);
+    auto it = memo.find(key);
+    if (it != memo.end() && (it->second >> cur_pos & 1)) continue;
+    memo[key] |= uint64_t(1) << next_role;
+    if (pc_walk(s, pc, reverse, memo, source, w, remaining - 1)) return true;
+  }
+  return false;
+}
+
+// PC step (multiple_label_pc_cpu.tpp:84-197).
+Results step_pc(State& s, const PathConstraint& pc) {
+  Results r;
+  EdgeMemo memo;
+  const size_t L = pc.length();
+#pragma omp parallel for private(memo) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    if (s.lab[v] != pc.initial_label) continue;
+    bool changed = false;
+    for (int end = 0; end < 2; ++end) {
+      uint32_t role = end == 0 ? pc.ids[0] : pc.ids[L - 1];
+      if (!s.has(v, role)) continue;
+      if (s.is_matched(v, role)) continue;
+      memo.clear();
+      if (!pc_walk(s, pc, end == 1, memo, v, v, L - 1)) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r);
+  return r;
+}
+
+// TDS walk (multiple_label_tds_cpu.tpp:14-127).
+struct TdsMemo {
+  std::unordered_map<uint32_t, std::unordered_map<uint32_t, std::vector<std::vector<uint32_t>>>> hyp;
+  EdgeMemo edges;
+  std::vector<uint32_t> history;
+  std::vector<uint32_t> stored;
+};
+
+bool tds_walk(State& s, const Walk& w, TdsMemo& m, uint32_t source, uint32_t cur, size_t pos) {
+  if (pos == w.length()) return true;
+  const int move = w.moves[pos];
+  if (move == kVertexNoStore || move == kVertexStore) {
+    const uint32_t cur_role = w.ids[pos - 1];
+    const uint32_t next_role = w.ids[pos];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb]) continue;
+      if (!s.has(nb, next_role)) continue;
+      auto key = undirected(cur, nb);
+      auto it = m.edges.find(key);
+      if (it != m.edges.end() && (it->second >> cur_role & 1)) continue;
+      auto hv = m.hyp.find(nb);
+      if (hv != m.hyp.end()) {
+        auto hr = hv->second.find(next_role);
+        if (hr != hv->second.end()) {
+          bool seen = false;
+          for (const auto& h : hr->second)
+            if (h == m.stored) {
+              seen = true;
+              break;
+            }
+          if (seen) continue;
+        }
+      }
+      if (move == kVertexStore) m.stored.push_back(nb);
+      m.hyp[nb][next_role].push_back(m.stored);
+      m.history.push_back(nb);
+      m.edges[key] |= uint64_t(1) << next_role;
+      if (tds_walk(s, w, m, source, nb, pos + 1)) {
+        s.mark_matched(nb, next_role);
+        return true;
+      }
+      m.history.pop_back();
+      if (move == kVertexStore) m.stored.pop_back();
+    }
+  } else if (move == kCheck) {
+    const uint32_t target = m.history[w.back[pos]];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb]) continue;
+      if (nb != target) continue;
+      if (tds_walk(s, w, m, source, cur, pos + 1)) return true;
+    }
+  } else {  // kMoveBack
+    const uint32_t back_to = m.history[w.back[pos]];
+    if (tds_walk(s, w, m, source, back_to, pos + 1)) return true;
+  }
+  return false;
+}
+
+// TDS step (multiple_label_tds_cpu.tpp:136-244).
+Results step_tds(State& s, const TemplateConstraint& t) {
+  Results r;
+  TdsMemo m;
+#pragma omp parallel for private(m) if (s.parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    bool changed = false;
+    for (const auto& kv : t.walks) {
+      uint32_t role = kv.first;
+      if (!s.has(v, role)) continue;
+      if (s.is_matched(v, role)) continue;
+      m.hyp.clear();
+      m.edges.clear();
+      m.history.clear();
+      m.history.push_back(v);
+      m.stored.clear();
+      if (!tds_walk(s, kv.second, m, v, v, 1)) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r);
+  return r;
+}
+
+// ENUMERATION walk (multiple_label_enumeration_cpu.tpp:39-118): injective
+// embeddings following the walk; CHECK follows only the first matching entry.
+uint64_t enum_walk(const State& s, const Walk& w, std::vector<uint32_t>& history, uint32_t cur, size_t pos) {
+  if (pos == w.length()) return 1;
+  const int move = w.moves[pos];
+  uint64_t count = 0;
+  if (move == kVertexNoStore || move == kVertexStore) {
+    const uint32_t next_role = w.ids[pos];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb]) continue;
+      if (!s.has(nb, next_role)) continue;
+      bool seen = false;
+      for (uint32_t h : history)
+        if (h == nb) {
+          seen = true;
+          break;
+        }
+      if (seen) continue;
+      history.push_back(nb);
+      count += enum_walk(s, w, history, nb, pos + 1);
+      history.pop_back();
+    }
+  } else if (move == kCheck) {
+    const uint32_t target = history[w.back[pos]];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb]) continue;
+      if (nb != target) continue;
+      return enum_walk(s, w, history, cur, pos + 1);
+    }
+  } else {
+    return enum_walk(s, w, history, history[w.back[pos]], pos + 1);
+  }
+  return count;
+}
+
+// ENUMERATION step (multiple_label_enumeration_cpu.tpp:126-174).
+Results step_enumeration(State& s, const TemplateConstraint& t, int64_t vertex_limit) {
+  Results r;
+  auto first = t.walks.cbegin();
+  const uint32_t start_role = first->first;
+  const Walk& w = first->second;
+  uint64_t total = 0;
+  const int64_t limit = vertex_limit > 0 && vertex_limit < s.V ? vertex_limit : s.V;
+  std::vector<uint32_t> history;
+#pragma omp parallel for reduction(+ : total) private(history) schedule(dynamic, 1000) if (s.parallel)
+  for (int64_t vi = 0; vi < limit; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v]) continue;
+    if (!s.has(v, start_role)) continue;
+    history.clear();
+    history.push_back(v);
+    total += enum_walk(s, w, history, v, 1);
+  }
+  r.enumeration = total;
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Runs the reference pipeline (MultipleLabelCpu::runPatternMatching,
+// multiple_label_cpu.cc:113-184, with MultipleLabelStep::getNextStep,
+// multiple_label_step.cc:30-83) over a host CSR graph and template.
+//   threads      1 = canonical sequential order; >1 OpenMP like the reference.
+//   stop_before_enumeration  1 = end the run when the schedule reaches
+//                ENUMERATION (pruning-only timing).
+//   enum_vertex_limit  >0 = enumerate only from sources below this id
+//                (bounded CPU-baseline samples); 0 = all.
+// Outputs (any may be NULL): step records (as pm_step_record), final role
+// sets, per-CSR-entry and per-vertex active flags, the matched count.
+// Returns 0, or a negative status on bad input.
+int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+            const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k, int threads,
+            int stop_before_enumeration, int64_t enum_vertex_limit, pm_step_record* records, int32_t cap,
+            int32_t* n_records, uint64_t* cand_out, uint8_t* edge_active_out, uint8_t* vertex_active_out) {
+  try {
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    QueryConstraints qc = compile_constraints(pg);
+    State s;
+    s.off = off;
+    s.adj = adj;
+    s.lab = lab;
+    s.V = V;
+    s.E = E;
+    s.k = k;
+    s.parallel = threads > 1;
+    if (threads >= 1) omp_set_num_threads(threads);
+    s.active.assign(V, 1);
+    s.modified.assign(V, 0);
+    s.scheduled.assign(V, 1);
+    s.edge_active.assign(E, 1);
+    const uint64_t full = k == 64 ? ~uint64_t(0) : ((uint64_t(1) << k) - 1);
+    s.cand.assign(V, full);
+    s.matched.assign(V, 0);
+    s.unmatch.assign(V, 0);
+    s.active_vertices = V;
+    s.active_edges = E;
+
+    enum { START, END, LCC0, LCC, CC, PC, TDS, ENUM };
+    int step = START;
+    size_t next_cc = 0, next_pc = 0, next_tds = 0;
+    Results res;
+    auto advance = [&](int cur) -> int {
+      switch (cur) {
+        case START: return LCC0;
+        case LCC0: return LCC;
+        case LCC:
+          if (!res.empty()) return LCC;
+          if (next_cc < qc.cycles.size()) return CC;
+          if (next_pc < qc.paths.size()) return PC;
+          if (next_tds < qc.templates.size()) return TDS;
+          return ENUM;
+        case CC: ++next_cc; return LCC;
+        case PC: ++next_pc; return LCC;
+        case TDS: ++next_tds; return LCC;
+        default: return END;
+      }
+    };
+    int32_t n = 0;
+    double total_ms = 0;
+    auto emit = [&](int kind, double ms, const Results& r) {
+      total_ms += ms;
+      if (records && n < cap) {
+        pm_step_record& rec = records[n];
+        rec.iteration = n;
+        rec.step = kind;
+        rec.step_ms = ms;
+        rec.cumulative_ms = total_ms;
+        rec.results.vertex_eliminated = r.vertex;
+        rec.results.edge_eliminated = r.edge;
+        rec.results.match_eliminated = r.match;
+        rec.results.enumeration = r.enumeration;
+        rec.active_vertex = s.active_vertices;
+        rec.total_vertex = V;
+        rec.active_edge = s.active_edges;
+        rec.total_edge = E;
+      }
+      ++n;
+    };
+    step = advance(START);
+    int iteration = 0;
+    bool finished = false;
+    while (!finished && iteration < 1000) {
+      if (step == CC || step == PC || step == TDS) std::fill(s.modified.begin(), s.modified.end(), 0);
+      if (step == ENUM && stop_before_enumeration) break;
+      auto t0 = std::chrono::steady_clock::now();
+      switch (step) {
+        case LCC0: res = step_lcc0(s, qc); break;
+        case LCC: res = step_lcc(s, qc); break;
+        case CC: res = step_cc(s, qc.cycles[next_cc]); break;
+        case PC: res = step_pc(s, qc.paths[next_pc]); break;
+        case TDS: res = step_tds(s, qc.templates[next_tds]); break;
+        case ENUM: res = step_enumeration(s, qc.enumeration, enum_vertex_limit); break;
+        default: res = Results(); break;
+      }
+      double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      emit(step + PM_STEP_START, ms, res);
+      int next = advance(step);
+      finished = (step == ENUM);
+      step = next;
+      ++iteration;
+    }
+    // Final row: logResults(iteration, true) with cleared results and the
+    // name of the step the machine would run next (END after ENUMERATION).
+    emit(finished || step == ENUM ? PM_STEP_END : step, 0.0, Results());
+    if (n_records) *n_records = n;
+    if (cand_out) memcpy(cand_out, s.cand.data(), sizeof(uint64_t) * V);
+    if (edge_active_out) memcpy(edge_active_out, s.edge_active.data(), E);
+    if (vertex_active_out) memcpy(vertex_active_out, s.active.data(), V);
+    return 0;
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
+// Compiles a template and returns the reference-format constraint dump
+// (for pinning the template compiler against log.totem).
+int pmo_dump_constraints(const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k, char* buf,
+                         size_t cap, size_t* needed) {
+  try {
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    std::string d = dump_constraints(compile_constraints(pg));
+    if (needed) *needed = d.size() + 1;
+    if (buf && cap) {
+      size_t c = d.size() < cap - 1 ? d.size() : cap - 1;
+      memcpy(buf, d.data(), c);
+      buf[c] = 0;
+    }
+    return 0;
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
+}  // extern "C"

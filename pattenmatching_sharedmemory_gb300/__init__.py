@@ -1,0 +1,345 @@
+"""GB300-native PruneJuice pruning pipeline (LCC / CC / PC / TDS / ENUMERATION).
+
+Python mirror of the reference's pattern-matching driver
+(src/patternmatching/multiple_label_cpu.{h,cc}: allocate, runPatternMatching,
+free) over the C ABI declared in include/pm_gb300.h.  Every compute call goes
+to the CUDA kernels in libpm_gb300.so; importing this package fails loudly
+when that library has not been built (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libpm_gb300.so"
+CLI_PATH = _PKG / "lib" / "patternmatching_gb300"
+
+STEP_NAMES = {0: "START", 1: "END", 2: "LCC0", 3: "LCC", 4: "CC", 5: "PC", 6: "TDS", 7: "ENUMERATION"}
+
+PM_SUCCESS = 0
+PM_FAILURE = -1
+PM_E_INVALID_ARG = -2
+PM_E_IO = -3
+PM_E_FORMAT = -4
+PM_E_PATTERN_TOO_LARGE = -5
+PM_E_ADMISSION_DENIED = -6
+PM_E_TIMEOUT = -7
+PM_E_DEVICE = -8
+PM_E_NO_DEVICE = -9
+PM_E_CANCELLED = -10
+PM_E_OOM = -11
+PM_E_BUSY = -12
+
+
+class PmError(RuntimeError):
+    """A non-zero pm_status_t with the library's last error message."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class AlgoResults(ctypes.Structure):
+    _fields_ = [("vertex_eliminated", ctypes.c_uint64), ("edge_eliminated", ctypes.c_uint64),
+                ("match_eliminated", ctypes.c_uint64), ("enumeration", ctypes.c_uint64)]
+
+
+class StepRecord(ctypes.Structure):
+    """One results.totem row (pm_step_record)."""
+
+    _fields_ = [("iteration", ctypes.c_int32), ("step", ctypes.c_int32), ("step_ms", ctypes.c_double),
+                ("cumulative_ms", ctypes.c_double), ("results", AlgoResults), ("active_vertex", ctypes.c_uint64),
+                ("total_vertex", ctypes.c_uint64), ("active_edge", ctypes.c_uint64),
+                ("total_edge", ctypes.c_uint64)]
+
+    def as_tuple(self):
+        """The row without its timing columns: (step, vertex eliminated, active vertex, total vertex,
+        edge eliminated, active edge, total edge, match eliminated, enumeration)."""
+        r = self.results
+        return (STEP_NAMES[self.step], r.vertex_eliminated, self.active_vertex, self.total_vertex,
+                r.edge_eliminated, self.active_edge, self.total_edge, r.match_eliminated, r.enumeration)
+
+
+def _load_library() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build the GB300 extension first "
+                          "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    P = ctypes.POINTER
+    c_u64p, c_u32p, c_u8p = P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint8)
+    sig = {
+        "pm_last_error": (ctypes.c_char_p, []),
+        "pm_version": (ctypes.c_char_p, []),
+        "pm_graph_load": (ctypes.c_int32, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                           P(ctypes.c_void_p)]),
+        "pm_graph_from_csr": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
+                                               ctypes.c_int, P(ctypes.c_void_p)]),
+        "pm_graph_store_binary": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p]),
+        "pm_graph_info": (ctypes.c_int32, [ctypes.c_void_p, c_u32p, c_u64p, c_u64p]),
+        "pm_graph_destroy": (None, [ctypes.c_void_p]),
+        "pm_graph_generate_rmat": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                                    ctypes.c_int32, P(ctypes.c_void_p)]),
+        "pm_graph_assign_labels": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32,
+                                                    ctypes.c_double, ctypes.c_uint64]),
+        "pm_graph_host_csr": (ctypes.c_int32, [ctypes.c_void_p, P(c_u64p), P(c_u32p), P(c_u64p)]),
+        "pm_graph_to_device": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
+        "pm_graph_write_text": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+        "pm_query_create": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_void_p)]),
+        "pm_query_create_from_csr": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, c_u64p, ctypes.c_uint32,
+                                                      ctypes.c_uint64, P(ctypes.c_void_p)]),
+        "pm_query_constraint_counts": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32),
+                                                        P(ctypes.c_int32)]),
+        "pm_query_dump_constraints": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
+                                                       P(ctypes.c_size_t)]),
+        "pm_query_step": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), P(ctypes.c_int)]),
+        "pm_query_run": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), ctypes.c_int32, P(ctypes.c_int32)]),
+        "pm_query_export": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u8p, c_u8p]),
+        "pm_query_write_outputs": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p]),
+        "pm_query_match_count": (ctypes.c_int32, [ctypes.c_void_p, c_u64p]),
+        "pm_query_device_bytes": (ctypes.c_int32, [ctypes.c_void_p, c_u64p]),
+        "pm_query_estimate_bytes": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, c_u64p]),
+        "pm_query_stats": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u64p]),
+        "pm_query_destroy": (None, [ctypes.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load_library()
+
+
+def _check(status: int) -> None:
+    if status != PM_SUCCESS:
+        raise PmError(status, lib.pm_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _enc(s) -> bytes | None:
+    if s is None:
+        return None
+    return os.fsencode(str(s))
+
+
+class Graph:
+    """A labelled CSR graph (TOTEM graph_t) resident on one GPU."""
+
+    def __init__(self, handle: ctypes.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def load(cls, graph_path, bin_path=None, labels_path=None, device: int = 0) -> "Graph":
+        h = ctypes.c_void_p()
+        _check(lib.pm_graph_load(_enc(graph_path), _enc(bin_path), _enc(labels_path), device, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_csr(cls, offsets, adj, labels=None, device: int = 0) -> "Graph":
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        ad = np.ascontiguousarray(adj, dtype=np.uint32)
+        lab = None if labels is None else np.ascontiguousarray(labels, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        _check(lib.pm_graph_from_csr(_ptr(off, ctypes.c_uint64), _ptr(ad, ctypes.c_uint32),
+                                     None if lab is None else _ptr(lab, ctypes.c_uint64), len(off) - 1, len(ad),
+                                     device, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, permute: bool = True) -> "Graph":
+        """Seeded undirected RMAT graph (host-only until a query or to_device)."""
+        h = ctypes.c_void_p()
+        _check(lib.pm_graph_generate_rmat(scale, edge_factor, a, b, c, seed, int(permute), ctypes.byref(h)))
+        return cls(h)
+
+    def assign_labels(self, kind: str, n_labels: int, s: float = 1.0, seed: int = 1) -> "Graph":
+        k = {"uniform": 0, "zipf": 1, "degree": 2}[kind]
+        _check(lib.pm_graph_assign_labels(self._h, k, n_labels, s, seed))
+        return self
+
+    def to_device(self, device: int = 0) -> "Graph":
+        _check(lib.pm_graph_to_device(self._h, device))
+        return self
+
+    @property
+    def vertex_count(self) -> int:
+        v = ctypes.c_uint32()
+        _check(lib.pm_graph_info(self._h, ctypes.byref(v), None, None))
+        return v.value
+
+    @property
+    def edge_count(self) -> int:
+        e = ctypes.c_uint64()
+        _check(lib.pm_graph_info(self._h, None, ctypes.byref(e), None))
+        return e.value
+
+    @property
+    def device_bytes(self) -> int:
+        b = ctypes.c_uint64()
+        _check(lib.pm_graph_info(self._h, None, None, ctypes.byref(b)))
+        return b.value
+
+    def host_csr(self):
+        """Zero-copy numpy views of the library-owned host CSR: (offsets, adj, labels)."""
+        o, a, l = ctypes.POINTER(ctypes.c_uint64)(), ctypes.POINTER(ctypes.c_uint32)(), ctypes.POINTER(ctypes.c_uint64)()
+        _check(lib.pm_graph_host_csr(self._h, ctypes.byref(o), ctypes.byref(a), ctypes.byref(l)))
+        V, E = self.vertex_count, self.edge_count
+        off = np.ctypeslib.as_array(o, shape=(V + 1,)) if V + 1 else np.zeros(0, np.uint64)
+        adj = np.ctypeslib.as_array(a, shape=(E,)) if E else np.zeros(0, np.uint32)
+        lab = np.ctypeslib.as_array(l, shape=(V,)) if V and l else np.zeros(V, np.uint64)
+        return off, adj, lab
+
+    def write_text(self, graph_path, labels_path=None) -> None:
+        _check(lib.pm_graph_write_text(self._h, _enc(graph_path), _enc(labels_path)))
+
+    def store_binary(self, path) -> None:
+        _check(lib.pm_graph_store_binary(self._h, _enc(path)))
+
+    def close(self) -> None:
+        if self._h:
+            lib.pm_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Pattern:
+    """A template graph in CSR form with per-vertex labels."""
+
+    offsets: np.ndarray
+    adj: np.ndarray
+    labels: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return len(self.offsets) - 1
+
+    @classmethod
+    def from_edges(cls, n: int, edges, labels) -> "Pattern":
+        """Undirected template from an edge list (both directions stored, sorted)."""
+        nbrs = [set() for _ in range(n)]
+        for u, v in edges:
+            nbrs[u].add(v)
+            nbrs[v].add(u)
+        off = np.zeros(n + 1, np.uint64)
+        adj = []
+        for u in range(n):
+            adj.extend(sorted(nbrs[u]))
+            off[u + 1] = len(adj)
+        return cls(off, np.asarray(adj, np.uint32), np.asarray(labels, np.uint64))
+
+    def write(self, directory) -> None:
+        """Writes pattern_edge (TOTEM text) and pattern_vertex_data."""
+        d = Path(directory)
+        d.mkdir(parents=True, exist_ok=True)
+        lines = [f"#Nodes:{self.n}", f"#Edges:{len(self.adj)}", "#Undirected"]
+        for u in range(self.n):
+            for e in range(int(self.offsets[u]), int(self.offsets[u + 1])):
+                lines.append(f"{u} {int(self.adj[e])}")
+        (d / "pattern_edge").write_text("\n".join(lines) + "\n")
+        (d / "pattern_vertex_data").write_text("".join(f"{u} {int(self.labels[u])}\n" for u in range(self.n)))
+
+
+class Query:
+    """One template over a resident graph: constraint generation, GPU pruning
+    steps and the reference's step schedule (MultipleLabelCpu)."""
+
+    def __init__(self, graph: Graph, pattern_dir=None, pattern: Pattern | None = None,
+                 load_pattern_labels: bool = True):
+        self.graph = graph
+        self._h = ctypes.c_void_p()
+        if pattern_dir is not None:
+            d = str(pattern_dir)
+            _check(lib.pm_query_create(graph._h, _enc(d), int(load_pattern_labels), ctypes.byref(self._h)))
+        else:
+            p = pattern
+            off = np.ascontiguousarray(p.offsets, np.uint64)
+            adj = np.ascontiguousarray(p.adj, np.uint32)
+            lab = np.ascontiguousarray(p.labels, np.uint64)
+            _check(lib.pm_query_create_from_csr(graph._h, _ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32),
+                                                _ptr(lab, ctypes.c_uint64), p.n, len(adj), ctypes.byref(self._h)))
+
+    def constraint_counts(self):
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib.pm_query_constraint_counts(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def dump_constraints(self) -> str:
+        need = ctypes.c_size_t()
+        _check(lib.pm_query_dump_constraints(self._h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        _check(lib.pm_query_dump_constraints(self._h, buf, need.value, None))
+        return buf.value.decode()
+
+    def step(self):
+        rec = StepRecord()
+        fin = ctypes.c_int()
+        _check(lib.pm_query_step(self._h, ctypes.byref(rec), ctypes.byref(fin)))
+        return rec, bool(fin.value)
+
+    def run(self) -> list[StepRecord]:
+        cap = 1100
+        recs = (StepRecord * cap)()
+        n = ctypes.c_int32()
+        _check(lib.pm_query_run(self._h, recs, cap, ctypes.byref(n)))
+        return [recs[i] for i in range(min(n.value, cap))]
+
+    def export(self):
+        V, E = self.graph.vertex_count, self.graph.edge_count
+        cand = np.zeros(V, np.uint64)
+        eact = np.zeros(E, np.uint8)
+        vact = np.zeros(V, np.uint8)
+        _check(lib.pm_query_export(self._h, _ptr(cand, ctypes.c_uint64), _ptr(eact, ctypes.c_uint8),
+                                   _ptr(vact, ctypes.c_uint8)))
+        return cand, eact, vact
+
+    def write_outputs(self, out_dir) -> None:
+        _check(lib.pm_query_write_outputs(self._h, _enc(out_dir)))
+
+    @property
+    def match_count(self) -> int:
+        c = ctypes.c_uint64()
+        _check(lib.pm_query_match_count(self._h, ctypes.byref(c)))
+        return c.value
+
+    @property
+    def device_bytes(self) -> int:
+        b = ctypes.c_uint64()
+        _check(lib.pm_query_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def stats(self):
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib.pm_query_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return {"exact_resolutions": a.value, "overflow_retries": b.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib.pm_query_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def version() -> str:
+    return lib.pm_version().decode()

@@ -1,0 +1,305 @@
+// The C ABI of include/pm_gb300.h and include/pm_gb300_tools.h.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/pm_gb300_tools.h"
+#include "engine.h"
+#include "generators.h"
+#include "totem_io.h"
+
+using namespace pmgb;
+
+struct pm_graph {
+  GraphImpl impl;
+};
+struct pm_query {
+  QueryImpl impl;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+pm_status_t fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <class F>
+pm_status_t guarded(F&& f) {
+  try {
+    g_last_error.clear();
+    return f();
+  } catch (const PmError& e) {
+    return fail(e.code, e.message);
+  } catch (const std::bad_alloc&) {
+    return fail(PM_E_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(PM_FAILURE, e.what());
+  }
+}
+
+#define PM_REQUIRE(cond, msg) \
+  if (!(cond)) return fail(PM_E_INVALID_ARG, msg)
+}  // namespace
+
+extern "C" {
+
+const char* pm_last_error(void) { return g_last_error.c_str(); }
+const char* pm_version(void) { return "pm_gb300 1.0 (sm_103a)"; }
+
+pm_status_t pm_graph_load(const char* graph_path, const char* bin_path, const char* labels_path, int device,
+                          pm_graph** out) {
+  PM_REQUIRE(out, "out is NULL");
+  return guarded([&]() -> pm_status_t {
+    auto* g = new pm_graph();
+    try {
+      const std::string bin = bin_path ? bin_path : "";
+      // MultipleLabelCpu::allocate (multiple_label_cpu.cc:22-35): an existing
+      // binary replaces the text graph and its labels; otherwise the text is
+      // parsed, labels applied and the binary cache written.
+      if (!bin.empty() && is_regular_file(bin)) {
+        g->impl.host = read_totem_graph(bin);
+      } else {
+        PM_REQUIRE(graph_path && *graph_path, "graph_path is empty");
+        g->impl.host = read_totem_graph(graph_path);
+        if (labels_path && *labels_path && is_regular_file(labels_path)) read_vertex_labels(labels_path, g->impl.host);
+        if (!bin.empty()) write_totem_binary(g->impl.host, bin, g->impl.host.edge_count > 0xFFFFFFFFull ? 8 : 4);
+      }
+      g->impl.finalize_host();
+      if (device >= 0) g->impl.to_device(device);
+    } catch (...) {
+      delete g;
+      throw;
+    }
+    *out = g;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_from_csr(const uint64_t* offsets, const uint32_t* adj, const uint64_t* labels,
+                              uint32_t vertex_count, uint64_t edge_count, int device, pm_graph** out) {
+  PM_REQUIRE(out && offsets && (adj || edge_count == 0), "null CSR buffer");
+  PM_REQUIRE(offsets[vertex_count] == edge_count, "offsets[vertex_count] != edge_count");
+  for (uint32_t v = 0; v < vertex_count; ++v) PM_REQUIRE(offsets[v] <= offsets[v + 1], "offsets not monotone");
+  for (uint64_t e = 0; e < edge_count; ++e) PM_REQUIRE(adj[e] < vertex_count, "edge target out of range");
+  return guarded([&]() -> pm_status_t {
+    auto* g = new pm_graph();
+    try {
+      HostGraph& h = g->impl.host;
+      h.vertex_count = vertex_count;
+      h.edge_count = edge_count;
+      h.offsets.assign(offsets, offsets + vertex_count + 1);
+      h.adj.assign(adj, adj + edge_count);
+      h.valued = labels != nullptr;
+      if (labels) h.labels.assign(labels, labels + vertex_count);
+      g->impl.finalize_host();
+      if (device >= 0) g->impl.to_device(device);
+    } catch (...) {
+      delete g;
+      throw;
+    }
+    *out = g;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_store_binary(const pm_graph* g, const char* path) {
+  PM_REQUIRE(g && path, "null argument");
+  return guarded([&]() -> pm_status_t {
+    write_totem_binary(g->impl.host, path, g->impl.host.edge_count > 0xFFFFFFFFull ? 8 : 4);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_info(const pm_graph* g, uint32_t* vertex_count, uint64_t* edge_count, uint64_t* device_bytes) {
+  PM_REQUIRE(g, "graph is NULL");
+  if (vertex_count) *vertex_count = g->impl.host.vertex_count;
+  if (edge_count) *edge_count = g->impl.host.edge_count;
+  if (device_bytes) *device_bytes = g->impl.device_bytes();
+  return PM_SUCCESS;
+}
+
+void pm_graph_destroy(pm_graph* g) { delete g; }
+
+pm_status_t pm_graph_generate_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed,
+                                   int32_t permute, pm_graph** out) {
+  PM_REQUIRE(out, "out is NULL");
+  return guarded([&]() -> pm_status_t {
+    auto* g = new pm_graph();
+    try {
+      g->impl.host = generate_rmat(scale, edge_factor, a, b, c, seed, permute != 0);
+      g->impl.finalize_host();
+    } catch (...) {
+      delete g;
+      throw;
+    }
+    *out = g;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_assign_labels(pm_graph* g, int32_t kind, uint32_t n_labels, double zipf_s, uint64_t seed) {
+  PM_REQUIRE(g, "graph is NULL");
+  PM_REQUIRE(kind >= 0 && kind <= 2, "label kind must be 0, 1 or 2");
+  PM_REQUIRE(g->impl.device < 0, "labels must be assigned before the graph moves to a device");
+  return guarded([&]() -> pm_status_t {
+    assign_labels(g->impl.host, kind, n_labels, zipf_s, seed);
+    g->impl.finalize_host();
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_host_csr(const pm_graph* g, const uint64_t** offsets, const uint32_t** adj,
+                              const uint64_t** labels) {
+  PM_REQUIRE(g, "graph is NULL");
+  if (offsets) *offsets = g->impl.host.offsets.data();
+  if (adj) *adj = g->impl.host.adj.data();
+  if (labels) *labels = g->impl.host.labels.data();
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_graph_to_device(pm_graph* g, int32_t device) {
+  PM_REQUIRE(g && device >= 0, "bad argument");
+  return guarded([&]() -> pm_status_t {
+    g->impl.to_device(device);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const char* labels_path) {
+  PM_REQUIRE(g, "graph is NULL");
+  return guarded([&]() -> pm_status_t {
+    if (graph_path && *graph_path) write_totem_text(g->impl.host, graph_path);
+    if (labels_path && *labels_path) write_vertex_labels(g->impl.host, labels_path);
+    return PM_SUCCESS;
+  });
+}
+
+static pm_status_t create_query(pm_graph* g, const PatternGraph& p, pm_query** out) {
+  auto* q = new pm_query();
+  try {
+    g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    q->impl.create(&g->impl, p, nullptr);
+  } catch (...) {
+    delete q;
+    throw;
+  }
+  *out = q;
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_query_create(pm_graph* g, const char* pattern_dir, int load_pattern_labels, pm_query** out) {
+  PM_REQUIRE(g && pattern_dir && out, "null argument");
+  return guarded([&]() -> pm_status_t { return create_query(g, load_pattern(pattern_dir, load_pattern_labels != 0), out); });
+}
+
+pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets, const uint32_t* p_adj,
+                                     const uint64_t* p_labels, uint32_t p_vertex_count, uint64_t p_edge_count,
+                                     pm_query** out) {
+  PM_REQUIRE(g && p_offsets && out, "null argument");
+  PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
+  for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
+  return guarded([&]() -> pm_status_t {
+    PatternGraph p;
+    p.n = p_vertex_count;
+    p.offsets.assign(p_offsets, p_offsets + p_vertex_count + 1);
+    p.adj.assign(p_adj, p_adj + p_edge_count);
+    p.labels = p_labels ? std::vector<uint64_t>(p_labels, p_labels + p_vertex_count)
+                        : std::vector<uint64_t>(p_vertex_count, 0);
+    return create_query(g, p, out);
+  });
+}
+
+pm_status_t pm_query_constraint_counts(const pm_query* q, int32_t* n_cycle, int32_t* n_path, int32_t* n_template) {
+  PM_REQUIRE(q, "query is NULL");
+  if (n_cycle) *n_cycle = static_cast<int32_t>(q->impl.cycles.size());
+  if (n_path) *n_path = static_cast<int32_t>(q->impl.paths.size());
+  if (n_template) *n_template = static_cast<int32_t>(q->impl.templates.size());
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_query_dump_constraints(const pm_query* q, char* buf, size_t cap, size_t* needed) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    const std::string d = dump_constraints(q->impl.qc);
+    if (needed) *needed = d.size() + 1;
+    if (buf && cap) {
+      const size_t n = d.size() < cap - 1 ? d.size() : cap - 1;
+      memcpy(buf, d.data(), n);
+      buf[n] = 0;
+    }
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_step(pm_query* q, pm_step_record* record, int* finished) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    pm_step_record r = q->impl.finished ? q->impl.final_record() : q->impl.run_step();
+    if (record) *record = r;
+    if (finished) *finished = q->impl.finished ? 1 : 0;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_run(pm_query* q, pm_step_record* records, int32_t cap, int32_t* n_records) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    q->impl.run_all();
+    int32_t n = 0;
+    for (const auto& r : q->impl.records) {
+      if (records && n < cap) records[n] = r;
+      ++n;
+    }
+    if (records && n < cap) records[n] = q->impl.final_record();
+    ++n;
+    if (n_records) *n_records = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_export(const pm_query* q, uint64_t* cand_masks, uint8_t* edge_active, uint8_t* vertex_active) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    const_cast<QueryImpl&>(q->impl).export_state(cand_masks, edge_active, vertex_active);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_write_outputs(const pm_query* q, const char* out_dir) {
+  PM_REQUIRE(q && out_dir, "null argument");
+  return guarded([&]() -> pm_status_t {
+    const_cast<QueryImpl&>(q->impl).write_outputs(out_dir);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_match_count(const pm_query* q, uint64_t* count) {
+  PM_REQUIRE(q && count, "null argument");
+  *count = q->impl.match_count;
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_query_device_bytes(const pm_query* q, uint64_t* bytes) {
+  PM_REQUIRE(q && bytes, "null argument");
+  *bytes = q->impl.device_bytes();
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count, uint64_t* bytes) {
+  PM_REQUIRE(g && bytes, "null argument");
+  *bytes = estimate_query_bytes(g->impl, p_vertex_count);
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries) {
+  PM_REQUIRE(q, "query is NULL");
+  if (exact_resolutions) *exact_resolutions = q->impl.exact_resolutions;
+  if (overflow_retries) *overflow_retries = q->impl.overflow_retries;
+  return PM_SUCCESS;
+}
+
+void pm_query_destroy(pm_query* q) { delete q; }
+
+}  // extern "C"

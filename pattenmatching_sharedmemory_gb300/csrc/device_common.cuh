@@ -1,0 +1,168 @@
+// Device-side layout of the resident graph and of one query's pruning state.
+//
+// HBM layout (one graph, many queries):
+//   graph   off  u64[V+1]   CSR offsets (eid_t, 64-bit)
+//           adj  u32[E]     neighbour ids (vid_t)
+//           lab  u32[V]     dense label id (index into the graph's sorted
+//                           distinct label values)
+//   query   vs   W[V]       packed vertex word: candidate role bits in the
+//                           low kCandBits, the vertex's label slot in the
+//                           pattern's label list above them (0xFF = a label
+//                           no template vertex carries).  Active <=> cand != 0
+//                           (the reference keeps a separate vertexActiveList,
+//                           multiple_label_common_cpu.h:49-53, but a vertex is
+//                           deactivated exactly when its role set empties).
+//           eact u32[ceil(E/32)]  one active bit per CSR entry
+//           mod  u8[V]      vertexModifiedList
+//           sch  u8[V]      vertexScheduledList
+//           unm  W[V]       vertexPatternToUnmatch (cand bits only)
+// The word type W is chosen per query from the template size k:
+//   k <= 8 -> u16, k <= 24 -> u32, k <= 56 -> u64, else a 16-byte pair.
+// One gather of W per neighbour yields both its role set (LCC possibility
+// test, NLCC role test) and its label slot (LCC label counting).
+#pragma once
+#include <cstdint>
+
+#include "walk_program.h"
+
+namespace pmgb {
+
+struct alignas(16) Wide {
+  uint64_t c;
+  uint64_t s;
+};
+
+template <class W>
+struct Pack;
+template <>
+struct Pack<uint16_t> {
+  static constexpr int kMaxK = 8;
+  static __host__ __device__ __forceinline__ uint64_t cand(uint16_t w) { return w & 0xFFu; }
+  static __host__ __device__ __forceinline__ uint32_t slot(uint16_t w) { return w >> 8; }
+  static __host__ __device__ __forceinline__ uint16_t make(uint64_t c, uint32_t s) {
+    return static_cast<uint16_t>((s << 8) | (c & 0xFFu));
+  }
+  static __host__ __device__ __forceinline__ uint16_t zero() { return 0; }
+};
+template <>
+struct Pack<uint32_t> {
+  static constexpr int kMaxK = 24;
+  static __host__ __device__ __forceinline__ uint64_t cand(uint32_t w) { return w & 0xFFFFFFu; }
+  static __host__ __device__ __forceinline__ uint32_t slot(uint32_t w) { return w >> 24; }
+  static __host__ __device__ __forceinline__ uint32_t make(uint64_t c, uint32_t s) {
+    return (s << 24) | static_cast<uint32_t>(c & 0xFFFFFFu);
+  }
+  static __host__ __device__ __forceinline__ uint32_t zero() { return 0; }
+};
+template <>
+struct Pack<uint64_t> {
+  static constexpr int kMaxK = 56;
+  static __host__ __device__ __forceinline__ uint64_t cand(uint64_t w) { return w & 0x00FFFFFFFFFFFFFFull; }
+  static __host__ __device__ __forceinline__ uint32_t slot(uint64_t w) { return static_cast<uint32_t>(w >> 56); }
+  static __host__ __device__ __forceinline__ uint64_t make(uint64_t c, uint32_t s) {
+    return (static_cast<uint64_t>(s) << 56) | (c & 0x00FFFFFFFFFFFFFFull);
+  }
+  static __host__ __device__ __forceinline__ uint64_t zero() { return 0; }
+};
+template <>
+struct Pack<Wide> {
+  static constexpr int kMaxK = 64;
+  static __host__ __device__ __forceinline__ uint64_t cand(const Wide& w) { return w.c; }
+  static __host__ __device__ __forceinline__ uint32_t slot(const Wide& w) { return static_cast<uint32_t>(w.s); }
+  static __host__ __device__ __forceinline__ Wide make(uint64_t c, uint32_t s) { return Wide{c, s}; }
+  static __host__ __device__ __forceinline__ Wide zero() { return Wide{0, 0}; }
+};
+
+struct DevGraph {
+  uint32_t V;
+  uint64_t E;
+  const uint64_t* __restrict__ off;
+  const uint32_t* __restrict__ adj;
+  const uint32_t* __restrict__ lab;
+  int sorted_unique;  // every adjacency list strictly increasing
+};
+
+template <class W>
+struct DevState {
+  W* vs;
+  uint32_t* eact;
+  uint8_t* mod;
+  uint8_t* sch;
+  W* unm;
+};
+
+// Device counters.  The first kStepCounterWords words are per step
+// (AlgoResults plus walker bookkeeping) and are cleared before every step;
+// modified_total lives across steps and is cleared together with the
+// modified flags (before CC/PC/TDS, as the reference's resetState does).
+struct StepCounters {
+  unsigned long long vertex_elim;
+  unsigned long long edge_elim;
+  unsigned long long match_elim;
+  unsigned long long enumeration;
+  unsigned long long overflow;   // walker items that ran out of memo space
+  unsigned long long flagged;    // failing items an earlier success may rescue
+  unsigned long long items;      // work counter for persistent kernels
+  unsigned long long error;      // device-side error status (0 = ok)
+  unsigned long long aux;        // list fill counter (overflow retry list)
+  unsigned long long modified_total;  // vertices with mod=1 since the last reset
+  unsigned long long pad[6];
+};
+constexpr int kStepCounterWords = 9;
+
+// Per-query tables derived from the local constraints
+// (multiple_label_constraint_local.h:18-32), in label-slot space.
+struct QueryTables {
+  uint32_t k;
+  uint32_t n_slots;
+  uint8_t role_slot[64];         // slot of originLabel(p)
+  uint64_t nbr_mask[64];         // localConstraintNeighborVertex(p)
+  uint64_t req_slots[64];        // slots with a required count for p
+  uint8_t req[64][64];           // required neighbour count, [role][slot]
+  uint64_t slot_roles[256];      // roles whose origin label has this slot
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint32_t warp_or32(uint32_t x) { return __reduce_or_sync(0xFFFFFFFFu, x); }
+
+__device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
+  uint32_t lo = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(x));
+  uint32_t hi = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(x >> 32));
+  return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+__device__ __forceinline__ bool edge_active(const uint32_t* __restrict__ eact, uint64_t e) {
+  return (eact[e >> 5] >> (e & 31)) & 1u;
+}
+
+// Clears the active bits of CSR entries base + j for every set bit j of m.
+__device__ __forceinline__ void clear_edge_bits(uint32_t* eact, uint64_t base, uint32_t m) {
+  const uint64_t word = base >> 5;
+  const uint32_t sh = static_cast<uint32_t>(base & 31);
+  const uint64_t wide = static_cast<uint64_t>(m) << sh;
+  const uint32_t lo = static_cast<uint32_t>(wide), hi = static_cast<uint32_t>(wide >> 32);
+  if (lo) atomicAnd(eact + word, ~lo);
+  if (hi) atomicAnd(eact + word + 1, ~hi);
+}
+#endif  // __CUDACC__
+
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h, uint32_t k) {
+  k *= 0xcc9e2d51u;
+  k = (k << 15) | (k >> 17);
+  k *= 0x1b873593u;
+  h ^= k;
+  h = (h << 13) | (h >> 19);
+  return h * 5u + 0xe6546b64u;
+}
+__host__ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+
+}  // namespace pmgb

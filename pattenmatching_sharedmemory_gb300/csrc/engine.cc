@@ -1,0 +1,661 @@
+// Host engine: device residency, step orchestration, output writers.
+#include "engine.h"
+
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "totem_io.h"
+
+namespace pmgb {
+
+void throw_cuda(cudaError_t e, const char* what) {
+  const int code = (e == cudaErrorMemoryAllocation) ? PM_E_OOM
+                   : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? PM_E_NO_DEVICE
+                                                                                 : PM_E_DEVICE;
+  throw PmError{code, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+void DeviceBuffer::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+void DeviceBuffer::ensure(size_t n) {
+  if (n <= bytes && ptr) return;
+  release();
+  if (n == 0) n = 16;
+  PM_CUDA(cudaMalloc(&ptr, n));
+  bytes = n;
+}
+
+// ---- graph ------------------------------------------------------------------
+void GraphImpl::finalize_host() {
+  const uint32_t V = host.vertex_count;
+  if (host.labels.size() != V) host.labels.assign(V, 0);
+  dense_values = host.labels;
+  std::sort(dense_values.begin(), dense_values.end());
+  dense_values.erase(std::unique(dense_values.begin(), dense_values.end()), dense_values.end());
+  dense_ids.resize(V);
+  for (uint32_t v = 0; v < V; ++v)
+    dense_ids[v] = static_cast<uint32_t>(std::lower_bound(dense_values.begin(), dense_values.end(), host.labels[v]) -
+                                         dense_values.begin());
+  sorted_unique = true;
+  for (uint32_t v = 0; v < V && sorted_unique; ++v)
+    for (uint64_t e = host.offsets[v] + 1; e < host.offsets[v + 1]; ++e)
+      if (host.adj[e - 1] >= host.adj[e]) {
+        sorted_unique = false;
+        break;
+      }
+}
+
+void GraphImpl::to_device(int dev) {
+  if (device == dev && d_off.ptr) return;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    throw PmError{PM_E_NO_DEVICE, "no CUDA device available for the GB300 pruning kernels"};
+  PM_CUDA(cudaSetDevice(dev));
+  const uint32_t V = host.vertex_count;
+  d_off.ensure(sizeof(uint64_t) * (static_cast<size_t>(V) + 1));
+  d_adj.ensure(sizeof(uint32_t) * std::max<uint64_t>(host.edge_count, 1));
+  d_lab.ensure(sizeof(uint32_t) * std::max<uint32_t>(V, 1));
+  PM_CUDA(cudaMemcpy(d_off.ptr, host.offsets.data(), sizeof(uint64_t) * (V + 1), cudaMemcpyHostToDevice));
+  if (host.edge_count)
+    PM_CUDA(cudaMemcpy(d_adj.ptr, host.adj.data(), sizeof(uint32_t) * host.edge_count, cudaMemcpyHostToDevice));
+  if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
+  device = dev;
+}
+
+DevGraph GraphImpl::dev() const {
+  return DevGraph{host.vertex_count, host.edge_count, d_off.as<uint64_t>(), d_adj.as<uint32_t>(), d_lab.as<uint32_t>(),
+                  sorted_unique ? 1 : 0};
+}
+
+// ---- walker scratch --------------------------------------------------------
+void WalkPool::ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, cudaStream_t s) {
+  if (sc.n_warps >= n_warps && sc.edge_cap == edge_cap && sc.hyp_cap == hyp_cap && sc.hyp_stride >= hyp_stride &&
+      edge.ptr)
+    return;
+  edge.ensure(sizeof(uint4) * static_cast<size_t>(n_warps) * edge_cap);
+  hyp.ensure(sizeof(uint32_t) * static_cast<size_t>(n_warps) * hyp_cap * hyp_stride);
+  epochs.ensure(sizeof(uint32_t) * n_warps);
+  PM_CUDA(cudaMemsetAsync(edge.ptr, 0, edge.bytes, s));
+  PM_CUDA(cudaMemsetAsync(hyp.ptr, 0, hyp.bytes, s));
+  PM_CUDA(cudaMemsetAsync(epochs.ptr, 0, epochs.bytes, s));
+  sc.edge_tab = edge.as<uint4>();
+  sc.hyp_tab = hyp.as<uint32_t>();
+  sc.epochs = epochs.as<uint32_t>();
+  sc.n_warps = n_warps;
+  sc.edge_cap = edge_cap;
+  sc.hyp_cap = hyp_cap;
+  sc.hyp_stride = hyp_stride;
+}
+
+// ---- query ------------------------------------------------------------------
+std::string step_name(int kind) {
+  switch (kind) {
+    case PM_STEP_START: return "START";
+    case PM_STEP_END: return "END";
+    case PM_STEP_LCC0: return "LCC0";
+    case PM_STEP_LCC: return "LCC";
+    case PM_STEP_CC: return "CC";
+    case PM_STEP_PC: return "PC";
+    case PM_STEP_TDS: return "TDS";
+    case PM_STEP_ENUMERATION: return "ENUMERATION";
+  }
+  return "?";
+}
+
+PatternGraph load_pattern(const std::string& dir, bool load_labels) {
+  // multiple_label_cpu.cc:37-47: pattern_edge.totem if present, else
+  // pattern_edge; labels from pattern_vertex_data.
+  std::string edge_path = dir + "pattern_edge.totem";
+  if (!is_regular_file(edge_path)) edge_path = dir + "pattern_edge";
+  HostGraph pg = read_totem_graph(edge_path);
+  if (load_labels && is_regular_file(dir + "pattern_vertex_data")) read_vertex_labels(dir + "pattern_vertex_data", pg);
+  PatternGraph p;
+  p.n = pg.vertex_count;
+  p.offsets = pg.offsets;
+  p.adj = pg.adj;
+  p.labels = pg.labels.empty() ? std::vector<uint64_t>(p.n, 0) : pg.labels;
+  return p;
+}
+
+namespace {
+DeviceConstraint make_device_constraint(CompiledConstraint cc) {
+  DeviceConstraint dc;
+  dc.cc = std::move(cc);
+  for (const auto& p : dc.cc.programs) dc.start_roles.push_back(p.start_role);
+  return dc;
+}
+
+uint32_t max_store(const std::vector<DeviceConstraint>& v) {
+  uint32_t m = 0;
+  for (const auto& dc : v)
+    for (const auto& p : dc.cc.programs) m = std::max<uint32_t>(m, p.n_store);
+  return m;
+}
+}  // namespace
+
+uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
+  const uint64_t V = g.host.vertex_count, E = g.host.edge_count;
+  const uint64_t wb = word_bytes(word_kind_for(k));
+  // state + per-step worklist/status/markers (items bounded by V * roles)
+  return V * (2 * wb + 2) + ((E + 31) / 32) * 4 + V * 8 + V * std::min<uint64_t>(k, 64) * 5 + (1 << 20);
+}
+
+QueryImpl::~QueryImpl() {
+  if (h_ctr) cudaFreeHost(h_ctr);
+  if (h_count) cudaFreeHost(h_count);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+QueryDevPtrs QueryImpl::ptrs() const {
+  return QueryDevPtrs{word_kind, d_vs.ptr, d_eact.as<uint32_t>(), d_mod.as<uint8_t>(), d_sch.as<uint8_t>(),
+                      d_unm.ptr, d_ctr.as<StepCounters>(), d_tables.as<QueryTables>()};
+}
+
+uint64_t QueryImpl::device_bytes() const {
+  return d_vs.bytes + d_eact.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
+         d_d2s.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
+         d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes +
+         pool.bytes() + big_pool.bytes();
+}
+
+void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) {
+  g = graph;
+  pattern = p;
+  k = p.n;
+  qc = compile_constraints(p);
+  for (const auto& c : qc.cycles) cycles.push_back(make_device_constraint(compile_cycle(c)));
+  for (const auto& pc : qc.paths) paths.push_back(make_device_constraint(compile_path(pc)));
+  for (const auto& t : qc.templates) templates.push_back(make_device_constraint(compile_template(t)));
+  enumeration = make_device_constraint(compile_enumeration(qc.enumeration));
+  word_kind = word_kind_for(k);
+
+  // Label slots: the pattern's distinct labels in order of first use.
+  std::vector<label_t> slot_labels;
+  for (uint32_t v = 0; v < k; ++v)
+    if (std::find(slot_labels.begin(), slot_labels.end(), p.labels[v]) == slot_labels.end())
+      slot_labels.push_back(p.labels[v]);
+  auto slot_of = [&](label_t l) -> int {
+    auto it = std::find(slot_labels.begin(), slot_labels.end(), l);
+    return it == slot_labels.end() ? 0xFF : static_cast<int>(it - slot_labels.begin());
+  };
+  memset(&tables, 0, sizeof(tables));
+  tables.k = k;
+  tables.n_slots = static_cast<uint32_t>(slot_labels.size());
+  for (uint32_t r = 0; r < k; ++r) {
+    const LocalConstraint& lc = qc.local[r];
+    tables.role_slot[r] = static_cast<uint8_t>(slot_of(lc.origin_label));
+    tables.nbr_mask[r] = lc.neighbor_mask;
+    for (const auto& kv : lc.required) {
+      int sl = slot_of(kv.first);
+      tables.req[r][sl] = static_cast<uint8_t>(std::min<size_t>(kv.second, 255));
+      tables.req_slots[r] |= uint64_t(1) << sl;
+    }
+    tables.slot_roles[tables.role_slot[r]] |= uint64_t(1) << r;
+  }
+  dense_to_slot.resize(std::max<size_t>(g->dense_values.size(), 1), 0xFF);
+  for (size_t i = 0; i < g->dense_values.size(); ++i) dense_to_slot[i] = static_cast<uint8_t>(slot_of(g->dense_values[i]));
+
+  if (s) {
+    stream = s;
+  } else {
+    PM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+  }
+  PM_CUDA(cudaEventCreate(&ev0));
+  PM_CUDA(cudaEventCreate(&ev1));
+  PM_CUDA(cudaMallocHost(&h_ctr, sizeof(StepCounters)));
+  PM_CUDA(cudaMallocHost(&h_count, sizeof(uint32_t)));
+
+  const uint64_t V = g->host.vertex_count, E = g->host.edge_count;
+  const size_t wb = word_bytes(word_kind);
+  d_vs.ensure(wb * std::max<uint64_t>(V, 1));
+  d_unm.ensure(wb * std::max<uint64_t>(V, 1));
+  d_eact.ensure(4 * std::max<uint64_t>((E + 31) / 32, 1));
+  d_mod.ensure(std::max<uint64_t>(V, 1));
+  d_sch.ensure(std::max<uint64_t>(V, 1));
+  d_ctr.ensure(sizeof(StepCounters));
+  d_tables.ensure(sizeof(QueryTables));
+  d_d2s.ensure(dense_to_slot.size());
+  d_wl.ensure(4 * std::max<uint64_t>(V, 1));
+  d_wl_index.ensure(4 * std::max<uint64_t>(V, 1));
+  d_blocks.ensure(4 * ((V + 4095) / 4096 + 2));
+  d_count.ensure(4);
+  PM_CUDA(cudaMemsetAsync(d_ctr.ptr, 0, sizeof(StepCounters), stream));
+  PM_CUDA(cudaMemcpyAsync(d_tables.ptr, &tables, sizeof(tables), cudaMemcpyHostToDevice, stream));
+  PM_CUDA(cudaMemcpyAsync(d_d2s.ptr, dense_to_slot.data(), dense_to_slot.size(), cudaMemcpyHostToDevice, stream));
+
+  // Every walk program of the query in one device array.
+  std::vector<WalkProgram> progs;
+  std::vector<uint8_t> start_roles, role_index;
+  size_t row = 0;
+  auto add = [&](DeviceConstraint& dc) {
+    dc.prog_offset = progs.size();
+    dc.role_row = row++;
+    progs.insert(progs.end(), dc.cc.programs.begin(), dc.cc.programs.end());
+    start_roles.insert(start_roles.end(), dc.start_roles.begin(), dc.start_roles.end());
+    role_index.insert(role_index.end(), dc.cc.role_index, dc.cc.role_index + 64);
+  };
+  for (auto& dc : cycles) add(dc);
+  for (auto& dc : paths) add(dc);
+  for (auto& dc : templates) add(dc);
+  add(enumeration);
+  d_progs.ensure(sizeof(WalkProgram) * progs.size());
+  d_start_roles.ensure(start_roles.size());
+  d_role_index.ensure(role_index.size());
+  PM_CUDA(cudaMemcpyAsync(d_progs.ptr, progs.data(), sizeof(WalkProgram) * progs.size(), cudaMemcpyHostToDevice,
+                          stream));
+  PM_CUDA(cudaMemcpyAsync(d_start_roles.ptr, start_roles.data(), start_roles.size(), cudaMemcpyHostToDevice, stream));
+  PM_CUDA(cudaMemcpyAsync(d_role_index.ptr, role_index.data(), role_index.size(), cudaMemcpyHostToDevice, stream));
+
+  const uint64_t full = k >= 64 ? ~uint64_t(0) : ((uint64_t(1) << k) - 1);
+  launch_init_state(g->dev(), ptrs(), d_d2s.as<uint8_t>(), full, stream);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaStreamSynchronize(stream));
+  active_vertices = V;
+  active_edges = E;
+  step = advance(PM_STEP_START);
+}
+
+void QueryImpl::reset_modified() {
+  PM_CUDA(cudaMemsetAsync(d_mod.ptr, 0, g->host.vertex_count ? g->host.vertex_count : 1, stream));
+  PM_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(d_ctr.ptr) + offsetof(StepCounters, modified_total), 0,
+                          sizeof(unsigned long long), stream));
+}
+
+void QueryImpl::clear_step_counters() {
+  PM_CUDA(cudaMemsetAsync(d_ctr.ptr, 0, sizeof(unsigned long long) * kStepCounterWords, stream));
+}
+
+void QueryImpl::read_counters() {
+  PM_CUDA(cudaMemcpyAsync(h_ctr, d_ctr.ptr, sizeof(StepCounters), cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  if (h_ctr->error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(h_ctr->error)};
+}
+
+StepResult QueryImpl::step_lcc0() {
+  launch_lcc0(g->dev(), ptrs(), stream);
+  PM_CUDA(cudaGetLastError());
+  read_counters();
+  StepResult r;
+  r.vertex = h_ctr->vertex_elim;
+  r.match = h_ctr->match_elim;
+  return r;
+}
+
+StepResult QueryImpl::step_lcc() {
+  launch_lcc_check(g->dev(), ptrs(), stream);
+  launch_apply(g->dev(), ptrs(), stream);
+  PM_CUDA(cudaGetLastError());
+  read_counters();
+  StepResult r;
+  r.vertex = h_ctr->vertex_elim;
+  r.edge = h_ctr->edge_elim;
+  r.match = h_ctr->match_elim;
+  return r;
+}
+
+uint32_t QueryImpl::build_worklist(uint64_t mask) {
+  launch_worklist(g->dev(), ptrs(), mask, d_wl.as<uint32_t>(), d_wl_index.as<uint32_t>(), d_blocks.as<uint32_t>(),
+                  d_count.as<uint32_t>(), stream);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaMemcpyAsync(h_count, d_count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  return *h_count;
+}
+
+namespace {
+constexpr uint32_t kEdgeCap = 1024, kHypCap = 1024;
+void zero_field(void* base, size_t offset, cudaStream_t s) {
+  PM_CUDA(cudaMemsetAsync(static_cast<char*>(base) + offset, 0, sizeof(unsigned long long), s));
+}
+}  // namespace
+
+void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks) {
+  const uint32_t R = static_cast<uint32_t>(dc.cc.programs.size());
+  const uint64_t n_items = static_cast<uint64_t>(n_wl) * R;
+  if (n_items >= 0xFFFFFFFFull) throw PmError{PM_E_DEVICE, "too many walker items for 32-bit item ids"};
+  d_status.ensure(std::max<uint64_t>(n_items, 1));
+  d_marker.ensure(4 * std::max<uint64_t>(n_items, 1));
+  const uint32_t M = std::max(1, dc.cc.marks_per_success);
+  if (record_marks) d_marks.ensure(4ull * std::max<uint64_t>(n_items, 1) * M);
+  if (!record_marks) PM_CUDA(cudaMemsetAsync(d_marker.ptr, 0xFF, 4 * n_items, stream));
+
+  const uint32_t hyp_stride = 3 + std::max<uint32_t>(max_store(templates), 1);
+  const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
+  pool.ensure(base_warps, kEdgeCap, kHypCap, hyp_stride, stream);
+
+  WalkLaunch w{};
+  w.progs = d_progs.as<WalkProgram>() + dc.prog_offset;
+  w.start_roles = d_start_roles.as<uint8_t>() + dc.prog_offset;
+  w.n_progs = R;
+  w.role_index = d_role_index.as<uint8_t>() + 64 * dc.role_row;
+  w.wl = d_wl.as<uint32_t>();
+  w.wl_index = d_wl_index.as<uint32_t>();
+  w.n_wl = n_wl;
+  w.status = d_status.as<uint8_t>();
+  w.min_marker = record_marks ? nullptr : d_marker.as<uint32_t>();
+  w.marks = record_marks ? d_marks.as<uint32_t>() : nullptr;
+  w.marks_stride = M;
+
+  zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+  zero_field(d_ctr.ptr, offsetof(StepCounters, overflow), stream);
+  launch_walk(g->dev(), ptrs(), w, pool.sc, stream);
+  PM_CUDA(cudaGetLastError());
+  read_counters();
+  uint64_t overflow = h_ctr->overflow;
+  int round = 0;
+  while (overflow) {
+    ++round;
+    ++overflow_retries;
+    if (round > 6) throw PmError{PM_E_DEVICE, "walk memo tables exceed the retry limit"};
+    d_list.ensure(4 * std::max<uint64_t>(n_items, 1));
+    zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
+    launch_collect_overflow(w, d_list.as<uint32_t>(), d_ctr.as<StepCounters>(), stream);
+    read_counters();
+    const uint32_t n_retry = static_cast<uint32_t>(h_ctr->aux);
+    const uint32_t warps = std::max<uint32_t>(kWalkWarpsPerBlock * 8, base_warps >> (3 * round));
+    big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, stream);
+    WalkLaunch r = w;
+    r.retry_items = d_list.as<uint32_t>();
+    r.n_retry = n_retry;
+    zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+    zero_field(d_ctr.ptr, offsetof(StepCounters, overflow), stream);
+    launch_walk(g->dev(), ptrs(), r, big_pool.sc, stream);
+    PM_CUDA(cudaGetLastError());
+    read_counters();
+    overflow = h_ctr->overflow;
+  }
+}
+
+// Exact emulation of the reference's sequential alreadyMatched shortcut
+// (cc :105-108, pc :104-128, tds :163-166 run with one thread): items in
+// order; an item marked by an earlier successful walk is skipped; a
+// successful walk marks every (vertex, role) it bound; a failed one unmatches.
+void QueryImpl::resolve_exact(const DeviceConstraint& dc, uint32_t n_wl) {
+  ++exact_resolutions;
+  run_walks(dc, n_wl, true);
+  const uint32_t R = static_cast<uint32_t>(dc.cc.programs.size());
+  const uint64_t n_items = static_cast<uint64_t>(n_wl) * R;
+  const uint32_t M = std::max(1, dc.cc.marks_per_success);
+  std::vector<uint8_t> status(n_items);
+  std::vector<uint32_t> marks(n_items * M), wl(n_wl);
+  PM_CUDA(cudaMemcpyAsync(status.data(), d_status.ptr, n_items, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaMemcpyAsync(marks.data(), d_marks.ptr, 4 * n_items * M, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, 4ull * n_wl, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  std::vector<uint8_t> marked(n_items, 0);
+  std::vector<uint64_t> unmatch(n_wl, 0);
+  for (uint64_t item = 0; item < n_items; ++item) {
+    const uint8_t st = status[item];
+    if (st == kItemSkip || marked[item]) continue;
+    const uint32_t r = static_cast<uint32_t>(item % R);
+    const WalkProgram& p = dc.cc.programs[r];
+    if (st == kItemSuccess) {
+      uint32_t j = 0;
+      for (int d = 1; d < p.n_steps; ++d) {
+        if (!p.steps[d].mark) continue;
+        const uint32_t x = marks[item * M + j++];
+        const uint8_t ri = dc.cc.role_index[p.steps[d].role];
+        if (ri == 0xFF) continue;
+        auto it = std::lower_bound(wl.begin(), wl.end(), x);
+        if (it == wl.end() || *it != x) continue;
+        marked[static_cast<uint64_t>(it - wl.begin()) * R + ri] = 1;
+      }
+    } else {
+      unmatch[item / R] |= uint64_t(1) << p.start_role;
+    }
+  }
+  std::vector<uint32_t> lv;
+  std::vector<uint64_t> lr;
+  for (uint32_t i = 0; i < n_wl; ++i)
+    if (unmatch[i]) {
+      lv.push_back(wl[i]);
+      lr.push_back(unmatch[i]);
+    }
+  if (!lv.empty()) {
+    d_apply_v.ensure(4 * lv.size());
+    d_apply_r.ensure(8 * lr.size());
+    PM_CUDA(cudaMemcpyAsync(d_apply_v.ptr, lv.data(), 4 * lv.size(), cudaMemcpyHostToDevice, stream));
+    PM_CUDA(cudaMemcpyAsync(d_apply_r.ptr, lr.data(), 8 * lr.size(), cudaMemcpyHostToDevice, stream));
+    launch_apply_unmatch_list(g->dev(), ptrs(), d_apply_v.as<uint32_t>(), d_apply_r.as<uint64_t>(),
+                              static_cast<uint32_t>(lv.size()), stream);
+    PM_CUDA(cudaGetLastError());
+  }
+}
+
+StepResult QueryImpl::step_nlcc(const DeviceConstraint& dc) {
+  const uint32_t n_wl = build_worklist(dc.cc.start_mask);
+  if (n_wl) {
+    run_walks(dc, n_wl, false);
+    const uint32_t R = static_cast<uint32_t>(dc.cc.programs.size());
+    WalkLaunch w{};
+    w.status = d_status.as<uint8_t>();
+    w.min_marker = d_marker.as<uint32_t>();
+    w.n_wl = n_wl;
+    w.n_progs = R;
+    w.wl = d_wl.as<uint32_t>();
+    w.start_roles = d_start_roles.as<uint8_t>() + dc.prog_offset;
+    zero_field(d_ctr.ptr, offsetof(StepCounters, flagged), stream);
+    launch_flag_rescue(w, d_ctr.as<StepCounters>(), stream);
+    read_counters();
+    if (h_ctr->flagged == 0)
+      launch_apply_failures(g->dev(), ptrs(), w, stream);
+    else
+      resolve_exact(dc, n_wl);
+  }
+  launch_apply(g->dev(), ptrs(), stream);
+  PM_CUDA(cudaGetLastError());
+  read_counters();
+  StepResult r;
+  r.vertex = h_ctr->vertex_elim;
+  r.match = h_ctr->match_elim;
+  return r;
+}
+
+StepResult QueryImpl::step_enumeration() {
+  const WalkProgram& p = enumeration.cc.programs[0];
+  const uint32_t n_wl = build_worklist(uint64_t(1) << p.start_role);
+  zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+  if (n_wl) {
+    launch_enumerate(g->dev(), ptrs(), d_progs.as<WalkProgram>() + enumeration.prog_offset, d_wl.as<uint32_t>(), n_wl,
+                     stream);
+    PM_CUDA(cudaGetLastError());
+  }
+  read_counters();
+  StepResult r;
+  r.enumeration = h_ctr->enumeration;
+  return r;
+}
+
+int QueryImpl::advance(int cur) {
+  switch (cur) {
+    case PM_STEP_START: return PM_STEP_LCC0;
+    case PM_STEP_LCC0: return PM_STEP_LCC;
+    case PM_STEP_LCC:
+      if (!last.empty()) return PM_STEP_LCC;
+      if (next_cc < cycles.size()) return PM_STEP_CC;
+      if (next_pc < paths.size()) return PM_STEP_PC;
+      if (next_tds < templates.size()) return PM_STEP_TDS;
+      return PM_STEP_ENUMERATION;
+    case PM_STEP_CC: ++next_cc; return PM_STEP_LCC;
+    case PM_STEP_PC: ++next_pc; return PM_STEP_LCC;
+    case PM_STEP_TDS: ++next_tds; return PM_STEP_LCC;
+    default: return PM_STEP_END;
+  }
+}
+
+pm_step_record QueryImpl::run_step() {
+  pm_step_record rec{};
+  if (finished) return final_record();
+  const int kind = step;
+  if (kind == PM_STEP_CC || kind == PM_STEP_PC || kind == PM_STEP_TDS) reset_modified();
+  clear_step_counters();
+  PM_CUDA(cudaEventRecord(ev0, stream));
+  StepResult r;
+  switch (kind) {
+    case PM_STEP_LCC0: r = step_lcc0(); break;
+    case PM_STEP_LCC: r = step_lcc(); break;
+    case PM_STEP_CC: r = step_nlcc(cycles[next_cc]); break;
+    case PM_STEP_PC: r = step_nlcc(paths[next_pc]); break;
+    case PM_STEP_TDS: r = step_nlcc(templates[next_tds]); break;
+    case PM_STEP_ENUMERATION: r = step_enumeration(); break;
+    default: break;
+  }
+  PM_CUDA(cudaEventRecord(ev1, stream));
+  PM_CUDA(cudaEventSynchronize(ev1));
+  float ms = 0;
+  PM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  r.kind = kind;
+  last = r;
+  active_vertices -= r.vertex;
+  active_edges -= r.edge;
+  if (kind == PM_STEP_ENUMERATION) match_count = r.enumeration;
+  total_ms += ms;
+  rec.iteration = iteration;
+  rec.step = kind;
+  rec.step_ms = ms;
+  rec.cumulative_ms = total_ms;
+  rec.results.vertex_eliminated = r.vertex;
+  rec.results.edge_eliminated = r.edge;
+  rec.results.match_eliminated = r.match;
+  rec.results.enumeration = r.enumeration;
+  rec.active_vertex = active_vertices;
+  rec.total_vertex = g->host.vertex_count;
+  rec.active_edge = active_edges;
+  rec.total_edge = g->host.edge_count;
+  records.push_back(rec);
+  step = advance(kind);
+  if (kind == PM_STEP_ENUMERATION) finished = true;
+  ++iteration;
+  if (iteration >= 1000) finished = true;
+  return rec;
+}
+
+pm_step_record QueryImpl::final_record() {
+  pm_step_record rec{};
+  rec.iteration = iteration;
+  rec.step = step;
+  rec.step_ms = 0;
+  rec.cumulative_ms = total_ms;
+  rec.active_vertex = active_vertices;
+  rec.total_vertex = g->host.vertex_count;
+  rec.active_edge = active_edges;
+  rec.total_edge = g->host.edge_count;
+  return rec;
+}
+
+void QueryImpl::run_all(int max_iterations) {
+  while (!finished && iteration < max_iterations) run_step();
+}
+
+void QueryImpl::export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact) {
+  const uint64_t V = g->host.vertex_count, E = g->host.edge_count;
+  DeviceBuffer dc, de, dv;
+  if (cand) dc.ensure(8 * std::max<uint64_t>(V, 1));
+  if (eact) de.ensure(std::max<uint64_t>(E, 1));
+  if (vact) dv.ensure(std::max<uint64_t>(V, 1));
+  launch_export(g->dev(), ptrs(), cand ? dc.as<uint64_t>() : nullptr, vact ? dv.as<uint8_t>() : nullptr,
+                eact ? de.as<uint8_t>() : nullptr, stream);
+  PM_CUDA(cudaGetLastError());
+  if (cand && V) PM_CUDA(cudaMemcpyAsync(cand, dc.ptr, 8 * V, cudaMemcpyDeviceToHost, stream));
+  if (eact && E) PM_CUDA(cudaMemcpyAsync(eact, de.ptr, E, cudaMemcpyDeviceToHost, stream));
+  if (vact && V) PM_CUDA(cudaMemcpyAsync(vact, dv.ptr, V, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+}
+
+namespace {
+void make_dirs(const std::string& path) {
+  std::string cur;
+  std::stringstream ss(path);
+  std::string item;
+  bool first = true;
+  while (std::getline(ss, item, '/')) {
+    if (!item.empty() || first) {
+      cur += item + "/";
+      mkdir(cur.c_str(), 0777);
+      first = false;
+    }
+  }
+}
+}  // namespace
+
+void QueryImpl::write_outputs(const std::string& dir_in) {
+  std::string dir = dir_in;
+  if (dir.empty() || dir.back() != '/') dir += "/";
+  make_dirs(dir);
+  const uint32_t V = g->host.vertex_count;
+  const uint64_t E = g->host.edge_count;
+  std::vector<uint64_t> cand(V);
+  std::vector<uint8_t> eact(E), vact(V);
+  export_state(cand.data(), eact.data(), vact.data());
+  const pm_step_record fin = final_record();
+  {
+    std::ofstream f(dir + "results.totem", std::ofstream::trunc);
+    if (!f) throw PmError{PM_E_IO, "cannot write " + dir + "results.totem"};
+    f << "Iteration; Step; Step time; Cumulative time; Eliminated vertex; Active vertex; Total vertex; "
+         "Eliminated edge; Active edge; Total edge; Eliminated match; Enumeration number\n";
+    char line[512];
+    auto row = [&](const pm_step_record& r) {
+      snprintf(line, sizeof(line), "%04d; %s; %.4f ; %.4f ; %llu; %llu; %llu; %llu; %llu; %llu; %llu; %llu\n",
+               r.iteration, step_name(r.step).c_str(), r.step_ms, r.cumulative_ms,
+               (unsigned long long)r.results.vertex_eliminated, (unsigned long long)r.active_vertex,
+               (unsigned long long)r.total_vertex, (unsigned long long)r.results.edge_eliminated,
+               (unsigned long long)r.active_edge, (unsigned long long)r.total_edge,
+               (unsigned long long)r.results.match_eliminated, (unsigned long long)r.results.enumeration);
+      f << line;
+    };
+    for (const auto& r : records) row(r);
+    row(fin);
+  }
+  char name[64];
+  snprintf(name, sizeof(name), "graph_%04d.totem", fin.iteration);
+  {
+    FILE* f = fopen((dir + name).c_str(), "wb");
+    if (!f) throw PmError{PM_E_IO, "cannot write " + dir + name};
+    const auto& lab = g->host.labels;
+    for (uint32_t v = 0; v < V; ++v) {
+      if (!vact[v]) continue;
+      for (uint64_t e = g->host.offsets[v]; e < g->host.offsets[v + 1]; ++e) {
+        if (!eact[e]) continue;
+        const uint32_t w = g->host.adj[e];
+        if (!vact[w]) continue;
+        fprintf(f, "%u %u %llu %llu\n", v, w, (unsigned long long)lab[v], (unsigned long long)lab[w]);
+      }
+    }
+    fputc('\n', f);
+    fclose(f);
+  }
+  snprintf(name, sizeof(name), "vertex_%04d.totem", fin.iteration);
+  {
+    FILE* f = fopen((dir + name).c_str(), "wb");
+    if (!f) throw PmError{PM_E_IO, "cannot write " + dir + name};
+    for (uint32_t v = 0; v < V; ++v) {
+      if (!vact[v]) continue;
+      fprintf(f, "%u ", v);
+      for (uint32_t p = 0; p < 64; ++p)
+        if (cand[v] >> p & 1) fprintf(f, "%u ", p);
+      fputc('\n', f);
+    }
+    fputc('\n', f);
+    fclose(f);
+  }
+  {
+    std::ofstream f(dir + "log.totem", std::ofstream::trunc);
+    f << dump_constraints(qc);
+  }
+  { std::ofstream f(dir + "effectiveness.totem", std::ofstream::trunc); }
+  { std::ofstream f(dir + "enumeration_0000.totem", std::ofstream::trunc); }
+}
+
+}  // namespace pmgb

@@ -1,0 +1,141 @@
+// Host engine: resident graph, per-query device state and the step machine.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "constraints.h"
+#include "kernels.h"
+#include "walk_compile.h"
+
+namespace pmgb {
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what);
+#define PM_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t pm_err_ = (call);                      \
+    if (pm_err_ != cudaSuccess) throw_cuda(pm_err_, #call); \
+  } while (0)
+
+// Device allocation owned by RAII.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  ~DeviceBuffer() { release(); }
+  void release();
+  void ensure(size_t n);  // grows (contents not kept)
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(ptr);
+  }
+};
+
+// The graph: host CSR (the caller-visible graph_t) plus its device copy.
+struct GraphImpl {
+  HostGraph host;
+  std::vector<label_t> dense_values;  // sorted distinct label values
+  std::vector<uint32_t> dense_ids;    // per vertex
+  bool sorted_unique = false;
+  int device = -1;
+  DeviceBuffer d_off, d_adj, d_lab;
+
+  void finalize_host();  // dense labels, adjacency checks
+  void to_device(int device);
+  DevGraph dev() const;
+  uint64_t device_bytes() const { return d_off.bytes + d_adj.bytes + d_lab.bytes; }
+};
+
+// Walker scratch pool (memo tables), sized on demand.
+struct WalkPool {
+  DeviceBuffer edge, hyp, epochs;
+  WalkScratch sc{};
+  void ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, cudaStream_t s);
+  uint64_t bytes() const { return edge.bytes + hyp.bytes + epochs.bytes; }
+};
+
+struct StepResult {
+  int kind = PM_STEP_START;
+  uint64_t vertex = 0, edge = 0, match = 0, enumeration = 0;
+  bool empty() const { return !vertex && !edge && !match && !enumeration; }
+};
+
+// One compiled constraint with its programs resident on the device.
+struct DeviceConstraint {
+  CompiledConstraint cc;
+  size_t prog_offset = 0;  // index into the query's device program array
+  size_t role_row = 0;     // row of the query's device role-index table
+  std::vector<uint8_t> start_roles;
+};
+
+struct QueryImpl {
+  GraphImpl* g = nullptr;
+  PatternGraph pattern;
+  QueryConstraints qc;
+  std::vector<DeviceConstraint> cycles, paths, templates;
+  DeviceConstraint enumeration;
+  uint32_t k = 0;
+  int word_kind = kWord16;
+  QueryTables tables{};
+  std::vector<uint8_t> dense_to_slot;
+
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DeviceBuffer d_vs, d_eact, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s;
+  DeviceBuffer d_progs, d_start_roles, d_role_index;
+  DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_apply_v, d_apply_r;
+  StepCounters* h_ctr = nullptr;  // pinned
+  uint32_t* h_count = nullptr;    // pinned
+  WalkPool pool, big_pool;
+
+  // step machine (MultipleLabelStep, multiple_label_step.cc:30-83)
+  int step = PM_STEP_START;
+  size_t next_cc = 0, next_pc = 0, next_tds = 0;
+  StepResult last;
+  bool finished = false;
+  int iteration = 0;
+  uint64_t active_vertices = 0, active_edges = 0;
+  double total_ms = 0;
+  uint64_t match_count = 0;
+  std::vector<pm_step_record> records;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // statistics of the alreadyMatched emulation
+  uint64_t exact_resolutions = 0, overflow_retries = 0;
+
+  ~QueryImpl();
+  void create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s);
+  QueryDevPtrs ptrs() const;
+  uint64_t device_bytes() const;
+
+  // Runs the current step and advances the machine; returns the row.
+  pm_step_record run_step();
+  void run_all(int max_iterations = 1000);
+  pm_step_record final_record();
+
+  void export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact);
+  void write_outputs(const std::string& dir);
+
+ private:
+  void reset_modified();
+  void clear_step_counters();
+  void read_counters();
+  StepResult step_lcc0();
+  StepResult step_lcc();
+  StepResult step_nlcc(const DeviceConstraint& dc);
+  StepResult step_enumeration();
+  uint32_t build_worklist(uint64_t mask);
+  void run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks);
+  void resolve_exact(const DeviceConstraint& dc, uint32_t n_wl);
+  int advance(int cur);
+};
+
+std::string step_name(int kind);
+PatternGraph load_pattern(const std::string& dir, bool load_labels);
+uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k);
+
+}  // namespace pmgb

@@ -1,0 +1,109 @@
+// Host-callable launchers for the GB300 kernels.  Plain pointers only; the
+// packed vertex-word type is selected at run time by QueryDevPtrs::word_kind.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "walk_program.h"
+
+namespace pmgb {
+
+enum WordKind : int { kWord16 = 0, kWord32 = 1, kWord64 = 2, kWordWide = 3 };
+
+inline int word_kind_for(uint32_t k) { return k <= 8 ? kWord16 : k <= 24 ? kWord32 : k <= 56 ? kWord64 : kWordWide; }
+inline size_t word_bytes(int kind) { return kind == kWord16 ? 2 : kind == kWord32 ? 4 : kind == kWord64 ? 8 : 16; }
+
+struct QueryDevPtrs {
+  int word_kind;
+  void* vs;
+  uint32_t* eact;
+  uint8_t* mod;
+  uint8_t* sch;
+  void* unm;
+  StepCounters* ctr;
+  const QueryTables* tables;
+};
+
+// Launch geometry shared by all kernels (SM count of the current device).
+int device_sm_count();
+
+// State initialisation: every vertex holds all k roles and its label slot,
+// every CSR entry is active, every vertex scheduled, nothing modified
+// (MultipleLabelGlobalState::allocate, multiple_label_common_cpu.tpp:30-66).
+void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* dense_to_slot, uint64_t full_cand,
+                       cudaStream_t s);
+
+// LCC0 (multiple_label_lcc0_cpu.tpp:15-87).
+void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
+
+// LCC sweep 1 (multiple_label_lcc_cpu.tpp:26-101).
+void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
+
+// Sweep 2 shared by LCC and CC/PC/TDS (lcc :107-141, cc :134-173).
+void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
+
+// Order-preserving compaction of the vertices that hold a role of
+// `start_mask`: wl[i] = i-th such vertex, wl_index[wl[i]] = i, *count = n.
+// block_counts needs ceil(V / 4096) + 1 entries.
+void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_mask, uint32_t* wl,
+                     uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
+
+// Walker item status.
+enum ItemStatus : uint8_t { kItemSkip = 0, kItemFail = 1, kItemSuccess = 2, kItemOverflow = 3 };
+
+// Per-warp scratch for the walkers' memo tables.
+struct WalkScratch {
+  uint4* edge_tab;       // n_warps * edge_cap entries {epoch, a, b, step}
+  uint32_t* hyp_tab;     // n_warps * hyp_cap * hyp_stride words
+  uint32_t* epochs;      // n_warps * 2 (edge, hyp)
+  uint32_t n_warps;
+  uint32_t edge_cap;     // power of two
+  uint32_t hyp_cap;      // power of two
+  uint32_t hyp_stride;   // words per hypothesis entry (3 + max stored vertices)
+};
+
+struct WalkLaunch {
+  const WalkProgram* progs;  // n_progs programs (device)
+  const uint8_t* start_roles;  // n_progs start roles (device)
+  uint32_t n_progs;
+  const uint8_t* role_index;  // 64 entries (device)
+  const uint32_t* wl;
+  const uint32_t* wl_index;
+  uint32_t n_wl;
+  const uint32_t* retry_items;  // when non-null: only these items (n_retry)
+  uint32_t n_retry;
+  uint8_t* status;        // n_wl * n_progs
+  uint32_t* min_marker;   // n_wl * n_progs, or null
+  uint32_t* marks;        // n_wl * n_progs * marks_stride, or null
+  uint32_t marks_stride;
+};
+
+// Phase 1 of CC/PC/TDS: every (vertex, start role) walk, in parallel.
+void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, const WalkScratch& scratch,
+                 cudaStream_t s);
+
+// Phase 2: count failing items that an earlier success marked.
+void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s);
+
+// Phase 3: failing items become roles to unmatch (all of them, or only
+// those listed by the host's exact resolution).
+void launch_apply_failures(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, cudaStream_t s);
+// Lists the items whose walk ran out of memo space (ctr->aux = count).
+void launch_collect_overflow(const WalkLaunch& w, uint32_t* list, StepCounters* ctr, cudaStream_t s);
+// Blocks of the persistent walker for a scratch pool of n_warps warps.
+uint32_t walk_grid_blocks(uint32_t n_warps_available);
+constexpr uint32_t kWalkWarpsPerBlock = 4;
+void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const uint32_t* vertices, const uint64_t* roles,
+                               uint32_t n, cudaStream_t s);
+
+// ENUMERATION: sums injective embeddings from every worklist vertex.
+void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
+                      uint32_t n_wl, cudaStream_t s);
+
+// Export of the pruned state.
+void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,
+                   cudaStream_t s);
+
+}  // namespace pmgb
