@@ -180,59 +180,6 @@ pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count,
 
 void pm_query_destroy(pm_query* q);
 
-/* ---- batched and served execution ------------------------------------- */
-
-/* Runs n_queries templates over one resident graph together: every query's
- * pruning steps are launched as fused multi-query kernels on one stream
- * (one launch per step kind covers every query currently in that step),
- * each query keeps its own step machine, and results are identical to
- * running each query alone.  Templates are given as concatenated CSR
- * buffers: query i uses p_offsets[off_index[i] .. off_index[i]+n_i] etc.
- * match_counts[i] receives query i's exact count; step_counts[i] the number
- * of result rows query i produced (may be NULL). */
-pm_status_t pm_batch_run(pm_graph* g, int32_t n_queries,
-                         const uint32_t* p_vertex_counts,
-                         const uint64_t* p_offsets, const uint32_t* p_adj,
-                         const uint64_t* p_labels, uint64_t* match_counts,
-                         int32_t* step_counts);
-
-typedef struct pm_server pm_server;
-
-typedef struct {
-  uint64_t memory_budget_bytes; /* admission limit for per-query arenas   */
-  int32_t max_slots;            /* queries resident on the device at once */
-  int32_t max_queue;            /* pending requests before PM_E_BUSY      */
-} pm_server_config;
-
-typedef struct {
-  pm_status_t status;      /* PM_SUCCESS, PM_E_TIMEOUT, PM_E_CANCELLED ... */
-  uint64_t match_count;
-  uint64_t active_vertex;
-  uint64_t active_edge;
-  int32_t n_steps;
-  double submit_to_start_ms; /* queueing delay                             */
-  double submit_to_done_ms;  /* end-to-end latency                         */
-} pm_request_result;
-
-/* Continuous-batching server over one resident graph: requests are admitted
- * as slots and memory free up, share fused multi-query launches with the
- * requests already running, and leave as soon as their own step machine
- * reaches END. */
-pm_status_t pm_server_create(pm_graph* g, const pm_server_config* cfg,
-                             pm_server** out);
-pm_status_t pm_server_submit(pm_server* s, const uint64_t* p_offsets,
-                             const uint32_t* p_adj, const uint64_t* p_labels,
-                             uint32_t p_vertex_count, double timeout_ms,
-                             uint64_t* ticket);
-/* Drives the server one scheduling round (admit, launch, retire). */
-pm_status_t pm_server_progress(pm_server* s, int32_t* n_running,
-                               int32_t* n_pending);
-/* *done = 1 and *out filled once the request finished (any status). */
-pm_status_t pm_server_poll(pm_server* s, uint64_t ticket, pm_request_result* out,
-                           int* done);
-pm_status_t pm_server_cancel(pm_server* s, uint64_t ticket);
-void pm_server_destroy(pm_server* s);
-
 #ifdef __cplusplus
 }
 #endif

@@ -35,6 +35,20 @@ pm_status_t pm_graph_to_device(pm_graph* g, int32_t device);
 /* Writes the graph as TOTEM text and its labels as a vertex file. */
 pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const char* labels_path);
 
+/* Number of visible CUDA devices (0 when none or the driver is missing). */
+int32_t pm_device_count(void);
+
+/* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
+ * 120000 ms).  A walk still running past it stops; the step then fails with
+ * PM_E_TIMEOUT and the query's state is no longer meaningful. */
+pm_status_t pm_set_walk_budget_ms(double ms);
+
+/* Compiles a template (no device needed) and writes the reference-format
+ * constraint dump, as pm_query_dump_constraints does. */
+pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32_t* p_adj, const uint64_t* p_labels,
+                                         uint32_t p_vertex_count, uint64_t p_edge_count, char* buf, size_t cap,
+                                         size_t* needed);
+
 /* Number of NLCC steps that needed the exact sequential emulation of the
  * reference's alreadyMatched shortcut, and of memo-table overflow retries. */
 pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries);

@@ -580,7 +580,10 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
         case LCC: res = step_lcc(s, qc); break;
         case CC: res = step_cc(s, qc.cycles[next_cc]); break;
         case PC: res = step_pc(s, qc.paths[next_pc]); break;
-        case TDS: res = step_tds(s, qc.templates[next_tds]); break;
+        // MultipleLabelTdsCpu::compute never advances its constraint
+        // iterator (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and
+        // pc :186), so every TDS step checks template constraint 0.
+        case TDS: res = step_tds(s, qc.templates[0]); break;
         case ENUM: res = step_enumeration(s, qc.enumeration, enum_vertex_limit); break;
         default: res = Results(); break;
       }

@@ -105,6 +105,10 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_device_bytes": (ctypes.c_int32, [ctypes.c_void_p, c_u64p]),
         "pm_query_estimate_bytes": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, c_u64p]),
         "pm_query_stats": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u64p]),
+        "pm_device_count": (ctypes.c_int32, []),
+        "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
+        "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
+                                                          ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
         "pm_query_destroy": (None, [ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
@@ -244,6 +248,18 @@ class Pattern:
             off[u + 1] = len(adj)
         return cls(off, np.asarray(adj, np.uint32), np.asarray(labels, np.uint64))
 
+    def dump_constraints(self) -> str:
+        """Reference-format constraint dump (log.totem) of this template."""
+        off = np.ascontiguousarray(self.offsets, np.uint64)
+        adj = np.ascontiguousarray(self.adj, np.uint32)
+        lab = np.ascontiguousarray(self.labels, np.uint64)
+        args = (_ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32), _ptr(lab, ctypes.c_uint64), self.n, len(adj))
+        need = ctypes.c_size_t()
+        _check(lib.pm_template_dump_constraints(*args, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        _check(lib.pm_template_dump_constraints(*args, buf, need.value, None))
+        return buf.value.decode()
+
     def write(self, directory) -> None:
         """Writes pattern_edge (TOTEM text) and pattern_vertex_data."""
         d = Path(directory)
@@ -343,3 +359,7 @@ class Query:
 
 def version() -> str:
     return lib.pm_version().decode()
+
+
+def device_count() -> int:
+    return int(lib.pm_device_count())

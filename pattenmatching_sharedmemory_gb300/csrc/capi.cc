@@ -293,6 +293,45 @@ pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count, 
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_walk_budget_ms(double ms) {
+  PM_REQUIRE(ms > 0, "budget must be positive");
+  set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));
+  return PM_SUCCESS;
+}
+
+int32_t pm_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32_t* p_adj, const uint64_t* p_labels,
+                                         uint32_t p_vertex_count, uint64_t p_edge_count, char* buf, size_t cap,
+                                         size_t* needed) {
+  PM_REQUIRE(p_offsets && (p_adj || p_edge_count == 0), "null argument");
+  PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
+  for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
+  return guarded([&]() -> pm_status_t {
+    PatternGraph p;
+    p.n = p_vertex_count;
+    p.offsets.assign(p_offsets, p_offsets + p_vertex_count + 1);
+    p.adj.assign(p_adj, p_adj + p_edge_count);
+    p.labels = p_labels ? std::vector<uint64_t>(p_labels, p_labels + p_vertex_count)
+                        : std::vector<uint64_t>(p_vertex_count, 0);
+    const std::string d = dump_constraints(compile_constraints(p));
+    if (needed) *needed = d.size() + 1;
+    if (buf && cap) {
+      const size_t n = d.size() < cap - 1 ? d.size() : cap - 1;
+      memcpy(buf, d.data(), n);
+      buf[n] = 0;
+    }
+    return PM_SUCCESS;
+  });
+}
+
 pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries) {
   PM_REQUIRE(q, "query is NULL");
   if (exact_resolutions) *exact_resolutions = q->impl.exact_resolutions;

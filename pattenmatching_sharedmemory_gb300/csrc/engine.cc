@@ -77,23 +77,30 @@ DevGraph GraphImpl::dev() const {
 }
 
 // ---- walker scratch --------------------------------------------------------
-void WalkPool::ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, cudaStream_t s) {
-  if (sc.n_warps >= n_warps && sc.edge_cap == edge_cap && sc.hyp_cap == hyp_cap && sc.hyp_stride >= hyp_stride &&
-      edge.ptr)
+void WalkPool::ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, uint32_t state_cap,
+                      uint32_t state_stride, cudaStream_t s) {
+  if (edge.ptr && sc.n_warps == n_warps && sc.edge_cap == edge_cap && sc.hyp_cap == hyp_cap &&
+      sc.hyp_stride == hyp_stride && sc.state_cap == state_cap && sc.state_stride == state_stride)
     return;
   edge.ensure(sizeof(uint4) * static_cast<size_t>(n_warps) * edge_cap);
   hyp.ensure(sizeof(uint32_t) * static_cast<size_t>(n_warps) * hyp_cap * hyp_stride);
+  state.ensure(sizeof(uint32_t) * static_cast<size_t>(n_warps) * state_cap * state_stride);
   epochs.ensure(sizeof(uint32_t) * n_warps);
+  // Epoch 0 marks every slot free; per-warp epochs start at 0 and walks use 1+.
   PM_CUDA(cudaMemsetAsync(edge.ptr, 0, edge.bytes, s));
   PM_CUDA(cudaMemsetAsync(hyp.ptr, 0, hyp.bytes, s));
+  PM_CUDA(cudaMemsetAsync(state.ptr, 0, state.bytes, s));
   PM_CUDA(cudaMemsetAsync(epochs.ptr, 0, epochs.bytes, s));
   sc.edge_tab = edge.as<uint4>();
   sc.hyp_tab = hyp.as<uint32_t>();
+  sc.state_tab = state.as<uint32_t>();
   sc.epochs = epochs.as<uint32_t>();
   sc.n_warps = n_warps;
   sc.edge_cap = edge_cap;
   sc.hyp_cap = hyp_cap;
   sc.hyp_stride = hyp_stride;
+  sc.state_cap = state_cap;
+  sc.state_stride = state_stride;
 }
 
 // ---- query ------------------------------------------------------------------
@@ -134,10 +141,9 @@ DeviceConstraint make_device_constraint(CompiledConstraint cc) {
   return dc;
 }
 
-uint32_t max_store(const std::vector<DeviceConstraint>& v) {
+uint32_t max_state_words(const std::vector<DeviceConstraint>& v) {
   uint32_t m = 0;
-  for (const auto& dc : v)
-    for (const auto& p : dc.cc.programs) m = std::max<uint32_t>(m, p.n_store);
+  for (const auto& dc : v) m = std::max<uint32_t>(m, dc.cc.max_state_words);
   return m;
 }
 }  // namespace
@@ -174,10 +180,10 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) 
   pattern = p;
   k = p.n;
   qc = compile_constraints(p);
-  for (const auto& c : qc.cycles) cycles.push_back(make_device_constraint(compile_cycle(c)));
-  for (const auto& pc : qc.paths) paths.push_back(make_device_constraint(compile_path(pc)));
-  for (const auto& t : qc.templates) templates.push_back(make_device_constraint(compile_template(t)));
-  enumeration = make_device_constraint(compile_enumeration(qc.enumeration));
+  for (const auto& c : qc.cycles) cycles.push_back(make_device_constraint(compile_cycle(c, p.labels)));
+  for (const auto& pc : qc.paths) paths.push_back(make_device_constraint(compile_path(pc, p.labels)));
+  for (const auto& t : qc.templates) templates.push_back(make_device_constraint(compile_template(t, p.labels)));
+  enumeration = make_device_constraint(compile_enumeration(qc.enumeration, p.labels));
   word_kind = word_kind_for(k);
 
   // Label slots: the pattern's distinct labels in order of first use.
@@ -280,6 +286,9 @@ void QueryImpl::clear_step_counters() {
 void QueryImpl::read_counters() {
   PM_CUDA(cudaMemcpyAsync(h_ctr, d_ctr.ptr, sizeof(StepCounters), cudaMemcpyDeviceToHost, stream));
   PM_CUDA(cudaStreamSynchronize(stream));
+  if (h_ctr->error == kDeviceErrorTimeout)
+    throw PmError{PM_E_TIMEOUT, "a walker launch exceeded its time budget of " +
+                                    std::to_string(walk_budget_ns() / 1000000) + " ms"};
   if (h_ctr->error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(h_ctr->error)};
 }
 
@@ -315,11 +324,29 @@ uint32_t QueryImpl::build_worklist(uint64_t mask) {
 }
 
 namespace {
-constexpr uint32_t kEdgeCap = 1024, kHypCap = 1024;
+constexpr uint32_t kEdgeCap = 1024, kHypCap = 1024, kStateCap = 2048;
 void zero_field(void* base, size_t offset, cudaStream_t s) {
   PM_CUDA(cudaMemsetAsync(static_cast<char*>(base) + offset, 0, sizeof(unsigned long long), s));
 }
+uint32_t max_hyp_words(const std::vector<DeviceConstraint>& v) {
+  uint32_t m = 0;
+  for (const auto& dc : v) m = std::max<uint32_t>(m, dc.cc.max_hyp_words);
+  return m;
+}
 }  // namespace
+
+void QueryImpl::pool_strides(uint32_t* hyp_stride, uint32_t* state_stride) const {
+  *hyp_stride = 3 + std::max<uint32_t>({max_hyp_words(cycles), max_hyp_words(paths), max_hyp_words(templates), 1u});
+  *state_stride = 5 + std::max<uint32_t>({max_state_words(cycles), max_state_words(paths), max_state_words(templates),
+                                          enumeration.cc.max_state_words, 1u});
+}
+
+void QueryImpl::ensure_pool() {
+  uint32_t hs, ss;
+  pool_strides(&hs, &ss);
+  const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
+  pool.ensure(base_warps, kEdgeCap, kHypCap, hs, kStateCap, ss, stream);
+}
 
 void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks) {
   const uint32_t R = static_cast<uint32_t>(dc.cc.programs.size());
@@ -328,12 +355,16 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   d_status.ensure(std::max<uint64_t>(n_items, 1));
   d_marker.ensure(4 * std::max<uint64_t>(n_items, 1));
   const uint32_t M = std::max(1, dc.cc.marks_per_success);
+  // Exact constraints cannot be rescued by alreadyMatched marks (see
+  // walk_program.h), so they skip the mark bookkeeping entirely.
+  const bool track_markers = !record_marks && !dc.cc.exact;
   if (record_marks) d_marks.ensure(4ull * std::max<uint64_t>(n_items, 1) * M);
-  if (!record_marks) PM_CUDA(cudaMemsetAsync(d_marker.ptr, 0xFF, 4 * n_items, stream));
+  if (track_markers) PM_CUDA(cudaMemsetAsync(d_marker.ptr, 0xFF, 4 * n_items, stream));
 
-  const uint32_t hyp_stride = 3 + std::max<uint32_t>(max_store(templates), 1);
+  uint32_t hyp_stride, state_stride;
+  pool_strides(&hyp_stride, &state_stride);
   const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
-  pool.ensure(base_warps, kEdgeCap, kHypCap, hyp_stride, stream);
+  ensure_pool();
 
   WalkLaunch w{};
   w.progs = d_progs.as<WalkProgram>() + dc.prog_offset;
@@ -344,7 +375,7 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   w.wl_index = d_wl_index.as<uint32_t>();
   w.n_wl = n_wl;
   w.status = d_status.as<uint8_t>();
-  w.min_marker = record_marks ? nullptr : d_marker.as<uint32_t>();
+  w.min_marker = track_markers ? d_marker.as<uint32_t>() : nullptr;
   w.marks = record_marks ? d_marks.as<uint32_t>() : nullptr;
   w.marks_stride = M;
 
@@ -365,7 +396,8 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
     read_counters();
     const uint32_t n_retry = static_cast<uint32_t>(h_ctr->aux);
     const uint32_t warps = std::max<uint32_t>(kWalkWarpsPerBlock * 8, base_warps >> (3 * round));
-    big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, stream);
+    big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, kStateCap << (3 * round),
+                    state_stride, stream);
     WalkLaunch r = w;
     r.retry_items = d_list.as<uint32_t>();
     r.n_retry = n_retry;
@@ -447,9 +479,11 @@ StepResult QueryImpl::step_nlcc(const DeviceConstraint& dc) {
     w.wl = d_wl.as<uint32_t>();
     w.start_roles = d_start_roles.as<uint8_t>() + dc.prog_offset;
     zero_field(d_ctr.ptr, offsetof(StepCounters, flagged), stream);
-    launch_flag_rescue(w, d_ctr.as<StepCounters>(), stream);
-    read_counters();
-    if (h_ctr->flagged == 0)
+    if (!dc.cc.exact) {
+      launch_flag_rescue(w, d_ctr.as<StepCounters>(), stream);
+      read_counters();
+    }
+    if (dc.cc.exact || h_ctr->flagged == 0)
       launch_apply_failures(g->dev(), ptrs(), w, stream);
     else
       resolve_exact(dc, n_wl);
@@ -468,9 +502,36 @@ StepResult QueryImpl::step_enumeration() {
   const uint32_t n_wl = build_worklist(uint64_t(1) << p.start_role);
   zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
   if (n_wl) {
-    launch_enumerate(g->dev(), ptrs(), d_progs.as<WalkProgram>() + enumeration.prog_offset, d_wl.as<uint32_t>(), n_wl,
+    ensure_pool();
+    d_list.ensure(4ull * n_wl);
+    d_list2.ensure(4ull * n_wl);
+    const WalkProgram* prog = d_progs.as<WalkProgram>() + enumeration.prog_offset;
+    zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
+    launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list.as<uint32_t>(), pool.sc,
                      stream);
     PM_CUDA(cudaGetLastError());
+    read_counters();
+    // Sources whose count memo overflowed are re-run with larger tables.
+    uint32_t n_over = static_cast<uint32_t>(h_ctr->aux);
+    DeviceBuffer* in = &d_list;
+    DeviceBuffer* out = &d_list2;
+    uint32_t hs, ss;
+    pool_strides(&hs, &ss);
+    const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
+    for (int round = 1; n_over; ++round) {
+      ++overflow_retries;
+      if (round > 6) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
+      const uint32_t warps = std::max<uint32_t>(kWalkWarpsPerBlock * 8, base_warps >> (3 * round));
+      big_pool.ensure(warps, kEdgeCap, kHypCap, hs, kStateCap << (3 * round), ss, stream);
+      zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+      zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
+      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, in->as<uint32_t>(), n_over,
+                       out->as<uint32_t>(), big_pool.sc, stream);
+      PM_CUDA(cudaGetLastError());
+      read_counters();
+      n_over = static_cast<uint32_t>(h_ctr->aux);
+      std::swap(in, out);
+    }
   }
   read_counters();
   StepResult r;
@@ -508,7 +569,10 @@ pm_step_record QueryImpl::run_step() {
     case PM_STEP_LCC: r = step_lcc(); break;
     case PM_STEP_CC: r = step_nlcc(cycles[next_cc]); break;
     case PM_STEP_PC: r = step_nlcc(paths[next_pc]); break;
-    case PM_STEP_TDS: r = step_nlcc(templates[next_tds]); break;
+    // The reference's TDS step never advances its constraint iterator
+    // (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and pc :186):
+    // each of the n_template TDS steps checks template constraint 0.
+    case PM_STEP_TDS: r = step_nlcc(templates[0]); break;
     case PM_STEP_ENUMERATION: r = step_enumeration(); break;
     default: break;
   }

@@ -52,10 +52,11 @@ struct GraphImpl {
 
 // Walker scratch pool (memo tables), sized on demand.
 struct WalkPool {
-  DeviceBuffer edge, hyp, epochs;
+  DeviceBuffer edge, hyp, state, epochs;
   WalkScratch sc{};
-  void ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, cudaStream_t s);
-  uint64_t bytes() const { return edge.bytes + hyp.bytes + epochs.bytes; }
+  void ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uint32_t hyp_stride, uint32_t state_cap,
+              uint32_t state_stride, cudaStream_t s);
+  uint64_t bytes() const { return edge.bytes + hyp.bytes + state.bytes + epochs.bytes; }
 };
 
 struct StepResult {
@@ -87,7 +88,8 @@ struct QueryImpl {
   bool own_stream = false;
   DeviceBuffer d_vs, d_eact, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s;
   DeviceBuffer d_progs, d_start_roles, d_role_index;
-  DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_apply_v, d_apply_r;
+  DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_list2, d_apply_v,
+      d_apply_r;
   StepCounters* h_ctr = nullptr;  // pinned
   uint32_t* h_count = nullptr;    // pinned
   WalkPool pool, big_pool;
@@ -129,6 +131,8 @@ struct QueryImpl {
   StepResult step_nlcc(const DeviceConstraint& dc);
   StepResult step_enumeration();
   uint32_t build_worklist(uint64_t mask);
+  void pool_strides(uint32_t* hyp_stride, uint32_t* state_stride) const;
+  void ensure_pool();
   void run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks);
   void resolve_exact(const DeviceConstraint& dc, uint32_t n_wl);
   int advance(int cur);

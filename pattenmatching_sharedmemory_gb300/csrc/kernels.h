@@ -51,17 +51,31 @@ void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_ma
                      uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
 
 // Walker item status.
-enum ItemStatus : uint8_t { kItemSkip = 0, kItemFail = 1, kItemSuccess = 2, kItemOverflow = 3 };
+enum ItemStatus : uint8_t { kItemSkip = 0, kItemFail = 1, kItemSuccess = 2, kItemOverflow = 3, kItemTimeout = 4 };
 
-// Per-warp scratch for the walkers' memo tables.
+// StepCounters::error values written by kernels.
+constexpr unsigned long long kDeviceErrorTimeout = 2;
+
+// Time budget of one walker launch (ns of %globaltimer per warp); a warp
+// past it stops, marks its item kItemTimeout and sets kDeviceErrorTimeout.
+void set_walk_budget_ns(uint64_t ns);
+uint64_t walk_budget_ns();
+
+// Per-warp scratch for the walkers' memo tables.  The edge and hypothesis
+// tables reproduce the reference's memos and must hold every entry (a walk
+// that fills them is re-run with larger tables); the state table is a
+// best-effort cache (state memo / count memo, see walk_program.h).
 struct WalkScratch {
   uint4* edge_tab;       // n_warps * edge_cap entries {epoch, a, b, step}
   uint32_t* hyp_tab;     // n_warps * hyp_cap * hyp_stride words
-  uint32_t* epochs;      // n_warps * 2 (edge, hyp)
+  uint32_t* state_tab;   // n_warps * state_cap * state_stride words
+  uint32_t* epochs;      // n_warps
   uint32_t n_warps;
   uint32_t edge_cap;     // power of two
   uint32_t hyp_cap;      // power of two
-  uint32_t hyp_stride;   // words per hypothesis entry (3 + max stored vertices)
+  uint32_t hyp_stride;   // 3 + stored vertices
+  uint32_t state_cap;    // power of two
+  uint32_t state_stride; // 5 + state key words (the last two hold a count)
 };
 
 struct WalkLaunch {
@@ -98,9 +112,12 @@ constexpr uint32_t kWalkWarpsPerBlock = 4;
 void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const uint32_t* vertices, const uint64_t* roles,
                                uint32_t n, cudaStream_t s);
 
-// ENUMERATION: sums injective embeddings from every worklist vertex.
+// ENUMERATION: sums injective embeddings from every worklist vertex (or
+// from the wl positions in `retry`); sources whose count memo overflowed are
+// written to `overflow` (count in ctr->aux) and contribute nothing.
 void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, cudaStream_t s);
+                      uint32_t n_wl, const uint32_t* retry, uint32_t n_retry, uint32_t* overflow,
+                      const WalkScratch& scratch, cudaStream_t s);
 
 // Export of the pruned state.
 void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,

@@ -14,8 +14,10 @@
 // multiple_label_cc_cpu.tpp:105-115, tds :46-63) become per-warp open-
 // addressing tables in global scratch, probed 32 slots per step by the whole
 // warp and invalidated per walk by an epoch number, so no clearing pass is
-// needed between walks.  A walk whose table passes half load stops with
-// kItemOverflow and is re-run by the host with larger tables.
+// needed between walks.  A walk whose reference-memo table passes half load
+// stops with kItemOverflow and is re-run by the host with larger tables.  A
+// third, best-effort table caches explored states (NLCC) and subtree counts
+// (ENUMERATION of distinct-label templates).
 //
 // Work items are (worklist vertex, start role) pairs handed out through an
 // atomic counter in role-major order, so consecutive items of a warp share
@@ -32,14 +34,17 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kWalkWarps = 4;  // warps per block
 constexpr int kSteps = kMaxWalkSteps;
+constexpr uint32_t kStateTag = 0x80000000u;
 
 struct WalkFrames {
   uint64_t next[kSteps + 1];
   uint64_t end[kSteps + 1];
   uint64_t chunk[kSteps + 1];
+  uint64_t leaves0[kSteps + 1];  // ENUMERATION count at descent (count memo)
   uint32_t mask[kSteps + 1];
   uint32_t cur[kSteps + 1];
   uint32_t bound[kSteps + 1];
+  uint8_t child[kSteps + 1];     // a descent from this step awaits its count
 };
 
 struct WarpShared {
@@ -49,13 +54,22 @@ struct WarpShared {
 
 enum : int { kNone = 0, kFound = 1, kOverflowHit = 2 };
 
+uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // ---- per-warp memo tables -------------------------------------------------
 struct WarpMemo {
   uint4* edge;
   uint32_t* hyp;
-  uint32_t edge_cap, hyp_cap, hyp_stride;
+  uint32_t* state;
+  uint32_t edge_cap, hyp_cap, hyp_stride, state_cap, state_stride;
   uint32_t epoch;
-  uint32_t edge_n, hyp_n;
+  uint32_t edge_n, hyp_n, state_n;
 };
 
 __device__ __forceinline__ uint32_t edge_hash(uint32_t a, uint32_t b, uint32_t step) {
@@ -98,49 +112,141 @@ __device__ bool edge_memo_insert(WarpMemo& m, uint32_t a, uint32_t b, uint32_t s
   return false;
 }
 
-__device__ __forceinline__ uint32_t hyp_hash(uint32_t nb, uint32_t step, const WarpShared& ws, int d) {
+// Key words after (nb, step) of the tuple memos: the stored vertices bound
+// before step d (the reference's TDS hypothesis, tds :51-61) or the history
+// entries of state_refs[d] (state / count memo).
+struct KeyTuple {
+  const WarpShared* ws;
+  int d;
+  int n;
+  bool refs;
+  __device__ __forceinline__ uint32_t operator[](int i) const {
+    if (refs) {
+      uint64_t r = ws->prog.state_refs[d];
+      for (int k = 0; k < i; ++k) r &= r - 1;
+      const int h = __ffsll(static_cast<long long>(r)) - 1;
+      return ws->f.bound[ws->prog.hist_step[h]];
+    }
+    return ws->f.bound[ws->prog.store_step[i]];
+  }
+};
+
+__device__ __forceinline__ KeyTuple stored_key(const WarpShared& ws, int d) {
+  int n = 0;
+  while (n < ws.prog.n_store && ws.prog.store_step[n] < d) ++n;
+  return KeyTuple{&ws, d, n, false};
+}
+__device__ __forceinline__ KeyTuple state_key(const WarpShared& ws, int d) {
+  return KeyTuple{&ws, d, __popcll(ws.prog.state_refs[d]), true};
+}
+
+__device__ __forceinline__ uint32_t tuple_hash(uint32_t nb, uint32_t step, const KeyTuple& t) {
   uint32_t h = mix32(mix32(0x1b873593u, nb), step);
-  for (int i = 0; i < ws.prog.n_store && ws.prog.store_step[i] < d; ++i) h = mix32(h, ws.f.bound[ws.prog.store_step[i]]);
+  for (int i = 0; i < t.n; ++i) h = mix32(h, t[i]);
   return fmix32(h);
 }
 
-// Hypothesis memo: entry = {epoch, nb, step, stored vertices..., pad 0xFFFFFFFF}.
-// find_or_insert: returns kFound if present; otherwise inserts and returns
-// kNone (or kOverflowHit when the table is past half load).
-__device__ int hyp_memo(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShared& ws, int d, bool insert) {
+// Open-addressing tuple table: entry = {epoch, nb, step, key words padded
+// with 0xFFFFFFFF, [count lo, count hi]}.  Probes 32 slots per round.
+// Returns the slot of a live match, or ~0 with *empty_slot set to the first
+// free slot (or ~0 when the table has no free slot in reach).
+__device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t stride, uint32_t key_words, uint32_t epoch,
+                               uint32_t nb, uint32_t step, const KeyTuple& t, uint32_t* empty_slot) {
   const unsigned lane = lane_id();
-  const uint32_t mask = m.hyp_cap - 1;
-  const uint32_t h = hyp_hash(nb, step, ws, d);
-  int n_h = 0;
-  while (n_h < ws.prog.n_store && ws.prog.store_step[n_h] < d) ++n_h;
-  const uint32_t n_words = m.hyp_stride - 3;
-  for (uint32_t probe = 0; probe < m.hyp_cap; probe += 32) {
+  const uint32_t mask = cap - 1;
+  const uint32_t h = tuple_hash(nb, step, t);
+  for (uint32_t probe = 0; probe < cap; probe += 32) {
     const uint32_t slot = (h + probe + lane) & mask;
-    const uint32_t* e = m.hyp + static_cast<uint64_t>(slot) * m.hyp_stride;
-    const bool live = __ldcg(e) == m.epoch;
+    const uint32_t* e = tab + static_cast<uint64_t>(slot) * stride;
+    const bool live = __ldcg(e) == epoch;
     bool match = live && __ldcg(e + 1) == nb && __ldcg(e + 2) == step;
-    for (uint32_t i = 0; match && i < n_words; ++i) {
-      const uint32_t want = static_cast<int>(i) < n_h ? ws.f.bound[ws.prog.store_step[i]] : 0xFFFFFFFFu;
+    for (uint32_t i = 0; match && i < key_words; ++i) {
+      const uint32_t want = static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu;
       if (__ldcg(e + 3 + i) != want) match = false;
     }
-    if (__any_sync(kFull, match)) return kFound;
+    const unsigned mm = __ballot_sync(kFull, match);
+    if (mm) return (h + probe + __ffs(mm) - 1) & mask;
     const unsigned em = __ballot_sync(kFull, !live);
     if (em) {
-      if (!insert) return kNone;
-      if (lane == static_cast<unsigned>(__ffs(em) - 1)) {
-        uint32_t* w = m.hyp + static_cast<uint64_t>(slot) * m.hyp_stride;
-        __stcg(w + 1, nb);
-        __stcg(w + 2, step);
-        for (uint32_t i = 0; i < n_words; ++i)
-          __stcg(w + 3 + i, static_cast<int>(i) < n_h ? ws.f.bound[ws.prog.store_step[i]] : 0xFFFFFFFFu);
-        __threadfence_block();
-        __stcg(w, m.epoch);
-      }
-      __syncwarp();
-      return ++m.hyp_n <= (m.hyp_cap >> 1) ? kNone : kOverflowHit;
+      *empty_slot = (h + probe + __ffs(em) - 1) & mask;
+      return ~0u;
     }
   }
-  return insert ? kOverflowHit : kNone;
+  *empty_slot = ~0u;
+  return ~0u;
+}
+
+__device__ void tuple_write(uint32_t* tab, uint32_t stride, uint32_t key_words, uint32_t slot, uint32_t epoch,
+                            uint32_t nb, uint32_t step, const KeyTuple& t, bool with_count, unsigned long long count) {
+  if (lane_id() == 0) {
+    uint32_t* w = tab + static_cast<uint64_t>(slot) * stride;
+    __stcg(w + 1, nb);
+    __stcg(w + 2, step);
+    for (uint32_t i = 0; i < key_words; ++i) __stcg(w + 3 + i, static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu);
+    if (with_count) {
+      __stcg(w + 3 + key_words, static_cast<uint32_t>(count));
+      __stcg(w + 4 + key_words, static_cast<uint32_t>(count >> 32));
+    }
+    __stcg(w, epoch);
+  }
+  __syncwarp();
+}
+
+// The reference's hypothesis memo (tds :51-63): kFound if (nb, step, stored)
+// was bound before; otherwise inserts it (kNone, or kOverflowHit when the
+// table is past half load — the host then re-runs the walk).
+__device__ int hyp_memo(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShared& ws, int d) {
+  const KeyTuple t = stored_key(ws, d);
+  uint32_t empty = ~0u;
+  const uint32_t key_words = m.hyp_stride - 3;
+  if (tuple_find(m.hyp, m.hyp_cap, m.hyp_stride, key_words, m.epoch, nb, step, t, &empty) != ~0u) return kFound;
+  if (empty == ~0u) return kOverflowHit;
+  tuple_write(m.hyp, m.hyp_stride, key_words, empty, m.epoch, nb, step, t, false, 0);
+  return ++m.hyp_n <= (m.hyp_cap >> 1) ? kNone : kOverflowHit;
+}
+
+// State memo: kFound when (nb, step, state key) was entered before; else
+// records it (kNone), or kOverflowHit once the table passes half load (the
+// walk is then re-run with a larger table: a walk that forgets states can
+// take exponential time).
+__device__ int state_seen(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShared& ws, int d) {
+  const KeyTuple t = state_key(ws, d);
+  uint32_t empty = ~0u;
+  const uint32_t key_words = m.state_stride - 5;
+  if (tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step | kStateTag, t, &empty) != ~0u)
+    return kFound;
+  if (empty == ~0u || m.state_n >= (m.state_cap >> 1)) return kOverflowHit;
+  tuple_write(m.state, m.state_stride, key_words, empty, m.epoch, nb, step | kStateTag, t, false, 0);
+  ++m.state_n;
+  return kNone;
+}
+
+// Count memo lookup: true and *count when the subtree count is cached.
+__device__ bool count_lookup(const WarpMemo& m, uint32_t nb, uint32_t step, const WarpShared& ws, int d,
+                             unsigned long long* count) {
+  const KeyTuple t = state_key(ws, d);
+  uint32_t empty = ~0u;
+  const uint32_t key_words = m.state_stride - 5;
+  const uint32_t slot = tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step, t, &empty);
+  if (slot == ~0u) return false;
+  const uint32_t* e = m.state + static_cast<uint64_t>(slot) * m.state_stride;
+  *count = static_cast<unsigned long long>(__ldcg(e + 3 + key_words)) |
+           (static_cast<unsigned long long>(__ldcg(e + 4 + key_words)) << 32);
+  return true;
+}
+
+// Caches a finished subtree's count; false once the table passes half load.
+__device__ bool count_store(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShared& ws, int d,
+                            unsigned long long count) {
+  if (m.state_n >= (m.state_cap >> 1)) return false;
+  const KeyTuple t = state_key(ws, d);
+  uint32_t empty = ~0u;
+  const uint32_t key_words = m.state_stride - 5;
+  if (tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step, t, &empty) != ~0u) return true;
+  if (empty == ~0u) return false;
+  tuple_write(m.state, m.state_stride, key_words, empty, m.epoch, nb, step, t, true, count);
+  ++m.state_n;
+  return true;
 }
 
 // ---- neighbour scans ------------------------------------------------------
@@ -149,7 +255,8 @@ __device__ __forceinline__ bool role_of(const DevState<W>& st, uint32_t v, uint3
   return (Pack<W>::cand(st.vs[v]) >> role) & 1;
 }
 
-// Index of `target` in the strictly increasing list adj[lo, hi), or ~0.
+// Index of `target` in the strictly increasing list adj[lo, hi), or ~0
+// (warp-cooperative 32-way search).
 __device__ uint64_t warp_find_sorted(const uint32_t* __restrict__ adj, uint64_t lo, uint64_t hi, uint32_t target) {
   const unsigned lane = lane_id();
   while (hi - lo > 32) {
@@ -171,49 +278,74 @@ __device__ uint64_t warp_find_sorted(const uint32_t* __restrict__ adj, uint64_t 
   return m ? lo + (__ffs(m) - 1) : ~uint64_t(0);
 }
 
-template <class W, bool kEnum>
+// Per-lane binary search of `target` in the strictly increasing adj[lo, hi).
+__device__ __forceinline__ uint64_t lane_find_sorted(const uint32_t* __restrict__ adj, uint64_t lo, uint64_t hi,
+                                                     uint32_t target) {
+  const uint64_t end = hi;
+  while (lo < hi) {
+    const uint64_t mid = lo + ((hi - lo) >> 1);
+    if (adj[mid] < target)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < end && adj[lo] == target) ? lo : ~uint64_t(0);
+}
+
 __device__ __forceinline__ void frame_enter(const DevGraph& g, WarpShared& ws, int d) {
   const uint32_t cur = ws.f.cur[d];
+  __syncwarp();
   if (lane_id() == 0) {
     ws.f.next[d] = g.off[cur];
     ws.f.end[d] = g.off[cur + 1];
     ws.f.mask[d] = 0;
+    ws.f.child[d] = 0;
   }
   __syncwarp();
 }
 
-// Next candidate of VERTEX / FINAL step d.
+// Loads the next chunk of up to 32 CSR entries of step d and returns the
+// candidate mask (VERTEX / FINAL filters), or false when the list is done.
+template <class W, bool kEnum>
+__device__ bool load_chunk(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
+                           uint32_t source) {
+  const unsigned lane = lane_id();
+  const uint64_t next = ws.f.next[d], end = ws.f.end[d];
+  if (next >= end) return false;
+  const uint32_t cnt = end - next < 32 ? static_cast<uint32_t>(end - next) : 32u;
+  const uint64_t e = next + lane;
+  bool ok = lane < cnt && edge_active(st.eact, e);
+  uint32_t nb = 0;
+  if (ok) {
+    nb = g.adj[e];
+    ok = role_of(st, nb, s.role);
+  }
+  if (s.kind == kStepFinal) ok = ok && nb != source;
+  if (kEnum && ok) {
+    for (int h = 0; h < ws.prog.n_hist && ws.prog.hist_step[h] < d; ++h)
+      if (ws.f.bound[ws.prog.hist_step[h]] == nb) ok = false;
+  }
+  const unsigned mask = __ballot_sync(kFull, ok);
+  __syncwarp();
+  if (lane == 0) {
+    ws.f.chunk[d] = next;
+    ws.f.next[d] = next + cnt;
+    ws.f.mask[d] = mask;
+  }
+  __syncwarp();
+  return true;
+}
+
+// Next candidate of VERTEX / FINAL step d, after the reference's memo tests
+// and inserts and the state memo.
 template <class W, bool kEnum>
 __device__ int next_vertex(const DevGraph& g, const DevState<W>& st, WarpShared& ws, WarpMemo& m, int d,
                            const WalkStep& s, uint32_t cur, uint32_t source, uint32_t* out) {
   const unsigned lane = lane_id();
   while (true) {
-    uint32_t mask = ws.f.mask[d];
+    const uint32_t mask = ws.f.mask[d];
     if (mask == 0) {
-      const uint64_t next = ws.f.next[d], end = ws.f.end[d];
-      if (next >= end) return kNone;
-      const uint32_t cnt = end - next < 32 ? static_cast<uint32_t>(end - next) : 32u;
-      const uint64_t e = next + lane;
-      bool ok = lane < cnt && edge_active(st.eact, e);
-      uint32_t nb = 0;
-      if (ok) {
-        nb = g.adj[e];
-        ok = role_of(st, nb, s.role);
-      }
-      if (s.kind == kStepFinal) ok = ok && nb != source;
-      if (kEnum && ok) {
-        const int n_hist = ws.prog.n_hist;
-        for (int h = 0; h < n_hist && ws.prog.hist_step[h] < d; ++h)
-          if (ws.f.bound[ws.prog.hist_step[h]] == nb) ok = false;
-      }
-      mask = __ballot_sync(kFull, ok);
-      __syncwarp();
-      if (lane == 0) {
-        ws.f.chunk[d] = next;
-        ws.f.next[d] = next + cnt;
-        ws.f.mask[d] = mask;
-      }
-      __syncwarp();
+      if (!load_chunk<W, kEnum>(g, st, ws, d, s, source)) return kNone;
       continue;
     }
     const unsigned j = __ffs(mask) - 1;
@@ -222,14 +354,21 @@ __device__ int next_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
     __syncwarp();
     const uint32_t nb = g.adj[ws.f.chunk[d] + j];
     if (!kEnum && s.kind == kStepVertex) {
-      const uint32_t a = cur < nb ? cur : nb, b = cur < nb ? nb : cur;
-      if (s.blocker >= 0 && edge_memo_find(m, a, b, static_cast<uint32_t>(s.blocker))) continue;
-      if (s.hyp) {
-        const int r = hyp_memo(m, nb, static_cast<uint32_t>(d), ws, d, true);
-        if (r == kFound) continue;
-        if (r == kOverflowHit) return kOverflowHit;
+      if (!ws.prog.exact) {
+        // The reference's memo tests and inserts, in its order (cc :105-114,
+        // tds :99-119).
+        const uint32_t a = cur < nb ? cur : nb, b = cur < nb ? nb : cur;
+        if (s.blocker >= 0 && edge_memo_find(m, a, b, static_cast<uint32_t>(s.blocker))) continue;
+        if (s.hyp) {
+          const int r = hyp_memo(m, nb, static_cast<uint32_t>(d), ws, d);
+          if (r == kFound) continue;
+          if (r == kOverflowHit) return kOverflowHit;
+        }
+        if (s.record && !edge_memo_insert(m, a, b, static_cast<uint32_t>(d))) return kOverflowHit;
       }
-      if (s.record && !edge_memo_insert(m, a, b, static_cast<uint32_t>(d))) return kOverflowHit;
+      const int sr = state_seen(m, nb, static_cast<uint32_t>(d), ws, d);
+      if (sr == kFound) continue;
+      if (sr == kOverflowHit) return kOverflowHit;
     }
     *out = nb;
     return kFound;
@@ -286,13 +425,61 @@ __device__ bool next_check(const DevGraph& g, const DevState<W>& st, WarpShared&
   }
 }
 
-// Runs one walk.  NLCC: returns kItemSuccess / kItemFail / kItemOverflow.
-// ENUMERATION: counts completed walks into *leaves and returns kItemFail.
+// The last VERTEX step of a walk whose remaining steps are CHECKs only, on
+// sorted adjacency: every lane binds its own candidate and evaluates all
+// remaining CHECKs itself (binary search in the candidate's list), so a
+// chunk of 32 candidates is finished in one pass instead of 32 descents.
+// NLCC (exact programs only): kFound with the first passing candidate in
+// CSR order.  ENUMERATION: adds the passing candidates to *leaves.
 template <class W, bool kEnum>
-__device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared& ws, WarpMemo& m, uint32_t source,
-                            unsigned long long* leaves) {
+__device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
+                           uint32_t* out, unsigned long long* leaves) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog.n_steps;
+  while (true) {
+    const uint64_t next = ws.f.next[d], end = ws.f.end[d];
+    if (next >= end) return kNone;
+    const uint32_t cnt = end - next < 32 ? static_cast<uint32_t>(end - next) : 32u;
+    const uint64_t e = next + lane;
+    bool ok = lane < cnt && edge_active(st.eact, e);
+    uint32_t nb = 0;
+    if (ok) {
+      nb = g.adj[e];
+      ok = role_of(st, nb, s.role);
+    }
+    if (kEnum && ok) {
+      for (int h = 0; h < ws.prog.n_hist && ws.prog.hist_step[h] < d; ++h)
+        if (ws.f.bound[ws.prog.hist_step[h]] == nb) ok = false;
+    }
+    for (int j = ws.prog.tail_from; ok && j < n_steps; ++j) {
+      const int hs = ws.prog.hist_step[ws.prog.steps[j].hist];
+      const uint32_t target = hs == d ? nb : ws.f.bound[hs];
+      const uint64_t idx = lane_find_sorted(g.adj, g.off[nb], g.off[nb + 1], target);
+      ok = idx != ~uint64_t(0) && edge_active(st.eact, idx) && Pack<W>::cand(st.vs[target]) != 0;
+    }
+    const unsigned mask = __ballot_sync(kFull, ok);
+    __syncwarp();
+    if (lane == 0) ws.f.next[d] = next + cnt;
+    __syncwarp();
+    if (kEnum) {
+      *leaves += __popc(mask);
+    } else if (mask) {
+      *out = __shfl_sync(kFull, nb, __ffs(mask) - 1);
+      return kFound;
+    }
+  }
+}
+
+// Runs one walk.  NLCC: returns kItemSuccess / kItemFail / kItemOverflow.
+// ENUMERATION: counts completed walks into *leaves and returns kItemFail.
+// Either returns kItemTimeout once %globaltimer passes `deadline`.
+template <class W, bool kEnum>
+__device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared& ws, WarpMemo& m, uint32_t source,
+                            unsigned long long* leaves, uint64_t deadline) {
+  const unsigned lane = lane_id();
+  const int n_steps = ws.prog.n_steps;
+  const bool count_memo = kEnum && ws.prog.count_memo;
+  uint32_t iters = 0;
   __syncwarp();
   if (lane == 0) {
     ws.f.bound[0] = source;
@@ -303,9 +490,15 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     if (kEnum) ++*leaves;
     return kEnum ? kItemFail : kItemSuccess;
   }
-  frame_enter<W, kEnum>(g, ws, 1);
+  frame_enter(g, ws, 1);
   int d = 1;
   while (true) {
+    if ((++iters & 1023u) == 0) {
+      uint64_t now = 0;
+      if (lane == 0) now = global_timer_ns();
+      now = __shfl_sync(kFull, now, 0);
+      if (now > deadline) return kItemTimeout;
+    }
     if (d == n_steps) {
       if (!kEnum) return kItemSuccess;
       ++*leaves;
@@ -313,17 +506,49 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       continue;
     }
     const WalkStep s = ws.prog.steps[d];
+    // Returning to a VERTEX step from a counted descent: cache the count of
+    // the subtree just finished.
+    if (count_memo && ws.f.child[d]) {
+      if (!count_store(m, ws.f.bound[d], static_cast<uint32_t>(d), ws, d, *leaves - ws.f.leaves0[d]))
+        return kItemOverflow;
+      __syncwarp();
+      if (lane == 0) ws.f.child[d] = 0;
+      __syncwarp();
+    }
     const uint32_t cur = ws.f.cur[d];
     bool adv = false;
-    if (s.kind == kStepVertex || s.kind == kStepFinal) {
+    if (s.kind == kStepVertex && d + 1 == ws.prog.tail_from && g.sorted_unique && (kEnum || ws.prog.exact)) {
       uint32_t nb = 0;
-      const int r = next_vertex<W, kEnum>(g, st, ws, m, d, s, cur, source, &nb);
+      if (tail_vertex<W, kEnum>(g, st, ws, d, s, &nb, leaves) == kFound) {
+        __syncwarp();
+        if (lane == 0) ws.f.bound[d] = nb;
+        __syncwarp();
+        return kItemSuccess;
+      }
+    } else if (s.kind == kStepVertex || s.kind == kStepFinal) {
+      uint32_t nb = 0;
+      int r;
+      while (true) {
+        r = next_vertex<W, kEnum>(g, st, ws, m, d, s, cur, source, &nb);
+        if (r != kFound || !count_memo || d + 1 >= n_steps) break;
+        // Count memo: a cached subtree adds its count instead of a descent.
+        unsigned long long c = 0;
+        __syncwarp();
+        if (lane == 0) ws.f.bound[d] = nb;
+        __syncwarp();
+        if (!count_lookup(m, nb, static_cast<uint32_t>(d), ws, d, &c)) break;
+        *leaves += c;
+      }
       if (r == kOverflowHit) return kItemOverflow;
       if (r == kFound) {
         __syncwarp();
         if (lane == 0) {
           ws.f.bound[d] = nb;
           ws.f.cur[d + 1] = nb;
+          if (count_memo && d + 1 < n_steps) {
+            ws.f.leaves0[d] = *leaves;
+            ws.f.child[d] = 1;
+          }
         }
         __syncwarp();
         adv = true;
@@ -353,10 +578,13 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       if (d < n_steps) {
         if (ws.prog.steps[d].kind == kStepMove) {
           __syncwarp();
-          if (lane == 0) ws.f.mask[d] = 0;
+          if (lane == 0) {
+            ws.f.mask[d] = 0;
+            ws.f.child[d] = 0;
+          }
           __syncwarp();
         } else {
-          frame_enter<W, kEnum>(g, ws, d);
+          frame_enter(g, ws, d);
         }
       }
     } else {
@@ -374,36 +602,48 @@ __device__ __forceinline__ void load_program(WarpShared& ws, const WalkProgram* 
   __syncwarp();
 }
 
-__device__ __forceinline__ uint32_t next_epoch(WarpMemo& m) {
+__device__ __forceinline__ void next_epoch(WarpMemo& m) {
   ++m.epoch;
   if (m.epoch == 0) {
     // 2^32 walks on this warp: wipe the tables once and restart at 1.
     for (uint32_t i = lane_id(); i < m.edge_cap; i += 32) m.edge[i] = make_uint4(0, 0, 0, 0);
     for (uint64_t i = lane_id(); i < static_cast<uint64_t>(m.hyp_cap) * m.hyp_stride; i += 32) m.hyp[i] = 0;
+    for (uint64_t i = lane_id(); i < static_cast<uint64_t>(m.state_cap) * m.state_stride; i += 32) m.state[i] = 0;
     __syncwarp();
     m.epoch = 1;
   }
   m.edge_n = 0;
   m.hyp_n = 0;
-  return m.epoch;
+  m.state_n = 0;
+}
+
+__device__ __forceinline__ WarpMemo warp_memo(const WalkScratch& sc, uint32_t gw) {
+  WarpMemo m;
+  m.edge = sc.edge_tab + static_cast<uint64_t>(gw) * sc.edge_cap;
+  m.hyp = sc.hyp_tab + static_cast<uint64_t>(gw) * sc.hyp_cap * sc.hyp_stride;
+  m.state = sc.state_tab + static_cast<uint64_t>(gw) * sc.state_cap * sc.state_stride;
+  m.edge_cap = sc.edge_cap;
+  m.hyp_cap = sc.hyp_cap;
+  m.hyp_stride = sc.hyp_stride;
+  m.state_cap = sc.state_cap;
+  m.state_stride = sc.state_stride;
+  m.epoch = sc.epochs[gw];
+  m.edge_n = m.hyp_n = m.state_n = 0;
+  return m;
 }
 
 template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W> st, WalkLaunch w, WalkScratch sc,
-                                                          StepCounters* ctr) {
+                                                          StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
-  WarpMemo m;
-  m.edge = sc.edge_tab + static_cast<uint64_t>(gw) * sc.edge_cap;
-  m.hyp = sc.hyp_tab + static_cast<uint64_t>(gw) * sc.hyp_cap * sc.hyp_stride;
-  m.edge_cap = sc.edge_cap;
-  m.hyp_cap = sc.hyp_cap;
-  m.hyp_stride = sc.hyp_stride;
-  m.epoch = sc.epochs[gw];
-  m.edge_n = m.hyp_n = 0;
+  uint64_t deadline = 0;
+  if (lane == 0) deadline = global_timer_ns() + budget_ns;
+  deadline = __shfl_sync(kFull, deadline, 0);
+  WarpMemo m = warp_memo(sc, gw);
   const uint64_t n_items = w.retry_items ? w.n_retry : static_cast<uint64_t>(w.n_wl) * w.n_progs;
   int cached = -1;
   unsigned long long overflow = 0;
@@ -433,9 +673,13 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
     }
     next_epoch(m);
     unsigned long long unused = 0;
-    const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused);
+    const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline);
     if (lane == 0) w.status[item] = res;
     if (res == kItemOverflow) ++overflow;
+    if (res == kItemTimeout) {
+      if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
+      break;
+    }
     if (res == kItemSuccess && (w.min_marker || w.marks)) {
       // alreadyMatched marks of the successful path (cc :64, pc :42, tds :74).
       uint32_t j = 0;
@@ -522,25 +766,53 @@ __global__ void k_apply_list(DevGraph g, DevState<W> st, const uint32_t* __restr
   if (lane_id() == 0 && newly) atomicAdd(&ctr->modified_total, static_cast<unsigned long long>(newly));
 }
 
+// ENUMERATION over worklist sources (or the `retry` subset).  A source
+// whose count memo overflows contributes nothing and is listed in
+// `overflow` (ctr->aux entries) for a re-run with larger tables.
 template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevState<W> st,
                                                                const WalkProgram* __restrict__ prog,
                                                                const uint32_t* __restrict__ wl, uint32_t n_wl,
-                                                               StepCounters* ctr) {
+                                                               const uint32_t* __restrict__ retry, uint32_t n_retry,
+                                                               uint32_t* overflow, WalkScratch sc, StepCounters* ctr,
+                                                               uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   const unsigned lane = lane_id();
-  WarpShared& ws = s_ws[threadIdx.x >> 5];
+  const unsigned wib = threadIdx.x >> 5;
+  WarpShared& ws = s_ws[wib];
+  const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   load_program(ws, prog);
-  WarpMemo m{};
+  WarpMemo m = warp_memo(sc, gw);
+  uint64_t deadline = 0;
+  if (lane == 0) deadline = global_timer_ns() + budget_ns;
+  deadline = __shfl_sync(kFull, deadline, 0);
+  const uint64_t n = retry ? n_retry : n_wl;
   unsigned long long leaves = 0;
   while (true) {
     unsigned long long gi = 0;
     if (lane == 0) gi = atomicAdd(&ctr->items, 1ull);
     gi = __shfl_sync(kFull, gi, 0);
-    if (gi >= n_wl) break;
-    run_walk<W, true>(g, st, ws, m, wl[gi], &leaves);
+    if (gi >= n) break;
+    const uint32_t src = retry ? retry[gi] : static_cast<uint32_t>(gi);
+    next_epoch(m);
+    const unsigned long long before = leaves;
+    const uint8_t res = run_walk<W, true>(g, st, ws, m, wl[src], &leaves, deadline);
+    if (res == kItemTimeout) {
+      if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
+      break;
+    }
+    if (res == kItemOverflow) {
+      leaves = before;
+      if (lane == 0) {
+        overflow[atomicAdd(&ctr->aux, 1ull)] = src;
+        atomicAdd(&ctr->overflow, 1ull);
+      }
+    }
   }
-  if (lane == 0 && leaves) atomicAdd(&ctr->enumeration, leaves);
+  if (lane == 0) {
+    sc.epochs[gw] = m.epoch;
+    if (leaves) atomicAdd(&ctr->enumeration, leaves);
+  }
 }
 
 template <class W>
@@ -570,8 +842,11 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 
 }  // namespace
 
+void set_walk_budget_ns(uint64_t ns) { g_walk_budget_ns = ns ? ns : 1; }
+uint64_t walk_budget_ns() { return g_walk_budget_ns; }
+
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {
-  uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * 12;
+  uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * 8;
   if (blocks * kWalkWarps > n_warps_available) blocks = n_warps_available / kWalkWarps;
   return blocks ? blocks : 1;
 }
@@ -579,7 +854,8 @@ uint32_t walk_grid_blocks(uint32_t n_warps_available) {
 void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, const WalkScratch& sc,
                  cudaStream_t s) {
   const uint32_t blocks = walk_grid_blocks(sc.n_warps);
-  PM_DISPATCH_WORD(q.word_kind, k_walk<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), w, sc, q.ctr));
+  PM_DISPATCH_WORD(q.word_kind, k_walk<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), w, sc, q.ctr,
+                                                                             g_walk_budget_ns));
 }
 
 void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s) {
@@ -608,10 +884,12 @@ void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const u
 }
 
 void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, cudaStream_t s) {
-  const int blocks = device_sm_count() * 12;
+                      uint32_t n_wl, const uint32_t* retry, uint32_t n_retry, uint32_t* overflow,
+                      const WalkScratch& sc, cudaStream_t s) {
+  const uint32_t blocks = walk_grid_blocks(sc.n_warps);
   PM_DISPATCH_WORD(q.word_kind,
-                   k_enumerate<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), prog, wl, n_wl, q.ctr));
+                   k_enumerate<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), prog, wl, n_wl, retry, n_retry,
+                                                                     overflow, sc, q.ctr, g_walk_budget_ns));
 }
 
 }  // namespace pmgb

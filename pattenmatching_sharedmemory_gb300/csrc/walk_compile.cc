@@ -32,9 +32,9 @@ WalkStep vertex_step(uint8_t role) {
   return s;
 }
 
-// Resolves blockers: a VERTEX step testing value X is blocked by the VERTEX
-// step (index >= 1) whose role is X.
-void finish(WalkProgram& p, const std::vector<int>& test_value) {
+// A VERTEX step testing value X is blocked by the VERTEX step (index >= 1)
+// whose role is X (see walk_program.h).
+void resolve_blockers(WalkProgram& p, const std::vector<int>& test_value) {
   for (int d = 1; d < p.n_steps; ++d) {
     WalkStep& s = p.steps[d];
     if (s.kind != kStepVertex || test_value[d] < 0) continue;
@@ -42,14 +42,88 @@ void finish(WalkProgram& p, const std::vector<int>& test_value) {
       const WalkStep& o = p.steps[t];
       if (o.kind == kStepVertex && o.role == static_cast<uint8_t>(test_value[d])) {
         s.blocker = static_cast<int8_t>(t);
-        p.steps[t].record = 1;
         break;
       }
     }
   }
+}
+
+// Static analysis (see walk_program.h): drops memo tests that can never
+// block, decides exactness, computes state keys and the CHECK-only tail.
+void analyze(WalkProgram& p, const std::vector<label_t>& role_label) {
+  const int n = p.n_steps;
+  auto hist_role = [&](int h) -> int { return h == 0 ? p.start_role : p.steps[p.hist_step[h]].role; };
+  std::vector<int> cur_role(n + 1, -1);
+  cur_role[1] = p.start_role;
+  for (int d = 1; d < n; ++d) {
+    const WalkStep& s = p.steps[d];
+    cur_role[d + 1] = (s.kind == kStepVertex || s.kind == kStepFinal) ? s.role
+                      : s.kind == kStepCheck                          ? cur_role[d]
+                                                                      : hist_role(s.hist);
+  }
+  auto compat = [&](int a, int b) { return a == b || role_label[a] == role_label[b]; };
+  for (int d = 1; d < n; ++d) {
+    WalkStep& s = p.steps[d];
+    if (s.kind != kStepVertex || s.blocker < 0) continue;
+    // The test at d (current role A -> candidate role B) is blocked only by
+    // a traversal at step t (current role X -> bound role Y) of the same
+    // undirected edge: {A-vertex, B-vertex} = {X-vertex, Y-vertex}.
+    const int t = s.blocker;
+    const int A = cur_role[d], B = s.role, X = cur_role[t], Y = p.steps[t].role;
+    const bool possible = (compat(A, X) && compat(B, Y)) || (compat(A, Y) && compat(B, X));
+    if (!possible) s.blocker = -1;
+  }
+  for (int t = 1; t < n; ++t) p.steps[t].record = 0;
   p.any_memo = 0;
-  for (int d = 1; d < p.n_steps; ++d)
+  for (int d = 1; d < n; ++d) {
+    if (p.steps[d].blocker >= 0) p.steps[p.steps[d].blocker].record = 1;
     if (p.steps[d].blocker >= 0 || p.steps[d].hyp) p.any_memo = 1;
+  }
+  // History entries read after step d that were bound before it.
+  std::vector<uint64_t> refs(n + 1, 0);
+  for (int d = 1; d < n; ++d)
+    for (int j = d + 1; j < n; ++j) {
+      const WalkStep& s = p.steps[j];
+      if (s.kind != kStepCheck && s.kind != kStepMove) continue;
+      const int h = s.hist;
+      if (h > 0 && p.hist_step[h] < d) refs[d] |= uint64_t(1) << h;
+    }
+  bool exact = p.family != kFamilyEnum;
+  for (int d = 1; d < n && exact; ++d) {
+    const WalkStep& s = p.steps[d];
+    if (s.kind == kStepVertex && s.blocker >= 0) exact = false;
+    if (s.kind == kStepVertex && s.hyp) {
+      for (int h = 1; h < p.n_hist; ++h)
+        if ((refs[d] >> h & 1) && !p.steps[p.hist_step[h]].store) exact = false;
+    }
+  }
+  p.exact = exact ? 1 : 0;
+  // State key: the history entries the subtree reads, plus (for programs
+  // that keep the reference's hypothesis memo) every stored vertex so far.
+  p.max_refs = 0;
+  for (int d = 1; d < n; ++d) {
+    uint64_t key = 0;
+    if (p.steps[d].kind == kStepVertex) {
+      key = refs[d];
+      if (!exact)
+        for (int h = 1; h < p.n_hist; ++h)
+          if (p.hist_step[h] < d && p.steps[p.hist_step[h]].store) key |= uint64_t(1) << h;
+    }
+    p.state_refs[d] = key;
+    const int c = __builtin_popcountll(key);
+    if (c > p.max_refs) p.max_refs = static_cast<uint8_t>(c);
+  }
+  bool distinct = true;
+  for (size_t a = 0; a < role_label.size() && distinct; ++a)
+    for (size_t b = a + 1; b < role_label.size(); ++b)
+      if (role_label[a] == role_label[b]) {
+        distinct = false;
+        break;
+      }
+  p.count_memo = (p.family == kFamilyEnum && distinct) ? 1 : 0;
+  int tail = n;
+  while (tail - 1 >= 1 && p.steps[tail - 1].kind == kStepCheck) --tail;
+  p.tail_from = static_cast<uint8_t>(tail);
 }
 
 void add_history(WalkProgram& p, int step) { p.hist_step[p.n_hist++] = static_cast<uint8_t>(step); }
@@ -59,6 +133,9 @@ void finalize(CompiledConstraint& cc) {
   cc.start_mask = 0;
   cc.marks_per_success = 0;
   cc.any_memo = false;
+  cc.exact = true;
+  cc.max_state_words = 0;
+  cc.max_hyp_words = 0;
   for (size_t i = 0; i < cc.programs.size(); ++i) {
     const WalkProgram& p = cc.programs[i];
     cc.role_index[p.start_role] = static_cast<uint8_t>(i);
@@ -67,12 +144,15 @@ void finalize(CompiledConstraint& cc) {
     for (int d = 1; d < p.n_steps; ++d) marks += p.steps[d].mark;
     if (marks > cc.marks_per_success) cc.marks_per_success = marks;
     cc.any_memo = cc.any_memo || p.any_memo;
+    cc.exact = cc.exact && p.exact;
+    if (p.max_refs > cc.max_state_words) cc.max_state_words = p.max_refs;
+    if (!p.exact && p.n_store > cc.max_hyp_words) cc.max_hyp_words = p.n_store;
   }
 }
 
 }  // namespace
 
-CompiledConstraint compile_cycle(const CycleConstraint& c) {
+CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label) {
   CompiledConstraint cc;
   cc.family = kFamilyCC;
   const int L = static_cast<int>(c.length());
@@ -93,14 +173,15 @@ CompiledConstraint compile_cycle(const CycleConstraint& c) {
     close.hist = 0;
     close.blocker = -1;
     p.steps[L] = close;
-    finish(p, test);
+    resolve_blockers(p, test);
+    analyze(p, role_label);
     cc.programs.push_back(p);
   }
   finalize(cc);
   return cc;
 }
 
-CompiledConstraint compile_path(const PathConstraint& pc) {
+CompiledConstraint compile_path(const PathConstraint& pc, const std::vector<label_t>& role_label) {
   CompiledConstraint cc;
   cc.family = kFamilyPC;
   const int L = static_cast<int>(pc.length());
@@ -121,7 +202,8 @@ CompiledConstraint compile_path(const PathConstraint& pc) {
     fin.mark = 1;
     p.steps[L - 1] = fin;
     add_history(p, L - 1);
-    finish(p, test);
+    resolve_blockers(p, test);
+    analyze(p, role_label);
     cc.programs.push_back(p);
   }
   finalize(cc);
@@ -129,7 +211,8 @@ CompiledConstraint compile_path(const PathConstraint& pc) {
 }
 
 namespace {
-WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family) {
+WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family,
+                              const std::vector<label_t>& role_label) {
   WalkProgram p = empty_program(family, static_cast<uint8_t>(start_role));
   const int n = static_cast<int>(w.length());
   check_length(n);
@@ -157,25 +240,28 @@ WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family
       p.steps[d] = s;
     }
   }
-  if (family == kFamilyTDS) finish(p, test);
+  if (family == kFamilyTDS) resolve_blockers(p, test);
+  analyze(p, role_label);
   return p;
 }
 }  // namespace
 
-CompiledConstraint compile_template(const TemplateConstraint& t) {
+CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label) {
   CompiledConstraint cc;
   cc.family = kFamilyTDS;
-  for (const auto& kv : t.walks) cc.programs.push_back(program_from_walk(kv.second, kv.first, kFamilyTDS));
+  for (const auto& kv : t.walks)
+    cc.programs.push_back(program_from_walk(kv.second, kv.first, kFamilyTDS, role_label));
   finalize(cc);
   return cc;
 }
 
-CompiledConstraint compile_enumeration(const TemplateConstraint& t) {
+CompiledConstraint compile_enumeration(const TemplateConstraint& t, const std::vector<label_t>& role_label) {
   CompiledConstraint cc;
   cc.family = kFamilyEnum;
   auto first = t.walks.cbegin();
-  cc.programs.push_back(program_from_walk(first->second, first->first, kFamilyEnum));
+  cc.programs.push_back(program_from_walk(first->second, first->first, kFamilyEnum, role_label));
   finalize(cc);
+  cc.exact = false;
   return cc;
 }
 

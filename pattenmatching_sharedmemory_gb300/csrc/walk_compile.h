@@ -1,4 +1,5 @@
 // Compiles CC / PC / TDS / enumeration constraints into WalkPrograms.
+// role_label[p] is the label of template vertex p (for the memo analysis).
 #pragma once
 #include <vector>
 
@@ -14,15 +15,18 @@ struct CompiledConstraint {
   uint8_t role_index[64];             // role -> program index (0xFF: not a start role)
   int marks_per_success = 0;          // marking steps of the longest program
   bool any_memo = false;
+  bool exact = false;                 // every program exact (see walk_program.h)
+  uint32_t max_state_words = 0;       // key words of the state / count memo
+  uint32_t max_hyp_words = 0;         // key words of the reference's hypothesis memo
 };
 
 // CC: one program per cycle position (multiple_label_cc_cpu.tpp:94-129).
-CompiledConstraint compile_cycle(const CycleConstraint& c);
+CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label);
 // PC: forward from ids[0], then backward from ids[L-1] (pc :104-142).
-CompiledConstraint compile_path(const PathConstraint& p);
+CompiledConstraint compile_path(const PathConstraint& p, const std::vector<label_t>& role_label);
 // TDS: one program per walkMap entry, in walkMap order (tds :153-195).
-CompiledConstraint compile_template(const TemplateConstraint& t);
+CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label);
 // ENUMERATION: the first walkMap entry (enumeration :133-135).
-CompiledConstraint compile_enumeration(const TemplateConstraint& t);
+CompiledConstraint compile_enumeration(const TemplateConstraint& t, const std::vector<label_t>& role_label);
 
 }  // namespace pmgb

@@ -54,6 +54,32 @@ struct WalkStep {
   uint8_t mark;     // success marks (bound vertex, role) — alreadyMatched
 };
 
+// Exact programs.  When no memo test of a program can ever block a hop (the
+// two roles involved in every possible block carry different labels, so no
+// vertex can hold both) and every TDS hypothesis memo keys on all history
+// entries its subtree reads, the reference's walk returns exactly whether a
+// valid walk exists: its memos only skip subtrees that already failed.  For
+// such programs the walker may prune any revisited state (neighbour, step,
+// values of the earlier history entries read later — `state_refs`), which
+// turns the exponential walk into a search over distinct states with the
+// same outcome, and no alreadyMatched rescue can occur (a vertex on a
+// successful walk has a valid walk itself).
+//
+// State memo (every CC/PC/TDS program).  The subtree below a hop depends only
+// on the bound neighbour, the step, the earlier history entries it reads
+// and — for the reference's hypothesis memo — the stored vertices bound so
+// far; the memos only ever block, so a second visit of the same state can
+// neither succeed where the first failed nor insert memo entries the first
+// did not.  The walker therefore skips revisits of a state keyed by
+// (neighbour, step, values of the history entries in state_refs[d]) after
+// doing the reference's own memo tests and inserts: same outcome, same memo
+// contents, polynomial instead of exponential work.  The table is
+// best-effort: when it fills up the walker stops inserting.
+//
+// Count memo (ENUMERATION of templates whose labels are pairwise distinct):
+// no vertex can hold two roles, so the embeddings are injective by
+// construction and the number of completions below a hop depends only on the
+// same state; it is memoized per source.
 struct WalkProgram {
   uint16_t n_steps;      // steps[1 .. n_steps-1]; step n_steps = success
   uint8_t start_role;
@@ -61,9 +87,15 @@ struct WalkProgram {
   uint8_t n_hist;        // history entries (source + VERTEX/FINAL steps)
   uint8_t n_store;       // store steps
   uint8_t any_memo;      // some step has blocker >= 0 or hyp
-  uint8_t pad;
+  uint8_t exact;         // see above
+  uint8_t max_refs;      // largest popcount of state_refs
+  uint8_t tail_from;     // first step of the trailing CHECK-only suffix
+  uint8_t count_memo;    // ENUMERATION: subtree counts may be memoized
+  uint8_t pad[5];
   uint8_t hist_step[kMaxWalkSteps];   // history index -> step index
   uint8_t store_step[kMaxWalkSteps];  // i-th store step
+  uint64_t state_refs[kMaxWalkSteps]; // history indices (>0) keyed by the
+                                      // state / count memo at step d
   WalkStep steps[kMaxWalkSteps];
 };
 
