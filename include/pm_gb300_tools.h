@@ -38,6 +38,14 @@ pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const
 /* Number of visible CUDA devices (0 when none or the driver is missing). */
 int32_t pm_device_count(void);
 
+/* Kernel launches issued by this library since the process started. */
+uint64_t pm_kernel_launches(void);
+
+/* Device time of the query so far: from the start of its first step to the
+ * end of its latest step, measured with CUDA events on the query's stream
+ * (host gaps between steps included). */
+pm_status_t pm_query_elapsed_ms(const pm_query* q, double* ms);
+
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with
  * PM_E_TIMEOUT and the query's state is no longer meaningful. */
@@ -48,6 +56,11 @@ pm_status_t pm_set_walk_budget_ms(double ms);
 pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32_t* p_adj, const uint64_t* p_labels,
                                          uint32_t p_vertex_count, uint64_t p_edge_count, char* buf, size_t cap,
                                          size_t* needed);
+
+/* Walker work of result row `row` (0-based, as returned by pm_query_run):
+ * CSR entries tested and hops taken by the CC/PC/TDS or ENUMERATION
+ * kernels of that step (0 for LCC0/LCC). */
+pm_status_t pm_query_step_walk_stats(const pm_query* q, int32_t row, uint64_t* scanned, uint64_t* descents);
 
 /* Number of NLCC steps that needed the exact sequential emulation of the
  * reference's alreadyMatched shortcut, and of memo-table overflow retries. */

@@ -78,8 +78,10 @@ class OracleResult:
 
 
 def run(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, stop_before_enumeration: bool = False,
-        enum_vertex_limit: int = 0) -> OracleResult:
-    """Runs the restated pipeline; threads=1 is the canonical sequential order."""
+        sample_stride: int = 1) -> OracleResult:
+    """Runs the restated pipeline; threads=1 is the canonical sequential order.
+    sample_stride > 1 is a timing sample (CC/PC/TDS/ENUMERATION visit only
+    sources with id % stride == 0); its results are not the pipeline's."""
     lib = _load()
     off = np.ascontiguousarray(offsets, np.uint64)
     ad = np.ascontiguousarray(adj, np.uint32)
@@ -96,7 +98,7 @@ def run(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, stop
     vact = np.zeros(V, np.uint8)
     st = lib.pmo_run(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), V, E,
                      _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k, threads,
-                     int(stop_before_enumeration), enum_vertex_limit, recs, cap, ctypes.byref(n),
+                     int(stop_before_enumeration), sample_stride, recs, cap, ctypes.byref(n),
                      _p(cand, ctypes.c_uint64), _p(eact, ctypes.c_uint8), _p(vact, ctypes.c_uint8))
     if st != 0:
         raise RuntimeError(f"oracle failed with status {st}")

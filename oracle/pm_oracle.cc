@@ -56,6 +56,8 @@ struct State {
   std::vector<uint64_t> cand, matched, unmatch;
   uint64_t active_vertices, active_edges;
   bool parallel;
+  int64_t sample_stride = 1;  // timing samples: NLCC / ENUMERATION sources v % stride == 0
+  bool sampled(int64_t v) const { return sample_stride <= 1 || v % sample_stride == 0; }
   void mark_matched(uint32_t v, uint32_t p) {
     if (parallel)
       __atomic_fetch_or(&matched[v], uint64_t(1) << p, __ATOMIC_RELAXED);
@@ -250,7 +252,7 @@ Results step_cc(State& s, const CycleConstraint& c) {
 #pragma omp parallel for private(memo) if (s.parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v]) continue;
+    if (!s.active[v] || !s.sampled(vi)) continue;
     bool changed = false;
     for (size_t pos = 0; pos < c.length(); ++pos) {
       uint32_t role = c.ids[pos];
@@ -310,7 +312,7 @@ Results step_pc(State& s, const PathConstraint& pc) {
 #pragma omp parallel for private(memo) if (s.parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v]) continue;
+    if (!s.active[v] || !s.sampled(vi)) continue;
     if (s.lab[v] != pc.initial_label) continue;
     bool changed = false;
     for (int end = 0; end < 2; ++end) {
@@ -398,7 +400,7 @@ Results step_tds(State& s, const TemplateConstraint& t) {
 #pragma omp parallel for private(m) if (s.parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v]) continue;
+    if (!s.active[v] || !s.sampled(vi)) continue;
     bool changed = false;
     for (const auto& kv : t.walks) {
       uint32_t role = kv.first;
@@ -460,18 +462,17 @@ uint64_t enum_walk(const State& s, const Walk& w, std::vector<uint32_t>& history
 }
 
 // ENUMERATION step (multiple_label_enumeration_cpu.tpp:126-174).
-Results step_enumeration(State& s, const TemplateConstraint& t, int64_t vertex_limit) {
+Results step_enumeration(State& s, const TemplateConstraint& t) {
   Results r;
   auto first = t.walks.cbegin();
   const uint32_t start_role = first->first;
   const Walk& w = first->second;
   uint64_t total = 0;
-  const int64_t limit = vertex_limit > 0 && vertex_limit < s.V ? vertex_limit : s.V;
   std::vector<uint32_t> history;
 #pragma omp parallel for reduction(+ : total) private(history) schedule(dynamic, 1000) if (s.parallel)
-  for (int64_t vi = 0; vi < limit; ++vi) {
+  for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v]) continue;
+    if (!s.active[v] || !s.sampled(vi)) continue;
     if (!s.has(v, start_role)) continue;
     history.clear();
     history.push_back(v);
@@ -491,14 +492,16 @@ extern "C" {
 //   threads      1 = canonical sequential order; >1 OpenMP like the reference.
 //   stop_before_enumeration  1 = end the run when the schedule reaches
 //                ENUMERATION (pruning-only timing).
-//   enum_vertex_limit  >0 = enumerate only from sources below this id
+//   sample_stride  >1 = timing sample: CC/PC/TDS/ENUMERATION visit only
+//                sources with id % sample_stride == 0 (results then differ
+//                from the full run; used to bound CPU-baseline timing)
 //                (bounded CPU-baseline samples); 0 = all.
 // Outputs (any may be NULL): step records (as pm_step_record), final role
 // sets, per-CSR-entry and per-vertex active flags, the matched count.
 // Returns 0, or a negative status on bad input.
 int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
             const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k, int threads,
-            int stop_before_enumeration, int64_t enum_vertex_limit, pm_step_record* records, int32_t cap,
+            int stop_before_enumeration, int64_t sample_stride, pm_step_record* records, int32_t cap,
             int32_t* n_records, uint64_t* cand_out, uint8_t* edge_active_out, uint8_t* vertex_active_out) {
   try {
     PatternGraph pg;
@@ -515,6 +518,7 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
     s.E = E;
     s.k = k;
     s.parallel = threads > 1;
+    s.sample_stride = sample_stride;
     if (threads >= 1) omp_set_num_threads(threads);
     s.active.assign(V, 1);
     s.modified.assign(V, 0);
@@ -584,7 +588,7 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
         // iterator (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and
         // pc :186), so every TDS step checks template constraint 0.
         case TDS: res = step_tds(s, qc.templates[0]); break;
-        case ENUM: res = step_enumeration(s, qc.enumeration, enum_vertex_limit); break;
+        case ENUM: res = step_enumeration(s, qc.enumeration); break;
         default: res = Results(); break;
       }
       double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

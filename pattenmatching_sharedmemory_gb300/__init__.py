@@ -105,7 +105,10 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_device_bytes": (ctypes.c_int32, [ctypes.c_void_p, c_u64p]),
         "pm_query_estimate_bytes": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, c_u64p]),
         "pm_query_stats": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u64p]),
+        "pm_query_step_walk_stats": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, c_u64p, c_u64p]),
         "pm_device_count": (ctypes.c_int32, []),
+        "pm_kernel_launches": (ctypes.c_uint64, []),
+        "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
                                                           ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
@@ -344,6 +347,19 @@ class Query:
         a, b = ctypes.c_uint64(), ctypes.c_uint64()
         _check(lib.pm_query_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
         return {"exact_resolutions": a.value, "overflow_retries": b.value}
+
+    @property
+    def elapsed_ms(self) -> float:
+        """Device time from the start of the first step to the end of the latest."""
+        ms = ctypes.c_double()
+        _check(lib.pm_query_elapsed_ms(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def step_walk_stats(self, row: int):
+        """(CSR entries tested, hops taken) by the walkers of result row `row`."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib.pm_query_step_walk_stats(self._h, row, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def close(self) -> None:
         if self._h:

@@ -293,6 +293,16 @@ pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count, 
   return PM_SUCCESS;
 }
 
+uint64_t pm_kernel_launches(void) { return launch_count(); }
+
+pm_status_t pm_query_elapsed_ms(const pm_query* q, double* ms) {
+  PM_REQUIRE(q && ms, "null argument");
+  return guarded([&]() -> pm_status_t {
+    *ms = const_cast<QueryImpl&>(q->impl).elapsed_ms();
+    return PM_SUCCESS;
+  });
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));
@@ -330,6 +340,14 @@ pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32
     }
     return PM_SUCCESS;
   });
+}
+
+pm_status_t pm_query_step_walk_stats(const pm_query* q, int32_t row, uint64_t* scanned, uint64_t* descents) {
+  PM_REQUIRE(q, "query is NULL");
+  PM_REQUIRE(row >= 0 && static_cast<size_t>(row) < q->impl.walk_stats.size(), "row out of range");
+  if (scanned) *scanned = q->impl.walk_stats[row].first;
+  if (descents) *descents = q->impl.walk_stats[row].second;
+  return PM_SUCCESS;
 }
 
 pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries) {

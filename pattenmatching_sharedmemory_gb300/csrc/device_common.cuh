@@ -105,10 +105,12 @@ struct StepCounters {
   unsigned long long items;      // work counter for persistent kernels
   unsigned long long error;      // device-side error status (0 = ok)
   unsigned long long aux;        // list fill counter (overflow retry list)
+  unsigned long long scanned;    // walkers: CSR entries tested
+  unsigned long long descents;   // walkers: hops taken (states entered)
   unsigned long long modified_total;  // vertices with mod=1 since the last reset
-  unsigned long long pad[6];
+  unsigned long long pad[4];
 };
-constexpr int kStepCounterWords = 9;
+constexpr int kStepCounterWords = 11;
 
 // Per-query tables derived from the local constraints
 // (multiple_label_constraint_local.h:18-32), in label-slot space.

@@ -160,6 +160,7 @@ QueryImpl::~QueryImpl() {
   if (h_count) cudaFreeHost(h_count);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (ev_first) cudaEventDestroy(ev_first);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -220,6 +221,7 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) 
   }
   PM_CUDA(cudaEventCreate(&ev0));
   PM_CUDA(cudaEventCreate(&ev1));
+  PM_CUDA(cudaEventCreate(&ev_first));
   PM_CUDA(cudaMallocHost(&h_ctr, sizeof(StepCounters)));
   PM_CUDA(cudaMallocHost(&h_count, sizeof(uint32_t)));
 
@@ -328,6 +330,17 @@ constexpr uint32_t kEdgeCap = 1024, kHypCap = 1024, kStateCap = 2048;
 void zero_field(void* base, size_t offset, cudaStream_t s) {
   PM_CUDA(cudaMemsetAsync(static_cast<char*>(base) + offset, 0, sizeof(unsigned long long), s));
 }
+// Warps of retry round r (tables 8^r times larger): as many as fit a 6 GB
+// scratch budget, at most half of the previous round's.
+uint32_t retry_warps(uint32_t base_warps, int round, uint32_t hyp_stride, uint32_t state_stride) {
+  const uint64_t per_warp = (uint64_t(16) * (1024ull << (3 * round))) + 4ull * hyp_stride * (1024ull << (3 * round)) +
+                            4ull * state_stride * (2048ull << (3 * round));
+  const uint64_t budget = 6ull << 30;
+  uint64_t w = std::min<uint64_t>(base_warps >> round, budget / per_warp);
+  w = std::max<uint64_t>(w, 32);
+  return static_cast<uint32_t>(w / kWalkWarpsPerBlock * kWalkWarpsPerBlock);
+}
+
 uint32_t max_hyp_words(const std::vector<DeviceConstraint>& v) {
   uint32_t m = 0;
   for (const auto& dc : v) m = std::max<uint32_t>(m, dc.cc.max_hyp_words);
@@ -395,7 +408,7 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
     launch_collect_overflow(w, d_list.as<uint32_t>(), d_ctr.as<StepCounters>(), stream);
     read_counters();
     const uint32_t n_retry = static_cast<uint32_t>(h_ctr->aux);
-    const uint32_t warps = std::max<uint32_t>(kWalkWarpsPerBlock * 8, base_warps >> (3 * round));
+    const uint32_t warps = retry_warps(base_warps, round, hyp_stride, state_stride);
     big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, kStateCap << (3 * round),
                     state_stride, stream);
     WalkLaunch r = w;
@@ -521,7 +534,7 @@ StepResult QueryImpl::step_enumeration() {
     for (int round = 1; n_over; ++round) {
       ++overflow_retries;
       if (round > 6) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
-      const uint32_t warps = std::max<uint32_t>(kWalkWarpsPerBlock * 8, base_warps >> (3 * round));
+      const uint32_t warps = retry_warps(base_warps, round, hs, ss);
       big_pool.ensure(warps, kEdgeCap, kHypCap, hs, kStateCap << (3 * round), ss, stream);
       zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
       zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
@@ -563,6 +576,10 @@ pm_step_record QueryImpl::run_step() {
   if (kind == PM_STEP_CC || kind == PM_STEP_PC || kind == PM_STEP_TDS) reset_modified();
   clear_step_counters();
   PM_CUDA(cudaEventRecord(ev0, stream));
+  if (!first_recorded) {
+    PM_CUDA(cudaEventRecord(ev_first, stream));
+    first_recorded = true;
+  }
   StepResult r;
   switch (kind) {
     case PM_STEP_LCC0: r = step_lcc0(); break;
@@ -599,11 +616,20 @@ pm_step_record QueryImpl::run_step() {
   rec.active_edge = active_edges;
   rec.total_edge = g->host.edge_count;
   records.push_back(rec);
+  walk_stats.emplace_back(h_ctr->scanned, h_ctr->descents);
   step = advance(kind);
   if (kind == PM_STEP_ENUMERATION) finished = true;
   ++iteration;
   if (iteration >= 1000) finished = true;
   return rec;
+}
+
+double QueryImpl::elapsed_ms() {
+  if (!first_recorded) return 0.0;
+  PM_CUDA(cudaEventSynchronize(ev1));
+  float ms = 0;
+  PM_CUDA(cudaEventElapsedTime(&ms, ev_first, ev1));
+  return ms;
 }
 
 pm_step_record QueryImpl::final_record() {

@@ -104,10 +104,14 @@ struct QueryImpl {
   double total_ms = 0;
   uint64_t match_count = 0;
   std::vector<pm_step_record> records;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_first = nullptr;
+  bool first_recorded = false;
+  double elapsed_ms();
 
   // statistics of the alreadyMatched emulation
   uint64_t exact_resolutions = 0, overflow_retries = 0;
+  // per step: walker CSR entries tested and hops taken (0 for LCC steps)
+  std::vector<std::pair<uint64_t, uint64_t>> walk_stats;
 
   ~QueryImpl();
   void create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s);

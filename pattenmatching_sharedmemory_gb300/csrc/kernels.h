@@ -29,6 +29,10 @@ struct QueryDevPtrs {
 // Launch geometry shared by all kernels (SM count of the current device).
 int device_sm_count();
 
+// Process-wide count of kernel launches issued by this library.
+void note_launch();
+uint64_t launch_count();
+
 // State initialisation: every vertex holds all k roles and its label slot,
 // every CSR entry is active, every vertex scheduled, nothing modified
 // (MultipleLabelGlobalState::allocate, multiple_label_common_cpu.tpp:30-66).

@@ -11,6 +11,8 @@
 // multiple_label_lcc_cpu.tpp:26-101); sweep 2 is a separate launch.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "kernels.h"
 
 namespace pmgb {
@@ -21,6 +23,7 @@ constexpr int kWarpsPerBlock = kThreads / 32;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
 int g_sm_count = 0;
+std::atomic<uint64_t> g_launches{0};
 
 inline int grid_for_tiles(uint64_t V, int blocks_per_sm) {
   uint64_t tiles = (V + 31) / 32;
@@ -368,6 +371,7 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 }
 
 #define PM_DISPATCH_WORD(kind, ...)            \
+  note_launch();                               \
   switch (kind) {                              \
     case kWord16: {                            \
       using W = uint16_t;                      \
@@ -388,6 +392,9 @@ DevState<W> state_of(const QueryDevPtrs& q) {
   }
 
 }  // namespace
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sm_count() {
   if (g_sm_count == 0) {
@@ -427,6 +434,7 @@ void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, ui
     return;
   }
   PM_DISPATCH_WORD(q.word_kind, k_wl_count<W><<<blocks, 256, 0, s>>>(g, state_of<W>(q), mask, block_counts));
+  note_launch();
   k_wl_scan<<<1, 1024, 0, s>>>(block_counts, blocks, count);
   PM_DISPATCH_WORD(q.word_kind,
                    k_wl_write<W><<<blocks, 256, 0, s>>>(g, state_of<W>(q), mask, block_counts, wl, wl_index));

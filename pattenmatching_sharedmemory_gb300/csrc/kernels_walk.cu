@@ -50,6 +50,8 @@ struct WalkFrames {
 struct WarpShared {
   WalkProgram prog;
   WalkFrames f;
+  unsigned long long scanned;   // CSR entries tested by this warp (lane 0 writes)
+  unsigned long long descents;  // hops taken by this warp
 };
 
 enum : int { kNone = 0, kFound = 1, kOverflowHit = 2 };
@@ -331,6 +333,7 @@ __device__ bool load_chunk(const DevGraph& g, const DevState<W>& st, WarpShared&
     ws.f.chunk[d] = next;
     ws.f.next[d] = next + cnt;
     ws.f.mask[d] = mask;
+    ws.scanned += cnt;
   }
   __syncwarp();
   return true;
@@ -459,7 +462,10 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
     }
     const unsigned mask = __ballot_sync(kFull, ok);
     __syncwarp();
-    if (lane == 0) ws.f.next[d] = next + cnt;
+    if (lane == 0) {
+      ws.f.next[d] = next + cnt;
+      ws.scanned += cnt;
+    }
     __syncwarp();
     if (kEnum) {
       *leaves += __popc(mask);
@@ -575,6 +581,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     }
     if (adv) {
       ++d;
+      if (lane == 0) ws.descents += 1;
       if (d < n_steps) {
         if (ws.prog.steps[d].kind == kStepMove) {
           __syncwarp();
@@ -639,6 +646,11 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
+  if (lane == 0) {
+    ws.scanned = 0;
+    ws.descents = 0;
+  }
+  __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   uint64_t deadline = 0;
   if (lane == 0) deadline = global_timer_ns() + budget_ns;
@@ -705,6 +717,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
   }
   if (lane == 0) {
     sc.epochs[gw] = m.epoch;
+    atomicAdd(&ctr->scanned, ws.scanned);
+    atomicAdd(&ctr->descents, ws.descents);
     if (overflow) atomicAdd(&ctr->overflow, overflow);
   }
 }
@@ -780,6 +794,11 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
+  if (lane == 0) {
+    ws.scanned = 0;
+    ws.descents = 0;
+  }
+  __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   load_program(ws, prog);
   WarpMemo m = warp_memo(sc, gw);
@@ -811,6 +830,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
   }
   if (lane == 0) {
     sc.epochs[gw] = m.epoch;
+    atomicAdd(&ctr->scanned, ws.scanned);
+    atomicAdd(&ctr->descents, ws.descents);
     if (leaves) atomicAdd(&ctr->enumeration, leaves);
   }
 }
@@ -821,6 +842,7 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 }
 
 #define PM_DISPATCH_WORD(kind, ...) \
+  note_launch();                    \
   switch (kind) {                   \
     case kWord16: {                 \
       using W = uint16_t;           \
@@ -861,12 +883,14 @@ void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, 
 void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s) {
   const uint64_t n = static_cast<uint64_t>(w.n_wl) * w.n_progs;
   const int grid = device_sm_count() * 4;
+  note_launch();
   k_flag_rescue<<<grid, 256, 0, s>>>(w.status, w.min_marker, n, ctr);
 }
 
 void launch_collect_overflow(const WalkLaunch& w, uint32_t* list, StepCounters* ctr, cudaStream_t s) {
   const uint64_t n = static_cast<uint64_t>(w.n_wl) * w.n_progs;
   const int grid = device_sm_count() * 4;
+  note_launch();
   k_collect_overflow<<<grid, 256, 0, s>>>(w.status, n, list, ctr);
 }
 
