@@ -180,6 +180,43 @@ pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count,
 
 void pm_query_destroy(pm_query* q);
 
+/* Allocation-free ENUMERATION.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory (code running inside a host
+ * framework that owns every device allocation through its own pool or arena,
+ * or a latency-critical path that must not reach the driver's allocator).
+ *
+ * Counts the injective embeddings of the template (p_*, CSR, 1 to 56
+ * vertices) in a pruned state the caller holds in device memory: the graph
+ * CSR (d_offsets[vertex_count + 1], d_adj[edge_count]), the candidate role
+ * mask of every vertex (d_cand_masks[vertex_count], bit p = template vertex
+ * p, as pm_query_export returns it) and the active flag of every CSR entry
+ * as bits (d_edge_active_bits[(edge_count + 31) / 32], bit e % 32 of word
+ * e / 32).  sorted_unique != 0 promises strictly increasing adjacency lists.
+ * The count is written to d_count (one device uint64_t); the call returns
+ * after `stream` (a cudaStream_t, NULL = default stream) has finished it.
+ *
+ * It calls no cudaMalloc, cudaFree or allocating library routine: the
+ * walker's tables, counters and retry bitmaps live in one file-scope 64 MiB
+ * __device__ array that every GPU loading this library holds until the
+ * process exits.  The first call on a device (with that device current)
+ * resolves the array's address with cudaGetSymbolAddress; make that first
+ * call before any stream capture begins.  Every call reuses the array and
+ * clears what must start at zero; calls that overlap on the GPU (other
+ * streams or host threads at the same time) race on it and must be
+ * serialised by the caller.
+ *
+ * Limits: vertex_count <= 67108864 (PM_E_INVALID_ARG beyond), template of
+ * at most 56 vertices (PM_E_PATTERN_TOO_LARGE), PM_E_OOM when one source's
+ * count memo outgrows the array, PM_E_TIMEOUT past pm_set_walk_budget_ms. */
+pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_adj,
+                                 uint32_t vertex_count, uint64_t edge_count,
+                                 int sorted_unique, const uint64_t* d_cand_masks,
+                                 const uint32_t* d_edge_active_bits,
+                                 const uint64_t* p_offsets, const uint32_t* p_adj,
+                                 const uint64_t* p_labels, uint32_t p_vertex_count,
+                                 uint64_t p_edge_count, uint64_t* d_count,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif

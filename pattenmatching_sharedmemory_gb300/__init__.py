@@ -113,6 +113,11 @@ def _load_library() -> ctypes.CDLL:
         "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
                                                           ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
         "pm_query_destroy": (None, [ctypes.c_void_p]),
+        # Device buffers (d_*) and the stream are passed as raw addresses.
+        "pm_enumerate_noalloc": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                                  ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                  c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
+                                                  ctypes.c_void_p, ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -359,4 +359,38 @@ pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint6
 
 void pm_query_destroy(pm_query* q) { delete q; }
 
+pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_adj, uint32_t vertex_count,
+                                 uint64_t edge_count, int sorted_unique, const uint64_t* d_cand_masks,
+                                 const uint32_t* d_edge_active_bits, const uint64_t* p_offsets,
+                                 const uint32_t* p_adj, const uint64_t* p_labels, uint32_t p_vertex_count,
+                                 uint64_t p_edge_count, uint64_t* d_count, void* stream) {
+  PM_REQUIRE(d_offsets && d_cand_masks && d_count && p_offsets, "null argument");
+  PM_REQUIRE((d_adj && d_edge_active_bits) || edge_count == 0, "null adjacency or edge-active buffer");
+  PM_REQUIRE(p_adj || p_edge_count == 0, "null pattern adjacency");
+  if (vertex_count > noalloc_max_vertices())
+    return fail(PM_E_INVALID_ARG,
+                "pm_enumerate_noalloc: graph of " + std::to_string(vertex_count) +
+                    " vertices exceeds the maximum of 67108864 (fixed 64 MiB scratch); use pm_query_run");
+  if (p_vertex_count == 0 || p_vertex_count > 56)
+    return fail(PM_E_PATTERN_TOO_LARGE, "pm_enumerate_noalloc: template of " + std::to_string(p_vertex_count) +
+                                            " vertices; 1 to 56 supported (56-bit role masks)");
+  PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
+  for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
+  return guarded([&]() -> pm_status_t {
+    PatternGraph p;
+    p.n = p_vertex_count;
+    p.offsets.assign(p_offsets, p_offsets + p_vertex_count + 1);
+    p.adj.assign(p_adj, p_adj + p_edge_count);
+    p.labels = p_labels ? std::vector<uint64_t>(p_labels, p_labels + p_vertex_count)
+                        : std::vector<uint64_t>(p_vertex_count, 0);
+    const QueryConstraints qc = compile_constraints(p);
+    const CompiledConstraint cc = compile_enumeration(qc.enumeration, p.labels);
+    PM_REQUIRE(!cc.programs.empty(), "template has no enumeration walk");
+    const DevGraph g{vertex_count, edge_count, d_offsets, d_adj, nullptr, sorted_unique ? 1 : 0};
+    enumerate_noalloc(g, d_cand_masks, d_edge_active_bits, cc.programs[0], cc.max_state_words, d_count,
+                      static_cast<cudaStream_t>(stream));
+    return PM_SUCCESS;
+  });
+}
+
 }  // extern "C"

@@ -127,4 +127,16 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
 void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,
                    cudaStream_t s);
 
+// Allocation-free ENUMERATION over a caller-held state (64-bit role masks
+// per vertex, one active bit per CSR entry): the walker's tables, counters
+// and retry bitmaps live in a fixed 64 MiB __device__ array instead of
+// device allocations.  Writes the embedding count to d_count (device) and
+// synchronises `s`.  The first call on a device resolves the array's address
+// (cudaGetSymbolAddress).  Calls share the array: overlapping calls race.
+// Throws PmError (PM_E_INVALID_ARG above noalloc_max_vertices(), PM_E_OOM
+// when one source's count memo outgrows the array, PM_E_TIMEOUT, PM_E_DEVICE).
+uint32_t noalloc_max_vertices();
+void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t* d_edge_active,
+                       const WalkProgram& prog, uint32_t state_words, uint64_t* d_count, cudaStream_t s);
+
 }  // namespace pmgb

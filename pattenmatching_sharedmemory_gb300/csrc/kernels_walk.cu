@@ -917,3 +917,213 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
 }
 
 }  // namespace pmgb
+
+// ===========================================================================
+// Allocation-free ENUMERATION (pm_enumerate_noalloc).
+//
+// Some callers cannot allocate device memory at all: code that runs inside a
+// host framework which owns every device allocation (a memory pool or
+// arena handed out by an embedding runtime, where a stray cudaMalloc
+// fragments or escapes its accounting), or code that must not reach the
+// driver's allocator on a latency-critical path.  For them this entry point
+// counts embeddings over a pruned state the caller already holds in device
+// memory, using only the fixed scratch array below for the walker's count
+// memo tables, its per-warp epochs, its work counters and the bitmaps of
+// sources re-run with larger tables.
+//
+// The array is a file-scope __device__ variable: every GPU that loads this
+// library keeps its 64 MiB until the process exits.  Host code may not take
+// its address directly (the host symbol is only a stand-in); the device
+// address is obtained once per device with cudaGetSymbolAddress by the first
+// call made with that device current, so that first call should be made
+// before any stream capture begins.  Every call reuses the array and it keeps
+// the previous call's contents, so each call clears the parts that must start
+// at zero; calls whose work overlaps on the GPU (different streams or host
+// threads at the same time) race on the array and must be serialised by the
+// caller.
+// ===========================================================================
+#include <algorithm>
+#include <mutex>
+
+#include "pm_types.h"
+
+namespace pmgb {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;  // 64 MiB
+constexpr uint32_t kNoAllocMaxVertices = 1u << 26;         // two 8 MiB source bitmaps
+constexpr size_t kNoAllocBitmapBytes = size_t(kNoAllocMaxVertices) / 8;
+constexpr size_t kNoAllocHeaderBytes = 256;
+constexpr size_t kNoAllocEpochBytes = 64 << 10;            // up to 16384 warps
+constexpr size_t kNoAllocTableOffset = kNoAllocHeaderBytes + 2 * kNoAllocBitmapBytes + kNoAllocEpochBytes;
+constexpr size_t kNoAllocTableBytes = kNoAllocScratchBytes - kNoAllocTableOffset;
+constexpr uint32_t kNoAllocMaxWarps = 4096;
+
+}  // namespace
+}  // namespace pmgb
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[pmgb::kNoAllocScratchBytes];
+
+namespace pmgb {
+namespace {
+
+struct NoAllocLayout {
+  StepCounters* ctr;
+  uint32_t* bitmap_in;   // sources to run (rounds >= 1)
+  uint32_t* bitmap_out;  // sources whose count memo overflowed
+  uint32_t* epochs;
+  uint32_t* tables;
+  uint32_t cap;
+  uint32_t stride;
+};
+
+// One round of ENUMERATION from every source holding the start role
+// (round 0: all vertices; later rounds: the sources set in bitmap_in).
+__global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph g, DevState<uint64_t> st,
+                                                                       WalkProgram prog, NoAllocLayout L, int round,
+                                                                       uint32_t n_units, uint64_t budget_ns) {
+  __shared__ WarpShared s_ws[kWalkWarps];
+  const unsigned lane = lane_id();
+  const unsigned wib = threadIdx.x >> 5;
+  WarpShared& ws = s_ws[wib];
+  const uint32_t gw = blockIdx.x * kWalkWarps + wib;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&prog);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ws.prog);
+    for (int i = lane; i < static_cast<int>(sizeof(WalkProgram) / 4); i += 32) dst[i] = src[i];
+  }
+  if (lane == 0) {
+    ws.scanned = 0;
+    ws.descents = 0;
+  }
+  __syncwarp();
+  WarpMemo m{};
+  m.state = L.tables + static_cast<uint64_t>(gw) * L.cap * L.stride;
+  m.state_cap = L.cap;
+  m.state_stride = L.stride;
+  m.epoch = L.epochs[gw];
+  uint64_t deadline = 0;
+  if (lane == 0) deadline = global_timer_ns() + budget_ns;
+  deadline = __shfl_sync(kFull, deadline, 0);
+  unsigned long long leaves = 0;
+  bool stop = false;
+  while (!stop) {
+    unsigned long long unit = 0;
+    if (lane == 0) unit = atomicAdd(&L.ctr->items, 1ull);
+    unit = __shfl_sync(kFull, unit, 0);
+    if (unit >= n_units) break;
+    uint32_t bits = 1u, base = static_cast<uint32_t>(unit);
+    if (round > 0) {
+      bits = L.bitmap_in[unit];
+      base = static_cast<uint32_t>(unit) * 32u;
+    }
+    while (bits) {
+      const uint32_t b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const uint32_t v = base + (round > 0 ? b : 0u);
+      if (!role_of(st, v, ws.prog.start_role)) continue;
+      next_epoch(m);
+      const unsigned long long before = leaves;
+      const uint8_t res = run_walk<uint64_t, true>(g, st, ws, m, v, &leaves, deadline);
+      if (res == kItemTimeout) {
+        if (lane == 0) atomicMax(&L.ctr->error, kDeviceErrorTimeout);
+        stop = true;
+        break;
+      }
+      if (res == kItemOverflow) {
+        leaves = before;
+        if (lane == 0) {
+          atomicOr(L.bitmap_out + (v >> 5), 1u << (v & 31));
+          atomicAdd(&L.ctr->overflow, 1ull);
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    L.epochs[gw] = m.epoch;
+    if (leaves) atomicAdd(&L.ctr->enumeration, leaves);
+  }
+}
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[128] = {};
+
+void noalloc_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw PmError{PM_E_DEVICE, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+// Device address of the scratch array on the current device.  Resolved once
+// per device, by the first call made with that device current, with
+// cudaGetSymbolAddress; later calls reuse the cached address.
+unsigned char* noalloc_scratch_current() {
+  int dev = 0;
+  noalloc_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= 128) throw PmError{PM_E_NO_DEVICE, "device index out of range"};
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    noalloc_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+    if (!p) throw PmError{PM_E_DEVICE, "cudaGetSymbolAddress(no-alloc scratch) returned NULL"};
+    g_noalloc_base[dev] = p;
+  }
+  return static_cast<unsigned char*>(g_noalloc_base[dev]);
+}
+
+}  // namespace
+
+uint32_t noalloc_max_vertices() { return kNoAllocMaxVertices; }
+
+void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t* d_edge_active,
+                       const WalkProgram& prog, uint32_t state_words, uint64_t* d_count, cudaStream_t s) {
+  if (g.V > kNoAllocMaxVertices)
+    throw PmError{PM_E_INVALID_ARG, "at most 67108864 vertices (fixed 64 MiB scratch)"};
+  unsigned char* base = noalloc_scratch_current();
+  NoAllocLayout L{};
+  L.ctr = reinterpret_cast<StepCounters*>(base);
+  uint32_t* bitmap_a = reinterpret_cast<uint32_t*>(base + kNoAllocHeaderBytes);
+  uint32_t* bitmap_b = reinterpret_cast<uint32_t*>(base + kNoAllocHeaderBytes + kNoAllocBitmapBytes);
+  L.epochs = reinterpret_cast<uint32_t*>(base + kNoAllocHeaderBytes + 2 * kNoAllocBitmapBytes);
+  L.tables = reinterpret_cast<uint32_t*>(base + kNoAllocTableOffset);
+  // Count-memo entry: 5 words of epoch / step / count plus the key words.
+  L.stride = 5 + std::max<uint32_t>(state_words, 1);
+  const DevState<uint64_t> st{const_cast<uint64_t*>(d_cand), const_cast<uint32_t*>(d_edge_active), nullptr, nullptr,
+                              nullptr};
+  const uint32_t words = (g.V + 31) / 32;
+  // The array keeps the previous call's contents: the counters (the total
+  // among them) start every call at zero.
+  noalloc_check(cudaMemsetAsync(L.ctr, 0, sizeof(StepCounters), s), "clear counters");
+  StepCounters host_ctr{};
+  for (int round = 0;; ++round) {
+    const uint64_t cap = uint64_t(2048) << (2 * round);
+    uint64_t warps = kNoAllocTableBytes / (cap * L.stride * 4);
+    warps = std::min<uint64_t>(warps, std::min<uint64_t>(kNoAllocMaxWarps,
+                                                         uint64_t(device_sm_count()) * 8 * kWalkWarps));
+    warps = warps / kWalkWarps * kWalkWarps;
+    if (warps == 0)
+      throw PmError{PM_E_OOM, "a source's count memo needs more than the fixed 64 MiB scratch"};
+    L.cap = static_cast<uint32_t>(cap);
+    L.bitmap_in = (round % 2) ? bitmap_a : bitmap_b;
+    L.bitmap_out = (round % 2) ? bitmap_b : bitmap_a;
+    // Each round starts with empty tables (epoch 0 marks a free slot), fresh
+    // epochs, no sources queued for the next round and the work counter at 0.
+    noalloc_check(cudaMemsetAsync(L.tables, 0, warps * cap * L.stride * 4, s), "clear tables");
+    noalloc_check(cudaMemsetAsync(L.epochs, 0, warps * 4, s), "clear epochs");
+    noalloc_check(cudaMemsetAsync(L.bitmap_out, 0, size_t(words) * 4, s), "clear bitmap");
+    noalloc_check(cudaMemsetAsync(&L.ctr->items, 0, sizeof(unsigned long long), s), "clear work counter");
+    noalloc_check(cudaMemsetAsync(&L.ctr->overflow, 0, sizeof(unsigned long long), s), "clear overflow");
+    note_launch();
+    k_enumerate_noalloc<<<static_cast<unsigned>(warps / kWalkWarps), kWalkWarps * 32, 0, s>>>(
+        g, st, prog, L, round, round == 0 ? g.V : words, g_walk_budget_ns);
+    noalloc_check(cudaGetLastError(), "k_enumerate_noalloc launch");
+    noalloc_check(cudaMemcpyAsync(&host_ctr, L.ctr, sizeof(StepCounters), cudaMemcpyDeviceToHost, s),
+                  "read counters");
+    noalloc_check(cudaStreamSynchronize(s), "k_enumerate_noalloc");
+    if (host_ctr.error == kDeviceErrorTimeout) throw PmError{PM_E_TIMEOUT, "walker time budget exceeded"};
+    if (host_ctr.overflow == 0) break;
+  }
+  noalloc_check(cudaMemcpyAsync(d_count, &L.ctr->enumeration, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s),
+                "write count");
+  noalloc_check(cudaStreamSynchronize(s), "write count");
+}
+
+}  // namespace pmgb
