@@ -32,6 +32,13 @@ pm_status_t pm_graph_host_csr(const pm_graph* g, const uint64_t** offsets, const
 /* Copies the CSR to device `device` (no-op when already there). */
 pm_status_t pm_graph_to_device(pm_graph* g, int32_t device);
 
+/* Degree classes of the LCC sweeps: vertices with more than hub_degree CSR
+ * entries (at most 2^26) are hubs whose adjacency is split into segments of
+ * seg_entries entries, each checked by its own warp (defaults 128 and 1024).
+ * Affects speed only, never results.  The graph must be on a device and no
+ * query of it may be running. */
+pm_status_t pm_graph_set_hub_plan(pm_graph* g, uint32_t hub_degree, uint32_t seg_entries);
+
 /* Writes the graph as TOTEM text and its labels as a vertex file. */
 pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const char* labels_path);
 
@@ -57,9 +64,11 @@ pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32
                                          uint32_t p_vertex_count, uint64_t p_edge_count, char* buf, size_t cap,
                                          size_t* needed);
 
-/* Walker work of result row `row` (0-based, as returned by pm_query_run):
- * CSR entries tested and hops taken by the CC/PC/TDS or ENUMERATION
- * kernels of that step (0 for LCC0/LCC). */
+/* Work of result row `row` (0-based, as returned by pm_query_run): for
+ * CC/PC/TDS and ENUMERATION, the CSR entries tested and hops taken by the
+ * walkers; for LCC, the CSR entries in the lists the sweep checked and how
+ * many of them it read a neighbour word for (the others point to vertices
+ * already seen without roles); 0 for LCC0. */
 pm_status_t pm_query_step_walk_stats(const pm_query* q, int32_t row, uint64_t* scanned, uint64_t* descents);
 
 /* Number of NLCC steps that needed the exact sequential emulation of the

@@ -90,6 +90,7 @@ def _load_library() -> ctypes.CDLL:
         "pm_graph_host_csr": (ctypes.c_int32, [ctypes.c_void_p, P(c_u64p), P(c_u32p), P(c_u64p)]),
         "pm_graph_to_device": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
         "pm_graph_write_text": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+        "pm_graph_set_hub_plan": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
         "pm_query_create": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_void_p)]),
         "pm_query_create_from_csr": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, c_u64p, ctypes.c_uint32,
                                                       ctypes.c_uint64, P(ctypes.c_void_p)]),
@@ -182,6 +183,12 @@ class Graph:
 
     def to_device(self, device: int = 0) -> "Graph":
         _check(lib.pm_graph_to_device(self._h, device))
+        return self
+
+    def set_hub_plan(self, hub_degree: int, seg_entries: int) -> "Graph":
+        """LCC degree classes: lists longer than hub_degree are split into
+        seg_entries-entry segments (speed only; results do not change)."""
+        _check(lib.pm_graph_set_hub_plan(self._h, hub_degree, seg_entries))
         return self
 
     @property

@@ -303,6 +303,17 @@ pm_status_t pm_query_elapsed_ms(const pm_query* q, double* ms) {
   });
 }
 
+pm_status_t pm_graph_set_hub_plan(pm_graph* g, uint32_t hub_degree, uint32_t seg_entries) {
+  PM_REQUIRE(g, "graph is NULL");
+  PM_REQUIRE(seg_entries > 0, "seg_entries must be positive");
+  PM_REQUIRE(g->impl.device >= 0, "graph is not on a device");
+  return guarded([&]() -> pm_status_t {
+    PM_CUDA(cudaSetDevice(g->impl.device));
+    g->impl.build_hub_plan(hub_degree, seg_entries);
+    return PM_SUCCESS;
+  });
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));

@@ -80,6 +80,32 @@ struct DevGraph {
   const uint32_t* __restrict__ adj;
   const uint32_t* __restrict__ lab;
   int sorted_unique;  // every adjacency list strictly increasing
+  // Degree classes of the LCC sweeps: a vertex with more than hub_degree
+  // CSR entries is a hub, its list cut into segments of seg_entries entries
+  // that one warp each streams; lighter vertices go in tiles of 32
+  // (n_seg == 0: every vertex is light).  seg[0, n_heavy) are the segments
+  // of hubs with several segments, seg[n_heavy, n_seg) the single-segment
+  // hubs.
+  uint32_t hub_degree;
+  uint32_t seg_shift;    // seg_entries = 1 << seg_shift, 32 to 1024
+  uint32_t n_seg;
+  uint32_t n_heavy;
+  uint32_t n_acc;                  // hubs with more than one segment
+  // Segment i of vertex v covers its entries in [(off[v] / seg_entries + i)
+  // * seg_entries, + seg_entries): segments never cross a seg_entries
+  // boundary, so one spans at most 32 words of edge bits.
+  const uint4* __restrict__ seg;   // [n_seg] {vertex, segment index, segments, accumulator}
+};
+
+// Per-query accumulator of a hub with several segments.  Zero between
+// launches: the last segment of the hub to finish reads and clears it.
+constexpr uint32_t kHubRanks = 16;  // needed label slots the sweep counts per owner
+struct HubAcc {
+  uint32_t cnt[kHubRanks];  // sweep 1: surviving neighbours per needed slot (by rank)
+  uint32_t elim;            // sweep 1: CSR entries eliminated
+  uint32_t ticket;          // sweep 1: segments finished
+  uint32_t hit;             // sweep 2: a segment saw a modified active neighbour
+  uint32_t ticket2;         // sweep 2: segments finished
 };
 
 template <class W>
@@ -89,6 +115,10 @@ struct DevState {
   uint8_t* mod;
   uint8_t* sch;
   W* unm;
+  // Live-target bits: a subset of eact without the entries whose target
+  // was seen with no role left (roles never come back).  The LCC sweep
+  // skips entries outside it; nothing else reads it.
+  uint32_t* lt;
 };
 
 // Device counters.  The first kStepCounterWords words are per step
@@ -105,12 +135,13 @@ struct StepCounters {
   unsigned long long items;      // work counter for persistent kernels
   unsigned long long error;      // device-side error status (0 = ok)
   unsigned long long aux;        // list fill counter (overflow retry list)
-  unsigned long long scanned;    // walkers: CSR entries tested
+  unsigned long long scanned;    // walkers: CSR entries tested; LCC: entries of the checked lists
   unsigned long long descents;   // walkers: hops taken (states entered)
+  unsigned long long gathered;   // LCC: entries whose neighbour word was read
   unsigned long long modified_total;  // vertices with mod=1 since the last reset
-  unsigned long long pad[4];
+  unsigned long long pad[3];
 };
-constexpr int kStepCounterWords = 11;
+constexpr int kStepCounterWords = 12;
 
 // Per-query tables derived from the local constraints
 // (multiple_label_constraint_local.h:18-32), in label-slot space.

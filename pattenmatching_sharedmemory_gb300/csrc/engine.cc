@@ -69,11 +69,55 @@ void GraphImpl::to_device(int dev) {
     PM_CUDA(cudaMemcpy(d_adj.ptr, host.adj.data(), sizeof(uint32_t) * host.edge_count, cudaMemcpyHostToDevice));
   if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
   device = dev;
+  build_hub_plan(hub_degree, seg_entries);
+}
+
+void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
+  if (entries < 32 || entries > 1024 || (entries & (entries - 1)))
+    throw PmError{PM_E_INVALID_ARG, "seg_entries must be a power of two in [32, 1024]"};
+  // Light tiles stream at most 32 * hub_degree entries (32-bit stream index).
+  if (degree > (1u << 26)) throw PmError{PM_E_INVALID_ARG, "hub_degree above 2^26"};
+  // Segments of multi-segment hubs first (one sweep task each), then the
+  // single-segment hubs (batched 32 to a task).
+  std::vector<uint4> seg, single;
+  uint32_t n_multi = 0;
+  const uint32_t V = host.vertex_count;
+  for (uint32_t v = 0; v < V; ++v) {
+    const uint64_t deg = host.offsets[v + 1] - host.offsets[v];
+    if (deg <= degree) continue;
+    // Segments end at multiples of `entries` (see DevGraph::seg).
+    const uint64_t n = (host.offsets[v + 1] - 1) / entries - host.offsets[v] / entries + 1;
+    if (seg.size() + single.size() + n > 0x7fffffffull) throw PmError{PM_E_INVALID_ARG, "too many hub segments"};
+    if (n == 1) {
+      single.push_back(make_uint4(v, 0, 1, 0xFFFFFFFFu));
+      continue;
+    }
+    const uint32_t acc = n_multi++;
+    for (uint64_t i = 0; i < n; ++i)
+      seg.push_back(make_uint4(v, static_cast<uint32_t>(i), static_cast<uint32_t>(n), acc));
+  }
+  const uint32_t heavy = static_cast<uint32_t>(seg.size());
+  seg.insert(seg.end(), single.begin(), single.end());
+  d_seg.ensure(sizeof(uint4) * std::max<size_t>(seg.size(), 1));
+  if (!seg.empty())
+    PM_CUDA(cudaMemcpy(d_seg.ptr, seg.data(), sizeof(uint4) * seg.size(), cudaMemcpyHostToDevice));
+  hub_degree = degree;
+  seg_entries = entries;
+  n_seg = static_cast<uint32_t>(seg.size());
+  n_heavy = heavy;
+  n_acc = n_multi;
 }
 
 DevGraph GraphImpl::dev() const {
-  return DevGraph{host.vertex_count, host.edge_count, d_off.as<uint64_t>(), d_adj.as<uint32_t>(), d_lab.as<uint32_t>(),
-                  sorted_unique ? 1 : 0};
+  DevGraph g{host.vertex_count, host.edge_count, d_off.as<uint64_t>(), d_adj.as<uint32_t>(), d_lab.as<uint32_t>(),
+             sorted_unique ? 1 : 0};
+  g.hub_degree = hub_degree;
+  g.seg_shift = static_cast<uint32_t>(__builtin_ctz(seg_entries));
+  g.n_seg = n_seg;
+  g.n_heavy = n_heavy;
+  g.n_acc = n_acc;
+  g.seg = d_seg.as<uint4>();
+  return g;
 }
 
 // ---- walker scratch --------------------------------------------------------
@@ -152,7 +196,8 @@ uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
   const uint64_t V = g.host.vertex_count, E = g.host.edge_count;
   const uint64_t wb = word_bytes(word_kind_for(k));
   // state + per-step worklist/status/markers (items bounded by V * roles)
-  return V * (2 * wb + 2) + ((E + 31) / 32) * 4 + V * 8 + V * std::min<uint64_t>(k, 64) * 5 + (1 << 20);
+  return V * (2 * wb + 2) + ((E + 31) / 32) * 8 + V * 8 + V * std::min<uint64_t>(k, 64) * 5 +
+         sizeof(HubAcc) * static_cast<uint64_t>(g.n_acc) + (1 << 20);
 }
 
 QueryImpl::~QueryImpl() {
@@ -166,12 +211,13 @@ QueryImpl::~QueryImpl() {
 
 QueryDevPtrs QueryImpl::ptrs() const {
   return QueryDevPtrs{word_kind, d_vs.ptr, d_eact.as<uint32_t>(), d_mod.as<uint8_t>(), d_sch.as<uint8_t>(),
-                      d_unm.ptr, d_ctr.as<StepCounters>(), d_tables.as<QueryTables>()};
+                      d_unm.ptr, d_ctr.as<StepCounters>(), d_tables.as<QueryTables>(), d_hub_acc.as<HubAcc>(),
+                      d_lt.as<uint32_t>()};
 }
 
 uint64_t QueryImpl::device_bytes() const {
-  return d_vs.bytes + d_eact.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
-         d_d2s.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
+  return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
+         d_d2s.bytes + d_hub_acc.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
          d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes +
          pool.bytes() + big_pool.bytes();
 }
@@ -230,6 +276,7 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) 
   d_vs.ensure(wb * std::max<uint64_t>(V, 1));
   d_unm.ensure(wb * std::max<uint64_t>(V, 1));
   d_eact.ensure(4 * std::max<uint64_t>((E + 31) / 32, 1));
+  d_lt.ensure(4 * std::max<uint64_t>((E + 31) / 32, 1));
   d_mod.ensure(std::max<uint64_t>(V, 1));
   d_sch.ensure(std::max<uint64_t>(V, 1));
   d_ctr.ensure(sizeof(StepCounters));
@@ -239,6 +286,8 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) 
   d_wl_index.ensure(4 * std::max<uint64_t>(V, 1));
   d_blocks.ensure(4 * ((V + 4095) / 4096 + 2));
   d_count.ensure(4);
+  d_hub_acc.ensure(sizeof(HubAcc) * std::max<uint32_t>(g->n_acc, 1));
+  PM_CUDA(cudaMemsetAsync(d_hub_acc.ptr, 0, d_hub_acc.bytes, stream));
   PM_CUDA(cudaMemsetAsync(d_ctr.ptr, 0, sizeof(StepCounters), stream));
   PM_CUDA(cudaMemcpyAsync(d_tables.ptr, &tables, sizeof(tables), cudaMemcpyHostToDevice, stream));
   PM_CUDA(cudaMemcpyAsync(d_d2s.ptr, dense_to_slot.data(), dense_to_slot.size(), cudaMemcpyHostToDevice, stream));
@@ -574,6 +623,11 @@ pm_step_record QueryImpl::run_step() {
   if (finished) return final_record();
   const int kind = step;
   if (kind == PM_STEP_CC || kind == PM_STEP_PC || kind == PM_STEP_TDS) reset_modified();
+  // The graph's hub plan may have changed since the last step.
+  if (d_hub_acc.bytes < sizeof(HubAcc) * static_cast<size_t>(g->n_acc)) {
+    d_hub_acc.ensure(sizeof(HubAcc) * static_cast<size_t>(g->n_acc));
+    PM_CUDA(cudaMemsetAsync(d_hub_acc.ptr, 0, d_hub_acc.bytes, stream));
+  }
   clear_step_counters();
   PM_CUDA(cudaEventRecord(ev0, stream));
   if (!first_recorded) {
@@ -616,7 +670,7 @@ pm_step_record QueryImpl::run_step() {
   rec.active_edge = active_edges;
   rec.total_edge = g->host.edge_count;
   records.push_back(rec);
-  walk_stats.emplace_back(h_ctr->scanned, h_ctr->descents);
+  walk_stats.emplace_back(h_ctr->scanned, kind == PM_STEP_LCC ? h_ctr->gathered : h_ctr->descents);
   step = advance(kind);
   if (kind == PM_STEP_ENUMERATION) finished = true;
   ++iteration;

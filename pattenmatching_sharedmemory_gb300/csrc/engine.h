@@ -43,11 +43,23 @@ struct GraphImpl {
   bool sorted_unique = false;
   int device = -1;
   DeviceBuffer d_off, d_adj, d_lab;
+  // Degree classes of the LCC sweeps (DevGraph::hub_degree and segments).
+  uint32_t hub_degree = kDefaultHubDegree, seg_entries = kDefaultSegEntries;
+  uint32_t n_seg = 0, n_heavy = 0, n_acc = 0;
+  DeviceBuffer d_seg;
+
+  static constexpr uint32_t kDefaultHubDegree = 32;
+  static constexpr uint32_t kDefaultSegEntries = 1024;
 
   void finalize_host();  // dense labels, adjacency checks
   void to_device(int device);
+  // Hubs = vertices of more than hub_degree CSR entries, in segments of
+  // seg_entries entries (device tables rebuilt; graph must be on a device).
+  void build_hub_plan(uint32_t hub_degree, uint32_t seg_entries);
   DevGraph dev() const;
-  uint64_t device_bytes() const { return d_off.bytes + d_adj.bytes + d_lab.bytes; }
+  uint64_t device_bytes() const {
+    return d_off.bytes + d_adj.bytes + d_lab.bytes + d_seg.bytes;
+  }
 };
 
 // Walker scratch pool (memo tables), sized on demand.
@@ -86,7 +98,7 @@ struct QueryImpl {
 
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DeviceBuffer d_vs, d_eact, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s;
+  DeviceBuffer d_vs, d_eact, d_lt, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s, d_hub_acc;
   DeviceBuffer d_progs, d_start_roles, d_role_index;
   DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_list2, d_apply_v,
       d_apply_r;

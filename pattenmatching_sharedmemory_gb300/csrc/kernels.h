@@ -24,6 +24,8 @@ struct QueryDevPtrs {
   void* unm;
   StepCounters* ctr;
   const QueryTables* tables;
+  HubAcc* hub_acc;  // [DevGraph::n_acc]
+  uint32_t* lt;     // live-target bits (DevState::lt)
 };
 
 // Launch geometry shared by all kernels (SM count of the current device).

@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(kThreads) k_init_state(DevGraph g, DevState<W>
   const uint64_t words = (g.E + 31) / 32;
   for (uint64_t i = tid; i < words; i += stride) {
     uint64_t remaining = g.E - i * 32;
-    st.eact[i] = remaining >= 32 ? 0xFFFFFFFFu : ((1u << remaining) - 1u);
+    const uint32_t w = remaining >= 32 ? 0xFFFFFFFFu : ((1u << remaining) - 1u);
+    st.eact[i] = w;
+    st.lt[i] = w;
   }
 }
 
@@ -83,173 +85,683 @@ __global__ void __launch_bounds__(kThreads) k_lcc0(DevGraph g, DevState<W> st, c
 }
 
 // ---- LCC sweep 1 --------------------------------------------------------
-template <class W>
-__global__ void __launch_bounds__(kThreads) k_lcc_check(DevGraph g, DevState<W> st, const QueryTables* __restrict__ qt,
-                                                        StepCounters* ctr) {
-  __shared__ uint64_t s_nbr[64];
-  __shared__ uint64_t s_need[64];
-  __shared__ uint8_t s_role_slot[64];
-  __shared__ uint8_t s_req[64][64];
-  const uint32_t k = qt->k;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
-    s_nbr[i] = qt->nbr_mask[i];
-    s_need[i] = qt->req_slots[i];
-    s_role_slot[i] = qt->role_slot[i];
-  }
-  for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) s_req[i / 64][i % 64] = qt->req[i / 64][i % 64];
-  __syncthreads();
+//
+// A grid of resident warps over a task list; warp w takes tasks w, w + W,
+// w + 2W, ...  The first tasks each cover 32 hub segments (seg_entries CSR
+// entries of a vertex with more than hub_degree entries): the lanes test the
+// 32 segments' vertices at once, then the warp streams each live segment,
+// kUnroll x 32 entries per iteration, every lane counting the surviving
+// neighbours of each needed label slot in its own shared counters.  A hub
+// with one segment decides its roles at once; the others add their counts
+// to the hub's HubAcc and its last segment to finish decides.  The remaining
+// tasks are tiles of 32 consecutive light vertices, whose adjacency lists
+// the warp streams back to back: a warp prefix sum over the lanes' degrees
+// maps a stream index to its owner lane, and counts go per (owner, slot)
+// with one update per group of equal keys (__match_any_sync).
 
+constexpr int kUnroll = 4;
+constexpr int kLccWarps = kThreads / 32;
+constexpr uint8_t kNoRank = 0xFF;
+
+struct LccTables {
+  uint64_t nbr[64];
+  uint64_t need[64];
+  uint8_t role_slot[64];
+  uint8_t req[64][64];
+};
+
+struct LccWarp {
+  uint32_t cnt[kHubRanks][32];  // tiles: [rank][owner lane]; segments: [rank][counting lane]
+  uint32_t tot[kHubRanks];      // segments: totals per rank
+  uint8_t rank_of[64];          // needed slot -> rank, kNoRank otherwise
+};
+
+// Rank table of `slots` and zeroed counters for its n_slots ranks.
+__device__ __forceinline__ void set_ranks(LccWarp& lw, uint64_t slots, uint32_t n_slots) {
   const unsigned lane = lane_id();
-  const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
-  unsigned long long edge_elim = 0, newly_modified = 0;
+  __syncwarp();
+  for (uint32_t s = lane; s < 64; s += 32)
+    lw.rank_of[s] = (slots >> s & 1) ? static_cast<uint8_t>(__popcll(slots & ((uint64_t(1) << s) - 1))) : kNoRank;
+  for (uint32_t r = 0; r < n_slots; ++r) lw.cnt[r][lane] = 0;
+  __syncwarp();
+}
 
-  for (uint64_t tile = warp * 32; tile < g.V; tile += n_warps * 32) {
-    const uint64_t v = tile + lane;
-    bool work = false;
-    if (v < g.V) work = st.sch[v] && Pack<W>::cand(st.vs[v]) != 0;
-    unsigned wm = __ballot_sync(kFull, work);
-    while (wm) {
-      const unsigned j = __ffs(wm) - 1;
-      wm &= wm - 1;
-      const uint32_t u = static_cast<uint32_t>(tile + j);
-      const W wu = st.vs[u];
-      const uint64_t cu = Pack<W>::cand(wu);
-      const uint32_t su = Pack<W>::slot(wu);
-      // Union of the template neighbours of u's roles, and the label slots
-      // any of u's roles needs counted.
-      uint64_t ncs = 0, need = 0;
-      for (uint32_t p = lane; p < k; p += 32)
-        if (cu >> p & 1) {
-          ncs |= s_nbr[p];
-          need |= s_need[p];
-        }
-      ncs = warp_or64(ncs);
-      need = warp_or64(need);
+__device__ __forceinline__ void load_lcc_tables(LccTables& t, const QueryTables* __restrict__ qt, uint32_t k) {
+  for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) {
+    t.nbr[i] = qt->nbr_mask[i];
+    t.need[i] = qt->req_slots[i];
+    t.role_slot[i] = qt->role_slot[i];
+  }
+  const uint32_t rows = k < 64 ? k : 64;
+  for (uint32_t i = threadIdx.x; i < rows * 64; i += blockDim.x) t.req[i / 64][i % 64] = qt->req[i / 64][i % 64];
+  __syncthreads();
+}
 
-      uint32_t cnt_lo = 0, cnt_hi = 0;  // counts of slot `lane` and `lane+32`
-      uint32_t elim_u = 0;
-      const uint64_t beg = g.off[u], end = g.off[u + 1];
-      for (uint64_t e0 = beg; e0 < end; e0 += 32) {
-        const uint64_t e = e0 + lane;
-        const bool act = e < end && edge_active(st.eact, e);
-        W ww = Pack<W>::zero();
-        if (act) ww = st.vs[g.adj[e]];
-        const uint64_t cw = Pack<W>::cand(ww);
-        const bool live = act && cw != 0;
-        const bool poss = live && (cw & ncs) != 0;
-        const unsigned em = __ballot_sync(kFull, live && !poss);
-        if (em) {
-          if (lane == 0) clear_edge_bits(st.eact, e0, em);
-          elim_u += __popc(em);
-        }
-        const uint32_t sw = Pack<W>::slot(ww);
-        uint64_t nd = need;
-        while (nd) {
-          const unsigned s = __ffsll(static_cast<long long>(nd)) - 1;
-          nd &= nd - 1;
-          const unsigned m = __ballot_sync(kFull, poss && sw == s);
-          if (lane == (s & 31)) {
-            if (s < 32)
-              cnt_lo += __popc(m);
-            else
-              cnt_hi += __popc(m);
-          }
-        }
+__device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
+  const uint32_t lo = __shfl_sync(kFull, static_cast<uint32_t>(x), src);
+  const uint32_t hi = __shfl_sync(kFull, static_cast<uint32_t>(x >> 32), src);
+  return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+// Mask of lanes [lo, hi) of a 32-lane slice, clamped to the slice.
+__device__ __forceinline__ uint32_t lane_range(int64_t lo, int64_t hi) {
+  lo = lo < 0 ? 0 : lo;
+  hi = hi > 32 ? 32 : hi;
+  if (hi <= lo) return 0;
+  const uint32_t n = static_cast<uint32_t>(hi - lo);
+  return (n == 32 ? kFull : ((1u << n) - 1)) << static_cast<uint32_t>(lo);
+}
+
+// CSR entry range [beg, end) of hub segment sd (DevGraph::seg).
+__device__ __forceinline__ void segment_range(const DevGraph& g, const uint4 sd, uint64_t* beg, uint64_t* end) {
+  const uint64_t a = g.off[sd.x], b = g.off[sd.x + 1];
+  const uint64_t blk = (a >> g.seg_shift) + sd.y;
+  *beg = sd.y == 0 ? a : blk << g.seg_shift;
+  const uint64_t lim = (blk + 1) << g.seg_shift;
+  *end = b < lim ? b : lim;
+}
+
+// Union of the template neighbours of the roles in cu, and the label slots
+// any of them needs counted.
+__device__ __forceinline__ void role_unions(const LccTables& t, uint64_t cu, uint64_t* ncs, uint64_t* need) {
+  uint64_t a = 0, b = 0;
+  for (uint64_t rr = cu; rr; rr &= rr - 1) {
+    const uint32_t p = __ffsll(static_cast<long long>(rr)) - 1;
+    a |= t.nbr[p];
+    b |= t.need[p];
+  }
+  *ncs = a;
+  *need = b;
+}
+
+// role_unions for one vertex held by the whole warp (lane p looks at roles
+// p and p + 32).
+__device__ __forceinline__ void role_unions_warp(const LccTables& t, uint64_t cu, uint64_t* ncs, uint64_t* need) {
+  const unsigned lane = lane_id();
+  uint64_t a = 0, b = 0;
+  if (cu >> lane & 1) {
+    a = t.nbr[lane];
+    b = t.need[lane];
+  }
+  if (cu >> (lane + 32) & 1) {
+    a |= t.nbr[lane + 32];
+    b |= t.need[lane + 32];
+  }
+  *ncs = warp_or64(a);
+  *need = warp_or64(b);
+}
+
+// failing_roles for one vertex held by the whole warp: lane p decides roles
+// p and p + 32 from the per-rank totals in lw.tot.
+__device__ __forceinline__ uint64_t failing_roles_warp(const LccTables& t, const LccWarp& lw, uint64_t cu,
+                                                       uint32_t su) {
+  const unsigned lane = lane_id();
+  bool bad[2] = {false, false};
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const uint32_t p = lane + 32 * half;
+    if (cu >> p & 1) {
+      bool b = t.role_slot[p] != su;
+      for (uint64_t ss = t.need[p]; ss && !b; ss &= ss - 1) {
+        const uint32_t sl = __ffsll(static_cast<long long>(ss)) - 1;
+        if (t.req[p][sl] > lw.tot[lw.rank_of[sl]]) b = true;
       }
-      // Role p fails if its label differs from u's or a required
-      // neighbour-label count is not met (lcc :79-100).
-      const bool has_lo = lane < k && (cu >> lane & 1);
-      const bool has_hi = lane + 32 < k && (cu >> (lane + 32) & 1);
-      bool bad_lo = has_lo && s_role_slot[lane] != su;
-      bool bad_hi = has_hi && s_role_slot[lane + 32] != su;
-      uint64_t nd = need;
-      while (nd) {
-        const unsigned s = __ffsll(static_cast<long long>(nd)) - 1;
-        nd &= nd - 1;
-        const uint32_t c = __shfl_sync(kFull, s < 32 ? cnt_lo : cnt_hi, s & 31);
-        if (has_lo && s_req[lane][s] > c) bad_lo = true;
-        if (has_hi && s_req[lane + 32][s] > c) bad_hi = true;
-      }
-      const uint64_t tu = static_cast<uint64_t>(__ballot_sync(kFull, bad_lo)) |
-                          (static_cast<uint64_t>(__ballot_sync(kFull, bad_hi)) << 32);
+      bad[half] = b;
+    }
+  }
+  return static_cast<uint64_t>(__ballot_sync(kFull, bad[0])) |
+         (static_cast<uint64_t>(__ballot_sync(kFull, bad[1])) << 32);
+}
+
+// Roles of u that fail: the role's label differs from u's, or a required
+// neighbour-label count is not met (lcc :79-100).  cnt(rank) is the count of
+// the rank-th set slot of `slots`.
+template <class F>
+__device__ __forceinline__ uint64_t failing_roles(const LccTables& t, uint64_t cu, uint32_t su, uint64_t slots,
+                                                  F cnt) {
+  uint64_t tu = 0;
+  for (uint64_t rr = cu; rr; rr &= rr - 1) {
+    const uint32_t p = __ffsll(static_cast<long long>(rr)) - 1;
+    bool bad = t.role_slot[p] != su;
+    uint32_t rank = 0;
+    for (uint64_t ss = slots; ss && !bad; ss &= ss - 1, ++rank) {
+      const uint32_t s = __ffsll(static_cast<long long>(ss)) - 1;
+      if (t.req[p][s] > cnt(rank)) bad = true;
+    }
+    if (bad) tu |= uint64_t(1) << p;
+  }
+  return tu;
+}
+
+// Per-lane tallies of a sweep-1 launch (one warp's share of a launch stays
+// below 2^32).
+struct LccTally {
+  uint32_t edge_elim = 0;       // CSR entries eliminated
+  uint32_t newly_modified = 0;  // vertices newly flagged modified
+  uint32_t streamed = 0;        // CSR entries in the checked lists
+  uint32_t gathered = 0;        // ... whose neighbour word was read
+};
+
+// Records the outcome of vertex u's check (lcc :65-100): modified when it
+// lost a role or an edge, roles to unmatch in unm.
+template <class W>
+__device__ __forceinline__ void lcc_record(const DevState<W>& st, uint32_t u, uint64_t tu, uint32_t elim,
+                                           uint32_t& newly_modified) {
+  if (tu || elim) {
+    if (!st.mod[u]) {
+      st.mod[u] = 1;
+      ++newly_modified;
+    }
+  }
+  if (tu) st.unm[u] = Pack<W>::make(tu, 0);
+}
+
+// Whole-list check of one vertex by one warp, for owners that need more than
+// kHubRanks label slots counted.
+template <class W>
+__device__ void lcc_vertex_warp(const DevGraph& g, const DevState<W>& st, const LccTables& t, uint32_t u,
+                                LccTally& tl) {
+  const unsigned lane = lane_id();
+  const W wu = st.vs[u];
+  const uint64_t cu = Pack<W>::cand(wu);
+  const uint32_t su = Pack<W>::slot(wu);
+  uint64_t ncs, need;
+  role_unions(t, cu, &ncs, &need);
+  uint32_t cnt_lo = 0, cnt_hi = 0;  // lane r: counts of the r-th and (r+32)-th slot of `need`
+  uint32_t elim_u = 0;
+  const uint64_t beg = g.off[u], end = g.off[u + 1];
+  for (uint64_t e0 = beg; e0 < end; e0 += 32) {
+    const uint64_t e = e0 + lane;
+    const bool act = e < end && edge_active(st.eact, e);
+    W ww = Pack<W>::zero();
+    if (act) {
+      ww = st.vs[g.adj[e]];
+      ++tl.gathered;
+    }
+    const uint64_t cw = Pack<W>::cand(ww);
+    const bool live = act && cw != 0;
+    const bool poss = live && (cw & ncs) != 0;
+    const unsigned em = __ballot_sync(kFull, live && !poss);
+    if (em) {
       if (lane == 0) {
-        if (tu || elim_u) {
-          if (!st.mod[u]) {
-            st.mod[u] = 1;
-            ++newly_modified;
-          }
-        }
-        if (tu) st.unm[u] = Pack<W>::make(tu, 0);
-        edge_elim += elim_u;
+        clear_edge_bits(st.eact, e0, em);
+        clear_edge_bits(st.lt, e0, em);
+      }
+      elim_u += __popc(em);
+    }
+    const uint32_t sw = Pack<W>::slot(ww);
+    uint32_t rank = 0;
+    for (uint64_t nd = need; nd; nd &= nd - 1, ++rank) {
+      const uint32_t s = __ffsll(static_cast<long long>(nd)) - 1;
+      const unsigned m = __ballot_sync(kFull, poss && sw == s);
+      if (lane == (rank & 31)) {
+        if (rank < 32)
+          cnt_lo += __popc(m);
+        else
+          cnt_hi += __popc(m);
       }
     }
   }
+  // cu and need are warp-uniform: every lane walks the same loops.
+  const uint64_t tu = failing_roles(t, cu, su, need, [&](uint32_t rank) {
+    return __shfl_sync(kFull, rank < 32 ? cnt_lo : cnt_hi, rank & 31);
+  });
   if (lane == 0) {
-    if (edge_elim) atomicAdd(&ctr->edge_elim, edge_elim);
-    if (newly_modified) atomicAdd(&ctr->modified_total, newly_modified);
+    lcc_record(st, u, tu, elim_u, tl.newly_modified);
+    tl.edge_elim += elim_u;
+    tl.streamed += end - beg;
+  }
+}
+
+// One live hub segment, streamed by the whole warp.  Lane j holds word j of
+// the segment's live-target bits; the warp then visits only the words with
+// a bit set, kUnroll words per round, loading the CSR entry and gathering
+// the neighbour word for set bits only.
+template <class W>
+__device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
+                            const uint4 sd, const W wv, const uint64_t beg, const uint64_t end, LccTally& tl) {
+  const unsigned lane = lane_id();
+  const uint32_t v = sd.x;
+  const uint64_t cu = Pack<W>::cand(wv);
+  const uint32_t su = Pack<W>::slot(wv);
+  uint64_t ncs, need;
+  role_unions_warp(t, cu, &ncs, &need);
+  const uint32_t n_slots = __popcll(need);
+  if (n_slots > kHubRanks) {
+    if (sd.y == 0) lcc_vertex_warp(g, st, t, v, tl);
+    return;
+  }
+  set_ranks(lw, need, n_slots);
+  const uint64_t w0 = beg >> 5;
+  const uint64_t wi = w0 + lane;
+  uint32_t word = 0;
+  if (wi <= (end - 1) >> 5) {
+    word = st.lt[wi];
+    const uint64_t lo = wi << 5;
+    if (beg > lo) word &= ~0u << static_cast<uint32_t>(beg - lo);
+    if (end < lo + 32) word &= (1u << static_cast<uint32_t>(end - lo)) - 1u;
+  }
+  if (lane == 0) tl.streamed += end - beg;
+  tl.gathered += __popc(word);
+  uint32_t elim = 0;
+  for (unsigned nz = __ballot_sync(kFull, word != 0); nz;) {
+    uint32_t idx[kUnroll], bits[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      idx[u] = nz ? static_cast<uint32_t>(__ffs(nz) - 1) : 32u;
+      nz &= nz - 1;
+      bits[u] = __shfl_sync(kFull, word, idx[u] & 31);
+      if (idx[u] == 32) bits[u] = 0;
+    }
+    uint32_t nb[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+      nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
+    W ww[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const bool in = (bits[u] >> lane) & 1u;
+      const uint64_t cw = Pack<W>::cand(ww[u]);
+      const bool live = in && cw != 0;
+      const bool poss = live && (cw & ncs) != 0;
+      const unsigned em = __ballot_sync(kFull, live && !poss);
+      const unsigned dm = __ballot_sync(kFull, in && cw == 0);
+      if (lane == 0 && (em | dm)) {
+        const uint64_t w = w0 + idx[u];
+        if (em) atomicAnd(st.eact + w, ~em);
+        atomicAnd(st.lt + w, ~(em | dm));
+      }
+      elim += __popc(em);
+      if (poss) {
+        const uint32_t sw = Pack<W>::slot(ww[u]);
+        if (sw < 64) {
+          const uint32_t r = lw.rank_of[sw];
+          if (r != kNoRank) ++lw.cnt[r][lane];
+        }
+      }
+    }
+  }
+  // Segment totals: lane r ends with the count of rank r.
+  uint32_t mine = 0;
+  for (uint32_t r = 0; r < n_slots; ++r) {
+    const uint32_t c = __reduce_add_sync(kFull, lw.cnt[r][lane]);
+    if (lane == r) mine = c;
+  }
+  if (sd.z == 1) {
+    if (lane < n_slots) lw.tot[lane] = mine;
+    __syncwarp();
+    const uint64_t tu = failing_roles_warp(t, lw, cu, su);
+    if (lane == 0) {
+      lcc_record(st, v, tu, elim, tl.newly_modified);
+      tl.edge_elim += elim;
+    }
+    return;
+  }
+  HubAcc& a = acc[sd.w];
+  if (lane < n_slots && mine) atomicAdd(&a.cnt[lane], mine);
+  if (lane == 0 && elim) {
+    atomicAdd(&a.elim, elim);
+    tl.edge_elim += elim;
+  }
+  __threadfence();
+  __syncwarp();
+  uint32_t done = 0;
+  if (lane == 0) done = atomicAdd(&a.ticket, 1u);
+  done = __shfl_sync(kFull, done, 0);
+  if (done + 1 == sd.z) {
+    // Last segment of this hub: every other segment's adds are visible.
+    __threadfence();
+    if (lane < n_slots) lw.tot[lane] = atomicExch(&a.cnt[lane], 0u);
+    uint32_t el = 0;
+    if (lane == 0) {
+      el = atomicExch(&a.elim, 0u);
+      atomicExch(&a.ticket, 0u);
+    }
+    __syncwarp();
+    const uint64_t tu = failing_roles_warp(t, lw, cu, su);
+    if (lane == 0) lcc_record(st, v, tu, el, tl.newly_modified);
+  }
+}
+
+// Segment i of a multi-segment hub.
+template <class W>
+__device__ void lcc_heavy(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
+                          uint64_t i, LccTally& tl) {
+  const uint4 sd = g.seg[i];
+  // Independent loads; the exits are warp-uniform (the hub is not scheduled
+  // or has no role left).
+  const uint8_t sch = st.sch[sd.x];
+  const W wv = st.vs[sd.x];
+  uint64_t beg, end;
+  segment_range(g, sd, &beg, &end);
+  if (!sch || !Pack<W>::cand(wv)) return;
+  lcc_segment(g, st, t, lw, acc, sd, wv, beg, end, tl);
+}
+
+template <class W>
+__device__ __forceinline__ W shfl_word(const W& w, int src) {
+  if constexpr (sizeof(W) <= 4) {
+    return static_cast<W>(__shfl_sync(kFull, static_cast<uint32_t>(w), src));
+  } else if constexpr (sizeof(W) == 8) {
+    return static_cast<W>(shfl64(static_cast<uint64_t>(w), src));
+  } else {
+    W r;
+    r.c = shfl64(w.c, src);
+    r.s = shfl64(w.s, src);
+    return r;
+  }
+}
+
+// 32 single-segment hubs: the lanes test them together (and fetch their
+// ranges), the warp streams the live ones.
+template <class W>
+__device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
+                             uint64_t block, LccTally& tl) {
+  const unsigned lane = lane_id();
+  const uint64_t i = g.n_heavy + block * 32 + lane;
+  uint4 sd = make_uint4(0, 0, 0, 0);
+  W wv = Pack<W>::zero();
+  uint64_t beg = 0, end = 0;
+  bool live = false;
+  if (i < g.n_seg) {
+    sd = g.seg[i];
+    const uint8_t sch = st.sch[sd.x];
+    wv = st.vs[sd.x];
+    beg = g.off[sd.x];  // single segment: the whole list
+    end = g.off[sd.x + 1];
+    live = sch && Pack<W>::cand(wv) != 0;
+  }
+  for (unsigned m = __ballot_sync(kFull, live); m; m &= m - 1) {
+    const int j = __ffs(m) - 1;
+    const uint4 s = make_uint4(__shfl_sync(kFull, sd.x, j), 0u, 1u, 0u);
+    lcc_segment(g, st, t, lw, acc, s, shfl_word(wv, j), shfl64(beg, j), shfl64(end, j), tl);
+  }
+}
+
+// One tile of 32 consecutive vertices (light ones only).
+template <class W>
+__device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, uint64_t v0,
+                         LccTally& tl) {
+  const unsigned lane = lane_id();
+  const uint64_t vv = v0 + lane;
+  const uint32_t v = static_cast<uint32_t>(vv);
+  bool work = false;
+  W wv = Pack<W>::zero();
+  uint64_t b = 0;
+  uint32_t len = 0;
+  if (vv < g.V) {
+    // Independent loads in one round.
+    const uint8_t sch = st.sch[v];
+    wv = st.vs[v];
+    b = g.off[v];
+    const uint64_t deg = g.off[v + 1] - b;
+    if (sch && Pack<W>::cand(wv) && (g.n_seg == 0 || deg <= g.hub_degree)) {
+      work = true;
+      len = static_cast<uint32_t>(deg);
+    }
+  }
+  const unsigned wm = __ballot_sync(kFull, work);
+  if (!wm) return;
+  const uint64_t cu = work ? Pack<W>::cand(wv) : 0;
+  const uint32_t su = Pack<W>::slot(wv);
+  uint64_t ncs, need;
+  role_unions(t, cu, &ncs, &need);
+  const uint64_t slots = warp_or64(need);
+  const uint32_t n_slots = __popcll(slots);
+  if (n_slots > kHubRanks) {
+    for (unsigned m = wm; m; m &= m - 1)
+      lcc_vertex_warp(g, st, t, static_cast<uint32_t>(v0 + __ffs(m) - 1), tl);
+    return;
+  }
+  set_ranks(lw, slots, n_slots);
+  // Stream index i belongs to the lane j with excl_j <= i < excl_j + len_j,
+  // at CSR entry base_j + i.  Totals stay below 2^31 (hub_degree <= 2^26).
+  uint32_t incl = len;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, incl, d);
+    if (lane >= static_cast<unsigned>(d)) incl += y;
+  }
+  const uint32_t excl = incl - len;
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  const uint64_t base = b - excl;
+  uint32_t elim_me = 0;
+  for (uint32_t c = 0; c < total; c += 32 * kUnroll) {
+    uint64_t e[kUnroll];
+    uint32_t own[kUnroll];
+    bool in[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const uint32_t i = c + 32 * u + lane;
+      in[u] = i < total;
+      uint32_t lo = 0;
+#pragma unroll
+      for (uint32_t step = 16; step; step >>= 1) {
+        const uint32_t x = __shfl_sync(kFull, excl, lo + step);
+        if (x <= i) lo += step;
+      }
+      own[u] = lo;
+      e[u] = shfl64(base, lo) + i;
+    }
+    uint32_t aw[kUnroll], nb[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      aw[u] = in[u] ? st.lt[e[u] >> 5] : 0u;
+      nb[u] = in[u] ? g.adj[e[u]] : 0u;
+    }
+    W ww[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) ww[u] = ((aw[u] >> (e[u] & 31)) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const bool act = (aw[u] >> (e[u] & 31)) & 1u;
+      tl.gathered += act;
+      const uint64_t cw = Pack<W>::cand(ww[u]);
+      const uint64_t own_ncs = shfl64(ncs, own[u]);
+      const bool live = cw != 0;  // entries outside lt gathered zero
+      const bool poss = live && (cw & own_ncs) != 0;
+      const bool el = live && !poss;
+      if (el) atomicAnd(st.eact + (e[u] >> 5), ~(1u << (e[u] & 31)));
+      if (act && !poss) atomicAnd(st.lt + (e[u] >> 5), ~(1u << (e[u] & 31)));
+      const int64_t s0 = static_cast<int64_t>(c) + 32 * u;
+      const uint32_t mine = lane_range(static_cast<int64_t>(excl) - s0, static_cast<int64_t>(excl) + len - s0);
+      elim_me += __popc(__ballot_sync(kFull, el) & mine);
+      const uint32_t sw = Pack<W>::slot(ww[u]);
+      const uint32_t r = (poss && sw < 64) ? lw.rank_of[sw] : kNoRank;
+      const uint32_t key = r != kNoRank ? (own[u] << 8 | r) : (0x10000u | lane);
+      const uint32_t grp = __match_any_sync(kFull, key);
+      if (r != kNoRank && lane == static_cast<unsigned>(__ffs(grp) - 1)) lw.cnt[r][own[u]] += __popc(grp);
+      __syncwarp();
+    }
+  }
+  if (work) {
+    const uint64_t tu = failing_roles(t, cu, su, slots, [&](uint32_t rank) { return lw.cnt[rank][lane]; });
+    lcc_record(st, v, tu, elim_me, tl.newly_modified);
+    tl.edge_elim += elim_me;
+  }
+  if (lane == 0) tl.streamed += total;
+}
+
+// Sweep 1 in two launches with their own register budgets: kTiles false
+// runs the hub segments (single- and multi-segment hubs), kTiles true the
+// tiles of light vertices.
+template <class W, bool kTiles>
+__global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph g, DevState<W> st,
+                                                                        const QueryTables* __restrict__ qt,
+                                                                        HubAcc* hub_acc, StepCounters* ctr) {
+  __shared__ LccTables t;
+  __shared__ LccWarp s_lw[kLccWarps];
+  load_lcc_tables(t, qt, qt->k);
+  LccWarp& lw = s_lw[threadIdx.x >> 5];
+  const uint64_t heavy = g.n_heavy;
+  const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  const uint64_t n_tasks = kTiles ? (static_cast<uint64_t>(g.V) + 31) / 32 : batched;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  LccTally tl;
+  for (uint64_t task = warp; task < n_tasks; task += n_warps) {
+    if (kTiles)
+      lcc_tile(g, st, t, lw, task * 32, tl);
+    else if (task < heavy)
+      lcc_heavy(g, st, t, lw, hub_acc, task, tl);
+    else
+      lcc_segments(g, st, t, lw, hub_acc, task - heavy, tl);
+  }
+  const uint32_t ee = __reduce_add_sync(kFull, tl.edge_elim);
+  const uint32_t nm = __reduce_add_sync(kFull, tl.newly_modified);
+  const uint32_t ga = __reduce_add_sync(kFull, tl.gathered);
+  if (lane_id() == 0) {
+    if (ee) atomicAdd(&ctr->edge_elim, static_cast<unsigned long long>(ee));
+    if (nm) atomicAdd(&ctr->modified_total, static_cast<unsigned long long>(nm));
+    if (ga) atomicAdd(&ctr->gathered, static_cast<unsigned long long>(ga));
+    if (tl.streamed) atomicAdd(&ctr->scanned, static_cast<unsigned long long>(tl.streamed));
   }
 }
 
 // ---- sweep 2 (LCC and NLCC) -------------------------------------------
+//
+// Applies the roles to unmatch and recomputes the schedule (lcc :107-141,
+// cc :134-173): a vertex is scheduled when it was modified, or when an
+// active CSR entry leads to a modified vertex.  Same task list as sweep 1:
+// hub segments are scanned for such a neighbour (a hub with several
+// segments gets its flag from the last one to finish); tiles do the rest.
+// Scans hub segment sd for an active entry to a modified vertex; a hub
+// with several segments gets its flag from the last segment to finish.
 template <class W>
-__global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, StepCounters* ctr) {
+__device__ void apply_segment(const DevGraph& g, const DevState<W>& st, HubAcc* acc, const uint4 sd) {
   const unsigned lane = lane_id();
-  const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
-  const bool any_modified = *reinterpret_cast<volatile unsigned long long*>(&ctr->modified_total) != 0;
-  unsigned me = 0, ve = 0;
-  for (uint64_t tile = warp * 32; tile < g.V; tile += n_warps * 32) {
-    const uint64_t v = tile + lane;
-    bool scan = false;
-    if (v < g.V) {
-      const W w = st.vs[v];
-      const uint64_t c = Pack<W>::cand(w);
-      if (c) {
-        if (st.mod[v]) {
-          const uint64_t tu = Pack<W>::cand(st.unm[v]);
-          if (tu) {
-            me += __popcll(tu);
-            const uint64_t nc = c & ~tu;
-            st.vs[v] = Pack<W>::make(nc, Pack<W>::slot(w));
-            if (!nc) ++ve;
-            st.unm[v] = Pack<W>::zero();
-          }
-          st.sch[v] = 1;
-        } else if (!any_modified) {
-          st.sch[v] = 0;
+  const uint32_t v = sd.x, nseg = sd.z, ai = sd.w;
+  uint64_t beg, end;
+  segment_range(g, sd, &beg, &end);
+  bool found = false;
+  for (uint64_t e0 = beg; e0 < end && !found; e0 += 32) {
+    const uint64_t e = e0 + lane;
+    const bool hit = e < end && edge_active(st.eact, e) && st.mod[g.adj[e]];
+    found = __any_sync(kFull, hit);
+    // Another segment of this hub already found one.
+    if (!found && nseg > 1 && ((e0 - beg) & 255) == 224)
+      found = *reinterpret_cast<volatile uint32_t*>(&acc[ai].hit) != 0;
+  }
+  if (lane == 0) {
+    if (nseg == 1) {
+      st.sch[v] = found ? 1 : 0;
+    } else {
+      if (found) atomicOr(&acc[ai].hit, 1u);
+      __threadfence();
+      const uint32_t done = atomicAdd(&acc[ai].ticket2, 1u);
+      if (done + 1 == nseg) {
+        __threadfence();
+        const uint32_t hit = atomicExch(&acc[ai].hit, 0u);
+        atomicExch(&acc[ai].ticket2, 0u);
+        st.sch[v] = hit ? 1 : 0;
+      }
+    }
+  }
+}
+
+// The tiles own modified hubs (and nothing needs a scan when no vertex was
+// modified); vs[v] is stable here because mod[v] == 0.
+template <class W>
+__device__ __forceinline__ bool apply_needs_scan(const DevState<W>& st, uint32_t v) {
+  return !st.mod[v] && Pack<W>::cand(st.vs[v]) != 0;
+}
+
+template <class W>
+__device__ void apply_segments(const DevGraph& g, const DevState<W>& st, HubAcc* acc, uint64_t block) {
+  const unsigned lane = lane_id();
+  const uint64_t i = g.n_heavy + block * 32 + lane;
+  uint4 sd = make_uint4(0, 0, 0, 0);
+  bool live = false;
+  if (i < g.n_seg) {
+    sd = g.seg[i];
+    live = apply_needs_scan(st, sd.x);
+  }
+  for (unsigned m = __ballot_sync(kFull, live); m; m &= m - 1) {
+    const int j = __ffs(m) - 1;
+    const uint4 s = make_uint4(__shfl_sync(kFull, sd.x, j), __shfl_sync(kFull, sd.y, j), __shfl_sync(kFull, sd.z, j),
+                               __shfl_sync(kFull, sd.w, j));
+    apply_segment(g, st, acc, s);
+  }
+}
+
+template <class W>
+__device__ void apply_tile(const DevGraph& g, const DevState<W>& st, uint64_t tile, bool any_modified, unsigned& me,
+                           unsigned& ve) {
+  const unsigned lane = lane_id();
+  const uint64_t v = tile + lane;
+  bool scan = false;
+  if (v < g.V) {
+    const W w = st.vs[v];
+    const uint64_t c = Pack<W>::cand(w);
+    if (c) {
+      if (st.mod[v]) {
+        const uint64_t tu = Pack<W>::cand(st.unm[v]);
+        if (tu) {
+          me += __popcll(tu);
+          const uint64_t nc = c & ~tu;
+          st.vs[v] = Pack<W>::make(nc, Pack<W>::slot(w));
+          if (!nc) ++ve;
+          st.unm[v] = Pack<W>::zero();
+        }
+        st.sch[v] = 1;
+      } else if (!any_modified) {
+        st.sch[v] = 0;
+      } else {
+        const uint64_t b = g.off[v], e = g.off[v + 1];
+        if (g.n_seg && e - b > g.hub_degree) {
+          // A hub: its segments decide.
+        } else if (e - b <= 8) {
+          // Short lists: the lane scans its own vertex.
+          bool found = false;
+          for (uint64_t x = b; x < e && !found; ++x)
+            if (edge_active(st.eact, x) && st.mod[g.adj[x]]) found = true;
+          st.sch[v] = found;
         } else {
-          const uint64_t b = g.off[v], e = g.off[v + 1];
-          if (e - b <= 8) {
-            // Short lists: the lane scans its own vertex.
-            bool found = false;
-            for (uint64_t x = b; x < e && !found; ++x)
-              if (edge_active(st.eact, x) && st.mod[g.adj[x]]) found = true;
-            st.sch[v] = found;
-          } else {
-            scan = true;
-          }
+          scan = true;
         }
       }
     }
-    unsigned sm = __ballot_sync(kFull, scan);
-    while (sm) {
-      const unsigned j = __ffs(sm) - 1;
-      sm &= sm - 1;
-      const uint32_t u = static_cast<uint32_t>(tile + j);
-      const uint64_t b = g.off[u], e = g.off[u + 1];
-      bool found = false;
-      for (uint64_t e0 = b; e0 < e && !found; e0 += 32) {
-        const uint64_t x = e0 + lane;
-        const bool hit = x < e && edge_active(st.eact, x) && st.mod[g.adj[x]];
-        found = __any_sync(kFull, hit);
-      }
-      if (lane == j) st.sch[u] = found;
+  }
+  unsigned sm = __ballot_sync(kFull, scan);
+  while (sm) {
+    const unsigned j = __ffs(sm) - 1;
+    sm &= sm - 1;
+    const uint64_t u = tile + j;
+    const uint64_t b = g.off[u], e = g.off[u + 1];
+    bool found = false;
+    for (uint64_t e0 = b; e0 < e && !found; e0 += 32) {
+      const uint64_t x = e0 + lane;
+      const bool hit = x < e && edge_active(st.eact, x) && st.mod[g.adj[x]];
+      found = __any_sync(kFull, hit);
+    }
+    if (lane == j) st.sch[u] = found;
+  }
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, HubAcc* hub_acc, StepCounters* ctr) {
+  const bool any_modified = *reinterpret_cast<volatile unsigned long long*>(&ctr->modified_total) != 0;
+  const uint64_t heavy = g.n_heavy;
+  const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  const uint64_t n_tasks = batched + (static_cast<uint64_t>(g.V) + 31) / 32;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned me = 0, ve = 0;
+  for (uint64_t task = warp; task < n_tasks; task += n_warps) {
+    if (task < heavy) {
+      const uint4 sd = g.seg[task];
+      if (any_modified && apply_needs_scan(st, sd.x)) apply_segment(g, st, hub_acc, sd);
+    } else if (task < batched) {
+      if (any_modified) apply_segments(g, st, hub_acc, task - heavy);
+    } else {
+      apply_tile(g, st, (task - batched) * 32, any_modified, me, ve);
     }
   }
   me = __reduce_add_sync(kFull, me);
   ve = __reduce_add_sync(kFull, ve);
-  if (lane == 0) {
+  if (lane_id() == 0) {
     if (me) atomicAdd(&ctr->match_elim, static_cast<unsigned long long>(me));
     if (ve) atomicAdd(&ctr->vertex_elim, static_cast<unsigned long long>(ve));
   }
@@ -367,7 +879,7 @@ __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st,
 
 template <class W>
 DevState<W> state_of(const QueryDevPtrs& q) {
-  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm)};
+  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt};
 }
 
 #define PM_DISPATCH_WORD(kind, ...)            \
@@ -416,14 +928,36 @@ void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
   PM_DISPATCH_WORD(q.word_kind, k_lcc0<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.ctr));
 }
 
+// Blocks for n_tasks one-warp tasks: at most `per_sm` resident blocks per SM.
+// Sweep tasks: segments of multi-segment hubs, blocks of 32 single-segment
+// hubs, tiles of 32 vertices.
+inline uint64_t sweep_tasks(const DevGraph& g) {
+  return g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32 + (static_cast<uint64_t>(g.V) + 31) / 32;
+}
+
+inline int grid_for_tasks(uint64_t n_tasks, int per_sm) {
+  uint64_t blocks = (n_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const uint64_t cap = static_cast<uint64_t>(device_sm_count()) * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return static_cast<int>(blocks);
+}
+
 void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
-  const int grid = grid_for_tiles(g.V, 8);
-  PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.ctr));
+  const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  if (hub_tasks) {
+    const int grid = grid_for_tasks(hub_tasks, 5);
+    PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W, false><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables,
+                                                                                   q.hub_acc, q.ctr));
+  }
+  const int grid = grid_for_tasks((static_cast<uint64_t>(g.V) + 31) / 32, 4);
+  PM_DISPATCH_WORD(q.word_kind,
+                   k_lcc_check<W, true><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.hub_acc, q.ctr));
 }
 
 void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
-  const int grid = grid_for_tiles(g.V, 8);
-  PM_DISPATCH_WORD(q.word_kind, k_apply<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.ctr));
+  const int grid = grid_for_tasks(sweep_tasks(g), 8);
+  PM_DISPATCH_WORD(q.word_kind, k_apply<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.hub_acc, q.ctr));
 }
 
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, uint32_t* wl, uint32_t* wl_index,

@@ -5,10 +5,12 @@
     python -m pattenmatching_sharedmemory_gb300.profile_case lcc22 [--scale S]
         LCC0 and the LCC fixpoint on RMAT scale S (default 22, 16 Zipf
         labels, two-cycle template on labels 0..5): the HBM-bound kernels
-        k_lcc_check / k_apply on a CSR larger than L2
+        k_lcc_check / k_apply on a CSR larger than L2; --hub-degree and
+        --seg-entries set the LCC degree classes
 
-Prints one line per step with its CUDA-event time and its eliminated
-vertices / CSR entries.
+Prints one line per step with its CUDA-event time, its eliminated vertices /
+CSR entries and, for LCC, the CSR entries of the lists its sweep checked and
+how many of them it read a neighbour word for.
 """
 from __future__ import annotations
 
@@ -24,6 +26,8 @@ def main() -> int:
     ap.add_argument("case", choices=["c1", "lcc22"])
     ap.add_argument("--queries", type=int, default=1)
     ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--hub-degree", type=int, default=None, help="LCC hub threshold (CSR entries)")
+    ap.add_argument("--seg-entries", type=int, default=2048, help="CSR entries per hub segment")
     a = ap.parse_args()
     if a.case == "c1":
         g = pm.Graph.rmat(16, 16, seed=1).assign_labels("uniform", 5, 1.0, 1).to_device(0)
@@ -35,11 +39,17 @@ def main() -> int:
             q.close()
         return 0
     g = pm.Graph.rmat(a.scale, 16, seed=1).assign_labels("zipf", 16, 1.0, 1).to_device(0)
+    if a.hub_degree is not None:
+        g.set_hub_plan(a.hub_degree, a.seg_entries)
     q = pm.Query(g, pattern=T.two_cycles_sharing_edge([0, 1, 2, 3, 4, 5]))
+    row = 0
     while True:
         rec, fin = q.step()
         name = pm.STEP_NAMES[rec.step]
-        print(name, f"{rec.step_ms:.3f} ms", rec.results.vertex_eliminated, rec.results.edge_eliminated)
+        streamed, gathered = q.step_walk_stats(row)
+        row += 1
+        print(name, f"{rec.step_ms:.3f} ms", rec.results.vertex_eliminated, rec.results.edge_eliminated,
+              f"listed={streamed} gathered={gathered} active_v={rec.active_vertex} active_e={rec.active_edge}")
         if name == "LCC" and rec.results.vertex_eliminated == 0 and rec.results.edge_eliminated == 0 and \
                 rec.results.match_eliminated == 0:
             break

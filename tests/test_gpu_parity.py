@@ -124,3 +124,59 @@ def test_queries_share_one_resident_graph():
     assert a["rows"] == case["rows"] and b["rows"] == other["rows"]
     if c is not None:
         assert c["rows"] == other["rows"]
+
+
+# LCC degree classes: (hub_degree, seg_entries).  (0, 32) makes every vertex
+# with an edge a hub, most of them with several 32-entry segments; the others
+# mix light tiles with multi-segment hubs.  The plan changes speed only.
+HUB_PLANS = [(0, 32), (4, 32), (16, 64), (64, 128), (8, 1024)]
+HUB_PLAN_CASES = ["scale12_tds", "two_cycles_zipf_s10", "path4_rep_s9", "degree_labels_s10"]
+
+
+@pytest.mark.parametrize("plan", HUB_PLANS, ids=lambda p: f"h{p[0]}_s{p[1]}")
+@pytest.mark.parametrize("name", HUB_PLAN_CASES)
+def test_hub_plan_outputs_identical(name, plan):
+    case = next(c for c in SYNTH if c["name"] == name)
+    g = C.make_graph(case).to_device(0)
+    g.set_hub_plan(*plan)
+    res = pmtest.product_run(g, pattern=C.make_pattern(case))
+    assert res["rows"] == case["rows"]
+    assert pmtest.sha(res["vertex"]) == case["vertex_sha256"]
+    assert pmtest.sha(res["graph"]) == case["graph_sha256"]
+
+
+@pytest.mark.parametrize("plan", [None, (4, 32)], ids=["default", "h4_s32"])
+def test_many_needed_slots_matches_oracle(plan):
+    """A 17-leaf star with distinct labels needs 17 label slots counted per
+    vertex: more than the per-owner counters, so light tiles and hubs take the
+    whole-list warp path.  Pruning rows and the final state equal the
+    oracle's."""
+    g = C.make_graph({"graph": C.graph_params(10, ef=16, n_labels=20, label_seed=77)}).to_device(0)
+    if plan:
+        g.set_hub_plan(*plan)
+    p = pm.Pattern.from_edges(18, [(0, i) for i in range(1, 18)], list(range(18)))
+    off, adj, lab = g.host_csr()
+    ref = oracle.run(off, adj, lab, p.offsets, p.adj, p.labels, threads=1, stop_before_enumeration=True)
+    q = pm.Query(g, pattern=p)
+    rows = [r.as_tuple() for r in q.run()]
+    assert rows[:-2] == ref.rows[:-1]
+    cand, eact, vact = q.export()
+    assert np.array_equal(cand, ref.cand)
+    assert np.array_equal(eact, ref.eact)
+    assert np.array_equal(vact, ref.vact)
+
+
+def test_hub_plan_change_with_live_query():
+    """A plan that adds hubs after a query was created: the query's hub
+    accumulators grow before its next step and results stay exact."""
+    case = next(c for c in SYNTH if c["name"] == "scale12_tds")
+    g = C.make_graph(case).to_device(0)
+    g.set_hub_plan(1 << 26, 1024)  # no hubs
+    q = pm.Query(g, pattern=C.make_pattern(case))
+    first, fin = q.step()
+    g.set_hub_plan(2, 32)
+    rows = [list(first.as_tuple())]
+    while not fin:
+        rec, fin = q.step()
+        rows.append(list(rec.as_tuple()))
+    assert rows == case["rows"][:-1]
