@@ -180,6 +180,94 @@ pm_status_t pm_query_estimate_bytes(const pm_graph* g, uint32_t p_vertex_count,
 
 void pm_query_destroy(pm_query* q);
 
+/* ---- Serving and batching ------------------------------------------------
+ *
+ * No counterpart in the reference, which runs one template per process
+ * (MultipleLabelCpu::runPatternMatching, multiple_label_cpu.cc:113-184).
+ * A server keeps one graph resident and runs submitted template queries on
+ * `slots` GPU slots at once (each slot: a host thread with its own CUDA
+ * stream).  Requests wait in FIFO order until a slot is free and the device
+ * bytes they are charged (pm_query_estimate_bytes) fit under the memory
+ * budget beside the running ones; requests that arrive while others run are
+ * admitted as slots and memory free up (continuous batching).  Each request
+ * runs the whole pipeline, LCC0 to ENUMERATION, with the same results as
+ * pm_query_run on its own. */
+typedef struct pm_server pm_server;
+
+typedef struct pm_server_config {
+  uint32_t slots;         /* queries on the GPU at once, >= 1 */
+  uint64_t memory_budget; /* device bytes for admitted queries; 0 = 90% of free memory */
+} pm_server_config;
+
+/* pm_server_submit flag: keep the final state for pm_server_export. */
+#define PM_SUBMIT_EXPORT_STATE 1u
+
+typedef struct pm_request_result {
+  int32_t status;          /* PM_SUCCESS, or the request's error code */
+  int32_t n_records;       /* results.totem rows (END included) */
+  uint64_t match_count;    /* ENUMERATION row */
+  double queue_ms;         /* submission to admission */
+  double run_ms;           /* admission to completion */
+  double latency_ms;       /* submission to completion */
+  double gpu_ms;           /* sum of the step times */
+  uint64_t charged_bytes;  /* device bytes charged at admission */
+} pm_request_result;
+
+typedef struct pm_server_stats {
+  uint64_t queued, running, done;
+  uint64_t bytes_in_use, peak_bytes, memory_budget;
+  uint32_t slots;
+} pm_server_stats;
+
+/* The graph must stay alive (and on its device) until pm_server_destroy. */
+pm_status_t pm_server_create(pm_graph* g, const pm_server_config* config, pm_server** out);
+
+/* Queues a template (CSR, as pm_query_create_from_csr); *ticket names it.
+ * PM_E_ADMISSION_DENIED when its charge exceeds the whole budget. */
+pm_status_t pm_server_submit(pm_server* s, const uint64_t* p_offsets, const uint32_t* p_adj,
+                             const uint64_t* p_labels, uint32_t p_vertex_count,
+                             uint64_t p_edge_count, uint32_t flags, uint64_t* ticket);
+
+/* *done = 1 and *result filled once the request finished (result may be
+ * NULL); *done = 0 while it is queued or running. */
+pm_status_t pm_server_poll(pm_server* s, uint64_t ticket, int* done, pm_request_result* result);
+
+/* Blocks until the request finished or timeout_ms passed (< 0: no limit);
+ * PM_E_TIMEOUT when it has not finished in time. */
+pm_status_t pm_server_wait(pm_server* s, uint64_t ticket, double timeout_ms,
+                           pm_request_result* result);
+
+/* The finished request's results.totem rows (as pm_query_run). */
+pm_status_t pm_server_records(pm_server* s, uint64_t ticket, pm_step_record* records,
+                              int32_t cap, int32_t* n_records);
+
+/* The finished request's final state (as pm_query_export); the request must
+ * have been submitted with PM_SUBMIT_EXPORT_STATE. */
+pm_status_t pm_server_export(pm_server* s, uint64_t ticket, uint64_t* cand_masks,
+                             uint8_t* edge_active, uint8_t* vertex_active);
+
+/* Forgets a finished request (its rows and state). */
+pm_status_t pm_server_release(pm_server* s, uint64_t ticket);
+
+pm_status_t pm_server_stats_get(pm_server* s, pm_server_stats* stats);
+
+/* Queued requests end with PM_E_CANCELLED; running ones finish first. */
+void pm_server_destroy(pm_server* s);
+
+/* Runs n templates over graph g on `slots` GPU slots (a server with the
+ * default budget): templates[i] is template i in CSR form.  Writes each
+ * template's match count and status. */
+typedef struct pm_template_csr {
+  const uint64_t* offsets;
+  const uint32_t* adj;
+  const uint64_t* labels;
+  uint32_t vertex_count;
+  uint64_t edge_count;
+} pm_template_csr;
+
+pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t slots,
+                         uint64_t* match_counts, int32_t* statuses);
+
 /* Allocation-free ENUMERATION.  No counterpart in the reference: it serves
  * callers that cannot allocate device memory (code running inside a host
  * framework that owns every device allocation through its own pool or arena,

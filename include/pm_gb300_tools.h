@@ -53,6 +53,14 @@ uint64_t pm_kernel_launches(void);
  * (host gaps between steps included). */
 pm_status_t pm_query_elapsed_ms(const pm_query* q, double* ms);
 
+/* ENUMERATION overflow policy (process-wide; speed only, never results): a
+ * source whose count memo overflowed with `after_levels` levels of 8x larger
+ * tables is split into up to `parts` slices of its first hop, run by
+ * separate warps with base-size tables (parts <= 1: never split); a slice
+ * that overflows again grows its tables.  Defaults 16 and 0.  Set it while
+ * no query runs. */
+pm_status_t pm_set_enum_split(uint32_t parts, uint32_t after_levels);
+
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with
  * PM_E_TIMEOUT and the query's state is no longer meaningful. */

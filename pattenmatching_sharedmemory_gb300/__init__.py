@@ -49,6 +49,33 @@ class AlgoResults(ctypes.Structure):
                 ("match_eliminated", ctypes.c_uint64), ("enumeration", ctypes.c_uint64)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+
+
+class RequestResult(ctypes.Structure):
+    """pm_request_result: outcome and timings of one served request."""
+
+    _fields_ = [("status", ctypes.c_int32), ("n_records", ctypes.c_int32), ("match_count", ctypes.c_uint64),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("gpu_ms", ctypes.c_double), ("charged_bytes", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_uint64), ("running", ctypes.c_uint64), ("done", ctypes.c_uint64),
+                ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("memory_budget", ctypes.c_uint64), ("slots", ctypes.c_uint32)]
+
+
+class TemplateCsr(ctypes.Structure):
+    _fields_ = [("offsets", ctypes.POINTER(ctypes.c_uint64)), ("adj", ctypes.POINTER(ctypes.c_uint32)),
+                ("labels", ctypes.POINTER(ctypes.c_uint64)), ("vertex_count", ctypes.c_uint32),
+                ("edge_count", ctypes.c_uint64)]
+
+
+PM_SUBMIT_EXPORT_STATE = 1
+
+
 class StepRecord(ctypes.Structure):
     """One results.totem row (pm_step_record)."""
 
@@ -111,9 +138,23 @@ def _load_library() -> ctypes.CDLL:
         "pm_kernel_launches": (ctypes.c_uint64, []),
         "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
+        "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
                                                           ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
         "pm_query_destroy": (None, [ctypes.c_void_p]),
+        "pm_server_create": (ctypes.c_int32, [ctypes.c_void_p, P(ServerConfig), P(ctypes.c_void_p)]),
+        "pm_server_submit": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, c_u64p, ctypes.c_uint32,
+                                              ctypes.c_uint64, ctypes.c_uint32, c_u64p]),
+        "pm_server_poll": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, P(ctypes.c_int), P(RequestResult)]),
+        "pm_server_wait": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, P(RequestResult)]),
+        "pm_server_records": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, P(StepRecord), ctypes.c_int32,
+                                               P(ctypes.c_int32)]),
+        "pm_server_export": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, c_u64p, c_u8p, c_u8p]),
+        "pm_server_release": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64]),
+        "pm_server_stats_get": (ctypes.c_int32, [ctypes.c_void_p, P(ServerStats)]),
+        "pm_server_destroy": (None, [ctypes.c_void_p]),
+        "pm_batch_run": (ctypes.c_int32, [ctypes.c_void_p, P(TemplateCsr), ctypes.c_uint32, ctypes.c_uint32,
+                                          c_u64p, P(ctypes.c_int32)]),
         # Device buffers (d_*) and the stream are passed as raw addresses.
         "pm_enumerate_noalloc": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                                   ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
@@ -383,6 +424,98 @@ class Query:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous batching of template queries over one resident graph
+    (pm_server_*): `slots` queries run on the GPU at once, admitted in FIFO
+    order as slots and the device-memory budget allow."""
+
+    def __init__(self, graph: Graph, slots: int = 4, memory_budget: int = 0):
+        self.graph = graph
+        self._h = ctypes.c_void_p()
+        cfg = ServerConfig(slots, memory_budget)
+        _check(lib.pm_server_create(graph._h, ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    def submit(self, pattern: Pattern, export_state: bool = False) -> int:
+        off = np.ascontiguousarray(pattern.offsets, np.uint64)
+        adj = np.ascontiguousarray(pattern.adj, np.uint32)
+        lab = np.ascontiguousarray(pattern.labels, np.uint64)
+        t = ctypes.c_uint64()
+        flags = PM_SUBMIT_EXPORT_STATE if export_state else 0
+        _check(lib.pm_server_submit(self._h, _ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32),
+                                    _ptr(lab, ctypes.c_uint64), pattern.n, len(adj), flags, ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int) -> RequestResult | None:
+        done = ctypes.c_int()
+        r = RequestResult()
+        _check(lib.pm_server_poll(self._h, ticket, ctypes.byref(done), ctypes.byref(r)))
+        return r if done.value else None
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0) -> RequestResult:
+        r = RequestResult()
+        _check(lib.pm_server_wait(self._h, ticket, timeout_ms, ctypes.byref(r)))
+        return r
+
+    def records(self, ticket: int) -> list[StepRecord]:
+        n = ctypes.c_int32()
+        _check(lib.pm_server_records(self._h, ticket, None, 0, ctypes.byref(n)))
+        recs = (StepRecord * max(n.value, 1))()
+        _check(lib.pm_server_records(self._h, ticket, recs, n.value, ctypes.byref(n)))
+        return [recs[i] for i in range(n.value)]
+
+    def export(self, ticket: int):
+        V, E = self.graph.vertex_count, self.graph.edge_count
+        cand = np.zeros(V, np.uint64)
+        eact = np.zeros(E, np.uint8)
+        vact = np.zeros(V, np.uint8)
+        _check(lib.pm_server_export(self._h, ticket, _ptr(cand, ctypes.c_uint64), _ptr(eact, ctypes.c_uint8),
+                                    _ptr(vact, ctypes.c_uint8)))
+        return cand, eact, vact
+
+    def release(self, ticket: int) -> None:
+        _check(lib.pm_server_release(self._h, ticket))
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(lib.pm_server_stats_get(self._h, ctypes.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if self._h:
+            lib.pm_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_run(graph: Graph, patterns, slots: int = 4):
+    """pm_batch_run: every template's match count and status, `slots` at a time."""
+    keep = []
+    arr = (TemplateCsr * max(len(patterns), 1))()
+    for i, p in enumerate(patterns):
+        off = np.ascontiguousarray(p.offsets, np.uint64)
+        adj = np.ascontiguousarray(p.adj, np.uint32)
+        lab = np.ascontiguousarray(p.labels, np.uint64)
+        keep += [off, adj, lab]
+        arr[i] = TemplateCsr(_ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32), _ptr(lab, ctypes.c_uint64),
+                             p.n, len(adj))
+    counts = np.zeros(len(patterns), np.uint64)
+    statuses = np.zeros(len(patterns), np.int32)
+    _check(lib.pm_batch_run(graph._h, arr, len(patterns), slots, _ptr(counts, ctypes.c_uint64),
+                            _ptr(statuses, ctypes.c_int32)))
+    return counts, statuses
 
 
 def version() -> str:

@@ -32,13 +32,13 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels_lcc.cu", "kernels_walk.cu"]
-CC_SOURCES = ["totem_io.cc", "constraints.cc", "walk_compile.cc", "generators.cc", "engine.cc", "capi.cc"]
-CC_EXTRA = ["server.cc"]  # compiled when present
+CC_SOURCES = ["totem_io.cc", "constraints.cc", "walk_compile.cc", "generators.cc", "engine.cc", "server.cc",
+              "capi.cc"]
 
 
 def _sources() -> tuple[list[Path], list[Path]]:
     cu = [CSRC / s for s in CU_SOURCES]
-    cc = [CSRC / s for s in CC_SOURCES] + [CSRC / s for s in CC_EXTRA if (CSRC / s).exists()]
+    cc = [CSRC / s for s in CC_SOURCES]
     return cu, cc
 
 

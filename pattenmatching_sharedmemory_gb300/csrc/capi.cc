@@ -6,6 +6,7 @@
 #include "../../include/pm_gb300_tools.h"
 #include "engine.h"
 #include "generators.h"
+#include "server.h"
 #include "totem_io.h"
 
 using namespace pmgb;
@@ -15,6 +16,9 @@ struct pm_graph {
 };
 struct pm_query {
   QueryImpl impl;
+};
+struct pm_server {
+  std::unique_ptr<Server> impl;
 };
 
 namespace {
@@ -314,6 +318,11 @@ pm_status_t pm_graph_set_hub_plan(pm_graph* g, uint32_t hub_degree, uint32_t seg
   });
 }
 
+pm_status_t pm_set_enum_split(uint32_t parts, uint32_t after_levels) {
+  set_enum_split(parts, after_levels);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));
@@ -369,6 +378,181 @@ pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint6
 }
 
 void pm_query_destroy(pm_query* q) { delete q; }
+
+namespace {
+PatternGraph pattern_from_csr(const uint64_t* p_offsets, const uint32_t* p_adj, const uint64_t* p_labels,
+                              uint32_t p_vertex_count, uint64_t p_edge_count) {
+  if (!p_offsets || (!p_adj && p_edge_count)) throw PmError{PM_E_INVALID_ARG, "null template buffer"};
+  if (p_offsets[p_vertex_count] != p_edge_count)
+    throw PmError{PM_E_INVALID_ARG, "pattern offsets do not end at the edge count"};
+  for (uint64_t e = 0; e < p_edge_count; ++e)
+    if (p_adj[e] >= p_vertex_count) throw PmError{PM_E_INVALID_ARG, "pattern edge out of range"};
+  if (p_vertex_count > 64) throw PmError{PM_E_PATTERN_TOO_LARGE, "templates of more than 64 vertices"};
+  PatternGraph p;
+  p.n = p_vertex_count;
+  p.offsets.assign(p_offsets, p_offsets + p_vertex_count + 1);
+  p.adj.assign(p_adj, p_adj + p_edge_count);
+  p.labels = p_labels ? std::vector<uint64_t>(p_labels, p_labels + p_vertex_count)
+                      : std::vector<uint64_t>(p_vertex_count, 0);
+  return p;
+}
+
+double ms_between(ServeRequest::Clock::time_point a, ServeRequest::Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+void fill_result(const ServeRequest& r, pm_request_result* out) {
+  if (!out) return;
+  out->status = r.status;
+  out->n_records = static_cast<int32_t>(r.records.size());
+  out->match_count = r.match_count;
+  const bool admitted = r.t_admit.time_since_epoch().count() != 0;
+  out->queue_ms = admitted ? ms_between(r.t_submit, r.t_admit) : ms_between(r.t_submit, r.t_done);
+  out->run_ms = admitted ? ms_between(r.t_admit, r.t_done) : 0.0;
+  out->latency_ms = ms_between(r.t_submit, r.t_done);
+  out->gpu_ms = r.gpu_ms;
+  out->charged_bytes = r.bytes;
+}
+
+std::shared_ptr<ServeRequest> finished_request(pm_server* s, uint64_t ticket) {
+  bool done = false;
+  auto r = s->impl->find(ticket, &done);
+  if (!r) throw PmError{PM_E_INVALID_ARG, "unknown ticket"};
+  if (!done) throw PmError{PM_E_BUSY, "request still queued or running"};
+  return r;
+}
+}  // namespace
+
+pm_status_t pm_server_create(pm_graph* g, const pm_server_config* config, pm_server** out) {
+  PM_REQUIRE(g && config && out, "null argument");
+  PM_REQUIRE(config->slots >= 1, "slots must be at least 1");
+  return guarded([&]() -> pm_status_t {
+    g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    auto* s = new pm_server();
+    try {
+      s->impl = std::make_unique<Server>(&g->impl, config->slots, config->memory_budget);
+    } catch (...) {
+      delete s;
+      throw;
+    }
+    *out = s;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_submit(pm_server* s, const uint64_t* p_offsets, const uint32_t* p_adj,
+                             const uint64_t* p_labels, uint32_t p_vertex_count, uint64_t p_edge_count,
+                             uint32_t flags, uint64_t* ticket) {
+  PM_REQUIRE(s && ticket, "null argument");
+  return guarded([&]() -> pm_status_t {
+    *ticket = s->impl->submit(pattern_from_csr(p_offsets, p_adj, p_labels, p_vertex_count, p_edge_count), flags);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_poll(pm_server* s, uint64_t ticket, int* done, pm_request_result* result) {
+  PM_REQUIRE(s && done, "null argument");
+  return guarded([&]() -> pm_status_t {
+    bool d = false;
+    auto r = s->impl->find(ticket, &d);
+    if (!r) throw PmError{PM_E_INVALID_ARG, "unknown ticket"};
+    *done = d ? 1 : 0;
+    if (d) fill_result(*r, result);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_wait(pm_server* s, uint64_t ticket, double timeout_ms, pm_request_result* result) {
+  PM_REQUIRE(s, "server is NULL");
+  return guarded([&]() -> pm_status_t {
+    if (!s->impl->wait(ticket, timeout_ms)) return fail(PM_E_TIMEOUT, "request not finished within the timeout");
+    fill_result(*finished_request(s, ticket), result);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_records(pm_server* s, uint64_t ticket, pm_step_record* records, int32_t cap,
+                              int32_t* n_records) {
+  PM_REQUIRE(s, "server is NULL");
+  return guarded([&]() -> pm_status_t {
+    auto r = finished_request(s, ticket);
+    const int32_t n = static_cast<int32_t>(r->records.size());
+    for (int32_t i = 0; records && i < n && i < cap; ++i) records[i] = r->records[i];
+    if (n_records) *n_records = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_export(pm_server* s, uint64_t ticket, uint64_t* cand_masks, uint8_t* edge_active,
+                             uint8_t* vertex_active) {
+  PM_REQUIRE(s, "server is NULL");
+  return guarded([&]() -> pm_status_t {
+    auto r = finished_request(s, ticket);
+    if (!(r->flags & kSubmitExportState)) return fail(PM_E_INVALID_ARG, "request was not submitted with PM_SUBMIT_EXPORT_STATE");
+    if (r->status != PM_SUCCESS) return fail(r->status, "request failed: " + r->error);
+    if (cand_masks && !r->cand.empty()) memcpy(cand_masks, r->cand.data(), r->cand.size() * 8);
+    if (edge_active && !r->eact.empty()) memcpy(edge_active, r->eact.data(), r->eact.size());
+    if (vertex_active && !r->vact.empty()) memcpy(vertex_active, r->vact.data(), r->vact.size());
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_release(pm_server* s, uint64_t ticket) {
+  PM_REQUIRE(s, "server is NULL");
+  return guarded([&]() -> pm_status_t {
+    s->impl->release(ticket);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_stats_get(pm_server* s, pm_server_stats* stats) {
+  PM_REQUIRE(s && stats, "null argument");
+  return guarded([&]() -> pm_status_t {
+    const ServerStats st = s->impl->stats();
+    stats->queued = st.queued;
+    stats->running = st.running;
+    stats->done = st.done;
+    stats->bytes_in_use = st.bytes_in_use;
+    stats->peak_bytes = st.peak_bytes;
+    stats->memory_budget = st.budget;
+    stats->slots = st.slots;
+    return PM_SUCCESS;
+  });
+}
+
+void pm_server_destroy(pm_server* s) { delete s; }
+
+pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t slots,
+                         uint64_t* match_counts, int32_t* statuses) {
+  PM_REQUIRE(g && (templates || n == 0) && slots >= 1, "bad argument");
+  return guarded([&]() -> pm_status_t {
+    g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    Server server(&g->impl, slots, 0);
+    std::vector<uint64_t> tickets(n, 0);
+    std::vector<int32_t> submit_status(n, PM_SUCCESS);
+    for (uint32_t i = 0; i < n; ++i) {
+      const pm_template_csr& t = templates[i];
+      try {
+        tickets[i] = server.submit(pattern_from_csr(t.offsets, t.adj, t.labels, t.vertex_count, t.edge_count), 0);
+      } catch (const PmError& e) {
+        submit_status[i] = e.code;
+      }
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+      int32_t st = submit_status[i];
+      uint64_t count = 0;
+      if (st == PM_SUCCESS) {
+        server.wait(tickets[i], -1.0);
+        auto r = server.find(tickets[i]);
+        st = r->status;
+        count = r->match_count;
+      }
+      if (match_counts) match_counts[i] = count;
+      if (statuses) statuses[i] = st;
+    }
+    return PM_SUCCESS;
+  });
+}
 
 pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_adj, uint32_t vertex_count,
                                  uint64_t edge_count, int sorted_unique, const uint64_t* d_cand_masks,

@@ -21,7 +21,12 @@ void throw_cuda(cudaError_t e, const char* what) {
 }
 
 void DeviceBuffer::release() {
-  if (ptr) cudaFree(ptr);
+  if (ptr) {
+    if (ordered)
+      cudaFreeAsync(ptr, stream);
+    else
+      cudaFree(ptr);
+  }
   ptr = nullptr;
   bytes = 0;
 }
@@ -30,7 +35,10 @@ void DeviceBuffer::ensure(size_t n) {
   if (n <= bytes && ptr) return;
   release();
   if (n == 0) n = 16;
-  PM_CUDA(cudaMalloc(&ptr, n));
+  if (ordered)
+    PM_CUDA(cudaMallocAsync(&ptr, n, stream));
+  else
+    PM_CUDA(cudaMalloc(&ptr, n));
   bytes = n;
 }
 
@@ -60,6 +68,13 @@ void GraphImpl::to_device(int dev) {
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
     throw PmError{PM_E_NO_DEVICE, "no CUDA device available for the GB300 pruning kernels"};
   PM_CUDA(cudaSetDevice(dev));
+  // Queries allocate stream-ordered from the device's default pool; keep
+  // freed blocks in the pool for the next query instead of returning them.
+  cudaMemPool_t mempool;
+  if (cudaDeviceGetDefaultMemPool(&mempool, dev) == cudaSuccess) {
+    uint64_t keep = ~uint64_t(0);
+    cudaMemPoolSetAttribute(mempool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   const uint32_t V = host.vertex_count;
   d_off.ensure(sizeof(uint64_t) * (static_cast<size_t>(V) + 1));
   d_adj.ensure(sizeof(uint32_t) * std::max<uint64_t>(host.edge_count, 1));
@@ -195,14 +210,25 @@ uint32_t max_state_words(const std::vector<DeviceConstraint>& v) {
 uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
   const uint64_t V = g.host.vertex_count, E = g.host.edge_count;
   const uint64_t wb = word_bytes(word_kind_for(k));
+  const uint64_t kk = std::min<uint64_t>(k, 64);
+  // Walker pool of the first walk round: per warp the edge memo, a
+  // hypothesis memo of (3 + stored vertices) words and a state memo of
+  // (5 + key words) words per entry, both bounded through k.
+  const uint64_t warps = static_cast<uint64_t>(walk_grid_blocks(1u << 30)) * kWalkWarpsPerBlock;
+  const uint64_t pool = warps * (16ull * kEdgeCapEntries + 4ull * kHypCapEntries * (3 + kk) +
+                                 4ull * kStateCapEntries * (7 + kk));
   // state + per-step worklist/status/markers (items bounded by V * roles)
-  return V * (2 * wb + 2) + ((E + 31) / 32) * 8 + V * 8 + V * std::min<uint64_t>(k, 64) * 5 +
-         sizeof(HubAcc) * static_cast<uint64_t>(g.n_acc) + (1 << 20);
+  return V * (2 * wb + 2) + ((E + 31) / 32) * 8 + V * 8 + V * kk * 5 +
+         sizeof(HubAcc) * static_cast<uint64_t>(g.n_acc) + pool + (1 << 20);
 }
 
 QueryImpl::~QueryImpl() {
-  if (h_ctr) cudaFreeHost(h_ctr);
-  if (h_count) cudaFreeHost(h_count);
+  // Stream-ordered frees go before the stream is destroyed.
+  for (DeviceBuffer* b : buffers()) b->release();
+  if (own_host) {
+    if (h_ctr) cudaFreeHost(h_ctr);
+    if (h_count) cudaFreeHost(h_count);
+  }
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (ev_first) cudaEventDestroy(ev_first);
@@ -222,7 +248,16 @@ uint64_t QueryImpl::device_bytes() const {
          pool.bytes() + big_pool.bytes();
 }
 
-void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) {
+std::vector<DeviceBuffer*> QueryImpl::buffers() {
+  return {&d_vs,          &d_eact,      &d_lt,        &d_mod,       &d_sch,        &d_unm,         &d_ctr,
+          &d_tables,      &d_d2s,       &d_hub_acc,   &d_progs,     &d_start_roles, &d_role_index,  &d_wl,
+          &d_wl_index,    &d_blocks,    &d_count,     &d_status,    &d_marker,     &d_marks,       &d_list,
+          &d_list2,       &d_apply_v,   &d_apply_r,   &pool.edge,   &pool.hyp,     &pool.state,    &pool.epochs,
+          &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs};
+}
+
+void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, StepCounters* ext_ctr,
+                       uint32_t* ext_count) {
   g = graph;
   pattern = p;
   k = p.n;
@@ -265,11 +300,21 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s) 
     PM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     own_stream = true;
   }
+  for (DeviceBuffer* b : buffers()) {
+    b->stream = stream;
+    b->ordered = true;
+  }
   PM_CUDA(cudaEventCreate(&ev0));
   PM_CUDA(cudaEventCreate(&ev1));
   PM_CUDA(cudaEventCreate(&ev_first));
-  PM_CUDA(cudaMallocHost(&h_ctr, sizeof(StepCounters)));
-  PM_CUDA(cudaMallocHost(&h_count, sizeof(uint32_t)));
+  if (ext_ctr && ext_count) {
+    h_ctr = ext_ctr;
+    h_count = ext_count;
+    own_host = false;
+  } else {
+    PM_CUDA(cudaMallocHost(&h_ctr, sizeof(StepCounters)));
+    PM_CUDA(cudaMallocHost(&h_count, sizeof(uint32_t)));
+  }
 
   const uint64_t V = g->host.vertex_count, E = g->host.edge_count;
   const size_t wb = word_bytes(word_kind);
@@ -375,7 +420,7 @@ uint32_t QueryImpl::build_worklist(uint64_t mask) {
 }
 
 namespace {
-constexpr uint32_t kEdgeCap = 1024, kHypCap = 1024, kStateCap = 2048;
+constexpr uint32_t kEdgeCap = kEdgeCapEntries, kHypCap = kHypCapEntries, kStateCap = kStateCapEntries;
 void zero_field(void* base, size_t offset, cudaStream_t s) {
   PM_CUDA(cudaMemsetAsync(static_cast<char*>(base) + offset, 0, sizeof(unsigned long long), s));
 }
@@ -559,40 +604,102 @@ StepResult QueryImpl::step_nlcc(const DeviceConstraint& dc) {
   return r;
 }
 
+namespace {
+uint32_t g_enum_split_parts = 16;  // slices per split source (<= 1: never split)
+uint32_t g_enum_split_after = 0;   // table growth levels before sources are split
+}  // namespace
+
+void set_enum_split(uint32_t parts, uint32_t after_levels) {
+  g_enum_split_parts = parts;
+  g_enum_split_after = after_levels;
+}
+
+// ENUMERATION (multiple_label_enumeration_cpu.tpp:39-118): every source of
+// the first walk's start role, one warp each.  A source whose count memo
+// overflows is re-run, either with tables 8x larger per growth level (the
+// memo keeps reusing subtree counts across the source's first hops), or,
+// once `after` growth levels were needed, split into slices of its first
+// hop that separate warps take with base-size tables (parallel, but the
+// slices do not share counts).  A slice is split once; after that it grows.
 StepResult QueryImpl::step_enumeration() {
+  const uint64_t kEnumSplit = g_enum_split_parts;
   const WalkProgram& p = enumeration.cc.programs[0];
   const uint32_t n_wl = build_worklist(uint64_t(1) << p.start_role);
   zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
   if (n_wl) {
     ensure_pool();
-    d_list.ensure(4ull * n_wl);
-    d_list2.ensure(4ull * n_wl);
     const WalkProgram* prog = d_progs.as<WalkProgram>() + enumeration.prog_offset;
+    // Slicing the first hop is exact when that step binds a new vertex.
+    const bool splittable =
+        p.n_steps > 1 && (p.steps[1].kind == kStepVertex || p.steps[1].kind == kStepFinal);
+    d_list2.ensure(sizeof(uint4) * n_wl);
     zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
-    launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list.as<uint32_t>(), pool.sc,
+    launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,
                      stream);
     PM_CUDA(cudaGetLastError());
     read_counters();
-    // Sources whose count memo overflowed are re-run with larger tables.
     uint32_t n_over = static_cast<uint32_t>(h_ctr->aux);
-    DeviceBuffer* in = &d_list;
-    DeviceBuffer* out = &d_list2;
     uint32_t hs, ss;
     pool_strides(&hs, &ss);
     const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
+    const std::vector<uint64_t>& off = g->host.offsets;
+    std::vector<uint4> over, items;
+    int grow_level = 0;
     for (int round = 1; n_over; ++round) {
       ++overflow_retries;
-      if (round > 6) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
-      const uint32_t warps = retry_warps(base_warps, round, hs, ss);
-      big_pool.ensure(warps, kEdgeCap, kHypCap, hs, kStateCap << (3 * round), ss, stream);
-      zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+      if (round > 32) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
+      over.resize(n_over);
+      PM_CUDA(cudaMemcpyAsync(over.data(), d_list2.ptr, sizeof(uint4) * n_over, cudaMemcpyDeviceToHost, stream));
+      PM_CUDA(cudaStreamSynchronize(stream));
+      // An overflow record is {position, lo, hi, source}; an item that was
+      // split carries lo/hi inside the list, an unsplit one [0, 2^32).
+      items.clear();
+      size_t n_split = 0;
+      auto split_now = [&](const uint4& it, uint64_t* lo, uint64_t* len) {
+        const uint64_t deg = off[it.w + 1] - off[it.w];
+        *lo = it.y;
+        const uint64_t hi = std::min<uint64_t>(it.z, deg);
+        *len = hi > *lo ? hi - *lo : 0;
+        const bool unsplit = it.y == 0 && it.z == 0xFFFFFFFFu;
+        return splittable && unsplit && kEnumSplit > 1 && *len > 1 &&
+               static_cast<uint32_t>(grow_level) >= g_enum_split_after;
+      };
+      for (const uint4& it : over) {
+        uint64_t lo, len;
+        if (!split_now(it, &lo, &len)) continue;
+        const uint64_t parts = std::min<uint64_t>(len, kEnumSplit);
+        for (uint64_t k = 0; k < parts; ++k)
+          items.push_back(make_uint4(it.x, static_cast<uint32_t>(lo + len * k / parts),
+                                     static_cast<uint32_t>(lo + len * (k + 1) / parts), 0));
+      }
+      n_split = items.size();
+      for (const uint4& it : over) {
+        uint64_t lo, len;
+        if (!split_now(it, &lo, &len)) items.push_back(make_uint4(it.x, it.y, it.z, 0));
+      }
+      const size_t n_grow = items.size() - n_split;
+      d_list.ensure(sizeof(uint4) * items.size());
+      d_list2.ensure(sizeof(uint4) * items.size());
+      PM_CUDA(cudaMemcpyAsync(d_list.ptr, items.data(), sizeof(uint4) * items.size(), cudaMemcpyHostToDevice,
+                              stream));
       zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
-      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, in->as<uint32_t>(), n_over,
-                       out->as<uint32_t>(), big_pool.sc, stream);
-      PM_CUDA(cudaGetLastError());
+      if (n_split) {
+        zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+        launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
+                         static_cast<uint32_t>(n_split), d_list2.as<uint4>(), pool.sc, stream);
+        PM_CUDA(cudaGetLastError());
+      }
+      if (n_grow) {
+        if (++grow_level > 6) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
+        const uint32_t warps = retry_warps(base_warps, grow_level, hs, ss);
+        big_pool.ensure(warps, kEdgeCap, kHypCap, hs, kStateCap << (3 * grow_level), ss, stream);
+        zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+        launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>() + n_split,
+                         static_cast<uint32_t>(n_grow), d_list2.as<uint4>(), big_pool.sc, stream);
+        PM_CUDA(cudaGetLastError());
+      }
       read_counters();
       n_over = static_cast<uint32_t>(h_ctr->aux);
-      std::swap(in, out);
     }
   }
   read_counters();
@@ -706,6 +813,10 @@ void QueryImpl::run_all(int max_iterations) {
 void QueryImpl::export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact) {
   const uint64_t V = g->host.vertex_count, E = g->host.edge_count;
   DeviceBuffer dc, de, dv;
+  for (DeviceBuffer* b : {&dc, &de, &dv}) {
+    b->stream = stream;
+    b->ordered = true;
+  }
   if (cand) dc.ensure(8 * std::max<uint64_t>(V, 1));
   if (eact) de.ensure(std::max<uint64_t>(E, 1));
   if (vact) dv.ensure(std::max<uint64_t>(V, 1));

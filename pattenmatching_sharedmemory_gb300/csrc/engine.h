@@ -19,10 +19,14 @@ namespace pmgb {
     if (pm_err_ != cudaSuccess) throw_cuda(pm_err_, #call); \
   } while (0)
 
-// Device allocation owned by RAII.
+// Device allocation owned by RAII.  With `stream` set, allocation and
+// release are stream-ordered (cudaMallocAsync / cudaFreeAsync on that
+// stream), so they never wait for work on other streams.
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  bool ordered = false;
   DeviceBuffer() = default;
   DeviceBuffer(const DeviceBuffer&) = delete;
   DeviceBuffer& operator=(const DeviceBuffer&) = delete;
@@ -104,6 +108,7 @@ struct QueryImpl {
       d_apply_r;
   StepCounters* h_ctr = nullptr;  // pinned
   uint32_t* h_count = nullptr;    // pinned
+  bool own_host = true;           // h_ctr / h_count allocated here
   WalkPool pool, big_pool;
 
   // step machine (MultipleLabelStep, multiple_label_step.cc:30-83)
@@ -126,7 +131,11 @@ struct QueryImpl {
   std::vector<std::pair<uint64_t, uint64_t>> walk_stats;
 
   ~QueryImpl();
-  void create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s);
+  // s: the query's stream (null: a stream of its own).  ext_ctr / ext_count:
+  // pinned host words the caller owns and keeps for the query's lifetime
+  // (null: allocated here).  Device buffers are stream-ordered on s.
+  void create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, StepCounters* ext_ctr = nullptr,
+              uint32_t* ext_count = nullptr);
   QueryDevPtrs ptrs() const;
   uint64_t device_bytes() const;
 
@@ -136,6 +145,8 @@ struct QueryImpl {
   pm_step_record final_record();
 
   void export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact);
+  // Every device buffer the query owns.
+  std::vector<DeviceBuffer*> buffers();
   void write_outputs(const std::string& dir);
 
  private:
@@ -154,8 +165,18 @@ struct QueryImpl {
   int advance(int cur);
 };
 
+// Walker memo table entries per warp in the first walk round.
+constexpr uint32_t kEdgeCapEntries = 1024, kHypCapEntries = 1024, kStateCapEntries = 2048;
+
 std::string step_name(int kind);
 PatternGraph load_pattern(const std::string& dir, bool load_labels);
+// ENUMERATION overflow policy (process-wide): sources whose count memo
+// overflowed `after_levels` times with growing tables are split into up to
+// `parts` first-hop slices (parts <= 1: never split).
+void set_enum_split(uint32_t parts, uint32_t after_levels);
+
+// Device bytes a query of a k-vertex template holds in its first walk
+// round (state, worklists, first walker pool); the admission charge.
 uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k);
 
 }  // namespace pmgb

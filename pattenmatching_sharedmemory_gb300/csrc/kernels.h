@@ -118,11 +118,13 @@ constexpr uint32_t kWalkWarpsPerBlock = 4;
 void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const uint32_t* vertices, const uint64_t* roles,
                                uint32_t n, cudaStream_t s);
 
-// ENUMERATION: sums injective embeddings from every worklist vertex (or
-// from the wl positions in `retry`); sources whose count memo overflowed are
-// written to `overflow` (count in ctr->aux) and contribute nothing.
+// ENUMERATION: sums injective embeddings from every worklist vertex, or
+// over `items` {worklist position, lo, hi, -} whose first hop is limited to
+// positions [lo, hi) of the source's adjacency list.  Items whose count memo
+// overflowed are written to `overflow` as {position, lo, hi, source vertex}
+// (count in ctr->aux) and contribute nothing.
 void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, const uint32_t* retry, uint32_t n_retry, uint32_t* overflow,
+                      uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow,
                       const WalkScratch& scratch, cudaStream_t s);
 
 // Export of the pruned state.

@@ -22,7 +22,7 @@ constexpr int kThreads = 256;
 constexpr int kWarpsPerBlock = kThreads / 32;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-int g_sm_count = 0;
+std::atomic<int> g_sm_count{0};
 std::atomic<uint64_t> g_launches{0};
 
 inline int grid_for_tiles(uint64_t V, int blocks_per_sm) {
@@ -909,13 +909,14 @@ void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sm_count() {
-  if (g_sm_count == 0) {
+  int n = g_sm_count.load(std::memory_order_relaxed);
+  if (n == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 1;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    g_sm_count.store(n, std::memory_order_relaxed);
   }
-  return g_sm_count;
+  return n;
 }
 
 void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* d2s, uint64_t full, cudaStream_t s) {

@@ -479,9 +479,12 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
 // Runs one walk.  NLCC: returns kItemSuccess / kItemFail / kItemOverflow.
 // ENUMERATION: counts completed walks into *leaves and returns kItemFail.
 // Either returns kItemTimeout once %globaltimer passes `deadline`.
+// [first_lo, first_hi) restricts the first hop to those positions of the
+// source's adjacency list (ENUMERATION slices; the first step binds a vertex).
 template <class W, bool kEnum>
 __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared& ws, WarpMemo& m, uint32_t source,
-                            unsigned long long* leaves, uint64_t deadline) {
+                            unsigned long long* leaves, uint64_t deadline, uint32_t first_lo = 0,
+                            uint32_t first_hi = 0xFFFFFFFFu) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog.n_steps;
   const bool count_memo = kEnum && ws.prog.count_memo;
@@ -497,6 +500,15 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     return kEnum ? kItemFail : kItemSuccess;
   }
   frame_enter(g, ws, 1);
+  if (first_lo != 0 || first_hi != 0xFFFFFFFFu) {
+    __syncwarp();
+    if (lane == 0) {
+      const uint64_t b = ws.f.next[1], e = ws.f.end[1];
+      ws.f.next[1] = e - b > first_lo ? b + first_lo : e;
+      ws.f.end[1] = e - b > first_hi ? b + first_hi : e;
+    }
+    __syncwarp();
+  }
   int d = 1;
   while (true) {
     if ((++iters & 1023u) == 0) {
@@ -780,15 +792,17 @@ __global__ void k_apply_list(DevGraph g, DevState<W> st, const uint32_t* __restr
   if (lane_id() == 0 && newly) atomicAdd(&ctr->modified_total, static_cast<unsigned long long>(newly));
 }
 
-// ENUMERATION over worklist sources (or the `retry` subset).  A source
-// whose count memo overflows contributes nothing and is listed in
-// `overflow` (ctr->aux entries) for a re-run with larger tables.
+// ENUMERATION over worklist sources, or over `items` ({worklist position,
+// first-hop slice lo, hi, -}) when given.  An item whose count memo
+// overflows contributes nothing and is listed in `overflow` ({position, lo,
+// hi, source vertex}, ctr->aux entries) for a re-run (split, or with larger
+// tables).
 template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevState<W> st,
                                                                const WalkProgram* __restrict__ prog,
                                                                const uint32_t* __restrict__ wl, uint32_t n_wl,
-                                                               const uint32_t* __restrict__ retry, uint32_t n_retry,
-                                                               uint32_t* overflow, WalkScratch sc, StepCounters* ctr,
+                                                               const uint4* __restrict__ items, uint32_t n_items,
+                                                               uint4* overflow, WalkScratch sc, StepCounters* ctr,
                                                                uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   const unsigned lane = lane_id();
@@ -805,17 +819,18 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
   uint64_t deadline = 0;
   if (lane == 0) deadline = global_timer_ns() + budget_ns;
   deadline = __shfl_sync(kFull, deadline, 0);
-  const uint64_t n = retry ? n_retry : n_wl;
+  const uint64_t n = items ? n_items : n_wl;
   unsigned long long leaves = 0;
   while (true) {
     unsigned long long gi = 0;
     if (lane == 0) gi = atomicAdd(&ctr->items, 1ull);
     gi = __shfl_sync(kFull, gi, 0);
     if (gi >= n) break;
-    const uint32_t src = retry ? retry[gi] : static_cast<uint32_t>(gi);
+    const uint4 it = items ? items[gi] : make_uint4(static_cast<uint32_t>(gi), 0u, 0xFFFFFFFFu, 0u);
+    const uint32_t source = wl[it.x];
     next_epoch(m);
     const unsigned long long before = leaves;
-    const uint8_t res = run_walk<W, true>(g, st, ws, m, wl[src], &leaves, deadline);
+    const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z);
     if (res == kItemTimeout) {
       if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
       break;
@@ -823,7 +838,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
     if (res == kItemOverflow) {
       leaves = before;
       if (lane == 0) {
-        overflow[atomicAdd(&ctr->aux, 1ull)] = src;
+        overflow[atomicAdd(&ctr->aux, 1ull)] = make_uint4(it.x, it.y, it.z, source);
         atomicAdd(&ctr->overflow, 1ull);
       }
     }
@@ -908,11 +923,11 @@ void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const u
 }
 
 void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, const uint32_t* retry, uint32_t n_retry, uint32_t* overflow,
-                      const WalkScratch& sc, cudaStream_t s) {
+                      uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow, const WalkScratch& sc,
+                      cudaStream_t s) {
   const uint32_t blocks = walk_grid_blocks(sc.n_warps);
   PM_DISPATCH_WORD(q.word_kind,
-                   k_enumerate<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), prog, wl, n_wl, retry, n_retry,
+                   k_enumerate<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), prog, wl, n_wl, items, n_items,
                                                                      overflow, sc, q.ctr, g_walk_budget_ns));
 }
 
