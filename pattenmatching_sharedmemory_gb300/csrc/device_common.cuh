@@ -95,6 +95,8 @@ struct DevGraph {
   // * seg_entries, + seg_entries): segments never cross a seg_entries
   // boundary, so one spans at most 32 words of edge bits.
   const uint4* __restrict__ seg;   // [n_seg] {vertex, segment index, segments, accumulator}
+  // Every CSR entry u -> w has its reverse w -> u (lists strictly increasing).
+  int symmetric;
 };
 
 // Per-query accumulator of a hub with several segments.  Zero between

@@ -85,6 +85,18 @@ void GraphImpl::to_device(int dev) {
   if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
   device = dev;
   build_hub_plan(hub_degree, seg_entries);
+  symmetric = false;
+  if (sorted_unique && V) {
+    uint32_t* d_flag = nullptr;
+    uint32_t asym = 0;
+    PM_CUDA(cudaMalloc(&d_flag, sizeof(uint32_t)));
+    PM_CUDA(cudaMemset(d_flag, 0, sizeof(uint32_t)));
+    launch_check_symmetric(this->dev(), d_flag, nullptr);
+    const cudaError_t e = cudaMemcpy(&asym, d_flag, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_flag);
+    PM_CUDA(e);
+    symmetric = asym == 0;
+  }
 }
 
 void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
@@ -132,6 +144,7 @@ DevGraph GraphImpl::dev() const {
   g.n_heavy = n_heavy;
   g.n_acc = n_acc;
   g.seg = d_seg.as<uint4>();
+  g.symmetric = symmetric ? 1 : 0;
   return g;
 }
 

@@ -45,6 +45,7 @@ struct GraphImpl {
   std::vector<label_t> dense_values;  // sorted distinct label values
   std::vector<uint32_t> dense_ids;    // per vertex
   bool sorted_unique = false;
+  bool symmetric = false;  // sorted_unique and every entry has its reverse (checked on the device)
   int device = -1;
   DeviceBuffer d_off, d_adj, d_lab;
   // Degree classes of the LCC sweeps (DevGraph::hub_degree and segments).

@@ -41,6 +41,10 @@ uint64_t launch_count();
 void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* dense_to_slot, uint64_t full_cand,
                        cudaStream_t s);
 
+// Sets *asymmetric to 1 when some CSR entry u -> w has no reverse entry
+// w -> u (adjacency lists must be strictly increasing).
+void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_t s);
+
 // LCC0 (multiple_label_lcc0_cpu.tpp:15-87).
 void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 

@@ -55,6 +55,39 @@ __global__ void __launch_bounds__(kThreads) k_init_state(DevGraph g, DevState<W>
   }
 }
 
+// ---- graph properties -------------------------------------------------------
+// Warp per vertex: every entry u -> w looks for u in w's sorted list.
+__global__ void __launch_bounds__(kThreads) k_check_symmetric(DevGraph g, uint32_t* asymmetric) {
+  const unsigned lane = lane_id();
+  const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t u = warp; u < g.V; u += n_warps) {
+    if (*reinterpret_cast<volatile uint32_t*>(asymmetric)) return;
+    const uint64_t b = g.off[u], e = g.off[u + 1];
+    for (uint64_t x0 = b; x0 < e; x0 += 32) {
+      const uint64_t x = x0 + lane;
+      bool missing = false;
+      if (x < e) {
+        const uint32_t w = g.adj[x];
+        uint64_t lo = g.off[w], hi = g.off[w + 1];
+        const uint64_t end = hi;
+        while (lo < hi) {
+          const uint64_t mid = lo + ((hi - lo) >> 1);
+          if (g.adj[mid] < u)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        missing = !(lo < end && g.adj[lo] == u);
+      }
+      if (__any_sync(kFull, missing)) {
+        if (lane == 0) atomicOr(asymmetric, 1u);
+        return;
+      }
+    }
+  }
+}
+
 // ---- LCC0 ---------------------------------------------------------------
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_lcc0(DevGraph g, DevState<W> st, const QueryTables* __restrict__ qt,
@@ -922,6 +955,11 @@ int device_sm_count() {
 void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* d2s, uint64_t full, cudaStream_t s) {
   const int grid = device_sm_count() * 8;
   PM_DISPATCH_WORD(q.word_kind, k_init_state<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), d2s, full));
+}
+
+void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_t s) {
+  note_launch();
+  k_check_symmetric<<<device_sm_count() * 8, kThreads, 0, s>>>(g, asymmetric);
 }
 
 void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {

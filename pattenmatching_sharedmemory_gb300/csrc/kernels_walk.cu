@@ -148,23 +148,26 @@ __device__ __forceinline__ uint32_t tuple_hash(uint32_t nb, uint32_t step, const
   return fmix32(h);
 }
 
-// Open-addressing tuple table: entry = {epoch, nb, step, key words padded
-// with 0xFFFFFFFF, [count lo, count hi]}.  Probes 32 slots per round.
-// Returns the slot of a live match, or ~0 with *empty_slot set to the first
-// free slot (or ~0 when the table has no free slot in reach).
-__device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t stride, uint32_t key_words, uint32_t epoch,
-                               uint32_t nb, uint32_t step, const KeyTuple& t, uint32_t* empty_slot) {
+// Open-addressing tuple table of `cap` entries, stored word-major: word w
+// of entry s at tab[w * cap + s], entry = {epoch, nb, step, key words padded
+// with 0xFFFFFFFF, [count lo, count hi]}.  Probes 32 consecutive slots per
+// round, so the epoch words of a probe are one 128-byte line and the key
+// words are read only where the epoch matches.  Returns the slot of a live
+// match, or ~0 with *empty_slot set to the first free slot (or ~0 when the
+// table has no free slot in reach).
+__device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t key_words, uint32_t epoch, uint32_t nb,
+                               uint32_t step, const KeyTuple& t, uint32_t* empty_slot) {
   const unsigned lane = lane_id();
   const uint32_t mask = cap - 1;
   const uint32_t h = tuple_hash(nb, step, t);
   for (uint32_t probe = 0; probe < cap; probe += 32) {
     const uint32_t slot = (h + probe + lane) & mask;
-    const uint32_t* e = tab + static_cast<uint64_t>(slot) * stride;
+    const uint32_t* e = tab + slot;
     const bool live = __ldcg(e) == epoch;
-    bool match = live && __ldcg(e + 1) == nb && __ldcg(e + 2) == step;
+    bool match = live && __ldcg(e + cap) == nb && __ldcg(e + 2 * cap) == step;
     for (uint32_t i = 0; match && i < key_words; ++i) {
       const uint32_t want = static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu;
-      if (__ldcg(e + 3 + i) != want) match = false;
+      if (__ldcg(e + static_cast<uint64_t>(3 + i) * cap) != want) match = false;
     }
     const unsigned mm = __ballot_sync(kFull, match);
     if (mm) return (h + probe + __ffs(mm) - 1) & mask;
@@ -178,16 +181,17 @@ __device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t strid
   return ~0u;
 }
 
-__device__ void tuple_write(uint32_t* tab, uint32_t stride, uint32_t key_words, uint32_t slot, uint32_t epoch,
+__device__ void tuple_write(uint32_t* tab, uint32_t cap, uint32_t key_words, uint32_t slot, uint32_t epoch,
                             uint32_t nb, uint32_t step, const KeyTuple& t, bool with_count, unsigned long long count) {
   if (lane_id() == 0) {
-    uint32_t* w = tab + static_cast<uint64_t>(slot) * stride;
-    __stcg(w + 1, nb);
-    __stcg(w + 2, step);
-    for (uint32_t i = 0; i < key_words; ++i) __stcg(w + 3 + i, static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu);
+    uint32_t* w = tab + slot;
+    __stcg(w + cap, nb);
+    __stcg(w + 2 * cap, step);
+    for (uint32_t i = 0; i < key_words; ++i)
+      __stcg(w + static_cast<uint64_t>(3 + i) * cap, static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu);
     if (with_count) {
-      __stcg(w + 3 + key_words, static_cast<uint32_t>(count));
-      __stcg(w + 4 + key_words, static_cast<uint32_t>(count >> 32));
+      __stcg(w + static_cast<uint64_t>(3 + key_words) * cap, static_cast<uint32_t>(count));
+      __stcg(w + static_cast<uint64_t>(4 + key_words) * cap, static_cast<uint32_t>(count >> 32));
     }
     __stcg(w, epoch);
   }
@@ -201,9 +205,9 @@ __device__ int hyp_memo(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShare
   const KeyTuple t = stored_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.hyp_stride - 3;
-  if (tuple_find(m.hyp, m.hyp_cap, m.hyp_stride, key_words, m.epoch, nb, step, t, &empty) != ~0u) return kFound;
+  if (tuple_find(m.hyp, m.hyp_cap, key_words, m.epoch, nb, step, t, &empty) != ~0u) return kFound;
   if (empty == ~0u) return kOverflowHit;
-  tuple_write(m.hyp, m.hyp_stride, key_words, empty, m.epoch, nb, step, t, false, 0);
+  tuple_write(m.hyp, m.hyp_cap, key_words, empty, m.epoch, nb, step, t, false, 0);
   return ++m.hyp_n <= (m.hyp_cap >> 1) ? kNone : kOverflowHit;
 }
 
@@ -215,10 +219,9 @@ __device__ int state_seen(WarpMemo& m, uint32_t nb, uint32_t step, const WarpSha
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  if (tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step | kStateTag, t, &empty) != ~0u)
-    return kFound;
+  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step | kStateTag, t, &empty) != ~0u) return kFound;
   if (empty == ~0u || m.state_n >= (m.state_cap >> 1)) return kOverflowHit;
-  tuple_write(m.state, m.state_stride, key_words, empty, m.epoch, nb, step | kStateTag, t, false, 0);
+  tuple_write(m.state, m.state_cap, key_words, empty, m.epoch, nb, step | kStateTag, t, false, 0);
   ++m.state_n;
   return kNone;
 }
@@ -229,11 +232,11 @@ __device__ bool count_lookup(const WarpMemo& m, uint32_t nb, uint32_t step, cons
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  const uint32_t slot = tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step, t, &empty);
+  const uint32_t slot = tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty);
   if (slot == ~0u) return false;
-  const uint32_t* e = m.state + static_cast<uint64_t>(slot) * m.state_stride;
-  *count = static_cast<unsigned long long>(__ldcg(e + 3 + key_words)) |
-           (static_cast<unsigned long long>(__ldcg(e + 4 + key_words)) << 32);
+  const uint32_t* e = m.state + slot;
+  *count = static_cast<unsigned long long>(__ldcg(e + static_cast<uint64_t>(3 + key_words) * m.state_cap)) |
+           (static_cast<unsigned long long>(__ldcg(e + static_cast<uint64_t>(4 + key_words) * m.state_cap)) << 32);
   return true;
 }
 
@@ -244,9 +247,9 @@ __device__ bool count_store(WarpMemo& m, uint32_t nb, uint32_t step, const WarpS
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  if (tuple_find(m.state, m.state_cap, m.state_stride, key_words, m.epoch, nb, step, t, &empty) != ~0u) return true;
+  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty) != ~0u) return true;
   if (empty == ~0u) return false;
-  tuple_write(m.state, m.state_stride, key_words, empty, m.epoch, nb, step, t, true, count);
+  tuple_write(m.state, m.state_cap, key_words, empty, m.epoch, nb, step, t, true, count);
   ++m.state_n;
   return true;
 }
@@ -456,9 +459,20 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
     }
     for (int j = ws.prog.tail_from; ok && j < n_steps; ++j) {
       const int hs = ws.prog.hist_step[ws.prog.steps[j].hist];
-      const uint32_t target = hs == d ? nb : ws.f.bound[hs];
-      const uint64_t idx = lane_find_sorted(g.adj, g.off[nb], g.off[nb + 1], target);
-      ok = idx != ~uint64_t(0) && edge_active(st.eact, idx) && Pack<W>::cand(st.vs[target]) != 0;
+      if (g.symmetric && hs != d) {
+        // A CHECK is a template edge between nb's role and the bound
+        // vertex's role.  LCC removes an entry only when its target holds
+        // no template neighbour of the source's roles, and roles only
+        // shrink, so while both hold these roles neither direction of the
+        // edge was ever removed: the check is adjacency, searched in the
+        // bound vertex's list, which every lane shares.
+        const uint32_t t = ws.f.bound[hs];
+        ok = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], nb) != ~uint64_t(0);
+      } else {
+        const uint32_t target = hs == d ? nb : ws.f.bound[hs];
+        const uint64_t idx = lane_find_sorted(g.adj, g.off[nb], g.off[nb + 1], target);
+        ok = idx != ~uint64_t(0) && edge_active(st.eact, idx) && Pack<W>::cand(st.vs[target]) != 0;
+      }
     }
     const unsigned mask = __ballot_sync(kFull, ok);
     __syncwarp();
