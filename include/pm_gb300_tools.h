@@ -61,6 +61,18 @@ pm_status_t pm_query_elapsed_ms(const pm_query* q, double* ms);
  * no query runs. */
 pm_status_t pm_set_enum_split(uint32_t parts, uint32_t after_levels);
 
+/* ENUMERATION sources with more than slice_entries first-hop entries start
+ * as slices of that many entries, queued before the other sources, so hub
+ * sources are spread over many warps from the start (0: every source starts
+ * whole; default 16).  Process-wide; speed only.  Set it while no query runs. */
+pm_status_t pm_set_enum_presplit(uint32_t slice_entries);
+
+/* Count-memo entries per warp in ENUMERATION's first round (power of two,
+ * 1024 to 2^20; default 8192).  Larger tables let more sources finish in
+ * the first round at the cost of device memory (warps x entries x (7 + k)
+ * words per query).  Process-wide; speed only.  Set it while no query runs. */
+pm_status_t pm_set_enum_table_entries(uint32_t entries);
+
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with
  * PM_E_TIMEOUT and the query's state is no longer meaningful. */

@@ -139,6 +139,8 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
+        "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_enum_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
                                                           ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
         "pm_query_destroy": (None, [ctypes.c_void_p]),

@@ -323,6 +323,18 @@ pm_status_t pm_set_enum_split(uint32_t parts, uint32_t after_levels) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_enum_presplit(uint32_t slice_entries) {
+  set_enum_presplit(slice_entries);
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_set_enum_table_entries(uint32_t entries) {
+  PM_REQUIRE(entries >= 1024 && entries <= (1u << 20) && !(entries & (entries - 1)),
+             "entries must be a power of two in [1024, 2^20]");
+  set_enum_table_entries(entries);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));

@@ -228,8 +228,9 @@ uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
   // hypothesis memo of (3 + stored vertices) words and a state memo of
   // (5 + key words) words per entry, both bounded through k.
   const uint64_t warps = static_cast<uint64_t>(walk_grid_blocks(1u << 30)) * kWalkWarpsPerBlock;
+  const uint64_t state_entries = std::max<uint64_t>(kStateCapEntries, enum_table_entries());
   const uint64_t pool = warps * (16ull * kEdgeCapEntries + 4ull * kHypCapEntries * (3 + kk) +
-                                 4ull * kStateCapEntries * (7 + kk));
+                                 4ull * state_entries * (7 + kk));
   // state + per-step worklist/status/markers (items bounded by V * roles)
   return V * (2 * wb + 2) + ((E + 31) / 32) * 8 + V * 8 + V * kk * 5 +
          sizeof(HubAcc) * static_cast<uint64_t>(g.n_acc) + pool + (1 << 20);
@@ -620,12 +621,19 @@ StepResult QueryImpl::step_nlcc(const DeviceConstraint& dc) {
 namespace {
 uint32_t g_enum_split_parts = 16;  // slices per split source (<= 1: never split)
 uint32_t g_enum_split_after = 0;   // table growth levels before sources are split
+uint32_t g_enum_state_cap = 8192;  // count-memo entries per warp, first round
+uint32_t g_enum_presplit = 16;     // first-hop entries per slice of a heavy source (0: no up-front slicing)
 }  // namespace
+
+void set_enum_presplit(uint32_t slice_entries) { g_enum_presplit = slice_entries; }
 
 void set_enum_split(uint32_t parts, uint32_t after_levels) {
   g_enum_split_parts = parts;
   g_enum_split_after = after_levels;
 }
+
+void set_enum_table_entries(uint32_t entries) { g_enum_state_cap = entries; }
+uint32_t enum_table_entries() { return g_enum_state_cap; }
 
 // ENUMERATION (multiple_label_enumeration_cpu.tpp:39-118): every source of
 // the first walk's start role, one warp each.  A source whose count memo
@@ -640,23 +648,51 @@ StepResult QueryImpl::step_enumeration() {
   const uint32_t n_wl = build_worklist(uint64_t(1) << p.start_role);
   zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
   if (n_wl) {
-    ensure_pool();
+    {
+      uint32_t hs0, ss0;
+      pool_strides(&hs0, &ss0);
+      pool.ensure(walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock, kEdgeCap, kHypCap, hs0, g_enum_state_cap, ss0,
+                  stream);
+    }
     const WalkProgram* prog = d_progs.as<WalkProgram>() + enumeration.prog_offset;
     // Slicing the first hop is exact when that step binds a new vertex.
     const bool splittable =
         p.n_steps > 1 && (p.steps[1].kind == kStepVertex || p.steps[1].kind == kStepFinal);
-    d_list2.ensure(sizeof(uint4) * n_wl);
+    const std::vector<uint64_t>& off = g->host.offsets;
+    std::vector<uint4> over, items;
     zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
-    launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,
-                     stream);
+    if (splittable && g_enum_presplit) {
+      // Sources with more first-hop entries than g_enum_presplit start as
+      // slices of that many entries, queued first (the longest work).
+      std::vector<uint32_t> wl(n_wl);
+      PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
+      PM_CUDA(cudaStreamSynchronize(stream));
+      const uint64_t t = g_enum_presplit;
+      for (uint32_t i = 0; i < n_wl; ++i) {
+        const uint64_t deg = off[wl[i] + 1] - off[wl[i]];
+        if (deg <= t) continue;
+        for (uint64_t lo = 0; lo < deg; lo += t)
+          items.push_back(make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(std::min(lo + t, deg)), 0));
+      }
+      for (uint32_t i = 0; i < n_wl; ++i)
+        if (off[wl[i] + 1] - off[wl[i]] <= t) items.push_back(make_uint4(i, 0, 0xFFFFFFFFu, 0));
+      d_list.ensure(sizeof(uint4) * items.size());
+      d_list2.ensure(sizeof(uint4) * items.size());
+      PM_CUDA(cudaMemcpyAsync(d_list.ptr, items.data(), sizeof(uint4) * items.size(), cudaMemcpyHostToDevice,
+                              stream));
+      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
+                       static_cast<uint32_t>(items.size()), d_list2.as<uint4>(), pool.sc, stream);
+    } else {
+      d_list2.ensure(sizeof(uint4) * n_wl);
+      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,
+                       stream);
+    }
     PM_CUDA(cudaGetLastError());
     read_counters();
     uint32_t n_over = static_cast<uint32_t>(h_ctr->aux);
     uint32_t hs, ss;
     pool_strides(&hs, &ss);
     const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
-    const std::vector<uint64_t>& off = g->host.offsets;
-    std::vector<uint4> over, items;
     int grow_level = 0;
     for (int round = 1; n_over; ++round) {
       ++overflow_retries;
@@ -704,8 +740,8 @@ StepResult QueryImpl::step_enumeration() {
       }
       if (n_grow) {
         if (++grow_level > 6) throw PmError{PM_E_DEVICE, "enumeration count memo exceeds the retry limit"};
-        const uint32_t warps = retry_warps(base_warps, grow_level, hs, ss);
-        big_pool.ensure(warps, kEdgeCap, kHypCap, hs, kStateCap << (3 * grow_level), ss, stream);
+        const uint32_t warps = retry_warps(base_warps, grow_level, hs, ss * (g_enum_state_cap / kStateCap));
+        big_pool.ensure(warps, kEdgeCap, kHypCap, hs, g_enum_state_cap << (3 * grow_level), ss, stream);
         zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
         launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>() + n_split,
                          static_cast<uint32_t>(n_grow), d_list2.as<uint4>(), big_pool.sc, stream);

@@ -175,6 +175,12 @@ PatternGraph load_pattern(const std::string& dir, bool load_labels);
 // overflowed `after_levels` times with growing tables are split into up to
 // `parts` first-hop slices (parts <= 1: never split).
 void set_enum_split(uint32_t parts, uint32_t after_levels);
+// ENUMERATION sources with more first-hop entries than this start as slices
+// of that many entries (0: every source starts whole).
+void set_enum_presplit(uint32_t slice_entries);
+// Count-memo entries per warp in ENUMERATION's first round (power of two).
+void set_enum_table_entries(uint32_t entries);
+uint32_t enum_table_entries();
 
 // Device bytes a query of a k-vertex template holds in its first walk
 // round (state, worklists, first walker pool); the admission charge.
