@@ -29,6 +29,8 @@ roofline   : the dominant kernel class of a query run alone (by device
              the measured HBM copy bandwidth.  Walker bytes: 16 B of CSR
              offsets per hop plus, per tested CSR entry, 4 B neighbour id +
              1/8 B edge bit + 1/8 B active bit + ceil(k/8) B neighbour roles.
+small_stream: served vs one-at-a-time on 35 small requests (the triangles
+             over the 5 labels, repeats allowed) on the same graph.
 lcc_roofline: LCC passes on RMAT scale L (default 22; 16 Zipf labels, the
              two-cycle template on labels 0..5): per pass 1/8 B of edge bits
              per listed CSR entry plus, per gathered entry, 4 B neighbour id
@@ -70,6 +72,15 @@ def stream_templates():
         for order in ([a, b, c, d], [a, b, d, c], [a, c, b, d]):
             out.append(T.cycle(order))
     return out
+
+
+def small_templates():
+    """The 35 triangles over labels 0..4 (labels may repeat)."""
+    import itertools
+
+    from pattenmatching_sharedmemory_gb300 import templates as T
+
+    return [T.cycle(list(c)) for c in itertools.combinations_with_replacement(range(5), 3)]
 
 
 def make_graph(w):
@@ -194,6 +205,43 @@ def lcc_roofline(scale: int, device: int):
            "frac": achieved / peak if achieved else None, "traffic": profile_traffic("lcc")}
     g.close()
     return out
+
+
+def small_stream(g, args, pm, torch):
+    """Served vs one-at-a-time on a stream of small requests (35 triangles)."""
+    tm = small_templates()
+    with pm.Server(g, slots=args.slots) as srv:  # warm-up
+        [srv.wait(srv.submit(t)) for t in tm]
+    reps = max(1, args.steps)
+    served_lat, seq_lat = [], []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    counts = None
+    for _ in range(reps):
+        with pm.Server(g, slots=args.slots) as srv:
+            rs = [srv.wait(x) for x in [srv.submit(t) for t in tm]]
+        served_lat += [r.latency_ms for r in rs]
+        counts = [int(r.match_count) for r in rs]
+    torch.cuda.synchronize()
+    served = len(tm) * reps / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        seq_counts = []
+        for t in tm:
+            t1 = time.perf_counter()
+            q = pm.Query(g, pattern=t)
+            q.run()
+            seq_counts.append(q.match_count)
+            q.close()
+            seq_lat.append((time.perf_counter() - t1) * 1e3)
+    torch.cuda.synchronize()
+    seq = len(tm) * reps / (time.perf_counter() - t0)
+    if seq_counts != counts:
+        raise RuntimeError("small stream: served and one-at-a-time counts differ")
+    return {"templates": "35 triangles over labels 0..4 (repeats allowed)", "requests_per_step": len(tm),
+            "served": served, "one_at_a_time": seq, "unit": "queries/s", "speedup": served / seq,
+            "latency_ms_p50": pct(served_lat, 0.5), "latency_ms_p99": pct(served_lat, 0.99),
+            "one_at_a_time_latency_ms_p50": pct(seq_lat, 0.5), "one_at_a_time_latency_ms_p99": pct(seq_lat, 0.99)}
 
 
 def run_gb300(args, w, rank, world):
@@ -337,6 +385,7 @@ def run_gb300(args, w, rank, world):
         "clocks": clocks.summary(),
         "gpu_launches": launches,
     }
+    out["small_stream"] = small_stream(g, args, pm, torch)
     if args.lcc_scale:
         out["lcc_roofline"] = lcc_roofline(args.lcc_scale, device)
     return out, g, tmpls

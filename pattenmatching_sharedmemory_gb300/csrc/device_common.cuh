@@ -91,9 +91,10 @@ struct DevGraph {
   uint32_t n_seg;
   uint32_t n_heavy;
   uint32_t n_acc;                  // hubs with more than one segment
-  // Segment i of vertex v covers its entries in [(off[v] / seg_entries + i)
-  // * seg_entries, + seg_entries): segments never cross a seg_entries
-  // boundary, so one spans at most 32 words of edge bits.
+  // A vertex with more than seg_entries entries has segments i covering its
+  // entries in [(off[v] / seg_entries + i) * seg_entries, + seg_entries)
+  // (never crossing a multiple of seg_entries); a shorter one has a single
+  // segment covering its whole list.
   const uint4* __restrict__ seg;   // [n_seg] {vertex, segment index, segments, accumulator}
   // Every CSR entry u -> w has its reverse w -> u (lists strictly increasing).
   int symmetric;

@@ -112,8 +112,9 @@ void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
   for (uint32_t v = 0; v < V; ++v) {
     const uint64_t deg = host.offsets[v + 1] - host.offsets[v];
     if (deg <= degree) continue;
-    // Segments end at multiples of `entries` (see DevGraph::seg).
-    const uint64_t n = (host.offsets[v + 1] - 1) / entries - host.offsets[v] / entries + 1;
+    // Lists longer than `entries` are cut at multiples of it (see
+    // DevGraph::seg); shorter ones are one segment.
+    const uint64_t n = deg <= entries ? 1 : (host.offsets[v + 1] - 1) / entries - host.offsets[v] / entries + 1;
     if (seg.size() + single.size() + n > 0x7fffffffull) throw PmError{PM_E_INVALID_ARG, "too many hub segments"};
     if (n == 1) {
       single.push_back(make_uint4(v, 0, 1, 0xFFFFFFFFu));
@@ -124,6 +125,11 @@ void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
       seg.push_back(make_uint4(v, static_cast<uint32_t>(i), static_cast<uint32_t>(n), acc));
   }
   const uint32_t heavy = static_cast<uint32_t>(seg.size());
+  // Single-segment hubs by degree, so the 32 lanes of a batch get lists of
+  // similar length.
+  std::stable_sort(single.begin(), single.end(), [&](const uint4& a, const uint4& b) {
+    return host.offsets[a.x + 1] - host.offsets[a.x] < host.offsets[b.x + 1] - host.offsets[b.x];
+  });
   seg.insert(seg.end(), single.begin(), single.end());
   d_seg.ensure(sizeof(uint4) * std::max<size_t>(seg.size(), 1));
   if (!seg.empty())

@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(kThreads) k_lcc0(DevGraph g, DevState<W> st, c
 // with one update per group of equal keys (__match_any_sync).
 
 constexpr int kUnroll = 4;
+constexpr int kTileGroup = 1;
 constexpr int kLccWarps = kThreads / 32;
 constexpr uint8_t kNoRank = 0xFF;
 
@@ -188,6 +189,11 @@ __device__ __forceinline__ uint32_t lane_range(int64_t lo, int64_t hi) {
 // CSR entry range [beg, end) of hub segment sd (DevGraph::seg).
 __device__ __forceinline__ void segment_range(const DevGraph& g, const uint4 sd, uint64_t* beg, uint64_t* end) {
   const uint64_t a = g.off[sd.x], b = g.off[sd.x + 1];
+  if (sd.z == 1) {
+    *beg = a;
+    *end = b;
+    return;
+  }
   const uint64_t blk = (a >> g.seg_shift) + sd.y;
   *beg = sd.y == 0 ? a : blk << g.seg_shift;
   const uint64_t lim = (blk + 1) << g.seg_shift;
@@ -365,53 +371,56 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
     return;
   }
   set_ranks(lw, need, n_slots);
-  const uint64_t w0 = beg >> 5;
-  const uint64_t wi = w0 + lane;
-  uint32_t word = 0;
-  if (wi <= (end - 1) >> 5) {
-    word = st.lt[wi];
-    const uint64_t lo = wi << 5;
-    if (beg > lo) word &= ~0u << static_cast<uint32_t>(beg - lo);
-    if (end < lo + 32) word &= (1u << static_cast<uint32_t>(end - lo)) - 1u;
-  }
   if (lane == 0) tl.streamed += end - beg;
-  tl.gathered += __popc(word);
   uint32_t elim = 0;
-  for (unsigned nz = __ballot_sync(kFull, word != 0); nz;) {
-    uint32_t idx[kUnroll], bits[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      idx[u] = nz ? static_cast<uint32_t>(__ffs(nz) - 1) : 32u;
-      nz &= nz - 1;
-      bits[u] = __shfl_sync(kFull, word, idx[u] & 31);
-      if (idx[u] == 32) bits[u] = 0;
+  // Windows of 32 words (one per lane); a segment of a multi-segment hub is
+  // one window, a single-segment hub's list may take two.
+  for (uint64_t w0 = beg >> 5; end > beg && w0 <= (end - 1) >> 5; w0 += 32) {
+    const uint64_t wi = w0 + lane;
+    uint32_t word = 0;
+    if (wi <= (end - 1) >> 5) {
+      word = st.lt[wi];
+      const uint64_t lo = wi << 5;
+      if (beg > lo) word &= ~0u << static_cast<uint32_t>(beg - lo);
+      if (end < lo + 32) word &= (1u << static_cast<uint32_t>(end - lo)) - 1u;
     }
-    uint32_t nb[kUnroll];
+    tl.gathered += __popc(word);
+    for (unsigned nz = __ballot_sync(kFull, word != 0); nz;) {
+      uint32_t idx[kUnroll], bits[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u)
-      nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
-    W ww[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const bool in = (bits[u] >> lane) & 1u;
-      const uint64_t cw = Pack<W>::cand(ww[u]);
-      const bool live = in && cw != 0;
-      const bool poss = live && (cw & ncs) != 0;
-      const unsigned em = __ballot_sync(kFull, live && !poss);
-      const unsigned dm = __ballot_sync(kFull, in && cw == 0);
-      if (lane == 0 && (em | dm)) {
-        const uint64_t w = w0 + idx[u];
-        if (em) atomicAnd(st.eact + w, ~em);
-        atomicAnd(st.lt + w, ~(em | dm));
+      for (int u = 0; u < kUnroll; ++u) {
+        idx[u] = nz ? static_cast<uint32_t>(__ffs(nz) - 1) : 32u;
+        nz &= nz - 1;
+        bits[u] = __shfl_sync(kFull, word, idx[u] & 31);
+        if (idx[u] == 32) bits[u] = 0;
       }
-      elim += __popc(em);
-      if (poss) {
-        const uint32_t sw = Pack<W>::slot(ww[u]);
-        if (sw < 64) {
-          const uint32_t r = lw.rank_of[sw];
-          if (r != kNoRank) ++lw.cnt[r][lane];
+      uint32_t nb[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u)
+        nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
+      W ww[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const bool in = (bits[u] >> lane) & 1u;
+        const uint64_t cw = Pack<W>::cand(ww[u]);
+        const bool live = in && cw != 0;
+        const bool poss = live && (cw & ncs) != 0;
+        const unsigned em = __ballot_sync(kFull, live && !poss);
+        const unsigned dm = __ballot_sync(kFull, in && cw == 0);
+        if (lane == 0 && (em | dm)) {
+          const uint64_t w = w0 + idx[u];
+          if (em) atomicAnd(st.eact + w, ~em);
+          atomicAnd(st.lt + w, ~(em | dm));
+        }
+        elim += __popc(em);
+        if (poss) {
+          const uint32_t sw = Pack<W>::slot(ww[u]);
+          if (sw < 64) {
+            const uint32_t r = lw.rank_of[sw];
+            if (r != kNoRank) ++lw.cnt[r][lane];
+          }
         }
       }
     }
@@ -513,28 +522,146 @@ __device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const Lcc
   }
 }
 
-// One tile of 32 consecutive vertices (light ones only).
+// 32 single-segment hubs, one per lane: each lane walks the live-target
+// words of its own list, up to kUnroll set bits per round, counting into its
+// own column of the warp's counters and clearing bits one atomic per word.
+// Falls back to lcc_segments when the batch needs more than kHubRanks slots.
 template <class W>
-__device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, uint64_t v0,
-                         LccTally& tl) {
+__device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw,
+                                HubAcc* acc, uint64_t block, LccTally& tl) {
   const unsigned lane = lane_id();
-  const uint64_t vv = v0 + lane;
-  const uint32_t v = static_cast<uint32_t>(vv);
-  bool work = false;
+  const uint64_t i = g.n_heavy + block * 32 + lane;
+  uint32_t v = 0;
   W wv = Pack<W>::zero();
-  uint64_t b = 0;
-  uint32_t len = 0;
-  if (vv < g.V) {
-    // Independent loads in one round.
+  uint64_t b = 0, e = 0;
+  bool live = false;
+  if (i < g.n_seg) {
+    v = g.seg[i].x;
     const uint8_t sch = st.sch[v];
     wv = st.vs[v];
     b = g.off[v];
-    const uint64_t deg = g.off[v + 1] - b;
-    if (sch && Pack<W>::cand(wv) && (g.n_seg == 0 || deg <= g.hub_degree)) {
-      work = true;
-      len = static_cast<uint32_t>(deg);
+    e = g.off[v + 1];
+    live = sch && Pack<W>::cand(wv) != 0;
+  }
+  if (!__ballot_sync(kFull, live)) return;
+  const uint64_t cu = live ? Pack<W>::cand(wv) : 0;
+  const uint32_t su = Pack<W>::slot(wv);
+  uint64_t ncs, need;
+  role_unions(t, cu, &ncs, &need);
+  const uint64_t slots = warp_or64(need);
+  const uint32_t n_slots = __popcll(slots);
+  if (n_slots > kHubRanks) {
+    lcc_segments(g, st, t, lw, acc, block, tl);
+    return;
+  }
+  set_ranks(lw, slots, n_slots);
+  // Current word w of [b, e), masked to the list; done when w > wl.
+  uint64_t w = b >> 5, wl = 0;
+  bool more = live && e > b;
+  if (more) wl = (e - 1) >> 5;
+  auto load_word = [&](uint64_t x) {
+    uint32_t word = st.lt[x];
+    const uint64_t lo = x << 5;
+    if (b > lo) word &= ~0u << static_cast<uint32_t>(b - lo);
+    if (e < lo + 32) word &= (1u << static_cast<uint32_t>(e - lo)) - 1u;
+    return word;
+  };
+  uint32_t word = more ? load_word(w) : 0u;
+  uint32_t clr = 0, elm = 0;  // bits of word w to clear in lt / eact
+  uint32_t elim = 0, gathered = 0;
+  while (__any_sync(kFull, more)) {
+    // Lanes whose word is used up flush it and move to the next one.
+    while (more && word == 0) {
+      if (clr) atomicAnd(st.lt + w, ~clr);
+      if (elm) atomicAnd(st.eact + w, ~elm);
+      clr = elm = 0;
+      if (++w > wl) {
+        more = false;
+      } else {
+        word = load_word(w);
+      }
+    }
+    uint32_t bit[kUnroll], nb[kUnroll];
+    bool in[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      in[u] = word != 0;
+      bit[u] = in[u] ? static_cast<uint32_t>(__ffs(word) - 1) : 0u;
+      word &= word - 1;
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) nb[u] = in[u] ? g.adj[(w << 5) + bit[u]] : 0u;
+    W ww[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) ww[u] = in[u] ? st.vs[nb[u]] : Pack<W>::zero();
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      if (!in[u]) continue;
+      ++gathered;
+      const uint64_t cw = Pack<W>::cand(ww[u]);
+      const bool poss = (cw & ncs) != 0;
+      if (!poss) {
+        clr |= 1u << bit[u];
+        if (cw) {
+          elm |= 1u << bit[u];
+          ++elim;
+        }
+      } else {
+        const uint32_t sw = Pack<W>::slot(ww[u]);
+        if (sw < 64) {
+          const uint32_t r = lw.rank_of[sw];
+          if (r != kNoRank) ++lw.cnt[r][lane];
+        }
+      }
     }
   }
+  if (clr) atomicAnd(st.lt + w, ~clr);
+  if (elm) atomicAnd(st.eact + w, ~elm);
+  if (live) {
+    const uint64_t tu = failing_roles(t, cu, su, slots, [&](uint32_t rank) { return lw.cnt[rank][lane]; });
+    lcc_record(st, v, tu, elim, tl.newly_modified);
+    tl.edge_elim += elim;
+    tl.gathered += gathered;
+    tl.streamed += static_cast<uint32_t>(e - b);
+  }
+}
+
+// Lane's vertex of a light tile: scheduled, holding a role, not a hub.
+template <class W>
+struct TileLane {
+  W wv;
+  uint64_t b;
+  uint32_t len;
+  bool work;
+};
+
+template <class W>
+__device__ __forceinline__ TileLane<W> tile_lane(const DevGraph& g, const DevState<W>& st, uint64_t vv) {
+  TileLane<W> x{Pack<W>::zero(), 0, 0, false};
+  if (vv < g.V) {
+    const uint32_t v = static_cast<uint32_t>(vv);
+    const uint8_t sch = st.sch[v];
+    x.wv = st.vs[v];
+    x.b = g.off[v];
+    const uint64_t deg = g.off[v + 1] - x.b;
+    if (sch && Pack<W>::cand(x.wv) && (g.n_seg == 0 || deg <= g.hub_degree)) {
+      x.work = true;
+      x.len = static_cast<uint32_t>(deg);
+    }
+  }
+  return x;
+}
+
+// One tile of 32 consecutive vertices (light ones only), lane state loaded.
+template <class W>
+__device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, uint64_t v0,
+                         const TileLane<W>& x, LccTally& tl) {
+  const unsigned lane = lane_id();
+  const uint32_t v = static_cast<uint32_t>(v0 + lane);
+  const bool work = x.work;
+  const W wv = x.wv;
+  const uint64_t b = x.b;
+  const uint32_t len = x.len;
   const unsigned wm = __ballot_sync(kFull, work);
   if (!wm) return;
   const uint64_t cu = work ? Pack<W>::cand(wv) : 0;
@@ -630,17 +757,27 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph
   LccWarp& lw = s_lw[threadIdx.x >> 5];
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
-  const uint64_t n_tasks = kTiles ? (static_cast<uint64_t>(g.V) + 31) / 32 : batched;
+  // Tile tasks cover kTileGroup consecutive tiles whose lane state is loaded
+  // in one round (most tiles have nothing scheduled).
+  const uint64_t n_tasks =
+      kTiles ? ((static_cast<uint64_t>(g.V) + 31) / 32 + kTileGroup - 1) / kTileGroup : batched;
   const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   LccTally tl;
   for (uint64_t task = warp; task < n_tasks; task += n_warps) {
-    if (kTiles)
-      lcc_tile(g, st, t, lw, task * 32, tl);
-    else if (task < heavy)
+    if (kTiles) {
+      const uint64_t v0 = task * 32 * kTileGroup;
+      TileLane<W> x[kTileGroup];
+#pragma unroll
+      for (int u = 0; u < kTileGroup; ++u) x[u] = tile_lane(g, st, v0 + 32 * u + lane_id());
+#pragma unroll
+      for (int u = 0; u < kTileGroup; ++u)
+        if (__any_sync(kFull, x[u].work)) lcc_tile(g, st, t, lw, v0 + 32 * u, x[u], tl);
+    } else if (task < heavy) {
       lcc_heavy(g, st, t, lw, hub_acc, task, tl);
-    else
-      lcc_segments(g, st, t, lw, hub_acc, task - heavy, tl);
+    } else {
+      lcc_batch_lanes(g, st, t, lw, hub_acc, task - heavy, tl);
+    }
   }
   const uint32_t ee = __reduce_add_sync(kFull, tl.edge_elim);
   const uint32_t nm = __reduce_add_sync(kFull, tl.newly_modified);
@@ -989,7 +1126,7 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) 
     PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W, false><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables,
                                                                                    q.hub_acc, q.ctr));
   }
-  const int grid = grid_for_tasks((static_cast<uint64_t>(g.V) + 31) / 32, 4);
+  const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + kTileGroup - 1) / kTileGroup, 4);
   PM_DISPATCH_WORD(q.word_kind,
                    k_lcc_check<W, true><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.hub_acc, q.ctr));
 }
