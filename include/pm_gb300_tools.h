@@ -64,8 +64,31 @@ pm_status_t pm_set_enum_split(uint32_t parts, uint32_t after_levels);
 /* ENUMERATION sources with more than slice_entries first-hop entries start
  * as slices of that many entries, queued before the other sources, so hub
  * sources are spread over many warps from the start (0: every source starts
- * whole; default 16).  Process-wide; speed only.  Set it while no query runs. */
+ * whole; defaults 32 for templates whose enumeration uses a count memo, 8
+ * for the others; this call sets both).  Process-wide; speed only.  Set it
+ * while no query runs. */
 pm_status_t pm_set_enum_presplit(uint32_t slice_entries);
+
+/* pm_set_enum_presplit per kind: templates whose enumeration uses a count
+ * memo, and the others. */
+pm_status_t pm_set_enum_presplit_by_kind(uint32_t with_count_memo, uint32_t without_count_memo);
+
+/* Autotuner over the speed-only choices (no counterpart in the reference):
+ * runs up to max_per_group of the templates whose enumeration uses a count
+ * memo (pairwise distinct labels) and up to max_per_group of the others
+ * under candidate LCC degree classes (pm_graph_set_hub_plan), enumeration
+ * slice sizes (per kind; pm_set_enum_presplit sets both) and count-memo
+ * sizes, keeps the choices with the least device time in force and reports
+ * them.  Every candidate must reproduce the same match counts.  No query of
+ * g may be running. */
+typedef struct pm_tune_result {
+  uint32_t hub_degree, seg_entries;
+  uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
+  uint32_t probes_memo, probes_plain, runs;
+} pm_tune_result;
+
+pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
+                        uint32_t max_per_group, pm_tune_result* result);
 
 /* Count-memo entries per warp in ENUMERATION's first round (power of two,
  * 1024 to 2^20; default 8192).  Larger tables let more sources finish in

@@ -73,6 +73,18 @@ class TemplateCsr(ctypes.Structure):
                 ("edge_count", ctypes.c_uint64)]
 
 
+class TuneResult(ctypes.Structure):
+    """pm_tune_result: the choices pm_autotune left in force."""
+
+    _fields_ = [("hub_degree", ctypes.c_uint32), ("seg_entries", ctypes.c_uint32),
+                ("enum_presplit_memo", ctypes.c_uint32), ("enum_presplit_plain", ctypes.c_uint32),
+                ("enum_table_entries", ctypes.c_uint32), ("probes_memo", ctypes.c_uint32),
+                ("probes_plain", ctypes.c_uint32), ("runs", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 PM_SUBMIT_EXPORT_STATE = 1
 
 
@@ -141,6 +153,9 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_enum_presplit_by_kind": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
+        "pm_autotune": (ctypes.c_int32, [ctypes.c_void_p, P(TemplateCsr), ctypes.c_uint32, ctypes.c_uint32,
+                                         P(TuneResult)]),
         "pm_template_dump_constraints": (ctypes.c_int32, [c_u64p, c_u32p, c_u64p, ctypes.c_uint32, ctypes.c_uint64,
                                                           ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]),
         "pm_query_destroy": (None, [ctypes.c_void_p]),
@@ -500,6 +515,29 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def _template_array(patterns):
+    keep = []
+    arr = (TemplateCsr * max(len(patterns), 1))()
+    for i, p in enumerate(patterns):
+        off = np.ascontiguousarray(p.offsets, np.uint64)
+        adj = np.ascontiguousarray(p.adj, np.uint32)
+        lab = np.ascontiguousarray(p.labels, np.uint64)
+        keep += [off, adj, lab]
+        arr[i] = TemplateCsr(_ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32), _ptr(lab, ctypes.c_uint64),
+                             p.n, len(adj))
+    return arr, keep
+
+
+def autotune(graph: Graph, patterns, max_per_group: int = 4) -> dict:
+    """pm_autotune: times candidate degree classes and enumeration settings
+    on the probe templates, keeps the fastest in force, returns them."""
+    arr, keep = _template_array(patterns)
+    r = TuneResult()
+    _check(lib.pm_autotune(graph._h, arr, len(patterns), max_per_group, ctypes.byref(r)))
+    del keep
+    return r.as_dict()
 
 
 def batch_run(graph: Graph, patterns, slots: int = 4):

@@ -1,0 +1,125 @@
+// Autotuner for the speed-only choices of the pipeline: the LCC degree
+// classes of a graph (hub_degree, seg_entries) and the ENUMERATION slicing
+// and count-memo size.  It runs the caller's probe templates under each
+// candidate, keeps the candidate with the least device time for the steps
+// it affects, and leaves it in force.  Every candidate must reproduce the
+// same match counts (the choices change speed only); a difference is an
+// internal error.
+#include "autotune.h"
+
+#include <algorithm>
+#include <limits>
+
+namespace pmgb {
+namespace {
+
+struct ProbeRun {
+  double lcc_ms = 0, enum_ms = 0;
+  std::vector<uint64_t> counts;
+};
+
+ProbeRun run_probes(GraphImpl* g, const std::vector<const PatternGraph*>& probes) {
+  ProbeRun r;
+  for (const PatternGraph* p : probes) {
+    QueryImpl q;
+    q.create(g, *p, nullptr);
+    q.run_all();
+    for (const pm_step_record& rec : q.records) {
+      if (rec.step == PM_STEP_LCC) r.lcc_ms += rec.step_ms;
+      if (rec.step == PM_STEP_ENUMERATION) r.enum_ms += rec.step_ms;
+    }
+    r.counts.push_back(q.match_count);
+  }
+  return r;
+}
+
+bool has_count_memo(const PatternGraph& p) {
+  const QueryConstraints qc = compile_constraints(p);
+  const CompiledConstraint cc = compile_enumeration(qc.enumeration, p.labels);
+  return !cc.programs.empty() && cc.programs[0].count_memo;
+}
+
+}  // namespace
+
+TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, uint32_t max_per_group) {
+  if (templates.empty()) throw PmError{PM_E_INVALID_ARG, "autotune needs at least one template"};
+  if (max_per_group == 0) max_per_group = 1;
+  std::vector<const PatternGraph*> memo, plain;
+  for (const PatternGraph& p : templates) {
+    auto& grp = has_count_memo(p) ? memo : plain;
+    if (grp.size() < max_per_group) grp.push_back(&p);
+  }
+  std::vector<const PatternGraph*> all(memo);
+  all.insert(all.end(), plain.begin(), plain.end());
+
+  TuneResult out;
+  const std::vector<uint64_t> reference = run_probes(g, all).counts;
+  auto check = [&](const ProbeRun& r, const std::vector<const PatternGraph*>& set) {
+    ++out.runs;
+    // Counts of `set`, which is a prefix (memo) or suffix (plain) of `all`.
+    const size_t off = (&set == &plain) ? memo.size() : 0;
+    for (size_t i = 0; i < r.counts.size(); ++i)
+      if (r.counts[i] != reference[off + i])
+        throw PmError{PM_FAILURE, "autotune: a candidate changed a match count"};
+  };
+
+  // 1. LCC degree classes, timed on the LCC steps of every probe.
+  const std::pair<uint32_t, uint32_t> plans[] = {{32, 1024}, {16, 1024}, {64, 1024}, {32, 512}, {128, 1024}};
+  double best = std::numeric_limits<double>::infinity();
+  std::pair<uint32_t, uint32_t> best_plan = {g->hub_degree, g->seg_entries};
+  for (const auto& pl : plans) {
+    g->build_hub_plan(pl.first, pl.second);
+    const ProbeRun r = run_probes(g, all);
+    check(r, all);
+    if (r.lcc_ms < best) {
+      best = r.lcc_ms;
+      best_plan = pl;
+    }
+  }
+  g->build_hub_plan(best_plan.first, best_plan.second);
+  out.hub_degree = best_plan.first;
+  out.seg_entries = best_plan.second;
+
+  // 2. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.
+  const uint32_t slices[] = {4, 8, 16, 32, 64};
+  for (int kind = 0; kind < 2; ++kind) {
+    const bool with_memo = kind == 0;
+    const auto& set = with_memo ? memo : plain;
+    if (set.empty()) continue;
+    double b = std::numeric_limits<double>::infinity();
+    uint32_t pick = enum_presplit(with_memo);
+    for (uint32_t sl : slices) {
+      set_enum_presplit(with_memo, sl);
+      const ProbeRun r = run_probes(g, set);
+      check(r, set);
+      if (r.enum_ms < b) {
+        b = r.enum_ms;
+        pick = sl;
+      }
+    }
+    set_enum_presplit(with_memo, pick);
+  }
+  out.enum_presplit_memo = enum_presplit(true);
+  out.enum_presplit_plain = enum_presplit(false);
+
+  // 3. Count-memo entries per warp, on every probe.
+  const uint32_t tables[] = {4096, 8192, 16384};
+  double bt = std::numeric_limits<double>::infinity();
+  uint32_t pick_t = enum_table_entries();
+  for (uint32_t t : tables) {
+    set_enum_table_entries(t);
+    const ProbeRun r = run_probes(g, all);
+    check(r, all);
+    if (r.enum_ms < bt) {
+      bt = r.enum_ms;
+      pick_t = t;
+    }
+  }
+  set_enum_table_entries(pick_t);
+  out.enum_table_entries = pick_t;
+  out.probes_memo = static_cast<uint32_t>(memo.size());
+  out.probes_plain = static_cast<uint32_t>(plain.size());
+  return out;
+}
+
+}  // namespace pmgb

@@ -6,6 +6,7 @@
 #include "../../include/pm_gb300_tools.h"
 #include "engine.h"
 #include "generators.h"
+#include "autotune.h"
 #include "server.h"
 #include "totem_io.h"
 
@@ -328,6 +329,7 @@ pm_status_t pm_set_enum_presplit(uint32_t slice_entries) {
   return PM_SUCCESS;
 }
 
+
 pm_status_t pm_set_enum_table_entries(uint32_t entries) {
   PM_REQUIRE(entries >= 1024 && entries <= (1u << 20) && !(entries & (entries - 1)),
              "entries must be a power of two in [1024, 2^20]");
@@ -564,6 +566,37 @@ pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t
     }
     return PM_SUCCESS;
   });
+}
+
+pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t max_per_group,
+                        pm_tune_result* result) {
+  PM_REQUIRE(g && templates && n > 0, "bad argument");
+  return guarded([&]() -> pm_status_t {
+    g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    std::vector<PatternGraph> ps;
+    for (uint32_t i = 0; i < n; ++i) {
+      const pm_template_csr& t = templates[i];
+      ps.push_back(pattern_from_csr(t.offsets, t.adj, t.labels, t.vertex_count, t.edge_count));
+    }
+    const TuneResult r = autotune(&g->impl, ps, max_per_group);
+    if (result) {
+      result->hub_degree = r.hub_degree;
+      result->seg_entries = r.seg_entries;
+      result->enum_presplit_memo = r.enum_presplit_memo;
+      result->enum_presplit_plain = r.enum_presplit_plain;
+      result->enum_table_entries = r.enum_table_entries;
+      result->probes_memo = r.probes_memo;
+      result->probes_plain = r.probes_plain;
+      result->runs = r.runs;
+    }
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_set_enum_presplit_by_kind(uint32_t with_count_memo, uint32_t without_count_memo) {
+  set_enum_presplit(true, with_count_memo);
+  set_enum_presplit(false, without_count_memo);
+  return PM_SUCCESS;
 }
 
 pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_adj, uint32_t vertex_count,

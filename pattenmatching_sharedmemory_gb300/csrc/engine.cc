@@ -628,10 +628,17 @@ namespace {
 uint32_t g_enum_split_parts = 16;  // slices per split source (<= 1: never split)
 uint32_t g_enum_split_after = 0;   // table growth levels before sources are split
 uint32_t g_enum_state_cap = 8192;  // count-memo entries per warp, first round
-uint32_t g_enum_presplit = 16;     // first-hop entries per slice of a heavy source (0: no up-front slicing)
+// First-hop entries per slice of a heavy source (0: no up-front slicing),
+// for programs with and without a count memo.
+uint32_t g_enum_presplit_memo = 32;
+uint32_t g_enum_presplit_plain = 8;
 }  // namespace
 
-void set_enum_presplit(uint32_t slice_entries) { g_enum_presplit = slice_entries; }
+void set_enum_presplit(uint32_t slice_entries) { g_enum_presplit_memo = g_enum_presplit_plain = slice_entries; }
+void set_enum_presplit(bool count_memo, uint32_t slice_entries) {
+  (count_memo ? g_enum_presplit_memo : g_enum_presplit_plain) = slice_entries;
+}
+uint32_t enum_presplit(bool count_memo) { return count_memo ? g_enum_presplit_memo : g_enum_presplit_plain; }
 
 void set_enum_split(uint32_t parts, uint32_t after_levels) {
   g_enum_split_parts = parts;
@@ -667,13 +674,14 @@ StepResult QueryImpl::step_enumeration() {
     const std::vector<uint64_t>& off = g->host.offsets;
     std::vector<uint4> over, items;
     zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
-    if (splittable && g_enum_presplit) {
-      // Sources with more first-hop entries than g_enum_presplit start as
-      // slices of that many entries, queued first (the longest work).
+    const uint32_t presplit = enum_presplit(p.count_memo != 0);
+    if (splittable && presplit) {
+      // Sources with more first-hop entries than `presplit` start as slices
+      // of that many entries, queued first (the longest work).
       std::vector<uint32_t> wl(n_wl);
       PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
       PM_CUDA(cudaStreamSynchronize(stream));
-      const uint64_t t = g_enum_presplit;
+      const uint64_t t = presplit;
       for (uint32_t i = 0; i < n_wl; ++i) {
         const uint64_t deg = off[wl[i] + 1] - off[wl[i]];
         if (deg <= t) continue;

@@ -176,8 +176,11 @@ PatternGraph load_pattern(const std::string& dir, bool load_labels);
 // `parts` first-hop slices (parts <= 1: never split).
 void set_enum_split(uint32_t parts, uint32_t after_levels);
 // ENUMERATION sources with more first-hop entries than this start as slices
-// of that many entries (0: every source starts whole).
+// of that many entries (0: every source starts whole); one value for both
+// program kinds, or for programs with / without a count memo.
 void set_enum_presplit(uint32_t slice_entries);
+void set_enum_presplit(bool count_memo, uint32_t slice_entries);
+uint32_t enum_presplit(bool count_memo);
 // Count-memo entries per warp in ENUMERATION's first round (power of two).
 void set_enum_table_entries(uint32_t entries);
 uint32_t enum_table_entries();

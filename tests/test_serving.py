@@ -151,3 +151,29 @@ def test_shutdown_with_queued_requests():
     # The graph is still usable afterwards.
     assert _alone(g, C.make_pattern(SYNTH["triangle_rep_s9"]))[1] == _alone(
         g, C.make_pattern(SYNTH["triangle_rep_s9"]))[1]
+
+
+def test_autotune_rejects_empty_list():
+    import ctypes
+
+    g = pm.Graph.rmat(6, 4, seed=1)
+    r = pm.TuneResult()
+    assert pm.lib.pm_autotune(g._h, None, 0, 4, ctypes.byref(r)) == pm.PM_E_INVALID_ARG
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results():
+    """The tuner's choices change speed only: counts before and after match."""
+    g = _graph()
+    patterns = [C.make_pattern(SYNTH[n]) for n in MIX[:4]]
+    before = [_alone(g, p)[1] for p in patterns]
+    chosen = pm.autotune(g, patterns, max_per_group=2)
+    assert chosen["runs"] > 0
+    assert chosen["probes_memo"] + chosen["probes_plain"] >= 1
+    assert chosen["seg_entries"] in (512, 1024)
+    after = [_alone(g, p)[1] for p in patterns]
+    assert after == before
+    # Leave the defaults for the tests that follow.
+    pm.lib.pm_set_enum_table_entries(8192)
+    pm.lib.pm_set_enum_presplit_by_kind(32, 8)
+    g.set_hub_plan(32, 1024)
