@@ -76,19 +76,32 @@ pm_status_t pm_set_enum_presplit_by_kind(uint32_t with_count_memo, uint32_t with
 /* Autotuner over the speed-only choices (no counterpart in the reference):
  * runs up to max_per_group of the templates whose enumeration uses a count
  * memo (pairwise distinct labels) and up to max_per_group of the others
- * under candidate LCC degree classes (pm_graph_set_hub_plan), enumeration
- * slice sizes (per kind; pm_set_enum_presplit sets both) and count-memo
- * sizes, keeps the choices with the least device time in force and reports
- * them.  Every candidate must reproduce the same match counts.  No query of
+ * under candidate LCC degree classes (pm_graph_set_hub_plan), walk slice
+ * and state-memo sizes, enumeration slice sizes (per kind;
+ * pm_set_enum_presplit sets both) and count-memo sizes, keeps the choices
+ * with the least device time in force and reports them.  Every candidate must reproduce the same match counts.  No query of
  * g may be running. */
 typedef struct pm_tune_result {
   uint32_t hub_degree, seg_entries;
   uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
+  uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
                         uint32_t max_per_group, pm_tune_result* result);
+
+/* CC/PC/TDS walks of exact programs (no memo test can block, see the
+ * walker): an item whose source has more than slice_entries first-hop
+ * entries runs as slices of that many entries on separate warps, and
+ * succeeds when any slice does (0: never; default 64).  Process-wide; speed
+ * only.  Set it while no query runs. */
+pm_status_t pm_set_walk_presplit(uint32_t slice_entries);
+
+/* State-memo entries per warp in the first CC/PC/TDS walk round (power of
+ * two, 1024 to 2^20; default 8192).  Process-wide; speed only.  Set it while
+ * no query runs. */
+pm_status_t pm_set_walk_table_entries(uint32_t entries);
 
 /* Count-memo entries per warp in ENUMERATION's first round (power of two,
  * 1024 to 2^20; default 8192).  Larger tables let more sources finish in

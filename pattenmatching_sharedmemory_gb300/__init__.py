@@ -78,7 +78,8 @@ class TuneResult(ctypes.Structure):
 
     _fields_ = [("hub_degree", ctypes.c_uint32), ("seg_entries", ctypes.c_uint32),
                 ("enum_presplit_memo", ctypes.c_uint32), ("enum_presplit_plain", ctypes.c_uint32),
-                ("enum_table_entries", ctypes.c_uint32), ("probes_memo", ctypes.c_uint32),
+                ("enum_table_entries", ctypes.c_uint32), ("walk_presplit", ctypes.c_uint32),
+                ("walk_table_entries", ctypes.c_uint32), ("probes_memo", ctypes.c_uint32),
                 ("probes_plain", ctypes.c_uint32), ("runs", ctypes.c_uint32)]
 
     def as_dict(self):
@@ -152,6 +153,8 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_walk_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_walk_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_presplit_by_kind": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_autotune": (ctypes.c_int32, [ctypes.c_void_p, P(TemplateCsr), ctypes.c_uint32, ctypes.c_uint32,

@@ -1,8 +1,9 @@
 // Autotuner for the speed-only choices of the pipeline: the LCC degree
-// classes of a graph (hub_degree, seg_entries) and the ENUMERATION slicing
-// and count-memo size.  It runs the caller's probe templates under each
-// candidate, keeps the candidate with the least device time for the steps
-// it affects, and leaves it in force.  Every candidate must reproduce the
+// classes of a graph (hub_degree, seg_entries), the CC/PC/TDS slicing and
+// state-memo size, and the ENUMERATION slicing and count-memo size.  It runs
+// the caller's probe templates under each candidate, keeps the candidate
+// with the least device time for the steps it affects, and leaves it in
+// force.  Every candidate must reproduce the
 // same match counts (the choices change speed only); a difference is an
 // internal error.
 #include "autotune.h"
@@ -14,7 +15,7 @@ namespace pmgb {
 namespace {
 
 struct ProbeRun {
-  double lcc_ms = 0, enum_ms = 0;
+  double lcc_ms = 0, walk_ms = 0, enum_ms = 0;
   std::vector<uint64_t> counts;
 };
 
@@ -26,6 +27,7 @@ ProbeRun run_probes(GraphImpl* g, const std::vector<const PatternGraph*>& probes
     q.run_all();
     for (const pm_step_record& rec : q.records) {
       if (rec.step == PM_STEP_LCC) r.lcc_ms += rec.step_ms;
+      if (rec.step == PM_STEP_CC || rec.step == PM_STEP_PC || rec.step == PM_STEP_TDS) r.walk_ms += rec.step_ms;
       if (rec.step == PM_STEP_ENUMERATION) r.enum_ms += rec.step_ms;
     }
     r.counts.push_back(q.match_count);
@@ -80,7 +82,39 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
   out.hub_degree = best_plan.first;
   out.seg_entries = best_plan.second;
 
-  // 2. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.
+  // 2. CC/PC/TDS slices and state-memo size, timed on those steps.
+  {
+    const uint32_t walk_slices[] = {0, 16, 64, 256};
+    double b = std::numeric_limits<double>::infinity();
+    uint32_t pick = walk_presplit();
+    for (uint32_t sl : walk_slices) {
+      set_walk_presplit(sl);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.walk_ms < b) {
+        b = r.walk_ms;
+        pick = sl;
+      }
+    }
+    set_walk_presplit(pick);
+    const uint32_t walk_tables[] = {2048, 8192, 32768};
+    b = std::numeric_limits<double>::infinity();
+    uint32_t pick_t = walk_table_entries();
+    for (uint32_t t : walk_tables) {
+      set_walk_table_entries(t);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.walk_ms < b) {
+        b = r.walk_ms;
+        pick_t = t;
+      }
+    }
+    set_walk_table_entries(pick_t);
+    out.walk_presplit = pick;
+    out.walk_table_entries = pick_t;
+  }
+
+  // 3. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.
   const uint32_t slices[] = {4, 8, 16, 32, 64};
   for (int kind = 0; kind < 2; ++kind) {
     const bool with_memo = kind == 0;
@@ -102,7 +136,7 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
   out.enum_presplit_memo = enum_presplit(true);
   out.enum_presplit_plain = enum_presplit(false);
 
-  // 3. Count-memo entries per warp, on every probe.
+  // 4. Count-memo entries per warp, on every probe.
   const uint32_t tables[] = {4096, 8192, 16384};
   double bt = std::numeric_limits<double>::infinity();
   uint32_t pick_t = enum_table_entries();

@@ -10,6 +10,7 @@ namespace pmgb {
 struct TuneResult {
   uint32_t hub_degree = 0, seg_entries = 0;
   uint32_t enum_presplit_memo = 0, enum_presplit_plain = 0, enum_table_entries = 0;
+  uint32_t walk_presplit = 0, walk_table_entries = 0;
   uint32_t probes_memo = 0, probes_plain = 0;  // probe templates per program kind
   uint32_t runs = 0;                            // candidate runs over the probes
 };

@@ -330,6 +330,18 @@ pm_status_t pm_set_enum_presplit(uint32_t slice_entries) {
 }
 
 
+pm_status_t pm_set_walk_presplit(uint32_t slice_entries) {
+  set_walk_presplit(slice_entries);
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_set_walk_table_entries(uint32_t entries) {
+  PM_REQUIRE(entries >= 1024 && entries <= (1u << 20) && !(entries & (entries - 1)),
+             "entries must be a power of two in [1024, 2^20]");
+  set_walk_table_entries(entries);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_enum_table_entries(uint32_t entries) {
   PM_REQUIRE(entries >= 1024 && entries <= (1u << 20) && !(entries & (entries - 1)),
              "entries must be a power of two in [1024, 2^20]");
@@ -585,6 +597,8 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->enum_presplit_memo = r.enum_presplit_memo;
       result->enum_presplit_plain = r.enum_presplit_plain;
       result->enum_table_entries = r.enum_table_entries;
+      result->walk_presplit = r.walk_presplit;
+      result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;
       result->probes_plain = r.probes_plain;
       result->runs = r.runs;

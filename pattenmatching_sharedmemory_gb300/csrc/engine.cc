@@ -234,7 +234,7 @@ uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
   // hypothesis memo of (3 + stored vertices) words and a state memo of
   // (5 + key words) words per entry, both bounded through k.
   const uint64_t warps = static_cast<uint64_t>(walk_grid_blocks(1u << 30)) * kWalkWarpsPerBlock;
-  const uint64_t state_entries = std::max<uint64_t>(kStateCapEntries, enum_table_entries());
+  const uint64_t state_entries = std::max<uint64_t>(walk_table_entries(), enum_table_entries());
   const uint64_t pool = warps * (16ull * kEdgeCapEntries + 4ull * kHypCapEntries * (3 + kk) +
                                  4ull * state_entries * (7 + kk));
   // state + per-step worklist/status/markers (items bounded by V * roles)
@@ -264,7 +264,7 @@ QueryDevPtrs QueryImpl::ptrs() const {
 uint64_t QueryImpl::device_bytes() const {
   return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
          d_d2s.bytes + d_hub_acc.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
-         d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes +
+         d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes + d_slices.bytes +
          pool.bytes() + big_pool.bytes();
 }
 
@@ -272,7 +272,7 @@ std::vector<DeviceBuffer*> QueryImpl::buffers() {
   return {&d_vs,          &d_eact,      &d_lt,        &d_mod,       &d_sch,        &d_unm,         &d_ctr,
           &d_tables,      &d_d2s,       &d_hub_acc,   &d_progs,     &d_start_roles, &d_role_index,  &d_wl,
           &d_wl_index,    &d_blocks,    &d_count,     &d_status,    &d_marker,     &d_marks,       &d_list,
-          &d_list2,       &d_apply_v,   &d_apply_r,   &pool.edge,   &pool.hyp,     &pool.state,    &pool.epochs,
+          &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &pool.edge,   &pool.hyp,     &pool.state,    &pool.epochs,
           &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs};
 }
 
@@ -441,6 +441,8 @@ uint32_t QueryImpl::build_worklist(uint64_t mask) {
 
 namespace {
 constexpr uint32_t kEdgeCap = kEdgeCapEntries, kHypCap = kHypCapEntries, kStateCap = kStateCapEntries;
+uint32_t g_walk_state_cap = 8192;  // CC/PC/TDS state-memo entries per warp, first round
+uint32_t g_walk_presplit = 64;     // exact programs: first-hop entries per slice of a heavy item (0: off)
 void zero_field(void* base, size_t offset, cudaStream_t s) {
   PM_CUDA(cudaMemsetAsync(static_cast<char*>(base) + offset, 0, sizeof(unsigned long long), s));
 }
@@ -462,6 +464,11 @@ uint32_t max_hyp_words(const std::vector<DeviceConstraint>& v) {
 }
 }  // namespace
 
+void set_walk_table_entries(uint32_t entries) { g_walk_state_cap = entries; }
+void set_walk_presplit(uint32_t slice_entries) { g_walk_presplit = slice_entries; }
+uint32_t walk_presplit() { return g_walk_presplit; }
+uint32_t walk_table_entries() { return g_walk_state_cap; }
+
 void QueryImpl::pool_strides(uint32_t* hyp_stride, uint32_t* state_stride) const {
   *hyp_stride = 3 + std::max<uint32_t>({max_hyp_words(cycles), max_hyp_words(paths), max_hyp_words(templates), 1u});
   *state_stride = 5 + std::max<uint32_t>({max_state_words(cycles), max_state_words(paths), max_state_words(templates),
@@ -472,7 +479,7 @@ void QueryImpl::ensure_pool() {
   uint32_t hs, ss;
   pool_strides(&hs, &ss);
   const uint32_t base_warps = walk_grid_blocks(1u << 30) * kWalkWarpsPerBlock;
-  pool.ensure(base_warps, kEdgeCap, kHypCap, hs, kStateCap, ss, stream);
+  pool.ensure(base_warps, kEdgeCap, kHypCap, hs, g_walk_state_cap, ss, stream);
 }
 
 void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks) {
@@ -506,12 +513,58 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   w.marks = record_marks ? d_marks.as<uint32_t>() : nullptr;
   w.marks_stride = M;
 
+  // Exact programs may split heavy items into first-hop slices: an item
+  // succeeds when any slice does (no alreadyMatched marks to keep).
+  bool sliced = dc.cc.exact && !record_marks && g_walk_presplit > 0 && g->sorted_unique;
+  for (const WalkProgram& pr : dc.cc.programs)
+    if (pr.n_steps < 2 || (pr.steps[1].kind != kStepVertex && pr.steps[1].kind != kStepFinal)) sliced = false;
+  std::vector<uint4> slices;
+  if (sliced) {
+    std::vector<uint32_t> wl(n_wl);
+    PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
+    PM_CUDA(cudaStreamSynchronize(stream));
+    const std::vector<uint64_t>& off = g->host.offsets;
+    const uint64_t t = g_walk_presplit;
+    for (uint32_t pos = 0; pos < n_wl; ++pos) {
+      const uint64_t deg = off[wl[pos] + 1] - off[wl[pos]];
+      if (deg <= t) continue;
+      for (uint32_t r = 0; r < R; ++r)
+        for (uint64_t lo = 0; lo < deg; lo += t)
+          slices.push_back(make_uint4(pos * R + r, static_cast<uint32_t>(lo),
+                                      static_cast<uint32_t>(std::min(lo + t, deg)), 0));
+    }
+    sliced = !slices.empty();
+  }
   zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
   zero_field(d_ctr.ptr, offsetof(StepCounters, overflow), stream);
+  if (sliced) {
+    w.skip_deg = g_walk_presplit;
+    w.prio = d_marker.as<uint32_t>();
+    PM_CUDA(cudaMemsetAsync(d_marker.ptr, 0, 4 * n_items, stream));
+  }
   launch_walk(g->dev(), ptrs(), w, pool.sc, stream);
   PM_CUDA(cudaGetLastError());
+  if (sliced) {
+    d_slices.ensure(sizeof(uint4) * slices.size());
+    PM_CUDA(cudaMemcpyAsync(d_slices.ptr, slices.data(), sizeof(uint4) * slices.size(), cudaMemcpyHostToDevice,
+                            stream));
+    WalkLaunch ws = w;
+    ws.slices = d_slices.as<uint4>();
+    ws.n_slices = static_cast<uint32_t>(slices.size());
+    zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
+    launch_walk(g->dev(), ptrs(), ws, pool.sc, stream);
+    PM_CUDA(cudaGetLastError());
+    launch_prio_to_status(g->dev(), w, stream);
+    PM_CUDA(cudaGetLastError());
+    // Overflowed items (sliced ones included) are counted from the statuses.
+    d_list.ensure(4 * std::max<uint64_t>(n_items, 1));
+    zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
+    launch_collect_overflow(w, d_list.as<uint32_t>(), d_ctr.as<StepCounters>(), stream);
+  }
   read_counters();
-  uint64_t overflow = h_ctr->overflow;
+  uint64_t overflow = sliced ? h_ctr->aux : h_ctr->overflow;
+  w.skip_deg = 0;
+  w.prio = nullptr;
   int round = 0;
   while (overflow) {
     ++round;
@@ -522,8 +575,8 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
     launch_collect_overflow(w, d_list.as<uint32_t>(), d_ctr.as<StepCounters>(), stream);
     read_counters();
     const uint32_t n_retry = static_cast<uint32_t>(h_ctr->aux);
-    const uint32_t warps = retry_warps(base_warps, round, hyp_stride, state_stride);
-    big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, kStateCap << (3 * round),
+    const uint32_t warps = retry_warps(base_warps, round, hyp_stride, state_stride * (g_walk_state_cap / kStateCap));
+    big_pool.ensure(warps, kEdgeCap << (3 * round), kHypCap << (3 * round), hyp_stride, g_walk_state_cap << (3 * round),
                     state_stride, stream);
     WalkLaunch r = w;
     r.retry_items = d_list.as<uint32_t>();

@@ -106,7 +106,7 @@ struct QueryImpl {
   DeviceBuffer d_vs, d_eact, d_lt, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s, d_hub_acc;
   DeviceBuffer d_progs, d_start_roles, d_role_index;
   DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_list2, d_apply_v,
-      d_apply_r;
+      d_apply_r, d_slices;
   StepCounters* h_ctr = nullptr;  // pinned
   uint32_t* h_count = nullptr;    // pinned
   bool own_host = true;           // h_ctr / h_count allocated here
@@ -181,6 +181,13 @@ void set_enum_split(uint32_t parts, uint32_t after_levels);
 void set_enum_presplit(uint32_t slice_entries);
 void set_enum_presplit(bool count_memo, uint32_t slice_entries);
 uint32_t enum_presplit(bool count_memo);
+// Exact CC/PC/TDS programs: items whose source has more first-hop entries
+// than this run as slices of that many entries (0: never).
+void set_walk_presplit(uint32_t slice_entries);
+uint32_t walk_presplit();
+// State-memo entries per warp in the first CC/PC/TDS walk round.
+void set_walk_table_entries(uint32_t entries);
+uint32_t walk_table_entries();
 // Count-memo entries per warp in ENUMERATION's first round (power of two).
 void set_enum_table_entries(uint32_t entries);
 uint32_t enum_table_entries();

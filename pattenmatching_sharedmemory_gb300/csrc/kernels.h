@@ -102,7 +102,20 @@ struct WalkLaunch {
   uint32_t* min_marker;   // n_wl * n_progs, or null
   uint32_t* marks;        // n_wl * n_progs * marks_stride, or null
   uint32_t marks_stride;
+  // Exact programs only: items whose source has more than skip_deg entries
+  // are left out of the main launch and run as `slices` ({item, first-hop
+  // lo, hi, -}) whose results meet in prio[item] (atomicMax of kPrio*).
+  uint32_t skip_deg;
+  const uint4* slices;
+  uint32_t n_slices;
+  uint32_t* prio;
 };
+
+// Result priorities of sliced items: success of any slice decides the item.
+enum SlicePrio : uint32_t { kPrioSkip = 0, kPrioFail = 1, kPrioOverflow = 2, kPrioTimeout = 3, kPrioSuccess = 4 };
+
+// status[item] of every sliced item (source degree > skip_deg) from prio.
+void launch_prio_to_status(const DevGraph& g, const WalkLaunch& w, cudaStream_t s);
 
 // Phase 1 of CC/PC/TDS: every (vertex, start role) walk, in parallel.
 void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, const WalkScratch& scratch,

@@ -682,7 +682,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
   if (lane == 0) deadline = global_timer_ns() + budget_ns;
   deadline = __shfl_sync(kFull, deadline, 0);
   WarpMemo m = warp_memo(sc, gw);
-  const uint64_t n_items = w.retry_items ? w.n_retry : static_cast<uint64_t>(w.n_wl) * w.n_progs;
+  const uint64_t n_items =
+      w.slices ? w.n_slices : w.retry_items ? w.n_retry : static_cast<uint64_t>(w.n_wl) * w.n_progs;
   int cached = -1;
   unsigned long long overflow = 0;
   while (true) {
@@ -690,8 +691,17 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
     if (lane == 0) gi = atomicAdd(&ctr->items, 1ull);
     gi = __shfl_sync(kFull, gi, 0);
     if (gi >= n_items) break;
-    uint32_t item, r, pos;
-    if (w.retry_items) {
+    uint32_t item, r, pos, lo = 0, hi = 0xFFFFFFFFu;
+    if (w.slices) {
+      const uint4 sl = w.slices[gi];
+      item = sl.x;
+      lo = sl.y;
+      hi = sl.z;
+      pos = item / w.n_progs;
+      r = item % w.n_progs;
+      // Another slice of this item already succeeded.
+      if (*reinterpret_cast<volatile uint32_t*>(w.prio + item) == kPrioSuccess) continue;
+    } else if (w.retry_items) {
       item = w.retry_items[gi];
       pos = item / w.n_progs;
       r = item % w.n_progs;
@@ -700,19 +710,32 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
       pos = static_cast<uint32_t>(gi % w.n_wl);
       item = pos * w.n_progs + r;
     }
+    const uint32_t v = w.wl[pos];
+    // Sliced items are left to the slice launch.
+    if (!w.slices && !w.retry_items && w.skip_deg && g.off[v + 1] - g.off[v] > w.skip_deg) continue;
     if (static_cast<int>(r) != cached) {
       load_program(ws, w.progs + r);
       cached = static_cast<int>(r);
     }
-    const uint32_t v = w.wl[pos];
     if (!role_of(st, v, ws.prog.start_role)) {
-      if (lane == 0) w.status[item] = kItemSkip;
+      if (lane == 0 && !w.slices) w.status[item] = kItemSkip;
       continue;
     }
     next_epoch(m);
     unsigned long long unused = 0;
-    const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline);
-    if (lane == 0) w.status[item] = res;
+    const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline, lo, hi);
+    if (lane == 0) {
+      if (w.slices) {
+        const uint32_t pr = res == kItemSuccess    ? kPrioSuccess
+                            : res == kItemTimeout  ? kPrioTimeout
+                            : res == kItemOverflow ? kPrioOverflow
+                            : res == kItemFail     ? kPrioFail
+                                                   : kPrioSkip;
+        atomicMax(w.prio + item, pr);
+      } else {
+        w.status[item] = res;
+      }
+    }
     if (res == kItemOverflow) ++overflow;
     if (res == kItemTimeout) {
       if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
@@ -757,6 +780,21 @@ __global__ void k_flag_rescue(const uint8_t* __restrict__ status, const uint32_t
     if (status[i] == kItemFail && min_marker[i] < i) ++c;
   c = __reduce_add_sync(kFull, c);
   if (lane_id() == 0 && c) atomicAdd(&ctr->flagged, static_cast<unsigned long long>(c));
+}
+
+__global__ void k_prio_to_status(DevGraph g, WalkLaunch w) {
+  const uint64_t n = static_cast<uint64_t>(w.n_wl) * w.n_progs;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride) {
+    const uint32_t v = w.wl[i / w.n_progs];
+    if (g.off[v + 1] - g.off[v] <= w.skip_deg) continue;
+    const uint32_t pr = w.prio[i];
+    w.status[i] = pr == kPrioSuccess    ? kItemSuccess
+                  : pr == kPrioTimeout  ? kItemTimeout
+                  : pr == kPrioOverflow ? kItemOverflow
+                  : pr == kPrioFail     ? kItemFail
+                                        : kItemSkip;
+  }
 }
 
 __global__ void k_collect_overflow(const uint8_t* __restrict__ status, uint64_t n_items, uint32_t* list,
@@ -914,6 +952,11 @@ void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s) 
   const int grid = device_sm_count() * 4;
   note_launch();
   k_flag_rescue<<<grid, 256, 0, s>>>(w.status, w.min_marker, n, ctr);
+}
+
+void launch_prio_to_status(const DevGraph& g, const WalkLaunch& w, cudaStream_t s) {
+  note_launch();
+  k_prio_to_status<<<device_sm_count() * 4, 256, 0, s>>>(g, w);
 }
 
 void launch_collect_overflow(const WalkLaunch& w, uint32_t* list, StepCounters* ctr, cudaStream_t s) {

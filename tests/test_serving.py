@@ -176,4 +176,6 @@ def test_autotune_keeps_results():
     # Leave the defaults for the tests that follow.
     pm.lib.pm_set_enum_table_entries(8192)
     pm.lib.pm_set_enum_presplit_by_kind(32, 8)
+    pm.lib.pm_set_walk_presplit(64)
+    pm.lib.pm_set_walk_table_entries(8192)
     g.set_hub_plan(32, 1024)
