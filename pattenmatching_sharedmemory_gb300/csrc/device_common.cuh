@@ -122,6 +122,10 @@ struct DevState {
   // was seen with no role left (roles never come back).  The LCC sweep
   // skips entries outside it; nothing else reads it.
   uint32_t* lt;
+  // Per 32-vertex tile: 0 when sweep 2 left no vertex of the tile both
+  // holding a role and scheduled (hubs under the current plan count as
+  // scheduled), so LCC sweep 1 can skip the tile.  Null: no summary.
+  uint8_t* tile_sch;
 };
 
 // Device counters.  The first kStepCounterWords words are per step

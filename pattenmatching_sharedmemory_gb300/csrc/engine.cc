@@ -258,11 +258,11 @@ QueryImpl::~QueryImpl() {
 QueryDevPtrs QueryImpl::ptrs() const {
   return QueryDevPtrs{word_kind, d_vs.ptr, d_eact.as<uint32_t>(), d_mod.as<uint8_t>(), d_sch.as<uint8_t>(),
                       d_unm.ptr, d_ctr.as<StepCounters>(), d_tables.as<QueryTables>(), d_hub_acc.as<HubAcc>(),
-                      d_lt.as<uint32_t>()};
+                      d_lt.as<uint32_t>(), d_tile_sch.as<uint8_t>()};
 }
 
 uint64_t QueryImpl::device_bytes() const {
-  return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
+  return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_tile_sch.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
          d_d2s.bytes + d_hub_acc.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
          d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes + d_slices.bytes +
          pool.bytes() + big_pool.bytes();
@@ -270,6 +270,7 @@ uint64_t QueryImpl::device_bytes() const {
 
 std::vector<DeviceBuffer*> QueryImpl::buffers() {
   return {&d_vs,          &d_eact,      &d_lt,        &d_mod,       &d_sch,        &d_unm,         &d_ctr,
+          &d_tile_sch,
           &d_tables,      &d_d2s,       &d_hub_acc,   &d_progs,     &d_start_roles, &d_role_index,  &d_wl,
           &d_wl_index,    &d_blocks,    &d_count,     &d_status,    &d_marker,     &d_marks,       &d_list,
           &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &pool.edge,   &pool.hyp,     &pool.state,    &pool.epochs,
@@ -344,6 +345,7 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, 
   d_lt.ensure(4 * std::max<uint64_t>((E + 31) / 32, 1));
   d_mod.ensure(std::max<uint64_t>(V, 1));
   d_sch.ensure(std::max<uint64_t>(V, 1));
+  d_tile_sch.ensure(std::max<uint64_t>((V + 31) / 32, 1));
   d_ctr.ensure(sizeof(StepCounters));
   d_tables.ensure(sizeof(QueryTables));
   d_d2s.ensure(dense_to_slot.size());

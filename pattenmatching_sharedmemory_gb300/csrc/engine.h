@@ -103,7 +103,7 @@ struct QueryImpl {
 
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DeviceBuffer d_vs, d_eact, d_lt, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s, d_hub_acc;
+  DeviceBuffer d_vs, d_eact, d_lt, d_mod, d_sch, d_unm, d_ctr, d_tables, d_d2s, d_hub_acc, d_tile_sch;
   DeviceBuffer d_progs, d_start_roles, d_role_index;
   DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_list2, d_apply_v,
       d_apply_r, d_slices;

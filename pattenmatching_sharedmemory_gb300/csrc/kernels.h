@@ -26,6 +26,7 @@ struct QueryDevPtrs {
   const QueryTables* tables;
   HubAcc* hub_acc;  // [DevGraph::n_acc]
   uint32_t* lt;     // live-target bits (DevState::lt)
+  uint8_t* tile_sch;  // DevState::tile_sch, ceil(V / 32) bytes
 };
 
 // Launch geometry shared by all kernels (SM count of the current device).

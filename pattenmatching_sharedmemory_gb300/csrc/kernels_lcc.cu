@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(kThreads) k_init_state(DevGraph g, DevState<W>
     st.unm[v] = Pack<W>::zero();
     st.mod[v] = 0;
     st.sch[v] = 1;
+    if ((v & 31) == 0 && st.tile_sch) st.tile_sch[v >> 5] = 1;
   }
   const uint64_t words = (g.E + 31) / 32;
   for (uint64_t i = tid; i < words; i += stride) {
@@ -133,7 +134,6 @@ __global__ void __launch_bounds__(kThreads) k_lcc0(DevGraph g, DevState<W> st, c
 // with one update per group of equal keys (__match_any_sync).
 
 constexpr int kUnroll = 4;
-constexpr int kTileGroup = 1;
 constexpr int kLccWarps = kThreads / 32;
 constexpr uint8_t kNoRank = 0xFF;
 
@@ -522,38 +522,22 @@ __device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const Lcc
   }
 }
 
-// 32 single-segment hubs, one per lane: each lane walks the live-target
-// words of its own list, up to kUnroll set bits per round, counting into its
-// own column of the warp's counters and clearing bits one atomic per word.
-// Falls back to lcc_segments when the batch needs more than kHubRanks slots.
+// One vertex per lane: each lane walks the live-target words of its own
+// list [b, e), up to kUnroll set bits per round, counting into its own column
+// of the warp's counters and clearing bits one atomic per word.  Returns
+// false (and does nothing) when the warp's live lanes need more than
+// kHubRanks label slots.
 template <class W>
-__device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw,
-                                HubAcc* acc, uint64_t block, LccTally& tl) {
+__device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, uint32_t v,
+                          W wv, uint64_t b, uint64_t e, bool live, LccTally& tl) {
   const unsigned lane = lane_id();
-  const uint64_t i = g.n_heavy + block * 32 + lane;
-  uint32_t v = 0;
-  W wv = Pack<W>::zero();
-  uint64_t b = 0, e = 0;
-  bool live = false;
-  if (i < g.n_seg) {
-    v = g.seg[i].x;
-    const uint8_t sch = st.sch[v];
-    wv = st.vs[v];
-    b = g.off[v];
-    e = g.off[v + 1];
-    live = sch && Pack<W>::cand(wv) != 0;
-  }
-  if (!__ballot_sync(kFull, live)) return;
   const uint64_t cu = live ? Pack<W>::cand(wv) : 0;
   const uint32_t su = Pack<W>::slot(wv);
   uint64_t ncs, need;
   role_unions(t, cu, &ncs, &need);
   const uint64_t slots = warp_or64(need);
   const uint32_t n_slots = __popcll(slots);
-  if (n_slots > kHubRanks) {
-    lcc_segments(g, st, t, lw, acc, block, tl);
-    return;
-  }
+  if (n_slots > kHubRanks) return false;
   set_ranks(lw, slots, n_slots);
   // Current word w of [b, e), masked to the list; done when w > wl.
   uint64_t w = b >> 5, wl = 0;
@@ -624,6 +608,29 @@ __device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const 
     tl.gathered += gathered;
     tl.streamed += static_cast<uint32_t>(e - b);
   }
+  return true;
+}
+
+// 32 single-segment hubs, one per lane (lcc_lanes); lcc_segments when the
+// batch needs more than kHubRanks slots.
+template <class W>
+__device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw,
+                                HubAcc* acc, uint64_t block, LccTally& tl) {
+  const uint64_t i = g.n_heavy + block * 32 + lane_id();
+  uint32_t v = 0;
+  W wv = Pack<W>::zero();
+  uint64_t b = 0, e = 0;
+  bool live = false;
+  if (i < g.n_seg) {
+    v = g.seg[i].x;
+    const uint8_t sch = st.sch[v];
+    wv = st.vs[v];
+    b = g.off[v];
+    e = g.off[v + 1];
+    live = sch && Pack<W>::cand(wv) != 0;
+  }
+  if (!__ballot_sync(kFull, live)) return;
+  if (!lcc_lanes(g, st, t, lw, v, wv, b, e, live, tl)) lcc_segments(g, st, t, lw, acc, block, tl);
 }
 
 // Lane's vertex of a light tile: scheduled, holding a role, not a hub.
@@ -757,22 +764,23 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph
   LccWarp& lw = s_lw[threadIdx.x >> 5];
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
-  // Tile tasks cover kTileGroup consecutive tiles whose lane state is loaded
-  // in one round (most tiles have nothing scheduled).
-  const uint64_t n_tasks =
-      kTiles ? ((static_cast<uint64_t>(g.V) + 31) / 32 + kTileGroup - 1) / kTileGroup : batched;
+  // Tile tasks cover 32 consecutive tiles: the lanes read the tiles'
+  // summary flags (sweep 2 leaves most tiles with nothing scheduled) and the
+  // warp checks the flagged ones.
+  const uint64_t n_tiles = (static_cast<uint64_t>(g.V) + 31) / 32;
+  const uint64_t n_tasks = kTiles ? (n_tiles + 31) / 32 : batched;
   const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   LccTally tl;
   for (uint64_t task = warp; task < n_tasks; task += n_warps) {
     if (kTiles) {
-      const uint64_t v0 = task * 32 * kTileGroup;
-      TileLane<W> x[kTileGroup];
-#pragma unroll
-      for (int u = 0; u < kTileGroup; ++u) x[u] = tile_lane(g, st, v0 + 32 * u + lane_id());
-#pragma unroll
-      for (int u = 0; u < kTileGroup; ++u)
-        if (__any_sync(kFull, x[u].work)) lcc_tile(g, st, t, lw, v0 + 32 * u, x[u], tl);
+      const uint64_t t0 = task * 32, ti = t0 + lane_id();
+      const bool flagged = ti < n_tiles && (!st.tile_sch || st.tile_sch[ti]);
+      for (unsigned m = __ballot_sync(kFull, flagged); m; m &= m - 1) {
+        const uint64_t v0 = (t0 + __ffs(m) - 1) * 32;
+        const TileLane<W> x = tile_lane(g, st, v0 + lane_id());
+        if (__any_sync(kFull, x.work)) lcc_tile(g, st, t, lw, v0, x, tl);
+      }
     } else if (task < heavy) {
       lcc_heavy(g, st, t, lw, hub_acc, task, tl);
     } else {
@@ -862,32 +870,37 @@ __device__ void apply_tile(const DevGraph& g, const DevState<W>& st, uint64_t ti
   const unsigned lane = lane_id();
   const uint64_t v = tile + lane;
   bool scan = false;
+  bool pending = false;  // holds a role after this sweep and is (or may be) scheduled
   if (v < g.V) {
     const W w = st.vs[v];
     const uint64_t c = Pack<W>::cand(w);
     if (c) {
       if (st.mod[v]) {
+        uint64_t nc = c;
         const uint64_t tu = Pack<W>::cand(st.unm[v]);
         if (tu) {
           me += __popcll(tu);
-          const uint64_t nc = c & ~tu;
+          nc = c & ~tu;
           st.vs[v] = Pack<W>::make(nc, Pack<W>::slot(w));
           if (!nc) ++ve;
           st.unm[v] = Pack<W>::zero();
         }
         st.sch[v] = 1;
+        pending = nc != 0;
       } else if (!any_modified) {
         st.sch[v] = 0;
       } else {
         const uint64_t b = g.off[v], e = g.off[v + 1];
         if (g.n_seg && e - b > g.hub_degree) {
           // A hub: its segments decide.
+          pending = true;
         } else if (e - b <= 8) {
           // Short lists: the lane scans its own vertex.
           bool found = false;
           for (uint64_t x = b; x < e && !found; ++x)
             if (edge_active(st.eact, x) && st.mod[g.adj[x]]) found = true;
           st.sch[v] = found;
+          pending = found;
         } else {
           scan = true;
         }
@@ -906,8 +919,13 @@ __device__ void apply_tile(const DevGraph& g, const DevState<W>& st, uint64_t ti
       const bool hit = x < e && edge_active(st.eact, x) && st.mod[g.adj[x]];
       found = __any_sync(kFull, hit);
     }
-    if (lane == j) st.sch[u] = found;
+    if (lane == j) {
+      st.sch[u] = found;
+      pending = found;
+    }
   }
+  const bool any = __any_sync(kFull, pending);
+  if (lane == 0 && st.tile_sch) st.tile_sch[tile >> 5] = any ? 1 : 0;
 }
 
 template <class W>
@@ -1049,7 +1067,7 @@ __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st,
 
 template <class W>
 DevState<W> state_of(const QueryDevPtrs& q) {
-  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt};
+  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt, q.tile_sch};
 }
 
 #define PM_DISPATCH_WORD(kind, ...)            \
@@ -1126,7 +1144,7 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) 
     PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W, false><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables,
                                                                                    q.hub_acc, q.ctr));
   }
-  const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + kTileGroup - 1) / kTileGroup, 4);
+  const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4);
   PM_DISPATCH_WORD(q.word_kind,
                    k_lcc_check<W, true><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.hub_acc, q.ctr));
 }

@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
 
 template <class W>
 DevState<W> state_of(const QueryDevPtrs& q) {
-  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt};
+  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt, q.tile_sch};
 }
 
 #define PM_DISPATCH_WORD(kind, ...) \
@@ -1159,7 +1159,7 @@ void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t
   // Count-memo entry: 5 words of epoch / step / count plus the key words.
   L.stride = 5 + std::max<uint32_t>(state_words, 1);
   const DevState<uint64_t> st{const_cast<uint64_t*>(d_cand), const_cast<uint32_t*>(d_edge_active), nullptr, nullptr,
-                              nullptr, nullptr};
+                              nullptr, nullptr, nullptr};
   const uint32_t words = (g.V + 31) / 32;
   // The array keeps the previous call's contents: the counters (the total
   // among them) start every call at zero.
