@@ -180,3 +180,42 @@ def test_hub_plan_change_with_live_query():
         rec, fin = q.step()
         rows.append(list(rec.as_tuple()))
     assert rows == case["rows"][:-1]
+
+
+# Speed knobs at extreme settings: 1-entry first-hop slices for walks and
+# enumeration (every source split), the smallest memo tables (overflow
+# re-runs and table growth), and no slicing at all.  Results must not move.
+KNOB_SETTINGS = {
+    "slice_everything": {"walk_presplit": 1, "enum_presplit": (1, 1), "walk_tables": 1024, "enum_tables": 1024},
+    "no_slicing": {"walk_presplit": 0, "enum_presplit": (0, 0), "walk_tables": 1024, "enum_tables": 1024},
+    "split_on_overflow_only": {"walk_presplit": 0, "enum_presplit": (0, 0), "walk_tables": 2048,
+                               "enum_tables": 1024, "enum_split": (2, 0)},
+}
+KNOB_CASES = ["scale12_tds", "cycle5_s10", "path4_rep_s9", "two_cycles_zipf_s10", "random_08", "k4_rep_s8"]
+
+
+def _set_knobs(k):
+    pm.lib.pm_set_walk_presplit(k["walk_presplit"])
+    pm.lib.pm_set_enum_presplit_by_kind(*k["enum_presplit"])
+    pm.lib.pm_set_walk_table_entries(k["walk_tables"])
+    pm.lib.pm_set_enum_table_entries(k["enum_tables"])
+    pm.lib.pm_set_enum_split(*k.get("enum_split", (16, 0)))
+
+
+DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                 "enum_split": (16, 0)}
+
+
+@pytest.mark.parametrize("setting", sorted(KNOB_SETTINGS))
+@pytest.mark.parametrize("name", KNOB_CASES)
+def test_knob_settings_outputs_identical(name, setting):
+    case = next(c for c in SYNTH if c["name"] == name)
+    g = C.make_graph(case).to_device(0)
+    _set_knobs(KNOB_SETTINGS[setting])
+    try:
+        res = pmtest.product_run(g, pattern=C.make_pattern(case))
+    finally:
+        _set_knobs(DEFAULT_KNOBS)
+    assert res["rows"] == case["rows"]
+    assert pmtest.sha(res["vertex"]) == case["vertex_sha256"]
+    assert pmtest.sha(res["graph"]) == case["graph_sha256"]
