@@ -164,6 +164,24 @@ def kernel_class(step_name: str) -> str:
         step_name, "other")
 
 
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    """Slowest rank's value (torch.distributed MAX all-reduce; `device` is the
+    tensor device of the process group's backend)."""
+    if world <= 1:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, world: int, slowest_seconds: float) -> float:
+    """Whole-job throughput of `world` independent replicas: every rank's
+    units over the slowest rank's time."""
+    return world * units_per_rank / slowest_seconds
+
+
 def word_bytes(k: int) -> int:
     return 2 if k <= 8 else 4 if k <= 24 else 8 if k <= 56 else 16
 
@@ -298,10 +316,7 @@ def run_gb300(args, w, rank, world):
             served_lat += [r.latency_ms for r in results]
             counts = [int(r.match_count) for r in results]
     launches = int(pm.lib.pm_kernel_launches()) - launches0
-    t = torch.tensor([served_s], device=f"cuda:{device}")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    served_max = float(t.item())
+    served_max = max_over_ranks(served_s, world, f"cuda:{device}")
 
     # One at a time: the same stream through pm_query_run, back to back.
     seq_s = 0.0
@@ -352,10 +367,7 @@ def run_gb300(args, w, rank, world):
         ge.close()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], device=f"cuda:{device}")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_qps = world * n * max(1, args.steps) / float(e2e_t.item())
+    e2e_qps = replica_throughput(n * max(1, args.steps), world, max_over_ranks(e2e_s, world, f"cuda:{device}"))
 
     dom = max(per_class_ms, key=per_class_ms.get)
     peak, peak_kind = measured_peaks()
@@ -367,7 +379,7 @@ def run_gb300(args, w, rank, world):
                 "steps_timed": per_class_launch.get(dom, 0),
                 "kernel_ms_per_query": per_class_ms[dom] / (n * seq_steps),
                 "note": "one query alone; latency-bound depth-first walk; bytes are the per-hop algorithmic bytes"}
-    qps = world * n * args.steps / served_max
+    qps = replica_throughput(n * args.steps, world, served_max)
     seq_qps = n * seq_steps / seq_s
     out = {
         "metric": "queries/s served (continuous batching) vs one-at-a-time, full PruneJuice pipeline per query",
