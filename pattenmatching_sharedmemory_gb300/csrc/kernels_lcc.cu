@@ -955,6 +955,112 @@ __global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, 
   }
 }
 
+// ---- sweep 2 on symmetric graphs: schedule by change -------------------
+//
+// A vertex's LCC outcome depends only on its own roles and the roles and
+// slots of the neighbours behind its active entries.  An eliminated entry
+// was not counted before either, so only role losses change anyone's
+// inputs: the next pass needs to check exactly the vertices that lost roles
+// in this step and their neighbours.  The reference reschedules every
+// vertex next to a vertex modified since the last NLCC step
+// (multiple_label_lcc_cpu.tpp:107-141); the vertices that this skips would
+// find nothing to change, so every result row and the final state are the
+// same.  On a symmetric CSR the changed vertices push the flag over their own
+// lists (marking a neighbour behind an inactive entry only adds a check that
+// finds nothing).
+
+// Phase 1: apply the roles to unmatch.  mod[v] becomes "lost roles in this
+// step", sch[v] keeps such vertices that still hold a role, tile_sch
+// summarises sch per tile.
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_changed(DevGraph g, DevState<W> st, StepCounters* ctr) {
+  const unsigned lane = lane_id();
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned me = 0, ve = 0;
+  for (uint64_t tile = warp * 32; tile < g.V; tile += n_warps * 32) {
+    const uint64_t v = tile + lane;
+    bool keep = false;
+    if (v < g.V) {
+      const W w = st.vs[v];
+      const uint64_t c = Pack<W>::cand(w);
+      const uint64_t tu = Pack<W>::cand(st.unm[v]);
+      bool chg = false;
+      if (c && tu) {
+        me += __popcll(tu);
+        const uint64_t nc = c & ~tu;
+        st.vs[v] = Pack<W>::make(nc, Pack<W>::slot(w));
+        if (!nc) ++ve;
+        chg = true;
+        keep = nc != 0;
+      }
+      if (tu) st.unm[v] = Pack<W>::zero();
+      st.mod[v] = chg ? 1 : 0;
+      st.sch[v] = keep ? 1 : 0;
+    }
+    const bool any = __any_sync(kFull, keep);
+    if (lane == 0 && st.tile_sch) st.tile_sch[tile >> 5] = any ? 1 : 0;
+  }
+  me = __reduce_add_sync(kFull, me);
+  ve = __reduce_add_sync(kFull, ve);
+  if (lane == 0) {
+    if (me) atomicAdd(&ctr->match_elim, static_cast<unsigned long long>(me));
+    if (ve) atomicAdd(&ctr->vertex_elim, static_cast<unsigned long long>(ve));
+  }
+}
+
+// Marks every entry target of [b, e) as scheduled (one warp).
+template <class W>
+__device__ __forceinline__ void push_range(const DevGraph& g, const DevState<W>& st, uint64_t b, uint64_t e) {
+  for (uint64_t x = b + lane_id(); x < e; x += 32) {
+    const uint32_t w = g.adj[x];
+    st.sch[w] = 1;
+    if (st.tile_sch) st.tile_sch[w >> 5] = 1;
+  }
+}
+
+// Phase 2: the vertices that lost roles mark their neighbours, with the
+// task layout of sweep 1 (hub segments, batches of 32 single-segment hubs,
+// tiles of 32 light vertices).
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_push_changed(DevGraph g, DevState<W> st) {
+  const unsigned lane = lane_id();
+  const uint64_t heavy = g.n_heavy;
+  const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  const uint64_t n_tasks = batched + (static_cast<uint64_t>(g.V) + 31) / 32;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t task = warp; task < n_tasks; task += n_warps) {
+    if (task < heavy) {
+      const uint4 sd = g.seg[task];
+      if (!st.mod[sd.x]) continue;
+      uint64_t b, e;
+      segment_range(g, sd, &b, &e);
+      push_range(g, st, b, e);
+      continue;
+    }
+    uint32_t v = 0;
+    bool chg = false;
+    if (task < batched) {
+      const uint64_t i = g.n_heavy + (task - heavy) * 32 + lane;
+      if (i < g.n_seg) {
+        v = g.seg[i].x;
+        chg = st.mod[v] != 0;
+      }
+    } else {
+      const uint64_t vv = (task - batched) * 32 + lane;
+      if (vv < g.V) {
+        v = static_cast<uint32_t>(vv);
+        chg = st.mod[v] && (g.n_seg == 0 || g.off[v + 1] - g.off[v] <= g.hub_degree);
+      }
+    }
+    for (unsigned m = __ballot_sync(kFull, chg); m; m &= m - 1) {
+      const uint32_t u = __shfl_sync(kFull, v, __ffs(m) - 1);
+      push_range(g, st, g.off[u], g.off[u + 1]);
+    }
+  }
+}
+
 // ---- worklist compaction ----------------------------------------------
 constexpr int kTileV = 4096;  // vertices per compaction block (256 threads x 16)
 
@@ -1150,6 +1256,13 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) 
 }
 
 void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
+  if (g.symmetric) {
+    const int grid1 = grid_for_tiles(g.V, 8);
+    PM_DISPATCH_WORD(q.word_kind, k_apply_changed<W><<<grid1, kThreads, 0, s>>>(g, state_of<W>(q), q.ctr));
+    const int grid2 = grid_for_tasks(sweep_tasks(g), 8);
+    PM_DISPATCH_WORD(q.word_kind, k_push_changed<W><<<grid2, kThreads, 0, s>>>(g, state_of<W>(q)));
+    return;
+  }
   const int grid = grid_for_tasks(sweep_tasks(g), 8);
   PM_DISPATCH_WORD(q.word_kind, k_apply<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.hub_acc, q.ctr));
 }
