@@ -52,7 +52,34 @@ struct WarpShared {
   WalkFrames f;
   unsigned long long scanned;   // CSR entries tested by this warp (lane 0 writes)
   unsigned long long descents;  // hops taken by this warp
+  // Adjacency list of the walk's source, copied to shared memory when it has
+  // at most kSrcCache entries (src_n == 0: not cached).
+  const uint32_t* src_adj;
+  uint32_t src_n;
 };
+
+// Source adjacency entries a warp caches in shared memory per walk.
+constexpr uint32_t kSrcCache = 256;
+
+// Copies the source's list into the warp's cache when it fits and the graph
+// is symmetric (the only case where tail CHECKs search the source's list).
+__device__ __forceinline__ void cache_source(const DevGraph& g, WarpShared& ws, uint32_t* cache, uint32_t source) {
+  const unsigned lane = lane_id();
+  uint32_t n = 0;
+  if (g.symmetric) {
+    const uint64_t b = g.off[source], e = g.off[source + 1];
+    if (e - b <= kSrcCache) {
+      n = static_cast<uint32_t>(e - b);
+      for (uint32_t i = lane; i < n; i += 32) cache[i] = g.adj[b + i];
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    ws.src_adj = cache;
+    ws.src_n = n;
+  }
+  __syncwarp();
+}
 
 enum : int { kNone = 0, kFound = 1, kOverflowHit = 2 };
 
@@ -465,9 +492,22 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
         // no template neighbour of the source's roles, and roles only
         // shrink, so while both hold these roles neither direction of the
         // edge was ever removed: the check is adjacency, searched in the
-        // bound vertex's list, which every lane shares.
-        const uint32_t t = ws.f.bound[hs];
-        ok = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], nb) != ~uint64_t(0);
+        // bound vertex's list, which every lane shares (for the source, in
+        // its shared-memory copy when it has one).
+        if (hs == 0 && ws.src_n) {
+          uint32_t lo = 0, hi = ws.src_n;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (ws.src_adj[mid] < nb)
+              lo = mid + 1;
+            else
+              hi = mid;
+          }
+          ok = lo < ws.src_n && ws.src_adj[lo] == nb;
+        } else {
+          const uint32_t t = ws.f.bound[hs];
+          ok = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], nb) != ~uint64_t(0);
+        }
       } else {
         const uint32_t target = hs == d ? nb : ws.f.bound[hs];
         const uint64_t idx = lane_find_sorted(g.adj, g.off[nb], g.off[nb + 1], target);
@@ -669,12 +709,14 @@ template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W> st, WalkLaunch w, WalkScratch sc,
                                                           StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
+  __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   if (lane == 0) {
     ws.scanned = 0;
     ws.descents = 0;
+    ws.src_n = 0;
   }
   __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
@@ -722,6 +764,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
       continue;
     }
     next_epoch(m);
+    cache_source(g, ws, s_src[wib], v);
     unsigned long long unused = 0;
     const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline, lo, hi);
     if (lane == 0) {
@@ -857,12 +900,14 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
                                                                uint4* overflow, WalkScratch sc, StepCounters* ctr,
                                                                uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
+  __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   if (lane == 0) {
     ws.scanned = 0;
     ws.descents = 0;
+    ws.src_n = 0;
   }
   __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
@@ -881,6 +926,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevSt
     const uint4 it = items ? items[gi] : make_uint4(static_cast<uint32_t>(gi), 0u, 0xFFFFFFFFu, 0u);
     const uint32_t source = wl[it.x];
     next_epoch(m);
+    cache_source(g, ws, s_src[wib], source);
     const unsigned long long before = leaves;
     const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z);
     if (res == kItemTimeout) {
@@ -1067,6 +1113,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
   if (lane == 0) {
     ws.scanned = 0;
     ws.descents = 0;
+    ws.src_n = 0;
   }
   __syncwarp();
   WarpMemo m{};
