@@ -48,7 +48,7 @@ struct WalkFrames {
 };
 
 struct WarpShared {
-  WalkProgram prog;
+  WalkProgram* prog;  // the warp's program (shared memory of the warp or the block)
   WalkFrames f;
   unsigned long long scanned;   // CSR entries tested by this warp (lane 0 writes)
   unsigned long long descents;  // hops taken by this warp
@@ -151,22 +151,22 @@ struct KeyTuple {
   bool refs;
   __device__ __forceinline__ uint32_t operator[](int i) const {
     if (refs) {
-      uint64_t r = ws->prog.state_refs[d];
+      uint64_t r = ws->prog->state_refs[d];
       for (int k = 0; k < i; ++k) r &= r - 1;
       const int h = __ffsll(static_cast<long long>(r)) - 1;
-      return ws->f.bound[ws->prog.hist_step[h]];
+      return ws->f.bound[ws->prog->hist_step[h]];
     }
-    return ws->f.bound[ws->prog.store_step[i]];
+    return ws->f.bound[ws->prog->store_step[i]];
   }
 };
 
 __device__ __forceinline__ KeyTuple stored_key(const WarpShared& ws, int d) {
   int n = 0;
-  while (n < ws.prog.n_store && ws.prog.store_step[n] < d) ++n;
+  while (n < ws.prog->n_store && ws.prog->store_step[n] < d) ++n;
   return KeyTuple{&ws, d, n, false};
 }
 __device__ __forceinline__ KeyTuple state_key(const WarpShared& ws, int d) {
-  return KeyTuple{&ws, d, __popcll(ws.prog.state_refs[d]), true};
+  return KeyTuple{&ws, d, __popcll(ws.prog->state_refs[d]), true};
 }
 
 __device__ __forceinline__ uint32_t tuple_hash(uint32_t nb, uint32_t step, const KeyTuple& t) {
@@ -354,8 +354,8 @@ __device__ bool load_chunk(const DevGraph& g, const DevState<W>& st, WarpShared&
   }
   if (s.kind == kStepFinal) ok = ok && nb != source;
   if (kEnum && ok) {
-    for (int h = 0; h < ws.prog.n_hist && ws.prog.hist_step[h] < d; ++h)
-      if (ws.f.bound[ws.prog.hist_step[h]] == nb) ok = false;
+    for (int h = 0; h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
+      if (ws.f.bound[ws.prog->hist_step[h]] == nb) ok = false;
   }
   const unsigned mask = __ballot_sync(kFull, ok);
   __syncwarp();
@@ -387,7 +387,7 @@ __device__ int next_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
     __syncwarp();
     const uint32_t nb = g.adj[ws.f.chunk[d] + j];
     if (!kEnum && s.kind == kStepVertex) {
-      if (!ws.prog.exact) {
+      if (!ws.prog->exact) {
         // The reference's memo tests and inserts, in its order (cc :105-114,
         // tds :99-119).
         const uint32_t a = cur < nb ? cur : nb, b = cur < nb ? nb : cur;
@@ -468,7 +468,7 @@ template <class W, bool kEnum>
 __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
                            uint32_t* out, unsigned long long* leaves) {
   const unsigned lane = lane_id();
-  const int n_steps = ws.prog.n_steps;
+  const int n_steps = ws.prog->n_steps;
   while (true) {
     const uint64_t next = ws.f.next[d], end = ws.f.end[d];
     if (next >= end) return kNone;
@@ -481,11 +481,11 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
       ok = role_of(st, nb, s.role);
     }
     if (kEnum && ok) {
-      for (int h = 0; h < ws.prog.n_hist && ws.prog.hist_step[h] < d; ++h)
-        if (ws.f.bound[ws.prog.hist_step[h]] == nb) ok = false;
+      for (int h = 0; h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
+        if (ws.f.bound[ws.prog->hist_step[h]] == nb) ok = false;
     }
-    for (int j = ws.prog.tail_from; ok && j < n_steps; ++j) {
-      const int hs = ws.prog.hist_step[ws.prog.steps[j].hist];
+    for (int j = ws.prog->tail_from; ok && j < n_steps; ++j) {
+      const int hs = ws.prog->hist_step[ws.prog->steps[j].hist];
       if (g.symmetric && hs != d) {
         // A CHECK is a template edge between nb's role and the bound
         // vertex's role.  LCC removes an entry only when its target holds
@@ -540,8 +540,8 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
                             unsigned long long* leaves, uint64_t deadline, uint32_t first_lo = 0,
                             uint32_t first_hi = 0xFFFFFFFFu) {
   const unsigned lane = lane_id();
-  const int n_steps = ws.prog.n_steps;
-  const bool count_memo = kEnum && ws.prog.count_memo;
+  const int n_steps = ws.prog->n_steps;
+  const bool count_memo = kEnum && ws.prog->count_memo;
   uint32_t iters = 0;
   __syncwarp();
   if (lane == 0) {
@@ -577,7 +577,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       --d;
       continue;
     }
-    const WalkStep s = ws.prog.steps[d];
+    const WalkStep s = ws.prog->steps[d];
     // Returning to a VERTEX step from a counted descent: cache the count of
     // the subtree just finished.
     if (count_memo && ws.f.child[d]) {
@@ -589,7 +589,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     }
     const uint32_t cur = ws.f.cur[d];
     bool adv = false;
-    if (s.kind == kStepVertex && d + 1 == ws.prog.tail_from && g.sorted_unique && (kEnum || ws.prog.exact)) {
+    if (s.kind == kStepVertex && d + 1 == ws.prog->tail_from && g.sorted_unique && (kEnum || ws.prog->exact)) {
       uint32_t nb = 0;
       if (tail_vertex<W, kEnum>(g, st, ws, d, s, &nb, leaves) == kFound) {
         __syncwarp();
@@ -626,7 +626,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
         adv = true;
       }
     } else if (s.kind == kStepCheck) {
-      const uint32_t target = ws.f.bound[ws.prog.hist_step[s.hist]];
+      const uint32_t target = ws.f.bound[ws.prog->hist_step[s.hist]];
       if (next_check<W, kEnum>(g, st, ws, d, cur, target)) {
         __syncwarp();
         if (lane == 0) ws.f.cur[d + 1] = cur;
@@ -635,7 +635,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       }
     } else {  // kStepMove
       if (ws.f.mask[d] == 0) {
-        const uint32_t back = ws.f.bound[ws.prog.hist_step[s.hist]];
+        const uint32_t back = ws.f.bound[ws.prog->hist_step[s.hist]];
         __syncwarp();
         if (lane == 0) {
           ws.f.mask[d] = 1;
@@ -649,7 +649,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       ++d;
       if (lane == 0) ws.descents += 1;
       if (d < n_steps) {
-        if (ws.prog.steps[d].kind == kStepMove) {
+        if (ws.prog->steps[d].kind == kStepMove) {
           __syncwarp();
           if (lane == 0) {
             ws.f.mask[d] = 0;
@@ -669,7 +669,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
 
 __device__ __forceinline__ void load_program(WarpShared& ws, const WalkProgram* __restrict__ src) {
   const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-  uint32_t* d = reinterpret_cast<uint32_t*>(&ws.prog);
+  uint32_t* d = reinterpret_cast<uint32_t*>(ws.prog);
   __syncwarp();
   for (int i = lane_id(); i < static_cast<int>(sizeof(WalkProgram) / 4); i += 32) d[i] = s[i];
   __syncwarp();
@@ -709,11 +709,13 @@ template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W> st, WalkLaunch w, WalkScratch sc,
                                                           StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
+  __shared__ WalkProgram s_prog[kWalkWarps];  // items of one launch mix programs
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   if (lane == 0) {
+    ws.prog = &s_prog[wib];
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
@@ -759,7 +761,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
       load_program(ws, w.progs + r);
       cached = static_cast<int>(r);
     }
-    if (!role_of(st, v, ws.prog.start_role)) {
+    if (!role_of(st, v, ws.prog->start_role)) {
       if (lane == 0 && !w.slices) w.status[item] = kItemSkip;
       continue;
     }
@@ -787,16 +789,16 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
     if (res == kItemSuccess && (w.min_marker || w.marks)) {
       // alreadyMatched marks of the successful path (cc :64, pc :42, tds :74).
       uint32_t j = 0;
-      for (int d0 = 1; d0 < ws.prog.n_steps; d0 += 32) {
+      for (int d0 = 1; d0 < ws.prog->n_steps; d0 += 32) {
         const int d = d0 + static_cast<int>(lane);
-        const bool mk = d < ws.prog.n_steps && ws.prog.steps[d].mark;
+        const bool mk = d < ws.prog->n_steps && ws.prog->steps[d].mark;
         const unsigned mm = __ballot_sync(kFull, mk);
         if (mk) {
           const uint32_t x = ws.f.bound[d];
           const uint32_t slot = j + __popc(mm & ((1u << lane) - 1));
           if (w.marks) w.marks[static_cast<uint64_t>(item) * w.marks_stride + slot] = x;
           if (w.min_marker) {
-            const uint8_t ri = w.role_index[ws.prog.steps[d].role];
+            const uint8_t ri = w.role_index[ws.prog->steps[d].role];
             if (ri != 0xFF) {
               const uint64_t xi = static_cast<uint64_t>(w.wl_index[x]) * w.n_progs + ri;
               atomicMin(w.min_marker + xi, item);
@@ -893,25 +895,32 @@ __global__ void k_apply_list(DevGraph g, DevState<W> st, const uint32_t* __restr
 // hi, source vertex}, ctr->aux entries) for a re-run (split, or with larger
 // tables).
 template <class W>
-__global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate(DevGraph g, DevState<W> st,
+__global__ void __launch_bounds__(kWalkWarps * 32, 9) k_enumerate(DevGraph g, DevState<W> st,
                                                                const WalkProgram* __restrict__ prog,
                                                                const uint32_t* __restrict__ wl, uint32_t n_wl,
                                                                const uint4* __restrict__ items, uint32_t n_items,
                                                                uint4* overflow, WalkScratch sc, StepCounters* ctr,
                                                                uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
+  __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   if (lane == 0) {
+    ws.prog = &s_prog;
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
   }
   __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
-  load_program(ws, prog);
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(prog);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&s_prog);
+    for (uint32_t i = threadIdx.x; i < sizeof(WalkProgram) / 4; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+  }
   WarpMemo m = warp_memo(sc, gw);
   uint64_t deadline = 0;
   if (lane == 0) deadline = global_timer_ns() + budget_ns;
@@ -1101,21 +1110,23 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
                                                                        WalkProgram prog, NoAllocLayout L, int round,
                                                                        uint32_t n_units, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
+  __shared__ WalkProgram s_prog;
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(&prog);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&ws.prog);
-    for (int i = lane; i < static_cast<int>(sizeof(WalkProgram) / 4); i += 32) dst[i] = src[i];
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&s_prog);
+    for (uint32_t i = threadIdx.x; i < sizeof(WalkProgram) / 4; i += blockDim.x) dst[i] = src[i];
   }
   if (lane == 0) {
+    ws.prog = &s_prog;
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
   }
-  __syncwarp();
+  __syncthreads();
   WarpMemo m{};
   m.state = L.tables + static_cast<uint64_t>(gw) * L.cap * L.stride;
   m.state_cap = L.cap;
@@ -1140,7 +1151,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
       const uint32_t b = __ffs(bits) - 1;
       bits &= bits - 1;
       const uint32_t v = base + (round > 0 ? b : 0u);
-      if (!role_of(st, v, ws.prog.start_role)) continue;
+      if (!role_of(st, v, ws.prog->start_role)) continue;
       next_epoch(m);
       const unsigned long long before = leaves;
       const uint8_t res = run_walk<uint64_t, true>(g, st, ws, m, v, &leaves, deadline);
