@@ -514,6 +514,8 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   w.min_marker = track_markers ? d_marker.as<uint32_t>() : nullptr;
   w.marks = record_marks ? d_marks.as<uint32_t>() : nullptr;
   w.marks_stride = M;
+  w.frame_steps = 1;
+  for (const WalkProgram& pr : dc.cc.programs) w.frame_steps = std::max<uint32_t>(w.frame_steps, pr.n_steps + 1u);
 
   // Exact programs may split heavy items into first-hop slices: an item
   // succeeds when any slice does (no alreadyMatched marks to keep).
@@ -749,11 +751,11 @@ StepResult QueryImpl::step_enumeration() {
       d_list2.ensure(sizeof(uint4) * items.size());
       PM_CUDA(cudaMemcpyAsync(d_list.ptr, items.data(), sizeof(uint4) * items.size(), cudaMemcpyHostToDevice,
                               stream));
-      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
+      launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
                        static_cast<uint32_t>(items.size()), d_list2.as<uint4>(), pool.sc, stream);
     } else {
       d_list2.ensure(sizeof(uint4) * n_wl);
-      launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,
+      launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,
                        stream);
     }
     PM_CUDA(cudaGetLastError());
@@ -803,7 +805,7 @@ StepResult QueryImpl::step_enumeration() {
       zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
       if (n_split) {
         zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
-        launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
+        launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
                          static_cast<uint32_t>(n_split), d_list2.as<uint4>(), pool.sc, stream);
         PM_CUDA(cudaGetLastError());
       }
@@ -812,7 +814,7 @@ StepResult QueryImpl::step_enumeration() {
         const uint32_t warps = retry_warps(base_warps, grow_level, hs, ss * (g_enum_state_cap / kStateCap));
         big_pool.ensure(warps, kEdgeCap, kHypCap, hs, g_enum_state_cap << (3 * grow_level), ss, stream);
         zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
-        launch_enumerate(g->dev(), ptrs(), prog, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>() + n_split,
+        launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>() + n_split,
                          static_cast<uint32_t>(n_grow), d_list2.as<uint4>(), big_pool.sc, stream);
         PM_CUDA(cudaGetLastError());
       }

@@ -110,7 +110,15 @@ struct WalkLaunch {
   const uint4* slices;
   uint32_t n_slices;
   uint32_t* prio;
+  uint32_t frame_steps;  // frame stack entries per warp: longest program's n_steps + 1
 };
+
+// Walker launch geometry: resident blocks per SM the kernels are built for,
+// and the dynamic shared memory of one warp's frame stack of `steps` entries.
+constexpr uint32_t kWalkBlocksPerSm = 12;
+__host__ __device__ constexpr uint32_t frame_bytes(uint32_t steps) {
+  return (steps * (4 * 8 + 3 * 4 + 1) + 15) / 16 * 16;
+}
 
 // Result priorities of sliced items: success of any slice decides the item.
 enum SlicePrio : uint32_t { kPrioSkip = 0, kPrioFail = 1, kPrioOverflow = 2, kPrioTimeout = 3, kPrioSuccess = 4 };
@@ -141,8 +149,8 @@ void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const u
 // positions [lo, hi) of the source's adjacency list.  Items whose count memo
 // overflowed are written to `overflow` as {position, lo, hi, source vertex}
 // (count in ctr->aux) and contribute nothing.
-void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow,
+void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, uint32_t frame_steps,
+                      const uint32_t* wl, uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow,
                       const WalkScratch& scratch, cudaStream_t s);
 
 // Export of the pruned state.

@@ -33,18 +33,20 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kWalkWarps = 4;  // warps per block
-constexpr int kSteps = kMaxWalkSteps;
 constexpr uint32_t kStateTag = 0x80000000u;
 
+// The frame stack of a walk, one entry per step (n_steps + 1 entries), in
+// dynamic shared memory sized to the launched programs: short programs
+// leave room for more resident blocks.
 struct WalkFrames {
-  uint64_t next[kSteps + 1];
-  uint64_t end[kSteps + 1];
-  uint64_t chunk[kSteps + 1];
-  uint64_t leaves0[kSteps + 1];  // ENUMERATION count at descent (count memo)
-  uint32_t mask[kSteps + 1];
-  uint32_t cur[kSteps + 1];
-  uint32_t bound[kSteps + 1];
-  uint8_t child[kSteps + 1];     // a descent from this step awaits its count
+  uint64_t* next;
+  uint64_t* end;
+  uint64_t* chunk;
+  uint64_t* leaves0;  // ENUMERATION count at descent (count memo)
+  uint32_t* mask;
+  uint32_t* cur;
+  uint32_t* bound;
+  uint8_t* child;     // a descent from this step awaits its count
 };
 
 struct WarpShared {
@@ -60,6 +62,23 @@ struct WarpShared {
 
 // Source adjacency entries a warp caches in shared memory per walk.
 constexpr uint32_t kSrcCache = 256;
+
+// Points the warp's frames at its part of the kernel's dynamic shared
+// memory (frame_bytes(steps) per warp).
+__device__ __forceinline__ void bind_frames(WarpShared& ws, unsigned char* base, uint32_t steps) {
+  if (lane_id() == 0) {
+    WalkFrames& f = ws.f;
+    f.next = reinterpret_cast<uint64_t*>(base);
+    f.end = f.next + steps;
+    f.chunk = f.end + steps;
+    f.leaves0 = f.chunk + steps;
+    f.mask = reinterpret_cast<uint32_t*>(f.leaves0 + steps);
+    f.cur = f.mask + steps;
+    f.bound = f.cur + steps;
+    f.child = reinterpret_cast<uint8_t*>(f.bound + steps);
+  }
+  __syncwarp();
+}
 
 // Copies the source's list into the warp's cache when it fits and the graph
 // is symmetric (the only case where tail CHECKs search the source's list).
@@ -706,11 +725,13 @@ __device__ __forceinline__ WarpMemo warp_memo(const WalkScratch& sc, uint32_t gw
 }
 
 template <class W>
-__global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W> st, WalkLaunch w, WalkScratch sc,
+__global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_walk(DevGraph g, DevState<W> st, WalkLaunch w,
+                                                                           WalkScratch sc,
                                                           StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog[kWalkWarps];  // items of one launch mix programs
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
+  extern __shared__ __align__(16) unsigned char s_frames[];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
@@ -720,7 +741,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(DevGraph g, DevState<W
     ws.descents = 0;
     ws.src_n = 0;
   }
-  __syncwarp();
+  bind_frames(ws, s_frames + wib * frame_bytes(w.frame_steps), w.frame_steps);
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   uint64_t deadline = 0;
   if (lane == 0) deadline = global_timer_ns() + budget_ns;
@@ -895,15 +916,14 @@ __global__ void k_apply_list(DevGraph g, DevState<W> st, const uint32_t* __restr
 // hi, source vertex}, ctr->aux entries) for a re-run (split, or with larger
 // tables).
 template <class W>
-__global__ void __launch_bounds__(kWalkWarps * 32, 9) k_enumerate(DevGraph g, DevState<W> st,
-                                                               const WalkProgram* __restrict__ prog,
-                                                               const uint32_t* __restrict__ wl, uint32_t n_wl,
-                                                               const uint4* __restrict__ items, uint32_t n_items,
-                                                               uint4* overflow, WalkScratch sc, StepCounters* ctr,
-                                                               uint64_t budget_ns) {
+__global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate(
+    DevGraph g, DevState<W> st, const WalkProgram* __restrict__ prog, uint32_t frame_steps,
+    const uint32_t* __restrict__ wl, uint32_t n_wl, const uint4* __restrict__ items, uint32_t n_items,
+    uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
+  extern __shared__ __align__(16) unsigned char s_frames[];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
@@ -913,6 +933,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 9) k_enumerate(DevGraph g, De
     ws.descents = 0;
     ws.src_n = 0;
   }
+  bind_frames(ws, s_frames + wib * frame_bytes(frame_steps), frame_steps);
   __syncwarp();
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
   {
@@ -990,7 +1011,7 @@ void set_walk_budget_ns(uint64_t ns) { g_walk_budget_ns = ns ? ns : 1; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
 
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {
-  uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * 8;
+  uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * kWalkBlocksPerSm;
   if (blocks * kWalkWarps > n_warps_available) blocks = n_warps_available / kWalkWarps;
   return blocks ? blocks : 1;
 }
@@ -998,8 +1019,9 @@ uint32_t walk_grid_blocks(uint32_t n_warps_available) {
 void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, const WalkScratch& sc,
                  cudaStream_t s) {
   const uint32_t blocks = walk_grid_blocks(sc.n_warps);
-  PM_DISPATCH_WORD(q.word_kind, k_walk<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), w, sc, q.ctr,
-                                                                             g_walk_budget_ns));
+  const size_t dyn = kWalkWarps * frame_bytes(w.frame_steps);
+  PM_DISPATCH_WORD(q.word_kind, k_walk<W><<<blocks, kWalkWarps * 32, dyn, s>>>(g, state_of<W>(q), w, sc, q.ctr,
+                                                                               g_walk_budget_ns));
 }
 
 void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s) {
@@ -1034,13 +1056,14 @@ void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const u
   PM_DISPATCH_WORD(q.word_kind, k_apply_list<W><<<grid, 256, 0, s>>>(g, state_of<W>(q), verts, roles, n, q.ctr));
 }
 
-void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
-                      uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow, const WalkScratch& sc,
-                      cudaStream_t s) {
+void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, uint32_t frame_steps,
+                      const uint32_t* wl, uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow,
+                      const WalkScratch& sc, cudaStream_t s) {
   const uint32_t blocks = walk_grid_blocks(sc.n_warps);
-  PM_DISPATCH_WORD(q.word_kind,
-                   k_enumerate<W><<<blocks, kWalkWarps * 32, 0, s>>>(g, state_of<W>(q), prog, wl, n_wl, items, n_items,
-                                                                     overflow, sc, q.ctr, g_walk_budget_ns));
+  const size_t dyn = kWalkWarps * frame_bytes(frame_steps);
+  PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
+                                    g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
+                                    q.ctr, g_walk_budget_ns));
 }
 
 }  // namespace pmgb
@@ -1111,6 +1134,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
                                                                        uint32_t n_units, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;
+  extern __shared__ __align__(16) unsigned char s_frames[];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
   WarpShared& ws = s_ws[wib];
@@ -1126,6 +1150,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
     ws.descents = 0;
     ws.src_n = 0;
   }
+  bind_frames(ws, s_frames + wib * frame_bytes(prog.n_steps + 1u), prog.n_steps + 1u);
   __syncthreads();
   WarpMemo m{};
   m.state = L.tables + static_cast<uint64_t>(gw) * L.cap * L.stride;
@@ -1242,7 +1267,8 @@ void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t
     noalloc_check(cudaMemsetAsync(&L.ctr->items, 0, sizeof(unsigned long long), s), "clear work counter");
     noalloc_check(cudaMemsetAsync(&L.ctr->overflow, 0, sizeof(unsigned long long), s), "clear overflow");
     note_launch();
-    k_enumerate_noalloc<<<static_cast<unsigned>(warps / kWalkWarps), kWalkWarps * 32, 0, s>>>(
+    k_enumerate_noalloc<<<static_cast<unsigned>(warps / kWalkWarps), kWalkWarps * 32,
+                          kWalkWarps * frame_bytes(prog.n_steps + 1u), s>>>(
         g, st, prog, L, round, round == 0 ? g.V : words, g_walk_budget_ns);
     noalloc_check(cudaGetLastError(), "k_enumerate_noalloc launch");
     noalloc_check(cudaMemcpyAsync(&host_ctr, L.ctr, sizeof(StepCounters), cudaMemcpyDeviceToHost, s),
