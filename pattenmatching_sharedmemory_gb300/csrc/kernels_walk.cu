@@ -33,6 +33,8 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kWalkWarps = 4;  // warps per block
+// k_walk (CC/PC/TDS) is built for two resident blocks fewer than the
+// enumeration kernels: 48 registers without spills instead of 40 with.
 constexpr uint32_t kStateTag = 0x80000000u;
 
 // The frame stack of a walk, one entry per step (n_steps + 1 entries), in
@@ -725,7 +727,7 @@ __device__ __forceinline__ WarpMemo warp_memo(const WalkScratch& sc, uint32_t gw
 }
 
 template <class W>
-__global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_walk(DevGraph g, DevState<W> st, WalkLaunch w,
+__global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(DevGraph g, DevState<W> st, WalkLaunch w,
                                                                            WalkScratch sc,
                                                           StepCounters* ctr, uint64_t budget_ns) {
   __shared__ WarpShared s_ws[kWalkWarps];
