@@ -218,9 +218,9 @@ def lcc_roofline(scale: int, device: int):
     ms = sum(p[0] for p in passes)
     by = sum(p[1] for p in passes)
     achieved = by / (ms / 1e3) / 1e9 if ms else None
-    out = {"bound": "hbm", "kernel": "lcc sweep (k_lcc_check x2 + k_apply)", "graph": f"rmat scale {scale} ef 16",
+    out = {"bound": "hbm", "kernel": "lcc sweep (k_lcc_check x2 + sweep 2)", "graph": f"rmat scale {scale} ef 16",
            "csr_entries": g.edge_count, "passes": len(passes), "ms_per_pass": ms / max(1, len(passes)),
-           "listed_per_pass": passes[-1][2] if passes else 0, "gathered_per_pass": passes[-1][3] if passes else 0,
+           "pass_ms": [round(p[0], 3) for p in passes], "gathered_per_pass": [p[3] for p in passes],
            "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
            "frac": achieved / peak if achieved else None, "traffic": profile_traffic("lcc")}
     g.close()
