@@ -392,6 +392,7 @@ def run_gb300(args, w, rank, world):
                    "templates": "15 distinct-label 4-cycles over labels 0..4", "requests_per_step": n,
                    "slots": args.slots, "arrival": "all requests of a step submitted at once",
                    "autotuned": tuned,
+                   "lcc_fixpoint": "one CUDA graph per fixpoint (conditional WHILE node over a pass)",
                    "match_counts": counts, "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step (512 MB write outside the timed interval)"},
         "latency_ms": {"p50": pct(served_lat, 0.5), "p99": pct(served_lat, 0.99)},

@@ -109,6 +109,17 @@ pm_status_t pm_set_walk_table_entries(uint32_t entries);
  * words per query).  Process-wide; speed only.  Set it while no query runs. */
 pm_status_t pm_set_enum_table_entries(uint32_t entries);
 
+/* Whole-run calls (pm_query_run, the server, pm_batch_run) run each LCC
+ * fixpoint (LCC repeated until a pass eliminates nothing,
+ * multiple_label_step.cc:30-83) as one CUDA-graph launch: a conditional
+ * WHILE node over one pass, whose last kernel records the pass's row and
+ * decides on the device whether another pass runs.  Rows, counts and state
+ * are those of the host-driven loop; only the step_ms column is measured
+ * differently (device timer per pass).  pm_query_step always runs one pass.
+ * enabled = 0 turns it off (default 1).  Process-wide; speed only.  No
+ * counterpart in the reference. */
+pm_status_t pm_set_lcc_graph(int32_t enabled);
+
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with
  * PM_E_TIMEOUT and the query's state is no longer meaningful. */

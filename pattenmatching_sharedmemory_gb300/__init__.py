@@ -153,6 +153,7 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_lcc_graph": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_walk_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_walk_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_presplit": (ctypes.c_int32, [ctypes.c_uint32]),

@@ -349,6 +349,11 @@ pm_status_t pm_set_enum_table_entries(uint32_t entries) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_lcc_graph(int32_t enabled) {
+  set_lcc_graph(enabled != 0);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));

@@ -150,6 +150,25 @@ struct StepCounters {
 };
 constexpr int kStepCounterWords = 12;
 
+// The LCC fixpoint loop as one CUDA graph (a conditional WHILE node over one
+// LCC pass): the tail of every pass appends its counters as a row, clears the
+// step counters and keeps the loop going while the pass eliminated anything
+// and the iteration cap allows (multiple_label_step.cc:30-83 repeats LCC
+// until its AlgoResults is empty; multiple_label_cpu.cc:113-184 caps the run
+// at 1000 iterations).
+struct LccPassRow {
+  unsigned long long vertex_elim, edge_elim, match_elim, scanned, gathered;
+  unsigned long long end_ns;  // %globaltimer at the end of the pass
+};
+struct LccLoopCtl {
+  unsigned long long start_ns;  // %globaltimer before the first pass
+  unsigned long long error;     // step-counter error status seen by a tail
+  uint32_t passes;              // passes run by this launch
+  uint32_t max_passes;          // set by the host before each launch, >= 1
+  unsigned long long pad;
+};
+constexpr uint32_t kLccLoopMaxPasses = 1000;
+
 // Per-query tables derived from the local constraints
 // (multiple_label_constraint_local.h:18-32), in label-slot space.
 struct QueryTables {

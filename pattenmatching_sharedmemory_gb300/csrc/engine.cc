@@ -97,6 +97,7 @@ void GraphImpl::to_device(int dev) {
     PM_CUDA(e);
     symmetric = asym == 0;
   }
+  ++plan_epoch;
 }
 
 void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
@@ -139,6 +140,7 @@ void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
   n_seg = static_cast<uint32_t>(seg.size());
   n_heavy = heavy;
   n_acc = n_multi;
+  ++plan_epoch;
 }
 
 DevGraph GraphImpl::dev() const {
@@ -243,6 +245,7 @@ uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
 }
 
 QueryImpl::~QueryImpl() {
+  destroy_lcc_loop();
   // Stream-ordered frees go before the stream is destroyed.
   for (DeviceBuffer* b : buffers()) b->release();
   if (own_host) {
@@ -846,15 +849,10 @@ int QueryImpl::advance(int cur) {
 }
 
 pm_step_record QueryImpl::run_step() {
-  pm_step_record rec{};
   if (finished) return final_record();
   const int kind = step;
   if (kind == PM_STEP_CC || kind == PM_STEP_PC || kind == PM_STEP_TDS) reset_modified();
-  // The graph's hub plan may have changed since the last step.
-  if (d_hub_acc.bytes < sizeof(HubAcc) * static_cast<size_t>(g->n_acc)) {
-    d_hub_acc.ensure(sizeof(HubAcc) * static_cast<size_t>(g->n_acc));
-    PM_CUDA(cudaMemsetAsync(d_hub_acc.ptr, 0, d_hub_acc.bytes, stream));
-  }
+  ensure_hub_acc();
   clear_step_counters();
   PM_CUDA(cudaEventRecord(ev0, stream));
   if (!first_recorded) {
@@ -878,6 +876,21 @@ pm_step_record QueryImpl::run_step() {
   PM_CUDA(cudaEventSynchronize(ev1));
   float ms = 0;
   PM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  append_record(r, kind, ms, h_ctr->scanned, kind == PM_STEP_LCC ? h_ctr->gathered : h_ctr->descents);
+  return records.back();
+}
+
+void QueryImpl::ensure_hub_acc() {
+  // The graph's hub plan may have changed since the last step.
+  if (d_hub_acc.bytes < sizeof(HubAcc) * static_cast<size_t>(g->n_acc)) {
+    d_hub_acc.ensure(sizeof(HubAcc) * static_cast<size_t>(g->n_acc));
+    PM_CUDA(cudaMemsetAsync(d_hub_acc.ptr, 0, d_hub_acc.bytes, stream));
+  }
+}
+
+void QueryImpl::append_record(const StepResult& r_in, int kind, double ms, uint64_t scanned, uint64_t second) {
+  pm_step_record rec{};
+  StepResult r = r_in;
   r.kind = kind;
   last = r;
   active_vertices -= r.vertex;
@@ -897,12 +910,119 @@ pm_step_record QueryImpl::run_step() {
   rec.active_edge = active_edges;
   rec.total_edge = g->host.edge_count;
   records.push_back(rec);
-  walk_stats.emplace_back(h_ctr->scanned, kind == PM_STEP_LCC ? h_ctr->gathered : h_ctr->descents);
+  walk_stats.emplace_back(scanned, second);
   step = advance(kind);
   if (kind == PM_STEP_ENUMERATION) finished = true;
   ++iteration;
   if (iteration >= 1000) finished = true;
-  return rec;
+}
+
+// ---- the LCC fixpoint as one CUDA graph ----------------------------------
+namespace {
+bool g_lcc_graph = true;
+}  // namespace
+
+void set_lcc_graph(bool on) { g_lcc_graph = on; }
+bool lcc_graph() { return g_lcc_graph; }
+
+void QueryImpl::destroy_lcc_loop() {
+  if (lcc_exec) cudaGraphExecDestroy(lcc_exec);
+  if (lcc_graph) cudaGraphDestroy(lcc_graph);
+  lcc_exec = nullptr;
+  lcc_graph = nullptr;
+}
+
+// Graph: head kernel -> WHILE(cond) { LCC sweep 1, sweep 2, tail kernel }.
+// The body is captured from the same launch sequence step_lcc issues, on a
+// capture-only stream (relaxed mode, so other threads may keep allocating).
+void QueryImpl::build_lcc_loop() {
+  destroy_lcc_loop();
+  d_loop.ensure(sizeof(LccLoopCtl) + sizeof(LccPassRow) * kLccLoopMaxPasses);
+  h_loop.resize(d_loop.bytes);
+  LccLoopCtl* ctl = d_loop.as<LccLoopCtl>();
+  cudaStream_t cs = nullptr;
+  PM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  try {
+    PM_CUDA(cudaGraphCreate(&lcc_graph, 0));
+    cudaGraphConditionalHandle handle;
+    PM_CUDA(cudaGraphConditionalHandleCreate(&handle, lcc_graph, 1, cudaGraphCondAssignDefault));
+    PM_CUDA(cudaStreamBeginCaptureToGraph(cs, lcc_graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_lcc_loop_head(ctl, cs);
+    PM_CUDA(cudaStreamEndCapture(cs, &lcc_graph));
+    cudaGraphNode_t head = nullptr;
+    size_t n_nodes = 1;
+    PM_CUDA(cudaGraphGetNodes(lcc_graph, &head, &n_nodes));
+    if (n_nodes != 1) throw PmError{PM_FAILURE, "LCC loop graph: unexpected head nodes"};
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop = nullptr;
+    PM_CUDA(cudaGraphAddNode(&loop, lcc_graph, &head, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const uint64_t before = launch_count();
+    PM_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_lcc_check(g->dev(), ptrs(), cs);
+    launch_apply(g->dev(), ptrs(), cs);
+    launch_lcc_loop_tail(d_ctr.as<StepCounters>(), ctl, handle, cs);
+    PM_CUDA(cudaStreamEndCapture(cs, &body));
+    lcc_pass_launches = static_cast<int64_t>(launch_count() - before);
+    // Captured launches ran nothing yet; runs add what they execute.
+    note_launches(-lcc_pass_launches - 1);
+    PM_CUDA(cudaGraphInstantiate(&lcc_exec, lcc_graph, 0));
+  } catch (...) {
+    cudaStreamDestroy(cs);
+    destroy_lcc_loop();
+    throw;
+  }
+  PM_CUDA(cudaStreamDestroy(cs));
+  lcc_epoch = g->plan_epoch;
+}
+
+void QueryImpl::run_lcc_loop(int max_iterations) {
+  ensure_hub_acc();
+  if (!lcc_exec || lcc_epoch != g->plan_epoch) build_lcc_loop();
+  const int cap = std::min(max_iterations, 1000) - iteration;
+  if (cap <= 0) return;
+  h_max_passes = static_cast<uint32_t>(cap);
+  LccLoopCtl* ctl = d_loop.as<LccLoopCtl>();
+  clear_step_counters();
+  PM_CUDA(cudaMemcpyAsync(&ctl->max_passes, &h_max_passes, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+  PM_CUDA(cudaEventRecord(ev0, stream));
+  if (!first_recorded) {
+    PM_CUDA(cudaEventRecord(ev_first, stream));
+    first_recorded = true;
+  }
+  PM_CUDA(cudaGraphLaunch(lcc_exec, stream));
+  PM_CUDA(cudaEventRecord(ev1, stream));
+  // Control block and the first rows in one read; the rest only if needed.
+  constexpr size_t kFirstRows = 64;
+  const size_t first = sizeof(LccLoopCtl) + sizeof(LccPassRow) * kFirstRows;
+  PM_CUDA(cudaMemcpyAsync(h_loop.data(), d_loop.ptr, first, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  LccLoopCtl hc;
+  std::memcpy(&hc, h_loop.data(), sizeof(hc));
+  if (hc.passes > kFirstRows) {
+    PM_CUDA(cudaMemcpyAsync(h_loop.data() + first, d_loop.as<unsigned char>() + first,
+                            sizeof(LccPassRow) * (hc.passes - kFirstRows), cudaMemcpyDeviceToHost, stream));
+    PM_CUDA(cudaStreamSynchronize(stream));
+  }
+  note_launches(1 + lcc_pass_launches * static_cast<int64_t>(hc.passes));
+  if (hc.error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(hc.error)};
+  if (hc.passes == 0 || hc.passes > static_cast<uint32_t>(cap))
+    throw PmError{PM_FAILURE, "LCC loop graph ran " + std::to_string(hc.passes) + " passes"};
+  const LccPassRow* rows = reinterpret_cast<const LccPassRow*>(h_loop.data() + sizeof(LccLoopCtl));
+  unsigned long long prev = hc.start_ns;
+  for (uint32_t i = 0; i < hc.passes; ++i) {
+    StepResult r;
+    r.vertex = rows[i].vertex_elim;
+    r.edge = rows[i].edge_elim;
+    r.match = rows[i].match_elim;
+    const double ms = rows[i].end_ns >= prev ? (rows[i].end_ns - prev) * 1e-6 : 0.0;
+    prev = rows[i].end_ns;
+    append_record(r, PM_STEP_LCC, ms, rows[i].scanned, rows[i].gathered);
+  }
 }
 
 double QueryImpl::elapsed_ms() {
@@ -927,7 +1047,12 @@ pm_step_record QueryImpl::final_record() {
 }
 
 void QueryImpl::run_all(int max_iterations) {
-  while (!finished && iteration < max_iterations) run_step();
+  while (!finished && iteration < max_iterations) {
+    if (step == PM_STEP_LCC && g_lcc_graph)
+      run_lcc_loop(max_iterations);
+    else
+      run_step();
+  }
 }
 
 void QueryImpl::export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact) {

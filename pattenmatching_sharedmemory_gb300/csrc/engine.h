@@ -52,6 +52,9 @@ struct GraphImpl {
   uint32_t hub_degree = kDefaultHubDegree, seg_entries = kDefaultSegEntries;
   uint32_t n_seg = 0, n_heavy = 0, n_acc = 0;
   DeviceBuffer d_seg;
+  // Bumped whenever dev() changes (hub plan, symmetric flag): captured
+  // graphs that baked the old DevGraph are rebuilt.
+  uint64_t plan_epoch = 0;
 
   static constexpr uint32_t kDefaultHubDegree = 32;
   static constexpr uint32_t kDefaultSegEntries = 1024;
@@ -126,6 +129,16 @@ struct QueryImpl {
   bool first_recorded = false;
   double elapsed_ms();
 
+  // The LCC fixpoint loop captured as one CUDA graph (built on first use,
+  // rebuilt when the graph's plan changes).
+  cudaGraph_t lcc_graph = nullptr;
+  cudaGraphExec_t lcc_exec = nullptr;
+  uint64_t lcc_epoch = 0;
+  int64_t lcc_pass_launches = 0;  // kernels per captured pass
+  DeviceBuffer d_loop;            // LccLoopCtl + kLccLoopMaxPasses rows
+  std::vector<unsigned char> h_loop;
+  uint32_t h_max_passes = 0;
+
   // statistics of the alreadyMatched emulation
   uint64_t exact_resolutions = 0, overflow_retries = 0;
   // per step: walker CSR entries tested and hops taken (0 for LCC steps)
@@ -164,6 +177,13 @@ struct QueryImpl {
   void run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks);
   void resolve_exact(const DeviceConstraint& dc, uint32_t n_wl);
   int advance(int cur);
+  void ensure_hub_acc();
+  void build_lcc_loop();
+  void destroy_lcc_loop();
+  // Runs LCC passes until the fixpoint (or max_iterations) in one graph
+  // launch and appends one row per pass, as run_step would.
+  void run_lcc_loop(int max_iterations);
+  void append_record(const StepResult& r, int kind, double ms, uint64_t scanned, uint64_t second);
 };
 
 // Walker memo table entries per warp in the first walk round.
@@ -191,6 +211,10 @@ uint32_t walk_table_entries();
 // Count-memo entries per warp in ENUMERATION's first round (power of two).
 void set_enum_table_entries(uint32_t entries);
 uint32_t enum_table_entries();
+// Whole-run paths (run_all) run each LCC fixpoint as one captured CUDA graph
+// (default on); off: one host-driven launch sequence per pass.
+void set_lcc_graph(bool on);
+bool lcc_graph();
 
 // Device bytes a query of a k-vertex template holds in its first walk
 // round (state, worklists, first walker pool); the admission charge.

@@ -54,6 +54,11 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 
 // Sweep 2 shared by LCC and CC/PC/TDS (lcc :107-141, cc :134-173).
 void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
+// Kernels of the captured LCC fixpoint loop (rows follow ctl in memory).
+void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s);
+void launch_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s);
+// Adds launches that ran inside graphs (captured launches count once).
+void note_launches(int64_t n);
 
 // Order-preserving compaction of the vertices that hold a role of
 // `start_mask`: wl[i] = i-th such vertex, wl_index[wl[i]] = i, *count = n.

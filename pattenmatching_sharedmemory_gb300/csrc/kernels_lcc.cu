@@ -1069,6 +1069,52 @@ __device__ __forceinline__ bool in_worklist(const DevGraph& g, const DevState<W>
   return v < g.V && (Pack<W>::cand(st.vs[v]) & mask) != 0;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Before the first pass of a captured fixpoint loop.
+__global__ void k_lcc_loop_head(LccLoopCtl* ctl) {
+  if (threadIdx.x != 0) return;
+  ctl->passes = 0;
+  ctl->error = 0;
+  ctl->start_ns = global_ns();
+}
+
+// After every pass: row `passes` gets the pass's counters; the loop goes on
+// while the pass eliminated a vertex, edge or role (the reference's
+// AlgoResults::isEmpty is false), no device error was raised and fewer than
+// max_passes passes ran.  The step counters start the next pass at zero.
+// rows holds kLccLoopMaxPasses rows and max_passes <= kLccLoopMaxPasses, so
+// the row index stays in bounds.
+__global__ void k_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, LccPassRow* rows, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  const uint32_t i = ctl->passes;
+  const uint32_t cap = min(ctl->max_passes, kLccLoopMaxPasses);
+  LccPassRow r;
+  r.vertex_elim = ctr->vertex_elim;
+  r.edge_elim = ctr->edge_elim;
+  r.match_elim = ctr->match_elim;
+  r.scanned = ctr->scanned;
+  r.gathered = ctr->gathered;
+  r.end_ns = global_ns();
+  bool more = false;
+  if (i < cap) {
+    rows[i] = r;
+    ctl->passes = i + 1;
+    more = (r.vertex_elim | r.edge_elim | r.match_elim) != 0 && i + 1 < cap;
+  }
+  if (ctr->error) {
+    ctl->error = ctr->error;
+    more = false;
+  }
+  unsigned long long* words = reinterpret_cast<unsigned long long*>(ctr);
+  for (int w = 0; w < kStepCounterWords; ++w) words[w] = 0;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
 template <class W>
 __global__ void __launch_bounds__(256) k_wl_count(DevGraph g, DevState<W> st, uint64_t mask, uint32_t* block_counts) {
   __shared__ uint32_t s_cnt[8];
@@ -1200,6 +1246,7 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 }  // namespace
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(int64_t n) { g_launches.fetch_add(static_cast<uint64_t>(n), std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sm_count() {
@@ -1265,6 +1312,16 @@ void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
   }
   const int grid = grid_for_tasks(sweep_tasks(g), 8);
   PM_DISPATCH_WORD(q.word_kind, k_apply<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.hub_acc, q.ctr));
+}
+
+void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s) {
+  note_launch();
+  k_lcc_loop_head<<<1, 32, 0, s>>>(ctl);
+}
+
+void launch_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s) {
+  note_launch();
+  k_lcc_loop_tail<<<1, 32, 0, s>>>(ctr, ctl, reinterpret_cast<LccPassRow*>(ctl + 1), h);
 }
 
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, uint32_t* wl, uint32_t* wl_index,

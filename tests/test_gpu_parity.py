@@ -219,3 +219,58 @@ def test_knob_settings_outputs_identical(name, setting):
     assert res["rows"] == case["rows"]
     assert pmtest.sha(res["vertex"]) == case["vertex_sha256"]
     assert pmtest.sha(res["graph"]) == case["graph_sha256"]
+
+
+LCC_GRAPH_CASES = ["scale12_tds", "cycle5_s10", "two_cycles_zipf_s10", "random_08", "fixture3_s9",
+                   "c1_scale10_cycle4", "k4_rep_s8"]
+
+
+def _rows_and_state(g, p):
+    q = pm.Query(g, pattern=p)
+    recs = q.run()
+    rows = [r.as_tuple() for r in recs]
+    cand, eact, vact = q.export()
+    count = q.match_count
+    q.close()
+    return recs, rows, count, cand, eact, vact
+
+
+@pytest.mark.parametrize("name", LCC_GRAPH_CASES)
+def test_lcc_graph_equals_host_loop(name):
+    """Each LCC fixpoint as one CUDA-graph launch (a conditional WHILE node
+    whose tail kernel records the pass and decides on the device whether
+    another pass runs) gives the rows, count and state of the host-driven
+    loop (one launch sequence and counter read-back per pass)."""
+    case = next(c for c in SYNTH if c["name"] == name)
+    g = C.make_graph(case).to_device(0)
+    p = C.make_pattern(case)
+    pm._check(pm.lib.pm_set_lcc_graph(0))
+    try:
+        host = _rows_and_state(g, p)
+    finally:
+        pm._check(pm.lib.pm_set_lcc_graph(1))
+    graph = _rows_and_state(g, p)
+    assert graph[1] == host[1]
+    assert graph[1] == [tuple(r) for r in case["rows"]]
+    assert graph[2] == host[2]
+    for a, b in zip(graph[3:], host[3:]):
+        assert np.array_equal(a, b)
+    lcc = [r for r in graph[0] if r.as_tuple()[0] == "LCC"]
+    assert lcc and all(r.step_ms >= 0 for r in lcc)
+    cum = [r.cumulative_ms for r in graph[0]]
+    assert cum == sorted(cum)
+
+
+def test_lcc_graph_follows_hub_plan_change():
+    """A plan change between queries rebuilds the captured loop (its kernels
+    bake the graph's segment table)."""
+    case = next(c for c in SYNTH if c["name"] == "scale12_tds")
+    g = C.make_graph(case).to_device(0)
+    p = C.make_pattern(case)
+    try:
+        for plan in [(16, 64), (32, 1024), (8, 32)]:
+            g.set_hub_plan(*plan)
+            rows = _rows_and_state(g, p)[1]
+            assert rows == [tuple(r) for r in case["rows"]], plan
+    finally:
+        g.set_hub_plan(32, 1024)
