@@ -230,20 +230,21 @@ def lcc_roofline(scale: int, device: int):
 def small_stream(g, args, pm, torch):
     """Served vs one-at-a-time on a stream of small requests (35 triangles)."""
     tm = small_templates()
-    with pm.Server(g, slots=args.slots) as srv:  # warm-up
-        [srv.wait(srv.submit(t)) for t in tm]
     reps = max(1, args.steps)
     served_lat, seq_lat = [], []
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
     counts = None
-    for _ in range(reps):
-        with pm.Server(g, slots=args.slots) as srv:
+    # One long-lived server, warmed up once, serves every timed burst.
+    with pm.Server(g, slots=args.slots) as srv:
+        for _ in range(max(1, args.warmup)):
+            [srv.wait(srv.submit(t)) for t in tm]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
             rs = [srv.wait(x) for x in [srv.submit(t) for t in tm]]
-        served_lat += [r.latency_ms for r in rs]
-        counts = [int(r.match_count) for r in rs]
-    torch.cuda.synchronize()
-    served = len(tm) * reps / (time.perf_counter() - t0)
+            served_lat += [r.latency_ms for r in rs]
+            counts = [int(r.match_count) for r in rs]
+        torch.cuda.synchronize()
+        served = len(tm) * reps / (time.perf_counter() - t0)
     t0 = time.perf_counter()
     for _ in range(reps):
         seq_counts = []
@@ -271,6 +272,7 @@ def run_gb300(args, w, rank, world):
 
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    pm._check(pm.lib.pm_set_lcc_graph(args.lcc_graph))
     g = make_graph(w)
     g.to_device(device)
     tmpls = stream_templates()
@@ -282,19 +284,27 @@ def run_gb300(args, w, rank, world):
     tuned["seconds"] = round(time.perf_counter() - t_tune, 2)
     k_word = 1  # ceil(k/8) B of neighbour roles for the 4-vertex templates
 
-    def serve_stream(graph, export=False):
-        with pm.Server(graph, slots=args.slots) as srv:
-            tickets = [srv.submit(t, export_state=export) for t in tmpls]
-            results = [srv.wait(t) for t in tickets]
-            states = [srv.export(t) for t in tickets] if export else None
-            rows = [srv.records(t) for t in tickets] if export else None
+    def serve_burst(srv, export=False):
+        tickets = [srv.submit(t, export_state=export) for t in tmpls]
+        results = [srv.wait(t) for t in tickets]
+        states = [srv.export(t) for t in tickets] if export else None
+        rows = [srv.records(t) for t in tickets] if export else None
+        for t in tickets:
+            srv.release(t)
         bad = [r.status for r in results if r.status != pm.PM_SUCCESS]
         if bad:
             raise RuntimeError(f"served requests failed: {bad}")
         return results, states, rows
 
+    def serve_stream(graph, export=False):
+        with pm.Server(graph, slots=args.slots) as srv:
+            return serve_burst(srv, export)
+
+    # The served measurement uses one long-lived server (created and warmed
+    # up outside the timed region), as a serving process would.
+    server = pm.Server(g, slots=args.slots)
     for _ in range(args.warmup):
-        serve_stream(g)
+        serve_burst(server)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -310,12 +320,13 @@ def run_gb300(args, w, rank, world):
             flush.fill_(1)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            results, _, _ = serve_stream(g)
+            results, _, _ = serve_burst(server)
             torch.cuda.synchronize()
             served_s += time.perf_counter() - t0
             served_lat += [r.latency_ms for r in results]
             counts = [int(r.match_count) for r in results]
     launches = int(pm.lib.pm_kernel_launches()) - launches0
+    server.close()
     served_max = max_over_ranks(served_s, world, f"cuda:{device}")
 
     # One at a time: the same stream through pm_query_run, back to back.
@@ -391,8 +402,10 @@ def run_gb300(args, w, rank, world):
                    "vertices": g.vertex_count, "csr_entries": g.edge_count, "labels": list(w["labels"]),
                    "templates": "15 distinct-label 4-cycles over labels 0..4", "requests_per_step": n,
                    "slots": args.slots, "arrival": "all requests of a step submitted at once",
+                   "server": "one long-lived server across the timed steps (e2e: one per step, new graph upload)",
                    "autotuned": tuned,
-                   "lcc_fixpoint": "one CUDA graph per fixpoint (conditional WHILE node over a pass)",
+                   "lcc_fixpoint": ("one CUDA graph launch per fixpoint (conditional WHILE node over a pass)"
+                                    if args.lcc_graph else "host-driven, one launch sequence per pass"),
                    "match_counts": counts, "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step (512 MB write outside the timed interval)"},
         "latency_ms": {"p50": pct(served_lat, 0.5), "p99": pct(served_lat, 0.99)},
@@ -445,6 +458,8 @@ def main():
     ap.add_argument("--lcc-scale", type=int, default=22)
     ap.add_argument("--sample-stride", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lcc-graph", type=int, default=1, choices=[0, 1],
+                    help="run each LCC fixpoint as one CUDA graph (1) or one host-driven launch sequence per pass (0)")
     args = ap.parse_args()
     w = WORKLOAD
     stride = args.sample_stride or w["sample_stride"]

@@ -4,6 +4,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -97,7 +98,7 @@ void GraphImpl::to_device(int dev) {
     PM_CUDA(e);
     symmetric = asym == 0;
   }
-  ++plan_epoch;
+  plan_epoch = next_plan_epoch();
 }
 
 void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
@@ -140,7 +141,7 @@ void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
   n_seg = static_cast<uint32_t>(seg.size());
   n_heavy = heavy;
   n_acc = n_multi;
-  ++plan_epoch;
+  plan_epoch = next_plan_epoch();
 }
 
 DevGraph GraphImpl::dev() const {
@@ -245,7 +246,6 @@ uint64_t estimate_query_bytes(const GraphImpl& g, uint32_t k) {
 }
 
 QueryImpl::~QueryImpl() {
-  destroy_lcc_loop();
   // Stream-ordered frees go before the stream is destroyed.
   for (DeviceBuffer* b : buffers()) b->release();
   if (own_host) {
@@ -918,110 +918,170 @@ void QueryImpl::append_record(const StepResult& r_in, int kind, double ms, uint6
 }
 
 // ---- the LCC fixpoint as one CUDA graph ----------------------------------
+//
+// Graph: head kernel -> WHILE(cond) { LCC sweep 1, sweep 2, tail kernel }.
+// Its kernels read the query's pointers from a device block, so one
+// instantiated graph per (graph plan, word type) serves every query a host
+// thread runs: a query writes its block and launches.  Each host thread keeps
+// its own graphs (a server slot is one thread), so no two queries share a
+// block at the same time; instantiating and destroying graphs (which may wait
+// for the whole device) stays out of the per-query path.
 namespace {
 bool g_lcc_graph = true;
+std::atomic<uint64_t> g_plan_epochs{0};
+
+constexpr size_t kArgsBytes = 256;  // QueryDevPtrs, padded
+constexpr size_t kLoopBytes = kArgsBytes + sizeof(LccLoopCtl) + sizeof(LccPassRow) * kLccLoopMaxPasses;
+static_assert(sizeof(QueryDevPtrs) <= kArgsBytes, "argument block");
+
+struct LccLoop {
+  const GraphImpl* g = nullptr;
+  uint64_t epoch = 0;
+  int device = -1, word_kind = -1;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned char* d_block = nullptr;  // arguments | control | rows
+  unsigned char* h_block = nullptr;  // pinned mirror
+  int64_t pass_launches = 0;         // kernels per pass
+  uint64_t used = 0;
+  LccLoop() = default;
+  LccLoop(const LccLoop&) = delete;
+  LccLoop& operator=(const LccLoop&) = delete;
+  ~LccLoop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (d_block) cudaFree(d_block);
+    if (h_block) cudaFreeHost(h_block);
+  }
+  QueryDevPtrs* d_args() const { return reinterpret_cast<QueryDevPtrs*>(d_block); }
+  LccLoopCtl* d_ctl() const { return reinterpret_cast<LccLoopCtl*>(d_block + kArgsBytes); }
+
+  void build(const GraphImpl& graph_impl, int kind) {
+    PM_CUDA(cudaMalloc(&d_block, kLoopBytes));
+    PM_CUDA(cudaMallocHost(&h_block, kLoopBytes));
+    cudaStream_t cs = nullptr;
+    PM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    try {
+      PM_CUDA(cudaGraphCreate(&graph, 0));
+      cudaGraphConditionalHandle handle;
+      PM_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+      // Relaxed capture: other host threads may allocate meanwhile.
+      PM_CUDA(cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+      launch_lcc_loop_head(d_ctl(), cs);
+      PM_CUDA(cudaStreamEndCapture(cs, &graph));
+      cudaGraphNode_t head = nullptr;
+      size_t n_nodes = 1;
+      PM_CUDA(cudaGraphGetNodes(graph, &head, &n_nodes));
+      if (n_nodes != 1 || !head) throw PmError{PM_FAILURE, "LCC loop graph: unexpected head nodes"};
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t loop = nullptr;
+      PM_CUDA(cudaGraphAddNode(&loop, graph, &head, nullptr, 1, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      const uint64_t before = thread_launch_count();
+      PM_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+      const DevGraph dg = graph_impl.dev();
+      launch_lcc_pass_at(dg, kind, d_args(), cs);
+      launch_lcc_loop_tail(d_args(), d_ctl(), handle, cs);
+      PM_CUDA(cudaStreamEndCapture(cs, &body));
+      pass_launches = static_cast<int64_t>(thread_launch_count() - before);
+      // Captured launches ran nothing; each run adds what it executes.
+      note_launches(-pass_launches - 1);
+      PM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    } catch (...) {
+      cudaStreamDestroy(cs);
+      throw;
+    }
+    PM_CUDA(cudaStreamDestroy(cs));
+    g = &graph_impl;
+    epoch = graph_impl.plan_epoch;
+    device = graph_impl.device;
+    word_kind = kind;
+  }
+};
+
+// Per host thread: the loops it built, least recently used dropped first.
+struct LccLoopCache {
+  static constexpr size_t kMax = 8;
+  std::vector<std::unique_ptr<LccLoop>> loops;
+  uint64_t tick = 0;
+  LccLoop& get(const GraphImpl& g, int kind) {
+    for (auto& l : loops)
+      if (l->g == &g && l->epoch == g.plan_epoch && l->device == g.device && l->word_kind == kind) {
+        l->used = ++tick;
+        return *l;
+      }
+    if (loops.size() >= kMax) {
+      auto lru = std::min_element(loops.begin(), loops.end(),
+                                  [](const auto& a, const auto& b) { return a->used < b->used; });
+      loops.erase(lru);
+    }
+    auto l = std::make_unique<LccLoop>();
+    l->build(g, kind);
+    l->used = ++tick;
+    loops.push_back(std::move(l));
+    return *loops.back();
+  }
+};
+thread_local LccLoopCache t_lcc_loops;
 }  // namespace
 
+uint64_t next_plan_epoch() { return g_plan_epochs.fetch_add(1, std::memory_order_relaxed) + 1; }
 void set_lcc_graph(bool on) { g_lcc_graph = on; }
 bool lcc_graph() { return g_lcc_graph; }
 
-void QueryImpl::destroy_lcc_loop() {
-  if (lcc_exec) cudaGraphExecDestroy(lcc_exec);
-  if (lcc_graph) cudaGraphDestroy(lcc_graph);
-  lcc_exec = nullptr;
-  lcc_graph = nullptr;
-}
-
-// Graph: head kernel -> WHILE(cond) { LCC sweep 1, sweep 2, tail kernel }.
-// The body is captured from the same launch sequence step_lcc issues, on a
-// capture-only stream (relaxed mode, so other threads may keep allocating).
-void QueryImpl::build_lcc_loop() {
-  destroy_lcc_loop();
-  d_loop.ensure(sizeof(LccLoopCtl) + sizeof(LccPassRow) * kLccLoopMaxPasses);
-  h_loop.resize(d_loop.bytes);
-  LccLoopCtl* ctl = d_loop.as<LccLoopCtl>();
-  cudaStream_t cs = nullptr;
-  PM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-  try {
-    PM_CUDA(cudaGraphCreate(&lcc_graph, 0));
-    cudaGraphConditionalHandle handle;
-    PM_CUDA(cudaGraphConditionalHandleCreate(&handle, lcc_graph, 1, cudaGraphCondAssignDefault));
-    PM_CUDA(cudaStreamBeginCaptureToGraph(cs, lcc_graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    launch_lcc_loop_head(ctl, cs);
-    PM_CUDA(cudaStreamEndCapture(cs, &lcc_graph));
-    cudaGraphNode_t head = nullptr;
-    size_t n_nodes = 1;
-    PM_CUDA(cudaGraphGetNodes(lcc_graph, &head, &n_nodes));
-    if (n_nodes != 1) throw PmError{PM_FAILURE, "LCC loop graph: unexpected head nodes"};
-    cudaGraphNodeParams cp{};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = handle;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t loop = nullptr;
-    PM_CUDA(cudaGraphAddNode(&loop, lcc_graph, &head, nullptr, 1, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    const uint64_t before = launch_count();
-    PM_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    launch_lcc_check(g->dev(), ptrs(), cs);
-    launch_apply(g->dev(), ptrs(), cs);
-    launch_lcc_loop_tail(d_ctr.as<StepCounters>(), ctl, handle, cs);
-    PM_CUDA(cudaStreamEndCapture(cs, &body));
-    lcc_pass_launches = static_cast<int64_t>(launch_count() - before);
-    // Captured launches ran nothing yet; runs add what they execute.
-    note_launches(-lcc_pass_launches - 1);
-    PM_CUDA(cudaGraphInstantiate(&lcc_exec, lcc_graph, 0));
-  } catch (...) {
-    cudaStreamDestroy(cs);
-    destroy_lcc_loop();
-    throw;
-  }
-  PM_CUDA(cudaStreamDestroy(cs));
-  lcc_epoch = g->plan_epoch;
-}
-
 void QueryImpl::run_lcc_loop(int max_iterations) {
-  ensure_hub_acc();
-  if (!lcc_exec || lcc_epoch != g->plan_epoch) build_lcc_loop();
   const int cap = std::min(max_iterations, 1000) - iteration;
   if (cap <= 0) return;
-  h_max_passes = static_cast<uint32_t>(cap);
-  LccLoopCtl* ctl = d_loop.as<LccLoopCtl>();
+  ensure_hub_acc();
+  LccLoop& loop = t_lcc_loops.get(*g, word_kind);
+  // Arguments and the pass cap in one copy; the head kernel resets the rest.
+  const QueryDevPtrs args = ptrs();
+  std::memcpy(loop.h_block, &args, sizeof(args));
+  LccLoopCtl ctl{};
+  ctl.max_passes = static_cast<uint32_t>(cap);
+  std::memcpy(loop.h_block + kArgsBytes, &ctl, sizeof(ctl));
   clear_step_counters();
-  PM_CUDA(cudaMemcpyAsync(&ctl->max_passes, &h_max_passes, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+  PM_CUDA(cudaMemcpyAsync(loop.d_block, loop.h_block, kArgsBytes + sizeof(LccLoopCtl), cudaMemcpyHostToDevice,
+                          stream));
   PM_CUDA(cudaEventRecord(ev0, stream));
   if (!first_recorded) {
     PM_CUDA(cudaEventRecord(ev_first, stream));
     first_recorded = true;
   }
-  PM_CUDA(cudaGraphLaunch(lcc_exec, stream));
+  PM_CUDA(cudaGraphLaunch(loop.exec, stream));
   PM_CUDA(cudaEventRecord(ev1, stream));
   // Control block and the first rows in one read; the rest only if needed.
   constexpr size_t kFirstRows = 64;
   const size_t first = sizeof(LccLoopCtl) + sizeof(LccPassRow) * kFirstRows;
-  PM_CUDA(cudaMemcpyAsync(h_loop.data(), d_loop.ptr, first, cudaMemcpyDeviceToHost, stream));
+  unsigned char* h_ctl = loop.h_block + kArgsBytes;
+  PM_CUDA(cudaMemcpyAsync(h_ctl, loop.d_ctl(), first, cudaMemcpyDeviceToHost, stream));
   PM_CUDA(cudaStreamSynchronize(stream));
   LccLoopCtl hc;
-  std::memcpy(&hc, h_loop.data(), sizeof(hc));
-  if (hc.passes > kFirstRows) {
-    PM_CUDA(cudaMemcpyAsync(h_loop.data() + first, d_loop.as<unsigned char>() + first,
+  std::memcpy(&hc, h_ctl, sizeof(hc));
+  if (hc.passes > kFirstRows && hc.passes <= kLccLoopMaxPasses) {
+    PM_CUDA(cudaMemcpyAsync(h_ctl + first, reinterpret_cast<unsigned char*>(loop.d_ctl()) + first,
                             sizeof(LccPassRow) * (hc.passes - kFirstRows), cudaMemcpyDeviceToHost, stream));
     PM_CUDA(cudaStreamSynchronize(stream));
   }
-  note_launches(1 + lcc_pass_launches * static_cast<int64_t>(hc.passes));
+  note_launches(1 + loop.pass_launches * static_cast<int64_t>(std::min(hc.passes, kLccLoopMaxPasses)));
   if (hc.error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(hc.error)};
   if (hc.passes == 0 || hc.passes > static_cast<uint32_t>(cap))
     throw PmError{PM_FAILURE, "LCC loop graph ran " + std::to_string(hc.passes) + " passes"};
-  const LccPassRow* rows = reinterpret_cast<const LccPassRow*>(h_loop.data() + sizeof(LccLoopCtl));
+  LccPassRow row;
   unsigned long long prev = hc.start_ns;
   for (uint32_t i = 0; i < hc.passes; ++i) {
+    std::memcpy(&row, h_ctl + sizeof(LccLoopCtl) + sizeof(LccPassRow) * i, sizeof(row));
     StepResult r;
-    r.vertex = rows[i].vertex_elim;
-    r.edge = rows[i].edge_elim;
-    r.match = rows[i].match_elim;
-    const double ms = rows[i].end_ns >= prev ? (rows[i].end_ns - prev) * 1e-6 : 0.0;
-    prev = rows[i].end_ns;
-    append_record(r, PM_STEP_LCC, ms, rows[i].scanned, rows[i].gathered);
+    r.vertex = row.vertex_elim;
+    r.edge = row.edge_elim;
+    r.match = row.match_elim;
+    const double ms = row.end_ns >= prev ? (row.end_ns - prev) * 1e-6 : 0.0;
+    prev = row.end_ns;
+    append_record(r, PM_STEP_LCC, ms, row.scanned, row.gathered);
   }
 }
 

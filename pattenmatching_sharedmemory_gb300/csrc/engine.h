@@ -52,8 +52,9 @@ struct GraphImpl {
   uint32_t hub_degree = kDefaultHubDegree, seg_entries = kDefaultSegEntries;
   uint32_t n_seg = 0, n_heavy = 0, n_acc = 0;
   DeviceBuffer d_seg;
-  // Bumped whenever dev() changes (hub plan, symmetric flag): captured
-  // graphs that baked the old DevGraph are rebuilt.
+  // New process-wide unique value whenever dev() changes (hub plan,
+  // symmetric flag): captured graphs that baked another DevGraph are not
+  // reused.
   uint64_t plan_epoch = 0;
 
   static constexpr uint32_t kDefaultHubDegree = 32;
@@ -129,16 +130,6 @@ struct QueryImpl {
   bool first_recorded = false;
   double elapsed_ms();
 
-  // The LCC fixpoint loop captured as one CUDA graph (built on first use,
-  // rebuilt when the graph's plan changes).
-  cudaGraph_t lcc_graph = nullptr;
-  cudaGraphExec_t lcc_exec = nullptr;
-  uint64_t lcc_epoch = 0;
-  int64_t lcc_pass_launches = 0;  // kernels per captured pass
-  DeviceBuffer d_loop;            // LccLoopCtl + kLccLoopMaxPasses rows
-  std::vector<unsigned char> h_loop;
-  uint32_t h_max_passes = 0;
-
   // statistics of the alreadyMatched emulation
   uint64_t exact_resolutions = 0, overflow_retries = 0;
   // per step: walker CSR entries tested and hops taken (0 for LCC steps)
@@ -178,8 +169,6 @@ struct QueryImpl {
   void resolve_exact(const DeviceConstraint& dc, uint32_t n_wl);
   int advance(int cur);
   void ensure_hub_acc();
-  void build_lcc_loop();
-  void destroy_lcc_loop();
   // Runs LCC passes until the fixpoint (or max_iterations) in one graph
   // launch and appends one row per pass, as run_step would.
   void run_lcc_loop(int max_iterations);
@@ -215,6 +204,7 @@ uint32_t enum_table_entries();
 // (default on); off: one host-driven launch sequence per pass.
 void set_lcc_graph(bool on);
 bool lcc_graph();
+uint64_t next_plan_epoch();
 
 // Device bytes a query of a k-vertex template holds in its first walk
 // round (state, worklists, first walker pool); the admission charge.

@@ -56,9 +56,13 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 // Kernels of the captured LCC fixpoint loop (rows follow ctl in memory).
 void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s);
-void launch_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s);
+void launch_lcc_loop_tail(const QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s);
+// One LCC pass with the query's pointers read from the device block `a`.
+void launch_lcc_pass_at(const DevGraph& g, int word_kind, const QueryDevPtrs* a, cudaStream_t s);
 // Adds launches that ran inside graphs (captured launches count once).
 void note_launches(int64_t n);
+// Launches issued by the calling host thread.
+uint64_t thread_launch_count();
 
 // Order-preserving compaction of the vertices that hold a role of
 // `start_mask`: wl[i] = i-th such vertex, wl_index[wl[i]] = i, *count = n.

@@ -755,9 +755,9 @@ __device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTabl
 // runs the hub segments (single- and multi-segment hubs), kTiles true the
 // tiles of light vertices.
 template <class W, bool kTiles>
-__global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph g, DevState<W> st,
-                                                                        const QueryTables* __restrict__ qt,
-                                                                        HubAcc* hub_acc, StepCounters* ctr) {
+__device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState<W>& st,
+                                               const QueryTables* __restrict__ qt, HubAcc* hub_acc,
+                                               StepCounters* ctr) {
   __shared__ LccTables t;
   __shared__ LccWarp s_lw[kLccWarps];
   load_lcc_tables(t, qt, qt->k);
@@ -795,6 +795,36 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph
     if (nm) atomicAdd(&ctr->modified_total, static_cast<unsigned long long>(nm));
     if (ga) atomicAdd(&ctr->gathered, static_cast<unsigned long long>(ga));
     if (tl.streamed) atomicAdd(&ctr->scanned, static_cast<unsigned long long>(tl.streamed));
+  }
+}
+
+// The query's pointers, read from a device block (captured LCC loops: one
+// instantiated graph serves every query that writes its block).
+template <class W>
+__device__ __forceinline__ DevState<W> state_at(const QueryDevPtrs* __restrict__ a) {
+  return DevState<W>{static_cast<W*>(a->vs), a->eact, a->mod, a->sch, static_cast<W*>(a->unm), a->lt, a->tile_sch};
+}
+
+template <class W, bool kTiles>
+__global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph g, DevState<W> st,
+                                                                        const QueryTables* __restrict__ qt,
+                                                                        HubAcc* hub_acc, StepCounters* ctr) {
+  lcc_check_body<W, kTiles>(g, st, qt, hub_acc, ctr);
+}
+
+template <class W, bool kTiles>
+__global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_at(DevGraph g,
+                                                                           const QueryDevPtrs* __restrict__ a) {
+  if constexpr (kTiles) {
+    // Staged in shared memory: read where used instead of held in
+    // registers (no spills at 64 registers; the hub form spills less
+    // without it).
+    __shared__ DevState<W> s_st;
+    if (threadIdx.x == 0) s_st = state_at<W>(a);
+    __syncthreads();
+    lcc_check_body<W, kTiles>(g, s_st, a->tables, a->hub_acc, a->ctr);
+  } else {
+    lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr);
   }
 }
 
@@ -929,7 +959,8 @@ __device__ void apply_tile(const DevGraph& g, const DevState<W>& st, uint64_t ti
 }
 
 template <class W>
-__global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, HubAcc* hub_acc, StepCounters* ctr) {
+__device__ __forceinline__ void apply_body(const DevGraph& g, const DevState<W>& st, HubAcc* hub_acc,
+                                           StepCounters* ctr) {
   const bool any_modified = *reinterpret_cast<volatile unsigned long long*>(&ctr->modified_total) != 0;
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
@@ -955,6 +986,16 @@ __global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, 
   }
 }
 
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, HubAcc* hub_acc, StepCounters* ctr) {
+  apply_body(g, st, hub_acc, ctr);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
+  apply_body(g, state_at<W>(a), a->hub_acc, a->ctr);
+}
+
 // ---- sweep 2 on symmetric graphs: schedule by change -------------------
 //
 // A vertex's LCC outcome depends only on its own roles and the roles and
@@ -973,7 +1014,7 @@ __global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, 
 // step", sch[v] keeps such vertices that still hold a role, tile_sch
 // summarises sch per tile.
 template <class W>
-__global__ void __launch_bounds__(kThreads) k_apply_changed(DevGraph g, DevState<W> st, StepCounters* ctr) {
+__device__ __forceinline__ void apply_changed_body(const DevGraph& g, const DevState<W>& st, StepCounters* ctr) {
   const unsigned lane = lane_id();
   const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -1009,6 +1050,16 @@ __global__ void __launch_bounds__(kThreads) k_apply_changed(DevGraph g, DevState
   }
 }
 
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_changed(DevGraph g, DevState<W> st, StepCounters* ctr) {
+  apply_changed_body(g, st, ctr);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_changed_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
+  apply_changed_body(g, state_at<W>(a), a->ctr);
+}
+
 // Marks every entry target of [b, e) as scheduled (one warp).
 template <class W>
 __device__ __forceinline__ void push_range(const DevGraph& g, const DevState<W>& st, uint64_t b, uint64_t e) {
@@ -1023,7 +1074,7 @@ __device__ __forceinline__ void push_range(const DevGraph& g, const DevState<W>&
 // task layout of sweep 1 (hub segments, batches of 32 single-segment hubs,
 // tiles of 32 light vertices).
 template <class W>
-__global__ void __launch_bounds__(kThreads) k_push_changed(DevGraph g, DevState<W> st) {
+__device__ __forceinline__ void push_changed_body(const DevGraph& g, const DevState<W>& st) {
   const unsigned lane = lane_id();
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
@@ -1061,6 +1112,16 @@ __global__ void __launch_bounds__(kThreads) k_push_changed(DevGraph g, DevState<
   }
 }
 
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_push_changed(DevGraph g, DevState<W> st) {
+  push_changed_body(g, st);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_push_changed_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
+  push_changed_body(g, state_at<W>(a));
+}
+
 // ---- worklist compaction ----------------------------------------------
 constexpr int kTileV = 4096;  // vertices per compaction block (256 threads x 16)
 
@@ -1089,8 +1150,10 @@ __global__ void k_lcc_loop_head(LccLoopCtl* ctl) {
 // max_passes passes ran.  The step counters start the next pass at zero.
 // rows holds kLccLoopMaxPasses rows and max_passes <= kLccLoopMaxPasses, so
 // the row index stays in bounds.
-__global__ void k_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, LccPassRow* rows, cudaGraphConditionalHandle h) {
+__global__ void k_lcc_loop_tail(const QueryDevPtrs* __restrict__ a, LccLoopCtl* ctl, LccPassRow* rows,
+                                cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0) return;
+  StepCounters* ctr = a->ctr;
   const uint32_t i = ctl->passes;
   const uint32_t cap = min(ctl->max_passes, kLccLoopMaxPasses);
   LccPassRow r;
@@ -1245,8 +1308,13 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 
 }  // namespace
 
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+thread_local uint64_t t_launches = 0;
+void note_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  ++t_launches;
+}
 void note_launches(int64_t n) { g_launches.fetch_add(static_cast<uint64_t>(n), std::memory_order_relaxed); }
+uint64_t thread_launch_count() { return t_launches; }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int device_sm_count() {
@@ -1319,9 +1387,30 @@ void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s) {
   k_lcc_loop_head<<<1, 32, 0, s>>>(ctl);
 }
 
-void launch_lcc_loop_tail(StepCounters* ctr, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s) {
+void launch_lcc_loop_tail(const QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s) {
   note_launch();
-  k_lcc_loop_tail<<<1, 32, 0, s>>>(ctr, ctl, reinterpret_cast<LccPassRow*>(ctl + 1), h);
+  k_lcc_loop_tail<<<1, 32, 0, s>>>(a, ctl, reinterpret_cast<LccPassRow*>(ctl + 1), h);
+}
+
+// One LCC pass (sweep 1 + sweep 2), grids as launch_lcc_check and
+// launch_apply, with the query's pointers read from the device block `a`.
+void launch_lcc_pass_at(const DevGraph& g, int word_kind, const QueryDevPtrs* a, cudaStream_t s) {
+  const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  if (hub_tasks) {
+    const int grid = grid_for_tasks(hub_tasks, 5);
+    PM_DISPATCH_WORD(word_kind, k_lcc_check_at<W, false><<<grid, kThreads, 0, s>>>(g, a));
+  }
+  const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4);
+  PM_DISPATCH_WORD(word_kind, k_lcc_check_at<W, true><<<grid, kThreads, 0, s>>>(g, a));
+  if (g.symmetric) {
+    const int grid1 = grid_for_tiles(g.V, 8);
+    PM_DISPATCH_WORD(word_kind, k_apply_changed_at<W><<<grid1, kThreads, 0, s>>>(g, a));
+    const int grid2 = grid_for_tasks(sweep_tasks(g), 8);
+    PM_DISPATCH_WORD(word_kind, k_push_changed_at<W><<<grid2, kThreads, 0, s>>>(g, a));
+    return;
+  }
+  const int grid2 = grid_for_tasks(sweep_tasks(g), 8);
+  PM_DISPATCH_WORD(word_kind, k_apply_at<W><<<grid2, kThreads, 0, s>>>(g, a));
 }
 
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, uint32_t* wl, uint32_t* wl_index,

@@ -274,3 +274,15 @@ def test_lcc_graph_follows_hub_plan_change():
             assert rows == [tuple(r) for r in case["rows"]], plan
     finally:
         g.set_hub_plan(32, 1024)
+
+
+def test_lcc_graph_alternating_graphs_one_thread():
+    """One host thread alternating between two resident graphs (and word
+    types) reuses a captured loop per graph: every run still gives the
+    golden rows."""
+    cases = [next(c for c in SYNTH if c["name"] == n) for n in ("scale12_tds", "k4_rep_s8")]
+    graphs = [C.make_graph(c).to_device(0) for c in cases]
+    for _ in range(2):
+        for c, g in zip(cases, graphs):
+            rows = _rows_and_state(g, C.make_pattern(c))[1]
+            assert rows == [tuple(r) for r in c["rows"]], c["name"]
