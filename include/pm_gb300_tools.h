@@ -86,6 +86,7 @@ typedef struct pm_tune_result {
   uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
+  uint32_t enum_tail_swap;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -119,6 +120,17 @@ pm_status_t pm_set_enum_table_entries(uint32_t entries);
  * enabled = 0 turns it off (default 1).  Process-wide; speed only.  No
  * counterpart in the reference. */
 pm_status_t pm_set_lcc_graph(int32_t enabled);
+
+/* ENUMERATION's last VERTEX step before the closing CHECKs (e.g. the fourth
+ * vertex of a 4-cycle, checked against the source): on symmetric graphs,
+ * when the source's list is cached (at most 256 entries) and the current
+ * vertex's list has at least `ratio` times as many 32-entry chunks as the
+ * source's entries holding the step's role, the step iterates over those
+ * source entries and searches the current vertex's list, instead of scanning
+ * the current vertex's list and searching the source's.  Both count the same
+ * set (enumeration_cpu.tpp:96-104 semantics).  0 = never; default 4.
+ * Process-wide; speed only.  No counterpart in the reference. */
+pm_status_t pm_set_enum_tail_swap(uint32_t ratio);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

@@ -136,7 +136,25 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
   out.enum_presplit_memo = enum_presplit(true);
   out.enum_presplit_plain = enum_presplit(false);
 
-  // 4. Count-memo entries per warp, on every probe.
+  // 4. ENUMERATION tail from the source's side: chunk ratio, on every probe.
+  {
+    const uint32_t ratios[] = {0, 2, 4, 8};
+    double b = std::numeric_limits<double>::infinity();
+    uint32_t pick = enum_tail_swap();
+    for (uint32_t rt : ratios) {
+      set_enum_tail_swap(rt);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.enum_ms < b) {
+        b = r.enum_ms;
+        pick = rt;
+      }
+    }
+    set_enum_tail_swap(pick);
+    out.enum_tail_swap = pick;
+  }
+
+  // 5. Count-memo entries per warp, on every probe.
   const uint32_t tables[] = {4096, 8192, 16384};
   double bt = std::numeric_limits<double>::infinity();
   uint32_t pick_t = enum_table_entries();

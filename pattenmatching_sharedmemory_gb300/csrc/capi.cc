@@ -349,6 +349,11 @@ pm_status_t pm_set_enum_table_entries(uint32_t entries) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_enum_tail_swap(uint32_t ratio) {
+  set_enum_tail_swap(ratio);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -602,6 +607,7 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->enum_presplit_memo = r.enum_presplit_memo;
       result->enum_presplit_plain = r.enum_presplit_plain;
       result->enum_table_entries = r.enum_table_entries;
+      result->enum_tail_swap = r.enum_tail_swap;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

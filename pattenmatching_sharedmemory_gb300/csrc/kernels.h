@@ -79,6 +79,11 @@ constexpr unsigned long long kDeviceErrorTimeout = 2;
 // Time budget of one walker launch (ns of %globaltimer per warp); a warp
 // past it stops, marks its item kItemTimeout and sets kDeviceErrorTimeout.
 void set_walk_budget_ns(uint64_t ns);
+// ENUMERATION tail step from the cached source's side when the bound
+// vertex's list has at least `ratio` times as many 32-entry chunks as the
+// source's entries holding the tail role (0: never).
+void set_enum_tail_swap(uint32_t ratio);
+uint32_t enum_tail_swap();
 uint64_t walk_budget_ns();
 
 // Per-warp scratch for the walkers' memo tables.  The edge and hypothesis

@@ -57,9 +57,15 @@ struct WarpShared {
   unsigned long long scanned;   // CSR entries tested by this warp (lane 0 writes)
   unsigned long long descents;  // hops taken by this warp
   // Adjacency list of the walk's source, copied to shared memory when it has
-  // at most kSrcCache entries (src_n == 0: not cached).
+  // at most kSrcCache entries (src_cached); ENUMERATION keeps only the
+  // entries whose target holds the tail step's role (src_n of them).
   const uint32_t* src_adj;
   uint32_t src_n;
+  uint32_t src_cached;
+  // ENUMERATION: the tail step iterates over the cached source entries
+  // instead of the bound vertex's list when that list has at least
+  // tail_swap times as many 32-entry chunks (0: never).
+  uint32_t tail_swap;
 };
 
 // Source adjacency entries a warp caches in shared memory per walk.
@@ -82,22 +88,51 @@ __device__ __forceinline__ void bind_frames(WarpShared& ws, unsigned char* base,
   __syncwarp();
 }
 
+template <class W>
+__device__ __forceinline__ bool role_of(const DevState<W>& st, uint32_t v, uint32_t role) {
+  return (Pack<W>::cand(st.vs[v]) >> role) & 1;
+}
+
 // Copies the source's list into the warp's cache when it fits and the graph
 // is symmetric (the only case where tail CHECKs search the source's list).
-__device__ __forceinline__ void cache_source(const DevGraph& g, WarpShared& ws, uint32_t* cache, uint32_t source) {
+// filter_role >= 0 keeps only the entries whose target holds that role, in
+// list order: a tail candidate holds the tail step's role, so it is in the
+// source's list exactly when it is in the filtered one (the state does not
+// change during a walk launch).
+template <class W>
+__device__ __forceinline__ void cache_source(const DevGraph& g, const DevState<W>& st, WarpShared& ws,
+                                             uint32_t* cache, uint32_t source, int filter_role) {
   const unsigned lane = lane_id();
-  uint32_t n = 0;
+  uint32_t n = 0, cached = 0;
   if (g.symmetric) {
     const uint64_t b = g.off[source], e = g.off[source + 1];
     if (e - b <= kSrcCache) {
-      n = static_cast<uint32_t>(e - b);
-      for (uint32_t i = lane; i < n; i += 32) cache[i] = g.adj[b + i];
+      cached = 1;
+      const uint32_t len = static_cast<uint32_t>(e - b);
+      if (filter_role < 0) {
+        n = len;
+        for (uint32_t i = lane; i < n; i += 32) cache[i] = g.adj[b + i];
+      } else {
+        for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+          const uint32_t i = i0 + lane;
+          uint32_t x = 0;
+          bool keep = false;
+          if (i < len) {
+            x = g.adj[b + i];
+            keep = role_of(st, x, static_cast<uint32_t>(filter_role));
+          }
+          const unsigned m = __ballot_sync(kFull, keep);
+          if (keep) cache[n + __popc(m & ((1u << lane) - 1u))] = x;
+          n += __popc(m);
+        }
+      }
     }
   }
   __syncwarp();
   if (lane == 0) {
     ws.src_adj = cache;
     ws.src_n = n;
+    ws.src_cached = cached;
   }
   __syncwarp();
 }
@@ -105,6 +140,7 @@ __device__ __forceinline__ void cache_source(const DevGraph& g, WarpShared& ws, 
 enum : int { kNone = 0, kFound = 1, kOverflowHit = 2 };
 
 uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
+uint32_t g_enum_tail_swap = 4;  // WarpShared::tail_swap of ENUMERATION launches
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
@@ -303,10 +339,6 @@ __device__ bool count_store(WarpMemo& m, uint32_t nb, uint32_t step, const WarpS
 }
 
 // ---- neighbour scans ------------------------------------------------------
-template <class W>
-__device__ __forceinline__ bool role_of(const DevState<W>& st, uint32_t v, uint32_t role) {
-  return (Pack<W>::cand(st.vs[v]) >> role) & 1;
-}
 
 // Index of `target` in the strictly increasing list adj[lo, hi), or ~0
 // (warp-cooperative 32-way search).
@@ -485,11 +517,62 @@ __device__ bool next_check(const DevGraph& g, const DevState<W>& st, WarpShared&
 // chunk of 32 candidates is finished in one pass instead of 32 descents.
 // NLCC (exact programs only): kFound with the first passing candidate in
 // CSR order.  ENUMERATION: adds the passing candidates to *leaves.
+// ENUMERATION tail from the source's side (symmetric graphs, source cached
+// and filtered to the tail role): the candidates are the cached source
+// entries x, kept when x is in the bound vertex's list [b2, e2) with that
+// entry active, differs from the history vertices the step compares, and
+// passes the other CHECKs.  This is the set the forward scan counts: x in
+// the source's list is the source CHECK, x in [b2, e2) active and holding
+// the role is the scan's entry test.
+template <class W>
+__device__ void tail_from_source(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, uint64_t b2,
+                                 uint64_t e2, unsigned long long* leaves) {
+  const unsigned lane = lane_id();
+  const int n_steps = ws.prog->n_steps;
+  unsigned long long found = 0;
+  for (uint32_t i0 = 0; i0 < ws.src_n; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    bool ok = i < ws.src_n;
+    uint32_t x = 0;
+    if (ok) x = ws.src_adj[i];
+    for (int h = 0; ok && h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
+      if (ws.f.bound[ws.prog->hist_step[h]] == x) ok = false;
+    if (ok) {
+      const uint64_t idx = lane_find_sorted(g.adj, b2, e2, x);
+      ok = idx != ~uint64_t(0) && edge_active(st.eact, idx);
+    }
+    for (int j = ws.prog->tail_from; ok && j < n_steps; ++j) {
+      const int hs = ws.prog->hist_step[ws.prog->steps[j].hist];
+      if (hs == 0) continue;
+      const uint32_t t = ws.f.bound[hs];
+      ok = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], x) != ~uint64_t(0);
+    }
+    found += __popc(__ballot_sync(kFull, ok));
+  }
+  __syncwarp();
+  if (lane == 0) {
+    ws.f.next[d] = e2;
+    ws.scanned += ws.src_n;
+  }
+  __syncwarp();
+  *leaves += found;
+}
+
 template <class W, bool kEnum>
 __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
                            uint32_t* out, unsigned long long* leaves) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog->n_steps;
+  if constexpr (kEnum) {
+    // tail_swap is set only where the swap applies (see k_enumerate).
+    if (ws.tail_swap && ws.src_cached) {
+      const uint64_t b2 = ws.f.next[d], e2 = ws.f.end[d];
+      if (static_cast<uint64_t>((ws.src_n + 31) >> 5) * ws.tail_swap <= (e2 - b2 + 31) >> 5) {
+        tail_from_source(g, st, ws, d, b2, e2, leaves);
+        return kNone;
+      }
+    }
+  }
   while (true) {
     const uint64_t next = ws.f.next[d], end = ws.f.end[d];
     if (next >= end) return kNone;
@@ -515,7 +598,7 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
         // edge was ever removed: the check is adjacency, searched in the
         // bound vertex's list, which every lane shares (for the source, in
         // its shared-memory copy when it has one).
-        if (hs == 0 && ws.src_n) {
+        if (hs == 0 && ws.src_cached) {
           uint32_t lo = 0, hi = ws.src_n;
           while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
@@ -623,7 +706,9 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
       int r;
       while (true) {
         r = next_vertex<W, kEnum>(g, st, ws, m, d, s, cur, source, &nb);
-        if (r != kFound || !count_memo || d + 1 >= n_steps) break;
+        // First hop on a sorted graph: each vertex comes once per item, so
+        // its subtree count is never looked up again.
+        if (r != kFound || !count_memo || d + 1 >= n_steps || (d == 1 && g.sorted_unique)) break;
         // Count memo: a cached subtree adds its count instead of a descent.
         unsigned long long c = 0;
         __syncwarp();
@@ -638,7 +723,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
         if (lane == 0) {
           ws.f.bound[d] = nb;
           ws.f.cur[d + 1] = nb;
-          if (count_memo && d + 1 < n_steps) {
+          if (count_memo && d + 1 < n_steps && !(d == 1 && g.sorted_unique)) {
             ws.f.leaves0[d] = *leaves;
             ws.f.child[d] = 1;
           }
@@ -742,6 +827,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
+    ws.src_cached = 0;
+    ws.tail_swap = 0;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(w.frame_steps), w.frame_steps);
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
@@ -789,7 +876,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
       continue;
     }
     next_epoch(m);
-    cache_source(g, ws, s_src[wib], v);
+    cache_source(g, st, ws, s_src[wib], v, -1);
     unsigned long long unused = 0;
     const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline, lo, hi);
     if (lane == 0) {
@@ -921,7 +1008,7 @@ template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate(
     DevGraph g, DevState<W> st, const WalkProgram* __restrict__ prog, uint32_t frame_steps,
     const uint32_t* __restrict__ wl, uint32_t n_wl, const uint4* __restrict__ items, uint32_t n_items,
-    uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns) {
+    uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns, uint32_t tail_swap) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
@@ -934,6 +1021,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
+    ws.src_cached = 0;
+    ws.tail_swap = 0;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(frame_steps), frame_steps);
   __syncwarp();
@@ -950,6 +1039,26 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
   deadline = __shfl_sync(kFull, deadline, 0);
   const uint64_t n = items ? n_items : n_wl;
   unsigned long long leaves = 0;
+  // The source cache serves only the tail CHECKs, whose candidates hold the
+  // tail step's role: keep just those entries.  The tail may start from the
+  // source's side when the graph is symmetric, the tail step is at depth 2
+  // or more, some closing CHECK is against the source and none against the
+  // tail vertex itself.
+  const int tail_d = static_cast<int>(s_prog.tail_from) - 1;
+  const int filter_role = (tail_d >= 1 && tail_d < s_prog.n_steps && s_prog.steps[tail_d].kind == kStepVertex)
+                              ? static_cast<int>(s_prog.steps[tail_d].role)
+                              : -1;
+  if (lane == 0) {
+    bool src_check = false, self_check = false;
+    for (int j = s_prog.tail_from; j < s_prog.n_steps; ++j) {
+      const int hs = s_prog.hist_step[s_prog.steps[j].hist];
+      src_check |= hs == 0;
+      self_check |= hs == tail_d;
+    }
+    const bool swap_ok = filter_role >= 0 && g.symmetric && tail_d >= 2 && src_check && !self_check;
+    ws.tail_swap = swap_ok ? tail_swap : 0u;
+  }
+  __syncwarp();
   while (true) {
     unsigned long long gi = 0;
     if (lane == 0) gi = atomicAdd(&ctr->items, 1ull);
@@ -958,7 +1067,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     const uint4 it = items ? items[gi] : make_uint4(static_cast<uint32_t>(gi), 0u, 0xFFFFFFFFu, 0u);
     const uint32_t source = wl[it.x];
     next_epoch(m);
-    cache_source(g, ws, s_src[wib], source);
+    cache_source(g, st, ws, s_src[wib], source, filter_role);
     const unsigned long long before = leaves;
     const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z);
     if (res == kItemTimeout) {
@@ -1010,6 +1119,8 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 }  // namespace
 
 void set_walk_budget_ns(uint64_t ns) { g_walk_budget_ns = ns ? ns : 1; }
+void set_enum_tail_swap(uint32_t ratio) { g_enum_tail_swap = ratio; }
+uint32_t enum_tail_swap() { return g_enum_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
 
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {
@@ -1065,7 +1176,7 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
   const size_t dyn = kWalkWarps * frame_bytes(frame_steps);
   PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
                                     g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
-                                    q.ctr, g_walk_budget_ns));
+                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap));
 }
 
 }  // namespace pmgb
@@ -1151,6 +1262,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
     ws.scanned = 0;
     ws.descents = 0;
     ws.src_n = 0;
+    ws.src_cached = 0;
+    ws.tail_swap = 0;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(prog.n_steps + 1u), prog.n_steps + 1u);
   __syncthreads();

@@ -190,8 +190,15 @@ KNOB_SETTINGS = {
     "no_slicing": {"walk_presplit": 0, "enum_presplit": (0, 0), "walk_tables": 1024, "enum_tables": 1024},
     "split_on_overflow_only": {"walk_presplit": 0, "enum_presplit": (0, 0), "walk_tables": 2048,
                                "enum_tables": 1024, "enum_split": (2, 0)},
+    # ENUMERATION tail from the source's side whenever the source is cached,
+    # and never.
+    "tail_swap_always": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                         "tail_swap": 1},
+    "tail_swap_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                      "tail_swap": 0},
 }
-KNOB_CASES = ["scale12_tds", "cycle5_s10", "path4_rep_s9", "two_cycles_zipf_s10", "random_08", "k4_rep_s8"]
+KNOB_CASES = ["scale12_tds", "cycle5_s10", "path4_rep_s9", "two_cycles_zipf_s10", "random_08", "k4_rep_s8",
+              "c1_scale10_cycle4"]
 
 
 def _set_knobs(k):
@@ -200,6 +207,7 @@ def _set_knobs(k):
     pm.lib.pm_set_walk_table_entries(k["walk_tables"])
     pm.lib.pm_set_enum_table_entries(k["enum_tables"])
     pm.lib.pm_set_enum_split(*k.get("enum_split", (16, 0)))
+    pm.lib.pm_set_enum_tail_swap(k.get("tail_swap", 4))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
