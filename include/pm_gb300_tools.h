@@ -86,7 +86,7 @@ typedef struct pm_tune_result {
   uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
-  uint32_t enum_tail_swap;
+  uint32_t enum_tail_swap, walk_tail_swap;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -131,6 +131,14 @@ pm_status_t pm_set_lcc_graph(int32_t enabled);
  * set (enumeration_cpu.tpp:96-104 semantics).  0 = never; default 4.
  * Process-wide; speed only.  No counterpart in the reference. */
 pm_status_t pm_set_enum_tail_swap(uint32_t ratio);
+
+/* The same choice for the last VERTEX step of exact CC/PC/TDS programs
+ * (no memo test can block them): from the source's side, the step's first
+ * passing candidate is still the smallest vertex id the forward scan would
+ * find first, so results and alreadyMatched marks are unchanged.  0 =
+ * never; default 4.  Process-wide; speed only.  No counterpart in the
+ * reference. */
+pm_status_t pm_set_walk_tail_swap(uint32_t ratio);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

@@ -112,6 +112,20 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     set_walk_table_entries(pick_t);
     out.walk_presplit = pick;
     out.walk_table_entries = pick_t;
+    const uint32_t ratios[] = {0, 2, 4, 8};
+    b = std::numeric_limits<double>::infinity();
+    uint32_t pick_r = walk_tail_swap();
+    for (uint32_t rt : ratios) {
+      set_walk_tail_swap(rt);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.walk_ms < b) {
+        b = r.walk_ms;
+        pick_r = rt;
+      }
+    }
+    set_walk_tail_swap(pick_r);
+    out.walk_tail_swap = pick_r;
   }
 
   // 3. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.

@@ -354,6 +354,11 @@ pm_status_t pm_set_enum_tail_swap(uint32_t ratio) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_walk_tail_swap(uint32_t ratio) {
+  set_walk_tail_swap(ratio);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -608,6 +613,7 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->enum_presplit_plain = r.enum_presplit_plain;
       result->enum_table_entries = r.enum_table_entries;
       result->enum_tail_swap = r.enum_tail_swap;
+      result->walk_tail_swap = r.walk_tail_swap;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

@@ -84,6 +84,9 @@ void set_walk_budget_ns(uint64_t ns);
 // source's entries holding the tail role (0: never).
 void set_enum_tail_swap(uint32_t ratio);
 uint32_t enum_tail_swap();
+// The same for the tail step of exact CC/PC/TDS programs (WalkLaunch::tail_swap).
+void set_walk_tail_swap(uint32_t ratio);
+uint32_t walk_tail_swap();
 uint64_t walk_budget_ns();
 
 // Per-warp scratch for the walkers' memo tables.  The edge and hypothesis
@@ -125,6 +128,7 @@ struct WalkLaunch {
   uint32_t n_slices;
   uint32_t* prio;
   uint32_t frame_steps;  // frame stack entries per warp: longest program's n_steps + 1
+  uint32_t tail_swap;    // exact programs: tail from the source's side (walk_tail_swap())
 };
 
 // Walker launch geometry: resident blocks per SM the kernels are built for,

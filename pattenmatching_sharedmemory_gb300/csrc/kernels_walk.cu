@@ -139,8 +139,28 @@ __device__ __forceinline__ void cache_source(const DevGraph& g, const DevState<W
 
 enum : int { kNone = 0, kFound = 1, kOverflowHit = 2 };
 
+// Role that the source cache keeps for program p (the tail VERTEX step's
+// role; -1: keep the whole list), and whether p's tail may start from the
+// source's side: symmetric graph, tail step at depth 2 or more, some closing
+// CHECK against the source and none against the tail vertex itself.
+__device__ __forceinline__ int tail_plan(const DevGraph& g, const WalkProgram& p, bool* swap_ok) {
+  const int tail_d = static_cast<int>(p.tail_from) - 1;
+  const int role =
+      (tail_d >= 1 && tail_d < p.n_steps && p.steps[tail_d].kind == kStepVertex) ? static_cast<int>(p.steps[tail_d].role)
+                                                                                  : -1;
+  bool src_check = false, self_check = false;
+  for (int j = p.tail_from; j < p.n_steps; ++j) {
+    const int hs = p.hist_step[p.steps[j].hist];
+    src_check |= hs == 0;
+    self_check |= hs == tail_d;
+  }
+  *swap_ok = role >= 0 && g.symmetric && tail_d >= 2 && src_check && !self_check;
+  return role;
+}
+
 uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
 uint32_t g_enum_tail_swap = 4;  // WarpShared::tail_swap of ENUMERATION launches
+uint32_t g_walk_tail_swap = 4;  // ... of CC/PC/TDS launches (exact programs)
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
@@ -517,26 +537,30 @@ __device__ bool next_check(const DevGraph& g, const DevState<W>& st, WarpShared&
 // chunk of 32 candidates is finished in one pass instead of 32 descents.
 // NLCC (exact programs only): kFound with the first passing candidate in
 // CSR order.  ENUMERATION: adds the passing candidates to *leaves.
-// ENUMERATION tail from the source's side (symmetric graphs, source cached
-// and filtered to the tail role): the candidates are the cached source
-// entries x, kept when x is in the bound vertex's list [b2, e2) with that
-// entry active, differs from the history vertices the step compares, and
-// passes the other CHECKs.  This is the set the forward scan counts: x in
-// the source's list is the source CHECK, x in [b2, e2) active and holding
-// the role is the scan's entry test.
-template <class W>
-__device__ void tail_from_source(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, uint64_t b2,
-                                 uint64_t e2, unsigned long long* leaves) {
+// Tail step from the source's side (symmetric graphs, source cached and
+// filtered to the tail role): the candidates are the cached source entries
+// x, kept when x is in the bound vertex's list [b2, e2) with that entry
+// active, (ENUMERATION) differs from the history vertices the step compares,
+// and passes the other CHECKs.  This is the set the forward scan accepts: x
+// in the source's list is the source CHECK, x in [b2, e2) active and holding
+// the role is the scan's entry test.  ENUMERATION adds the set's size to
+// *leaves; NLCC returns its smallest vertex, which is the forward scan's
+// first hit (both lists are sorted by vertex id).
+template <class W, bool kEnum>
+__device__ int tail_from_source(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, uint64_t b2,
+                                uint64_t e2, uint32_t* out, unsigned long long* leaves) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog->n_steps;
   unsigned long long found = 0;
+  int res = kNone;
   for (uint32_t i0 = 0; i0 < ws.src_n; i0 += 32) {
     const uint32_t i = i0 + lane;
     bool ok = i < ws.src_n;
     uint32_t x = 0;
     if (ok) x = ws.src_adj[i];
-    for (int h = 0; ok && h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
-      if (ws.f.bound[ws.prog->hist_step[h]] == x) ok = false;
+    if (kEnum)
+      for (int h = 0; ok && h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
+        if (ws.f.bound[ws.prog->hist_step[h]] == x) ok = false;
     if (ok) {
       const uint64_t idx = lane_find_sorted(g.adj, b2, e2, x);
       ok = idx != ~uint64_t(0) && edge_active(st.eact, idx);
@@ -547,7 +571,14 @@ __device__ void tail_from_source(const DevGraph& g, const DevState<W>& st, WarpS
       const uint32_t t = ws.f.bound[hs];
       ok = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], x) != ~uint64_t(0);
     }
-    found += __popc(__ballot_sync(kFull, ok));
+    const unsigned mask = __ballot_sync(kFull, ok);
+    if (kEnum) {
+      found += __popc(mask);
+    } else if (mask) {
+      *out = __shfl_sync(kFull, x, __ffs(mask) - 1);
+      res = kFound;
+      break;
+    }
   }
   __syncwarp();
   if (lane == 0) {
@@ -555,7 +586,8 @@ __device__ void tail_from_source(const DevGraph& g, const DevState<W>& st, WarpS
     ws.scanned += ws.src_n;
   }
   __syncwarp();
-  *leaves += found;
+  if (kEnum) *leaves += found;
+  return res;
 }
 
 template <class W, bool kEnum>
@@ -563,15 +595,11 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
                            uint32_t* out, unsigned long long* leaves) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog->n_steps;
-  if constexpr (kEnum) {
-    // tail_swap is set only where the swap applies (see k_enumerate).
-    if (ws.tail_swap && ws.src_cached) {
-      const uint64_t b2 = ws.f.next[d], e2 = ws.f.end[d];
-      if (static_cast<uint64_t>((ws.src_n + 31) >> 5) * ws.tail_swap <= (e2 - b2 + 31) >> 5) {
-        tail_from_source(g, st, ws, d, b2, e2, leaves);
-        return kNone;
-      }
-    }
+  // tail_swap is set only where the swap applies (see k_enumerate, k_walk).
+  if (ws.tail_swap && ws.src_cached) {
+    const uint64_t b2 = ws.f.next[d], e2 = ws.f.end[d];
+    if (static_cast<uint64_t>((ws.src_n + 31) >> 5) * ws.tail_swap <= (e2 - b2 + 31) >> 5)
+      return tail_from_source<W, kEnum>(g, st, ws, d, b2, e2, out, leaves);
   }
   while (true) {
     const uint64_t next = ws.f.next[d], end = ws.f.end[d];
@@ -838,7 +866,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
   WarpMemo m = warp_memo(sc, gw);
   const uint64_t n_items =
       w.slices ? w.n_slices : w.retry_items ? w.n_retry : static_cast<uint64_t>(w.n_wl) * w.n_progs;
-  int cached = -1;
+  int cached = -1, filter_role = -1;
   unsigned long long overflow = 0;
   while (true) {
     unsigned long long gi = 0;
@@ -870,13 +898,21 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
     if (static_cast<int>(r) != cached) {
       load_program(ws, w.progs + r);
       cached = static_cast<int>(r);
+      // Exact programs run the tail step on sorted lists (run_walk): cache
+      // only the tail role's source entries and allow the swapped tail.
+      bool swap_ok = false;
+      const int role = tail_plan(g, *ws.prog, &swap_ok);
+      filter_role = ws.prog->exact ? role : -1;
+      __syncwarp();
+      if (lane == 0) ws.tail_swap = (ws.prog->exact && swap_ok) ? w.tail_swap : 0u;
+      __syncwarp();
     }
     if (!role_of(st, v, ws.prog->start_role)) {
       if (lane == 0 && !w.slices) w.status[item] = kItemSkip;
       continue;
     }
     next_epoch(m);
-    cache_source(g, st, ws, s_src[wib], v, -1);
+    cache_source(g, st, ws, s_src[wib], v, filter_role);
     unsigned long long unused = 0;
     const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline, lo, hi);
     if (lane == 0) {
@@ -1044,20 +1080,9 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
   // source's side when the graph is symmetric, the tail step is at depth 2
   // or more, some closing CHECK is against the source and none against the
   // tail vertex itself.
-  const int tail_d = static_cast<int>(s_prog.tail_from) - 1;
-  const int filter_role = (tail_d >= 1 && tail_d < s_prog.n_steps && s_prog.steps[tail_d].kind == kStepVertex)
-                              ? static_cast<int>(s_prog.steps[tail_d].role)
-                              : -1;
-  if (lane == 0) {
-    bool src_check = false, self_check = false;
-    for (int j = s_prog.tail_from; j < s_prog.n_steps; ++j) {
-      const int hs = s_prog.hist_step[s_prog.steps[j].hist];
-      src_check |= hs == 0;
-      self_check |= hs == tail_d;
-    }
-    const bool swap_ok = filter_role >= 0 && g.symmetric && tail_d >= 2 && src_check && !self_check;
-    ws.tail_swap = swap_ok ? tail_swap : 0u;
-  }
+  bool swap_ok = false;
+  const int filter_role = tail_plan(g, s_prog, &swap_ok);
+  if (lane == 0) ws.tail_swap = swap_ok ? tail_swap : 0u;
   __syncwarp();
   while (true) {
     unsigned long long gi = 0;
@@ -1121,6 +1146,8 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 void set_walk_budget_ns(uint64_t ns) { g_walk_budget_ns = ns ? ns : 1; }
 void set_enum_tail_swap(uint32_t ratio) { g_enum_tail_swap = ratio; }
 uint32_t enum_tail_swap() { return g_enum_tail_swap; }
+void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
+uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
 
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {

@@ -193,9 +193,13 @@ KNOB_SETTINGS = {
     # ENUMERATION tail from the source's side whenever the source is cached,
     # and never.
     "tail_swap_always": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
-                         "tail_swap": 1},
+                         "tail_swap": 1, "walk_tail_swap": 1},
     "tail_swap_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
-                      "tail_swap": 0},
+                      "tail_swap": 0, "walk_tail_swap": 0},
+    # Exact CC/PC/TDS slices (first-hop slices of every item) with the
+    # swapped tail on every cached source.
+    "walk_slices_tail_swap": {"walk_presplit": 1, "enum_presplit": (32, 8), "walk_tables": 8192,
+                              "enum_tables": 8192, "walk_tail_swap": 1},
 }
 KNOB_CASES = ["scale12_tds", "cycle5_s10", "path4_rep_s9", "two_cycles_zipf_s10", "random_08", "k4_rep_s8",
               "c1_scale10_cycle4"]
@@ -208,6 +212,7 @@ def _set_knobs(k):
     pm.lib.pm_set_enum_table_entries(k["enum_tables"])
     pm.lib.pm_set_enum_split(*k.get("enum_split", (16, 0)))
     pm.lib.pm_set_enum_tail_swap(k.get("tail_swap", 4))
+    pm.lib.pm_set_walk_tail_swap(k.get("walk_tail_swap", 4))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,

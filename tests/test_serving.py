@@ -172,6 +172,7 @@ def test_autotune_keeps_results():
     assert chosen["probes_memo"] + chosen["probes_plain"] >= 1
     assert chosen["seg_entries"] in (512, 1024)
     assert chosen["enum_tail_swap"] in (0, 2, 4, 8)
+    assert chosen["walk_tail_swap"] in (0, 2, 4, 8)
     after = [_alone(g, p)[1] for p in patterns]
     assert after == before
     # Leave the defaults for the tests that follow.
@@ -180,4 +181,5 @@ def test_autotune_keeps_results():
     pm.lib.pm_set_walk_presplit(64)
     pm.lib.pm_set_walk_table_entries(8192)
     pm.lib.pm_set_enum_tail_swap(4)
+    pm.lib.pm_set_walk_tail_swap(4)
     g.set_hub_plan(32, 1024)
