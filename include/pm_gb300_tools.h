@@ -86,7 +86,7 @@ typedef struct pm_tune_result {
   uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
-  uint32_t enum_tail_swap, walk_tail_swap;
+  uint32_t enum_tail_swap, walk_tail_swap, enum_count_memo;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -139,6 +139,13 @@ pm_status_t pm_set_enum_tail_swap(uint32_t ratio);
  * never; default 4.  Process-wide; speed only.  No counterpart in the
  * reference. */
 pm_status_t pm_set_walk_tail_swap(uint32_t ratio);
+
+/* ENUMERATION of templates with distinct labels keeps, per source, a table of
+ * subtree counts (a vertex reached again at the same step with the same
+ * history adds the cached count instead of walking again).  enabled = 0
+ * walks every subtree.  Counts are the same either way; default 1.
+ * Process-wide; speed only.  No counterpart in the reference. */
+pm_status_t pm_set_enum_count_memo(int32_t enabled);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

@@ -168,7 +168,24 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     out.enum_tail_swap = pick;
   }
 
-  // 5. Count-memo entries per warp, on every probe.
+  // 5. Count memo on or off, on the probes that can use it.
+  if (!memo.empty()) {
+    double b = std::numeric_limits<double>::infinity();
+    bool pick = enum_count_memo();
+    for (bool on : {true, false}) {
+      set_enum_count_memo(on);
+      const ProbeRun r = run_probes(g, memo);
+      check(r, memo);
+      if (r.enum_ms < b) {
+        b = r.enum_ms;
+        pick = on;
+      }
+    }
+    set_enum_count_memo(pick);
+  }
+  out.enum_count_memo = enum_count_memo() ? 1 : 0;
+
+  // 6. Count-memo entries per warp, on every probe.
   const uint32_t tables[] = {4096, 8192, 16384};
   double bt = std::numeric_limits<double>::infinity();
   uint32_t pick_t = enum_table_entries();

@@ -359,6 +359,11 @@ pm_status_t pm_set_walk_tail_swap(uint32_t ratio) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_enum_count_memo(int32_t enabled) {
+  set_enum_count_memo(enabled != 0);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -614,6 +619,7 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->enum_table_entries = r.enum_table_entries;
       result->enum_tail_swap = r.enum_tail_swap;
       result->walk_tail_swap = r.walk_tail_swap;
+      result->enum_count_memo = r.enum_count_memo;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

@@ -84,6 +84,9 @@ void set_walk_budget_ns(uint64_t ns);
 // source's entries holding the tail role (0: never).
 void set_enum_tail_swap(uint32_t ratio);
 uint32_t enum_tail_swap();
+// ENUMERATION programs that allow a count memo use it (default on).
+void set_enum_count_memo(bool on);
+bool enum_count_memo();
 // The same for the tail step of exact CC/PC/TDS programs (WalkLaunch::tail_swap).
 void set_walk_tail_swap(uint32_t ratio);
 uint32_t walk_tail_swap();

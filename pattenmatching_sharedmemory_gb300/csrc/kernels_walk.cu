@@ -66,6 +66,8 @@ struct WarpShared {
   // instead of the bound vertex's list when that list has at least
   // tail_swap times as many 32-entry chunks (0: never).
   uint32_t tail_swap;
+  // ENUMERATION: programs that allow a count memo use it (0: never).
+  uint32_t memo_on;
 };
 
 // Source adjacency entries a warp caches in shared memory per walk.
@@ -161,6 +163,7 @@ __device__ __forceinline__ int tail_plan(const DevGraph& g, const WalkProgram& p
 uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
 uint32_t g_enum_tail_swap = 4;  // WarpShared::tail_swap of ENUMERATION launches
 uint32_t g_walk_tail_swap = 4;  // ... of CC/PC/TDS launches (exact programs)
+uint32_t g_enum_count_memo = 1;  // WarpShared::memo_on of ENUMERATION launches
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
@@ -673,7 +676,7 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
                             uint32_t first_hi = 0xFFFFFFFFu) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog->n_steps;
-  const bool count_memo = kEnum && ws.prog->count_memo;
+  const bool count_memo = kEnum && ws.prog->count_memo && ws.memo_on;
   uint32_t iters = 0;
   __syncwarp();
   if (lane == 0) {
@@ -857,6 +860,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.memo_on = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(w.frame_steps), w.frame_steps);
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
@@ -1044,7 +1048,8 @@ template <class W>
 __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate(
     DevGraph g, DevState<W> st, const WalkProgram* __restrict__ prog, uint32_t frame_steps,
     const uint32_t* __restrict__ wl, uint32_t n_wl, const uint4* __restrict__ items, uint32_t n_items,
-    uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns, uint32_t tail_swap) {
+    uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns, uint32_t tail_swap,
+    uint32_t count_memo) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
@@ -1059,6 +1064,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.memo_on = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(frame_steps), frame_steps);
   __syncwarp();
@@ -1082,7 +1088,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
   // tail vertex itself.
   bool swap_ok = false;
   const int filter_role = tail_plan(g, s_prog, &swap_ok);
-  if (lane == 0) ws.tail_swap = swap_ok ? tail_swap : 0u;
+  if (lane == 0) {
+    ws.tail_swap = swap_ok ? tail_swap : 0u;
+    ws.memo_on = count_memo;
+  }
   __syncwarp();
   while (true) {
     unsigned long long gi = 0;
@@ -1146,6 +1155,8 @@ DevState<W> state_of(const QueryDevPtrs& q) {
 void set_walk_budget_ns(uint64_t ns) { g_walk_budget_ns = ns ? ns : 1; }
 void set_enum_tail_swap(uint32_t ratio) { g_enum_tail_swap = ratio; }
 uint32_t enum_tail_swap() { return g_enum_tail_swap; }
+void set_enum_count_memo(bool on) { g_enum_count_memo = on ? 1u : 0u; }
+bool enum_count_memo() { return g_enum_count_memo != 0; }
 void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
 uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
@@ -1203,7 +1214,7 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
   const size_t dyn = kWalkWarps * frame_bytes(frame_steps);
   PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
                                     g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
-                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap));
+                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap, g_enum_count_memo));
 }
 
 }  // namespace pmgb
@@ -1291,6 +1302,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.memo_on = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(prog.n_steps + 1u), prog.n_steps + 1u);
   __syncthreads();

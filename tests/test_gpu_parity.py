@@ -196,6 +196,9 @@ KNOB_SETTINGS = {
                          "tail_swap": 1, "walk_tail_swap": 1},
     "tail_swap_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                       "tail_swap": 0, "walk_tail_swap": 0},
+    # ENUMERATION without the count memo (every subtree walked).
+    "count_memo_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                       "count_memo": 0},
     # Exact CC/PC/TDS slices (first-hop slices of every item) with the
     # swapped tail on every cached source.
     "walk_slices_tail_swap": {"walk_presplit": 1, "enum_presplit": (32, 8), "walk_tables": 8192,
@@ -213,6 +216,7 @@ def _set_knobs(k):
     pm.lib.pm_set_enum_split(*k.get("enum_split", (16, 0)))
     pm.lib.pm_set_enum_tail_swap(k.get("tail_swap", 4))
     pm.lib.pm_set_walk_tail_swap(k.get("walk_tail_swap", 4))
+    pm.lib.pm_set_enum_count_memo(k.get("count_memo", 1))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
