@@ -86,7 +86,7 @@ typedef struct pm_tune_result {
   uint32_t enum_presplit_memo, enum_presplit_plain, enum_table_entries;
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
-  uint32_t enum_tail_swap, walk_tail_swap, enum_count_memo;
+  uint32_t enum_tail_swap, walk_tail_swap, enum_count_memo, walk_tail_state_memo;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -146,6 +146,14 @@ pm_status_t pm_set_walk_tail_swap(uint32_t ratio);
  * walks every subtree.  Counts are the same either way; default 1.
  * Process-wide; speed only.  No counterpart in the reference. */
 pm_status_t pm_set_enum_count_memo(int32_t enabled);
+
+/* Exact CC/PC/TDS programs keep a per-walk state memo (a state that failed
+ * once fails again, since a success ends the walk).  enabled = 0 leaves it
+ * out at the step just before the closing CHECKs, where repeating the tail
+ * step can cost less than a memo probe and insert.  Results are the same
+ * either way; default 1.  Process-wide; speed only.  No counterpart in the
+ * reference. */
+pm_status_t pm_set_walk_tail_state_memo(int32_t enabled);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

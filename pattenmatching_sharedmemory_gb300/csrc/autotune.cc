@@ -126,6 +126,19 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     }
     set_walk_tail_swap(pick_r);
     out.walk_tail_swap = pick_r;
+    b = std::numeric_limits<double>::infinity();
+    bool pick_m = walk_tail_state_memo();
+    for (bool on : {true, false}) {
+      set_walk_tail_state_memo(on);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.walk_ms < b) {
+        b = r.walk_ms;
+        pick_m = on;
+      }
+    }
+    set_walk_tail_state_memo(pick_m);
+    out.walk_tail_state_memo = pick_m ? 1 : 0;
   }
 
   // 3. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.

@@ -364,6 +364,11 @@ pm_status_t pm_set_enum_count_memo(int32_t enabled) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_walk_tail_state_memo(int32_t enabled) {
+  set_walk_tail_state_memo(enabled != 0);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -620,6 +625,7 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->enum_tail_swap = r.enum_tail_swap;
       result->walk_tail_swap = r.walk_tail_swap;
       result->enum_count_memo = r.enum_count_memo;
+      result->walk_tail_state_memo = r.walk_tail_state_memo;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

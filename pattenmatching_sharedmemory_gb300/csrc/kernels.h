@@ -87,6 +87,10 @@ uint32_t enum_tail_swap();
 // ENUMERATION programs that allow a count memo use it (default on).
 void set_enum_count_memo(bool on);
 bool enum_count_memo();
+// Exact CC/PC/TDS programs use the state memo at the step before the tail
+// (default on; off re-runs the tail step for a repeated state).
+void set_walk_tail_state_memo(bool on);
+bool walk_tail_state_memo();
 // The same for the tail step of exact CC/PC/TDS programs (WalkLaunch::tail_swap).
 void set_walk_tail_swap(uint32_t ratio);
 uint32_t walk_tail_swap();
@@ -132,6 +136,7 @@ struct WalkLaunch {
   uint32_t* prio;
   uint32_t frame_steps;  // frame stack entries per warp: longest program's n_steps + 1
   uint32_t tail_swap;    // exact programs: tail from the source's side (walk_tail_swap())
+  uint32_t tail_state_memo;  // exact programs: state memo at the step before the tail
 };
 
 // Walker launch geometry: resident blocks per SM the kernels are built for,

@@ -68,6 +68,9 @@ struct WarpShared {
   uint32_t tail_swap;
   // ENUMERATION: programs that allow a count memo use it (0: never).
   uint32_t memo_on;
+  // Exact CC/PC/TDS programs: the step before the tail records and tests
+  // states in the state memo (0: it re-runs the tail step instead).
+  uint32_t tail_state_memo;
 };
 
 // Source adjacency entries a warp caches in shared memory per walk.
@@ -164,6 +167,7 @@ uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
 uint32_t g_enum_tail_swap = 4;  // WarpShared::tail_swap of ENUMERATION launches
 uint32_t g_walk_tail_swap = 4;  // ... of CC/PC/TDS launches (exact programs)
 uint32_t g_enum_count_memo = 1;  // WarpShared::memo_on of ENUMERATION launches
+uint32_t g_walk_tail_state_memo = 1;  // WalkLaunch::tail_state_memo
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
@@ -475,9 +479,13 @@ __device__ int next_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
         }
         if (s.record && !edge_memo_insert(m, a, b, static_cast<uint32_t>(d))) return kOverflowHit;
       }
-      const int sr = state_seen(m, nb, static_cast<uint32_t>(d), ws, d);
-      if (sr == kFound) continue;
-      if (sr == kOverflowHit) return kOverflowHit;
+      // Exact programs fail a state the same way every time (a success ends
+      // the walk), so skipping the memo only repeats the work.
+      if (ws.tail_state_memo || !ws.prog->exact || d + 1 != ws.prog->tail_from) {
+        const int sr = state_seen(m, nb, static_cast<uint32_t>(d), ws, d);
+        if (sr == kFound) continue;
+        if (sr == kOverflowHit) return kOverflowHit;
+      }
     }
     *out = nb;
     return kFound;
@@ -861,6 +869,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
     ws.src_cached = 0;
     ws.tail_swap = 0;
     ws.memo_on = 1;
+    ws.tail_state_memo = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(w.frame_steps), w.frame_steps);
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
@@ -908,7 +917,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
       const int role = tail_plan(g, *ws.prog, &swap_ok);
       filter_role = ws.prog->exact ? role : -1;
       __syncwarp();
-      if (lane == 0) ws.tail_swap = (ws.prog->exact && swap_ok) ? w.tail_swap : 0u;
+      if (lane == 0) {
+        ws.tail_swap = (ws.prog->exact && swap_ok) ? w.tail_swap : 0u;
+        ws.tail_state_memo = w.tail_state_memo;
+      }
       __syncwarp();
     }
     if (!role_of(st, v, ws.prog->start_role)) {
@@ -1065,6 +1077,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     ws.src_cached = 0;
     ws.tail_swap = 0;
     ws.memo_on = 1;
+    ws.tail_state_memo = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(frame_steps), frame_steps);
   __syncwarp();
@@ -1157,6 +1170,8 @@ void set_enum_tail_swap(uint32_t ratio) { g_enum_tail_swap = ratio; }
 uint32_t enum_tail_swap() { return g_enum_tail_swap; }
 void set_enum_count_memo(bool on) { g_enum_count_memo = on ? 1u : 0u; }
 bool enum_count_memo() { return g_enum_count_memo != 0; }
+void set_walk_tail_state_memo(bool on) { g_walk_tail_state_memo = on ? 1u : 0u; }
+bool walk_tail_state_memo() { return g_walk_tail_state_memo != 0; }
 void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
 uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
@@ -1303,6 +1318,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
     ws.src_cached = 0;
     ws.tail_swap = 0;
     ws.memo_on = 1;
+    ws.tail_state_memo = 1;
   }
   bind_frames(ws, s_frames + wib * frame_bytes(prog.n_steps + 1u), prog.n_steps + 1u);
   __syncthreads();

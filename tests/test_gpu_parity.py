@@ -199,6 +199,12 @@ KNOB_SETTINGS = {
     # ENUMERATION without the count memo (every subtree walked).
     "count_memo_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                        "count_memo": 0},
+    # Exact CC/PC/TDS without the state memo before the tail, with and
+    # without the swapped tail.
+    "walk_tail_no_state_memo": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192,
+                                "enum_tables": 8192, "tail_state_memo": 0},
+    "walk_tail_no_state_memo_no_swap": {"walk_presplit": 0, "enum_presplit": (32, 8), "walk_tables": 8192,
+                                        "enum_tables": 8192, "tail_state_memo": 0, "walk_tail_swap": 0},
     # Exact CC/PC/TDS slices (first-hop slices of every item) with the
     # swapped tail on every cached source.
     "walk_slices_tail_swap": {"walk_presplit": 1, "enum_presplit": (32, 8), "walk_tables": 8192,
@@ -217,6 +223,7 @@ def _set_knobs(k):
     pm.lib.pm_set_enum_tail_swap(k.get("tail_swap", 4))
     pm.lib.pm_set_walk_tail_swap(k.get("walk_tail_swap", 4))
     pm.lib.pm_set_enum_count_memo(k.get("count_memo", 1))
+    pm.lib.pm_set_walk_tail_state_memo(k.get("tail_state_memo", 1))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
