@@ -87,6 +87,7 @@ typedef struct pm_tune_result {
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
   uint32_t enum_tail_swap, walk_tail_swap, enum_count_memo, walk_tail_state_memo;
+  uint32_t enum_pair_tail, walk_pair_tail;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -154,6 +155,16 @@ pm_status_t pm_set_enum_count_memo(int32_t enabled);
  * either way; default 1.  Process-wide; speed only.  No counterpart in the
  * reference. */
 pm_status_t pm_set_walk_tail_state_memo(int32_t enabled);
+
+/* The step just before such a tail (e.g. the third vertex of a 4-cycle):
+ * instead of binding each candidate and running the tail step below it, the
+ * warp tests every (candidate, cached source entry) pair, one pair per lane.
+ * ENUMERATION counts the passing pairs; an exact CC/PC/TDS walk takes the
+ * first passing pair in (candidate CSR order, entry ascending) order, its
+ * depth-first first success.  Results are the same either way.  Separate
+ * switches for ENUMERATION and for walks; default 1 / 1.  Process-wide; speed
+ * only.  No counterpart in the reference. */
+pm_status_t pm_set_pair_tail(int32_t enumeration, int32_t walks);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

@@ -139,6 +139,19 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     }
     set_walk_tail_state_memo(pick_m);
     out.walk_tail_state_memo = pick_m ? 1 : 0;
+    b = std::numeric_limits<double>::infinity();
+    bool pick_p = pair_tail_on(false);
+    for (bool on : {true, false}) {
+      set_pair_tail(false, on);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.walk_ms < b) {
+        b = r.walk_ms;
+        pick_p = on;
+      }
+    }
+    set_pair_tail(false, pick_p);
+    out.walk_pair_tail = pick_p ? 1 : 0;
   }
 
   // 3. ENUMERATION slices, per program kind, timed on the ENUMERATION steps.
@@ -197,6 +210,23 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     set_enum_count_memo(pick);
   }
   out.enum_count_memo = enum_count_memo() ? 1 : 0;
+
+  // ENUMERATION's pair-parallel step before the tail, on every probe.
+  {
+    double b = std::numeric_limits<double>::infinity();
+    bool pick = pair_tail_on(true);
+    for (bool on : {true, false}) {
+      set_pair_tail(true, on);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.enum_ms < b) {
+        b = r.enum_ms;
+        pick = on;
+      }
+    }
+    set_pair_tail(true, pick);
+    out.enum_pair_tail = pick ? 1 : 0;
+  }
 
   // 6. Count-memo entries per warp, on every probe.
   const uint32_t tables[] = {4096, 8192, 16384};

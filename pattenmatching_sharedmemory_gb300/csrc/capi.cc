@@ -369,6 +369,12 @@ pm_status_t pm_set_walk_tail_state_memo(int32_t enabled) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_pair_tail(int32_t enumeration, int32_t walks) {
+  set_pair_tail(true, enumeration != 0);
+  set_pair_tail(false, walks != 0);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -626,6 +632,8 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->walk_tail_swap = r.walk_tail_swap;
       result->enum_count_memo = r.enum_count_memo;
       result->walk_tail_state_memo = r.walk_tail_state_memo;
+      result->enum_pair_tail = r.enum_pair_tail;
+      result->walk_pair_tail = r.walk_pair_tail;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

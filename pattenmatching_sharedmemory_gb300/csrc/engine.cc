@@ -521,6 +521,7 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   for (const WalkProgram& pr : dc.cc.programs) w.frame_steps = std::max<uint32_t>(w.frame_steps, pr.n_steps + 1u);
   w.tail_swap = walk_tail_swap();
   w.tail_state_memo = walk_tail_state_memo() ? 1u : 0u;
+  w.pair_tail = pair_tail_on(false) ? 1u : 0u;
 
   // Exact programs may split heavy items into first-hop slices: an item
   // succeeds when any slice does (no alreadyMatched marks to keep).

@@ -91,6 +91,10 @@ bool enum_count_memo();
 // (default on; off re-runs the tail step for a repeated state).
 void set_walk_tail_state_memo(bool on);
 bool walk_tail_state_memo();
+// The step before a qualifying tail tests (candidate, cached source entry)
+// pairs one per lane (ENUMERATION, or exact CC/PC/TDS programs; default on).
+void set_pair_tail(bool enumeration, bool on);
+bool pair_tail_on(bool enumeration);
 // The same for the tail step of exact CC/PC/TDS programs (WalkLaunch::tail_swap).
 void set_walk_tail_swap(uint32_t ratio);
 uint32_t walk_tail_swap();
@@ -137,6 +141,7 @@ struct WalkLaunch {
   uint32_t frame_steps;  // frame stack entries per warp: longest program's n_steps + 1
   uint32_t tail_swap;    // exact programs: tail from the source's side (walk_tail_swap())
   uint32_t tail_state_memo;  // exact programs: state memo at the step before the tail
+  uint32_t pair_tail;        // exact programs: pair-parallel step before the tail
 };
 
 // Walker launch geometry: resident blocks per SM the kernels are built for,

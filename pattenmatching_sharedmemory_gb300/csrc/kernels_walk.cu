@@ -56,9 +56,10 @@ struct WarpShared {
   WalkFrames f;
   unsigned long long scanned;   // CSR entries tested by this warp (lane 0 writes)
   unsigned long long descents;  // hops taken by this warp
-  // Adjacency list of the walk's source, copied to shared memory when it has
-  // at most kSrcCache entries (src_cached); ENUMERATION keeps only the
-  // entries whose target holds the tail step's role (src_n of them).
+  // Adjacency list of the walk's source in shared memory (src_cached): the
+  // whole list when it has at most kSrcCache entries, or, for programs with
+  // a tail step, only the entries whose target holds the tail step's role
+  // when at most kSrcCache of them do (src_n entries).
   const uint32_t* src_adj;
   uint32_t src_n;
   uint32_t src_cached;
@@ -66,6 +67,9 @@ struct WarpShared {
   // instead of the bound vertex's list when that list has at least
   // tail_swap times as many 32-entry chunks (0: never).
   uint32_t tail_swap;
+  // The step before the tail tests (candidate, cached source entry) pairs
+  // one per lane instead of descending per candidate (0: never).
+  uint32_t pair_tail;
   // ENUMERATION: programs that allow a count memo use it (0: never).
   uint32_t memo_on;
   // Exact CC/PC/TDS programs: the step before the tail records and tests
@@ -73,8 +77,11 @@ struct WarpShared {
   uint32_t tail_state_memo;
 };
 
-// Source adjacency entries a warp caches in shared memory per walk.
+// Source adjacency entries a warp caches in shared memory per walk; a
+// filtered cache (one role's entries) scans source lists of up to
+// kSrcFilterScan entries.
 constexpr uint32_t kSrcCache = 256;
+constexpr uint32_t kSrcFilterScan = 4096;
 
 // Points the warp's frames at its part of the kernel's dynamic shared
 // memory (frame_bytes(steps) per warp).
@@ -111,25 +118,33 @@ __device__ __forceinline__ void cache_source(const DevGraph& g, const DevState<W
   uint32_t n = 0, cached = 0;
   if (g.symmetric) {
     const uint64_t b = g.off[source], e = g.off[source + 1];
-    if (e - b <= kSrcCache) {
-      cached = 1;
-      const uint32_t len = static_cast<uint32_t>(e - b);
-      if (filter_role < 0) {
-        n = len;
+    if (filter_role < 0) {
+      if (e - b <= kSrcCache) {
+        cached = 1;
+        n = static_cast<uint32_t>(e - b);
         for (uint32_t i = lane; i < n; i += 32) cache[i] = g.adj[b + i];
-      } else {
-        for (uint32_t i0 = 0; i0 < len; i0 += 32) {
-          const uint32_t i = i0 + lane;
-          uint32_t x = 0;
-          bool keep = false;
-          if (i < len) {
-            x = g.adj[b + i];
-            keep = role_of(st, x, static_cast<uint32_t>(filter_role));
-          }
-          const unsigned m = __ballot_sync(kFull, keep);
-          if (keep) cache[n + __popc(m & ((1u << lane) - 1u))] = x;
-          n += __popc(m);
+      }
+    } else if (e - b <= kSrcFilterScan) {
+      // Cached when the role's entries fit (n stays <= kSrcCache: a chunk
+      // is written only while the entries so far plus its own fit).
+      const uint32_t len = static_cast<uint32_t>(e - b);
+      cached = 1;
+      for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        uint32_t x = 0;
+        bool keep = false;
+        if (i < len) {
+          x = g.adj[b + i];
+          keep = role_of(st, x, static_cast<uint32_t>(filter_role));
         }
+        const unsigned m = __ballot_sync(kFull, keep);
+        if (n + __popc(m) > kSrcCache) {
+          cached = 0;
+          n = 0;
+          break;
+        }
+        if (keep) cache[n + __popc(m & ((1u << lane) - 1u))] = x;
+        n += __popc(m);
       }
     }
   }
@@ -167,6 +182,8 @@ uint64_t g_walk_budget_ns = 120ull * 1000000000ull;
 uint32_t g_enum_tail_swap = 4;  // WarpShared::tail_swap of ENUMERATION launches
 uint32_t g_walk_tail_swap = 4;  // ... of CC/PC/TDS launches (exact programs)
 uint32_t g_enum_count_memo = 1;  // WarpShared::memo_on of ENUMERATION launches
+uint32_t g_enum_pair_tail = 1;   // WarpShared::pair_tail of ENUMERATION launches
+uint32_t g_walk_pair_tail = 1;   // WalkLaunch::pair_tail
 uint32_t g_walk_tail_state_memo = 1;  // WalkLaunch::tail_state_memo
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
@@ -601,6 +618,110 @@ __device__ int tail_from_source(const DevGraph& g, const DevState<W>& st, WarpSh
   return res;
 }
 
+// Position of the n-th (0-based) set bit of m (n < popc(m)).
+__device__ __forceinline__ int nth_set_bit(unsigned m, unsigned n) {
+  for (unsigned k = 0; k < n; ++k) m &= m - 1;
+  return __ffs(m) - 1;
+}
+
+// Step d just before the tail step d + 1 (whose closing CHECKs include the
+// source and not the tail vertex; the source's tail-role entries cached):
+// instead of binding each candidate v of step d and running the tail step
+// below it, every chunk of 32 entries tests all (candidate v, cached entry
+// x) pairs, one pair per lane and round, candidate-major.  A pair passes
+// when x is in v's list with that entry active, (ENUMERATION) differs from
+// the history vertices the tail step compares (v for step d), and passes
+// the other CHECKs: exactly what the tail step below v accepts.  ENUMERATION
+// adds the passing pairs to *leaves.  NLCC (exact programs): the first
+// passing pair in (candidate CSR order, x ascending) order is the
+// depth-first walk's first success; it binds steps d and d + 1 and returns
+// kFound.  Both then leave step d exhausted.
+template <class W, bool kEnum>
+__device__ int pair_tail_step(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
+                         unsigned long long* leaves) {
+  const unsigned lane = lane_id();
+  const int n_steps = ws.prog->n_steps;
+  const int t_step = d + 1;
+  const uint32_t n_f = ws.src_n;
+  unsigned long long found = 0;
+  while (true) {
+    const uint64_t next = ws.f.next[d], end = ws.f.end[d];
+    if (next >= end) break;
+    const uint32_t cnt = end - next < 32 ? static_cast<uint32_t>(end - next) : 32u;
+    const uint64_t e = next + lane;
+    bool ok = lane < cnt && edge_active(st.eact, e);
+    uint32_t nb = 0;
+    if (ok) {
+      nb = g.adj[e];
+      ok = role_of(st, nb, s.role);
+    }
+    if (kEnum && ok) {
+      for (int h = 0; h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
+        if (ws.f.bound[ws.prog->hist_step[h]] == nb) ok = false;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      ws.f.next[d] = next + cnt;
+      ws.scanned += cnt;
+    }
+    __syncwarp();
+    const unsigned cm = __ballot_sync(kFull, ok);
+    if (!cm || n_f == 0) continue;
+    uint64_t b2 = 0, e2 = 0;
+    if (ok) {
+      b2 = g.off[nb];
+      e2 = g.off[nb + 1];
+    }
+    const uint32_t total = static_cast<uint32_t>(__popc(cm)) * n_f;
+    for (uint32_t p0 = 0; p0 < total; p0 += 32) {
+      const uint32_t p = p0 + lane;
+      const bool act = p < total;
+      const uint32_t c = act ? p / n_f : 0u, i = act ? p % n_f : 0u;
+      const int from = nth_set_bit(cm, c);
+      const uint32_t v = __shfl_sync(kFull, nb, from);
+      const uint64_t lb = __shfl_sync(kFull, static_cast<unsigned long long>(b2), from);
+      const uint64_t le = __shfl_sync(kFull, static_cast<unsigned long long>(e2), from);
+      bool pass = act;
+      uint32_t x = 0;
+      if (pass) {
+        x = ws.src_adj[i];
+        if (kEnum)
+          for (int h = 0; pass && h < ws.prog->n_hist && ws.prog->hist_step[h] < t_step; ++h) {
+            const int hs = ws.prog->hist_step[h];
+            if ((hs == d ? v : ws.f.bound[hs]) == x) pass = false;
+          }
+      }
+      if (pass) {
+        const uint64_t idx = lane_find_sorted(g.adj, lb, le, x);
+        pass = idx != ~uint64_t(0) && edge_active(st.eact, idx);
+      }
+      for (int j = ws.prog->tail_from; pass && j < n_steps; ++j) {
+        const int hs = ws.prog->hist_step[ws.prog->steps[j].hist];
+        if (hs == 0) continue;
+        const uint32_t t = hs == d ? v : ws.f.bound[hs];
+        pass = lane_find_sorted(g.adj, g.off[t], g.off[t + 1], x) != ~uint64_t(0);
+      }
+      const unsigned pm = __ballot_sync(kFull, pass);
+      if (kEnum) {
+        found += __popc(pm);
+      } else if (pm) {
+        const int w = __ffs(pm) - 1;
+        const uint32_t bv = __shfl_sync(kFull, v, w), bx = __shfl_sync(kFull, x, w);
+        __syncwarp();
+        if (lane == 0) {
+          ws.f.bound[d] = bv;
+          ws.f.bound[t_step] = bx;
+          ws.f.next[d] = end;
+        }
+        __syncwarp();
+        return kFound;
+      }
+    }
+  }
+  if (kEnum) *leaves += found;
+  return kNone;
+}
+
 template <class W, bool kEnum>
 __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared& ws, int d, const WalkStep& s,
                            uint32_t* out, unsigned long long* leaves) {
@@ -732,7 +853,12 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     }
     const uint32_t cur = ws.f.cur[d];
     bool adv = false;
-    if (s.kind == kStepVertex && d + 1 == ws.prog->tail_from && g.sorted_unique && (kEnum || ws.prog->exact)) {
+    if (ws.pair_tail && ws.src_cached && s.kind == kStepVertex && d + 2 == ws.prog->tail_from &&
+        (kEnum || ws.prog->exact)) {
+      // pair_tail is set only for programs whose tail qualifies (k_enumerate, k_walk).
+      if (pair_tail_step<W, kEnum>(g, st, ws, d, s, leaves) == kFound) return kItemSuccess;
+    } else if (s.kind == kStepVertex && d + 1 == ws.prog->tail_from && g.sorted_unique &&
+               (kEnum || ws.prog->exact)) {
       uint32_t nb = 0;
       if (tail_vertex<W, kEnum>(g, st, ws, d, s, &nb, leaves) == kFound) {
         __syncwarp();
@@ -868,6 +994,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.pair_tail = 0;
     ws.memo_on = 1;
     ws.tail_state_memo = 1;
   }
@@ -919,6 +1046,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
       __syncwarp();
       if (lane == 0) {
         ws.tail_swap = (ws.prog->exact && swap_ok) ? w.tail_swap : 0u;
+        ws.pair_tail = (ws.prog->exact && swap_ok) ? w.pair_tail : 0u;
         ws.tail_state_memo = w.tail_state_memo;
       }
       __syncwarp();
@@ -1061,7 +1189,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     DevGraph g, DevState<W> st, const WalkProgram* __restrict__ prog, uint32_t frame_steps,
     const uint32_t* __restrict__ wl, uint32_t n_wl, const uint4* __restrict__ items, uint32_t n_items,
     uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns, uint32_t tail_swap,
-    uint32_t count_memo) {
+    uint32_t count_memo, uint32_t pair) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
@@ -1076,6 +1204,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.pair_tail = 0;
     ws.memo_on = 1;
     ws.tail_state_memo = 1;
   }
@@ -1103,6 +1232,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
   const int filter_role = tail_plan(g, s_prog, &swap_ok);
   if (lane == 0) {
     ws.tail_swap = swap_ok ? tail_swap : 0u;
+    ws.pair_tail = swap_ok ? pair : 0u;
     ws.memo_on = count_memo;
   }
   __syncwarp();
@@ -1172,6 +1302,8 @@ void set_enum_count_memo(bool on) { g_enum_count_memo = on ? 1u : 0u; }
 bool enum_count_memo() { return g_enum_count_memo != 0; }
 void set_walk_tail_state_memo(bool on) { g_walk_tail_state_memo = on ? 1u : 0u; }
 bool walk_tail_state_memo() { return g_walk_tail_state_memo != 0; }
+void set_pair_tail(bool enumeration, bool on) { (enumeration ? g_enum_pair_tail : g_walk_pair_tail) = on ? 1u : 0u; }
+bool pair_tail_on(bool enumeration) { return (enumeration ? g_enum_pair_tail : g_walk_pair_tail) != 0; }
 void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
 uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
@@ -1229,7 +1361,8 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
   const size_t dyn = kWalkWarps * frame_bytes(frame_steps);
   PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
                                     g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
-                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap, g_enum_count_memo));
+                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap, g_enum_count_memo,
+                                    g_enum_pair_tail));
 }
 
 }  // namespace pmgb
@@ -1317,6 +1450,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
     ws.src_n = 0;
     ws.src_cached = 0;
     ws.tail_swap = 0;
+    ws.pair_tail = 0;
     ws.memo_on = 1;
     ws.tail_state_memo = 1;
   }

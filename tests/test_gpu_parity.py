@@ -196,6 +196,12 @@ KNOB_SETTINGS = {
                          "tail_swap": 1, "walk_tail_swap": 1},
     "tail_swap_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                       "tail_swap": 0, "walk_tail_swap": 0},
+    # The step before the tail one candidate at a time (pair-parallel off),
+    # and pair-parallel with the source-side tail off.
+    "pair_tail_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                      "pair_tail": (0, 0)},
+    "pair_tail_no_swap": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                          "pair_tail": (1, 1), "tail_swap": 0, "walk_tail_swap": 0},
     # ENUMERATION without the count memo (every subtree walked).
     "count_memo_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                        "count_memo": 0},
@@ -224,6 +230,7 @@ def _set_knobs(k):
     pm.lib.pm_set_walk_tail_swap(k.get("walk_tail_swap", 4))
     pm.lib.pm_set_enum_count_memo(k.get("count_memo", 1))
     pm.lib.pm_set_walk_tail_state_memo(k.get("tail_state_memo", 1))
+    pm.lib.pm_set_pair_tail(*k.get("pair_tail", (1, 1)))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
