@@ -59,7 +59,7 @@ struct WarpShared {
   // Adjacency list of the walk's source in shared memory (src_cached): the
   // whole list when it has at most kSrcCache entries, or, for programs with
   // a tail step, only the entries whose target holds the tail step's role
-  // when at most kSrcCache of them do (src_n entries).
+  // when they fit the kernel's cache (src_n entries).
   const uint32_t* src_adj;
   uint32_t src_n;
   uint32_t src_cached;
@@ -77,11 +77,15 @@ struct WarpShared {
   uint32_t tail_state_memo;
 };
 
-// Source adjacency entries a warp caches in shared memory per walk; a
-// filtered cache (one role's entries) scans source lists of up to
-// kSrcFilterScan entries.
+// Source adjacency entries a warp caches in shared memory per walk (CC/PC/TDS
+// walks; ENUMERATION, limited by registers rather than shared memory, keeps
+// up to kSrcCacheEnum); a filtered cache (one role's entries) scans source
+// lists of up to kSrcFilterScan entries.  The pair-parallel step before the
+// tail runs on caches of at most kPairMaxSrc entries.
 constexpr uint32_t kSrcCache = 256;
-constexpr uint32_t kSrcFilterScan = 4096;
+constexpr uint32_t kSrcCacheEnum = 768;
+constexpr uint32_t kSrcFilterScan = 8192;
+constexpr uint32_t kPairMaxSrc = 256;
 
 // Points the warp's frames at its part of the kernel's dynamic shared
 // memory (frame_bytes(steps) per warp).
@@ -113,20 +117,20 @@ __device__ __forceinline__ bool role_of(const DevState<W>& st, uint32_t v, uint3
 // change during a walk launch).
 template <class W>
 __device__ __forceinline__ void cache_source(const DevGraph& g, const DevState<W>& st, WarpShared& ws,
-                                             uint32_t* cache, uint32_t source, int filter_role) {
+                                             uint32_t* cache, uint32_t cap, uint32_t source, int filter_role) {
   const unsigned lane = lane_id();
   uint32_t n = 0, cached = 0;
   if (g.symmetric) {
     const uint64_t b = g.off[source], e = g.off[source + 1];
     if (filter_role < 0) {
-      if (e - b <= kSrcCache) {
+      if (e - b <= cap) {
         cached = 1;
         n = static_cast<uint32_t>(e - b);
         for (uint32_t i = lane; i < n; i += 32) cache[i] = g.adj[b + i];
       }
     } else if (e - b <= kSrcFilterScan) {
-      // Cached when the role's entries fit (n stays <= kSrcCache: a chunk
-      // is written only while the entries so far plus its own fit).
+      // Cached when the role's entries fit (n stays <= cap: a chunk is
+      // written only while the entries so far plus its own fit).
       const uint32_t len = static_cast<uint32_t>(e - b);
       cached = 1;
       for (uint32_t i0 = 0; i0 < len; i0 += 32) {
@@ -138,7 +142,7 @@ __device__ __forceinline__ void cache_source(const DevGraph& g, const DevState<W
           keep = role_of(st, x, static_cast<uint32_t>(filter_role));
         }
         const unsigned m = __ballot_sync(kFull, keep);
-        if (n + __popc(m) > kSrcCache) {
+        if (n + __popc(m) > cap) {
           cached = 0;
           n = 0;
           break;
@@ -853,8 +857,8 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
     }
     const uint32_t cur = ws.f.cur[d];
     bool adv = false;
-    if (ws.pair_tail && ws.src_cached && s.kind == kStepVertex && d + 2 == ws.prog->tail_from &&
-        (kEnum || ws.prog->exact)) {
+    if (ws.pair_tail && ws.src_cached && ws.src_n <= kPairMaxSrc && s.kind == kStepVertex &&
+        d + 2 == ws.prog->tail_from && (kEnum || ws.prog->exact)) {
       // pair_tail is set only for programs whose tail qualifies (k_enumerate, k_walk).
       if (pair_tail_step<W, kEnum>(g, st, ws, d, s, leaves) == kFound) return kItemSuccess;
     } else if (s.kind == kStepVertex && d + 1 == ws.prog->tail_from && g.sorted_unique &&
@@ -1056,7 +1060,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
       continue;
     }
     next_epoch(m);
-    cache_source(g, st, ws, s_src[wib], v, filter_role);
+    cache_source(g, st, ws, s_src[wib], kSrcCache, v, filter_role);
     unsigned long long unused = 0;
     const uint8_t res = run_walk<W, false>(g, st, ws, m, v, &unused, deadline, lo, hi);
     if (lane == 0) {
@@ -1192,7 +1196,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     uint32_t count_memo, uint32_t pair) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
-  __shared__ uint32_t s_src[kWalkWarps][kSrcCache];
+  __shared__ uint32_t s_src[kWalkWarps][kSrcCacheEnum];
   extern __shared__ __align__(16) unsigned char s_frames[];
   const unsigned lane = lane_id();
   const unsigned wib = threadIdx.x >> 5;
@@ -1244,7 +1248,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     const uint4 it = items ? items[gi] : make_uint4(static_cast<uint32_t>(gi), 0u, 0xFFFFFFFFu, 0u);
     const uint32_t source = wl[it.x];
     next_epoch(m);
-    cache_source(g, st, ws, s_src[wib], source, filter_role);
+    cache_source(g, st, ws, s_src[wib], kSrcCacheEnum, source, filter_role);
     const unsigned long long before = leaves;
     const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z);
     if (res == kItemTimeout) {
