@@ -87,7 +87,7 @@ typedef struct pm_tune_result {
   uint32_t walk_presplit, walk_table_entries;
   uint32_t probes_memo, probes_plain, runs;
   uint32_t enum_tail_swap, walk_tail_swap, enum_count_memo, walk_tail_state_memo;
-  uint32_t enum_pair_tail, walk_pair_tail;
+  uint32_t enum_pair_tail, walk_pair_tail, enum_second_split;
 } pm_tune_result;
 
 pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t n,
@@ -165,6 +165,15 @@ pm_status_t pm_set_walk_tail_state_memo(int32_t enabled);
  * switches for ENUMERATION and for walks; default 1 / 1.  Process-wide; speed
  * only.  No counterpart in the reference. */
 pm_status_t pm_set_pair_tail(int32_t enumeration, int32_t walks);
+
+/* ENUMERATION work items below the first hop: in a source of more than
+ * `entries` first-hop entries, a first-hop vertex whose own list has more
+ * than 2 x `entries` entries runs as separate items, one per `entries`-entry
+ * slice of its list at the second hop (for templates whose second step binds
+ * a new vertex and whose tail does not start at the second step).  Counts
+ * are the same; 0 = never; default 256.  Process-wide; speed only.  No
+ * counterpart in the reference. */
+pm_status_t pm_set_enum_second_split(uint32_t entries);
 
 /* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
  * 120000 ms).  A walk still running past it stops; the step then fails with

@@ -83,7 +83,8 @@ class TuneResult(ctypes.Structure):
                 ("probes_plain", ctypes.c_uint32), ("runs", ctypes.c_uint32),
                 ("enum_tail_swap", ctypes.c_uint32), ("walk_tail_swap", ctypes.c_uint32),
                 ("enum_count_memo", ctypes.c_uint32), ("walk_tail_state_memo", ctypes.c_uint32),
-                ("enum_pair_tail", ctypes.c_uint32), ("walk_pair_tail", ctypes.c_uint32)]
+                ("enum_pair_tail", ctypes.c_uint32), ("walk_pair_tail", ctypes.c_uint32),
+                ("enum_second_split", ctypes.c_uint32)]
 
     def as_dict(self):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
@@ -162,6 +163,7 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_enum_count_memo": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_walk_tail_state_memo": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_pair_tail": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
+        "pm_set_enum_second_split": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_walk_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_walk_presplit": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_presplit": (ctypes.c_int32, [ctypes.c_uint32]),

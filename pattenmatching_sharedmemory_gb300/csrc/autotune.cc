@@ -228,6 +228,24 @@ TuneResult autotune(GraphImpl* g, const std::vector<PatternGraph>& templates, ui
     out.enum_pair_tail = pick ? 1 : 0;
   }
 
+  // ENUMERATION second-hop slices, on every probe.
+  {
+    const uint32_t sizes[] = {0, 64, 256, 1024};
+    double b = std::numeric_limits<double>::infinity();
+    uint32_t pick = enum_second_split();
+    for (uint32_t sz : sizes) {
+      set_enum_second_split(sz);
+      const ProbeRun r = run_probes(g, all);
+      check(r, all);
+      if (r.enum_ms < b) {
+        b = r.enum_ms;
+        pick = sz;
+      }
+    }
+    set_enum_second_split(pick);
+    out.enum_second_split = pick;
+  }
+
   // 6. Count-memo entries per warp, on every probe.
   const uint32_t tables[] = {4096, 8192, 16384};
   double bt = std::numeric_limits<double>::infinity();

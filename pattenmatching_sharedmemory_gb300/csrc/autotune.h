@@ -14,7 +14,7 @@ struct TuneResult {
   uint32_t probes_memo = 0, probes_plain = 0;  // probe templates per program kind
   uint32_t runs = 0;                            // candidate runs over the probes
   uint32_t enum_tail_swap = 0, walk_tail_swap = 0, enum_count_memo = 1, walk_tail_state_memo = 1;
-  uint32_t enum_pair_tail = 1, walk_pair_tail = 1;
+  uint32_t enum_pair_tail = 1, walk_pair_tail = 1, enum_second_split = 0;
 };
 
 // Times up to max_per_group templates with and without a count memo under

@@ -375,6 +375,11 @@ pm_status_t pm_set_pair_tail(int32_t enumeration, int32_t walks) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_enum_second_split(uint32_t entries) {
+  set_enum_second_split(entries);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_lcc_graph(int32_t enabled) {
   set_lcc_graph(enabled != 0);
   return PM_SUCCESS;
@@ -634,6 +639,7 @@ pm_status_t pm_autotune(pm_graph* g, const pm_template_csr* templates, uint32_t 
       result->walk_tail_state_memo = r.walk_tail_state_memo;
       result->enum_pair_tail = r.enum_pair_tail;
       result->walk_pair_tail = r.walk_pair_tail;
+      result->enum_second_split = r.enum_second_split;
       result->walk_presplit = r.walk_presplit;
       result->walk_table_entries = r.walk_table_entries;
       result->probes_memo = r.probes_memo;

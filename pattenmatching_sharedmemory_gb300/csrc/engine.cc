@@ -745,11 +745,45 @@ StepResult QueryImpl::step_enumeration() {
       PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
       PM_CUDA(cudaStreamSynchronize(stream));
       const uint64_t t = presplit;
+      // In sources of more than s2 entries, a first-hop vertex whose list has
+      // more than twice s2 entries takes its own items, one per s2-entry
+      // slice of its list at the second hop (exact when the second step also
+      // binds a new vertex; not when the tail starts at step 2, whose pair
+      // step at step 1 would read whole lists).  The other positions go in
+      // runs of at most t.
+      const uint64_t s2 = enum_second_split();
+      const bool second_ok = s2 && p.n_steps > 2 &&
+                             (p.steps[2].kind == kStepVertex || p.steps[2].kind == kStepFinal) && p.tail_from != 3;
+      const std::vector<uint32_t>& adj = g->host.adj;
       for (uint32_t i = 0; i < n_wl; ++i) {
         const uint64_t deg = off[wl[i] + 1] - off[wl[i]];
         if (deg <= t) continue;
-        for (uint64_t lo = 0; lo < deg; lo += t)
-          items.push_back(make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(std::min(lo + t, deg)), 0));
+        if (!second_ok || deg <= s2) {
+          for (uint64_t lo = 0; lo < deg; lo += t)
+            items.push_back(
+                make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(std::min(lo + t, deg)), 0));
+          continue;
+        }
+        const uint64_t base = off[wl[i]];
+        uint64_t run = 0;
+        for (uint64_t pos = 0; pos < deg; ++pos) {
+          const uint32_t v1 = adj[base + pos];
+          const uint64_t d1 = off[v1 + 1] - off[v1];
+          const bool hub = d1 > 2 * s2;
+          if ((hub || pos - run == t) && pos > run) {
+            items.push_back(make_uint4(i, static_cast<uint32_t>(run), static_cast<uint32_t>(pos), 0));
+            run = pos;
+          }
+          if (hub) {
+            const uint64_t n_sl = (d1 + s2 - 1) / s2;
+            for (uint64_t k = 0; k < n_sl; ++k)
+              items.push_back(make_uint4(i, static_cast<uint32_t>(pos), static_cast<uint32_t>(pos + 1),
+                                         static_cast<uint32_t>(k + 1)));
+            run = pos + 1;
+          }
+        }
+        if (deg > run)
+          items.push_back(make_uint4(i, static_cast<uint32_t>(run), static_cast<uint32_t>(deg), 0));
       }
       for (uint32_t i = 0; i < n_wl; ++i)
         if (off[wl[i] + 1] - off[wl[i]] <= t) items.push_back(make_uint4(i, 0, 0xFFFFFFFFu, 0));

@@ -95,6 +95,10 @@ bool walk_tail_state_memo();
 // pairs one per lane (ENUMERATION, or exact CC/PC/TDS programs; default on).
 void set_pair_tail(bool enumeration, bool on);
 bool pair_tail_on(bool enumeration);
+// ENUMERATION items may restrict the second hop to slices of this many
+// entries of the first-hop vertex's list (item.w = slice + 1; 0: never).
+void set_enum_second_split(uint32_t entries);
+uint32_t enum_second_split();
 // The same for the tail step of exact CC/PC/TDS programs (WalkLaunch::tail_swap).
 void set_walk_tail_swap(uint32_t ratio);
 uint32_t walk_tail_swap();

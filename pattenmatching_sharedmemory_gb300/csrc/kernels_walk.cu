@@ -188,6 +188,7 @@ uint32_t g_walk_tail_swap = 4;  // ... of CC/PC/TDS launches (exact programs)
 uint32_t g_enum_count_memo = 1;  // WarpShared::memo_on of ENUMERATION launches
 uint32_t g_enum_pair_tail = 1;   // WarpShared::pair_tail of ENUMERATION launches
 uint32_t g_walk_pair_tail = 1;   // WalkLaunch::pair_tail
+uint32_t g_enum_second_split = 256;  // second-hop slice entries of ENUMERATION items (0: none)
 uint32_t g_walk_tail_state_memo = 1;  // WalkLaunch::tail_state_memo
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
@@ -806,10 +807,15 @@ __device__ int tail_vertex(const DevGraph& g, const DevState<W>& st, WarpShared&
 template <class W, bool kEnum>
 __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared& ws, WarpMemo& m, uint32_t source,
                             unsigned long long* leaves, uint64_t deadline, uint32_t first_lo = 0,
-                            uint32_t first_hi = 0xFFFFFFFFu) {
+                            uint32_t first_hi = 0xFFFFFFFFu, uint32_t second_lo = 0,
+                            uint32_t second_hi = 0xFFFFFFFFu) {
   const unsigned lane = lane_id();
   const int n_steps = ws.prog->n_steps;
-  const bool count_memo = kEnum && ws.prog->count_memo && ws.memo_on;
+  // [second_lo, second_hi) restricts the second hop the same way (ENUMERATION
+  // items with one first-hop position); such items keep no count memo, so
+  // they never overflow and are never re-run without the restriction.
+  const bool second = second_lo != 0 || second_hi != 0xFFFFFFFFu;
+  const bool count_memo = kEnum && ws.prog->count_memo && ws.memo_on && !second;
   uint32_t iters = 0;
   __syncwarp();
   if (lane == 0) {
@@ -933,6 +939,15 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
           __syncwarp();
         } else {
           frame_enter(g, ws, d);
+          if (second && d == 2) {
+            __syncwarp();
+            if (lane == 0) {
+              const uint64_t b = ws.f.next[2], e = ws.f.end[2];
+              ws.f.next[2] = e - b > second_lo ? b + second_lo : e;
+              ws.f.end[2] = e - b > second_hi ? b + second_hi : e;
+            }
+            __syncwarp();
+          }
         }
       }
     } else {
@@ -1193,7 +1208,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     DevGraph g, DevState<W> st, const WalkProgram* __restrict__ prog, uint32_t frame_steps,
     const uint32_t* __restrict__ wl, uint32_t n_wl, const uint4* __restrict__ items, uint32_t n_items,
     uint4* overflow, WalkScratch sc, StepCounters* ctr, uint64_t budget_ns, uint32_t tail_swap,
-    uint32_t count_memo, uint32_t pair) {
+    uint32_t count_memo, uint32_t pair, uint32_t second_slice) {
   __shared__ WarpShared s_ws[kWalkWarps];
   __shared__ WalkProgram s_prog;  // every item runs the same program
   __shared__ uint32_t s_src[kWalkWarps][kSrcCacheEnum];
@@ -1250,7 +1265,16 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     next_epoch(m);
     cache_source(g, st, ws, s_src[wib], kSrcCacheEnum, source, filter_role);
     const unsigned long long before = leaves;
-    const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z);
+    // it.w = k + 1: entries [k * second_slice, (k + 1) * second_slice) of the
+    // first-hop vertex's list at the second hop.
+    uint32_t s_lo = 0, s_hi = 0xFFFFFFFFu;
+    if (items && it.w && second_slice) {
+      const uint64_t lo2 = static_cast<uint64_t>(it.w - 1) * second_slice;
+      const uint64_t hi2 = lo2 + second_slice;
+      s_lo = static_cast<uint32_t>(lo2 < 0xFFFFFFFEull ? lo2 : 0xFFFFFFFEull);
+      s_hi = static_cast<uint32_t>(hi2 < 0xFFFFFFFEull ? hi2 : 0xFFFFFFFEull);
+    }
+    const uint8_t res = run_walk<W, true>(g, st, ws, m, source, &leaves, deadline, it.y, it.z, s_lo, s_hi);
     if (res == kItemTimeout) {
       if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
       break;
@@ -1308,6 +1332,8 @@ void set_walk_tail_state_memo(bool on) { g_walk_tail_state_memo = on ? 1u : 0u; 
 bool walk_tail_state_memo() { return g_walk_tail_state_memo != 0; }
 void set_pair_tail(bool enumeration, bool on) { (enumeration ? g_enum_pair_tail : g_walk_pair_tail) = on ? 1u : 0u; }
 bool pair_tail_on(bool enumeration) { return (enumeration ? g_enum_pair_tail : g_walk_pair_tail) != 0; }
+void set_enum_second_split(uint32_t entries) { g_enum_second_split = entries; }
+uint32_t enum_second_split() { return g_enum_second_split; }
 void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
 uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
@@ -1366,7 +1392,7 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
   PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
                                     g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
                                     q.ctr, g_walk_budget_ns, g_enum_tail_swap, g_enum_count_memo,
-                                    g_enum_pair_tail));
+                                    g_enum_pair_tail, g_enum_second_split));
 }
 
 }  // namespace pmgb

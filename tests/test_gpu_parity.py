@@ -202,6 +202,15 @@ KNOB_SETTINGS = {
                       "pair_tail": (0, 0)},
     "pair_tail_no_swap": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                           "pair_tail": (1, 1), "tail_swap": 0, "walk_tail_swap": 0},
+    # Second-hop slices everywhere they apply (every source sliced, 4-entry
+    # second-hop slices of lists above 8 entries), with and without the pair
+    # step, and never.
+    "second_split_small": {"walk_presplit": 64, "enum_presplit": (1, 1), "walk_tables": 8192, "enum_tables": 8192,
+                           "second_split": 4},
+    "second_split_small_no_pair": {"walk_presplit": 64, "enum_presplit": (2, 2), "walk_tables": 8192,
+                                   "enum_tables": 8192, "second_split": 4, "pair_tail": (0, 0)},
+    "second_split_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
+                         "second_split": 0},
     # ENUMERATION without the count memo (every subtree walked).
     "count_memo_off": {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,
                        "count_memo": 0},
@@ -231,6 +240,7 @@ def _set_knobs(k):
     pm.lib.pm_set_enum_count_memo(k.get("count_memo", 1))
     pm.lib.pm_set_walk_tail_state_memo(k.get("tail_state_memo", 1))
     pm.lib.pm_set_pair_tail(*k.get("pair_tail", (1, 1)))
+    pm.lib.pm_set_enum_second_split(k.get("second_split", 256))
 
 
 DEFAULT_KNOBS = {"walk_presplit": 64, "enum_presplit": (32, 8), "walk_tables": 8192, "enum_tables": 8192,

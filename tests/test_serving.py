@@ -185,4 +185,5 @@ def test_autotune_keeps_results():
     pm.lib.pm_set_enum_count_memo(1)
     pm.lib.pm_set_walk_tail_state_memo(1)
     pm.lib.pm_set_pair_tail(1, 1)
+    pm.lib.pm_set_enum_second_split(256)
     g.set_hub_plan(32, 1024)
