@@ -150,3 +150,33 @@ def test_version_and_last_error():
     with pytest.raises(pm.PmError):
         pm.Graph.load("/nonexistent", None, None, device=-1)
     assert "nonexistent" in pm.lib.pm_last_error().decode()
+
+
+def _c_struct_fields(header: str, name: str) -> list[str]:
+    """Field names of `typedef struct name {...} name;` in an include/ header, in order."""
+    text = (Path(__file__).resolve().parent.parent / "include" / header).read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", text, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        names = decl.split(None, 1)[1] if decl.split()[0] != "const" else decl.split(None, 2)[2]
+        fields += [n.strip().lstrip("*").split("[")[0] for n in names.split(",")]
+    return fields
+
+
+@pytest.mark.parametrize("header,c_name,py_cls", [
+    ("pm_gb300_tools.h", "pm_tune_result", "TuneResult"),
+    ("pm_gb300.h", "pm_server_config", "ServerConfig"),
+    ("pm_gb300.h", "pm_request_result", "RequestResult"),
+    ("pm_gb300.h", "pm_server_stats", "ServerStats"),
+])
+def test_python_structs_mirror_the_header(header, c_name, py_cls):
+    """The ctypes mirrors list the C structs' fields in the same order."""
+    import ctypes
+
+    cls = getattr(pm, py_cls)
+    assert [n for n, _ in cls._fields_] == _c_struct_fields(header, c_name)
+    assert all(ctypes.sizeof(t) in (4, 8) for _, t in cls._fields_)
