@@ -191,6 +191,15 @@ def pct(xs, q):
     return xs[min(len(xs) - 1, int(round(q * (len(xs) - 1))))]
 
 
+def lcc_pass_bytes(listed: int, edges_eliminated: int, k: int) -> float:
+    """Algorithmic bytes of one LCC pass, per entry of every checked list:
+    neighbour id 4 B, its edge bit and active bit 1/8 B each, its label 1 B
+    and its ceil(k/8) B of roles; plus 1/8 B written per eliminated entry.
+    The per-vertex terms (offsets, own label and roles) are left out, so this
+    is a lower bound."""
+    return listed * (4 + 0.125 + 0.125 + 1 + (k + 7) // 8) + edges_eliminated / 8
+
+
 def lcc_roofline(scale: int, device: int):
     """LCC passes on a CSR larger than L2: algorithmic bytes / step time."""
     import pattenmatching_sharedmemory_gb300 as pm
@@ -208,7 +217,8 @@ def lcc_roofline(scale: int, device: int):
         listed, gathered = q.step_walk_stats(row)
         row += 1
         if name == "LCC":
-            passes.append((rec.step_ms, listed / 8 + gathered * (4 + wb), listed, gathered))
+            passes.append((rec.step_ms, lcc_pass_bytes(listed, rec.results.edge_eliminated, 6), listed, gathered,
+                           listed / 8 + gathered * (4 + wb)))
             if rec.results.vertex_eliminated == 0 and rec.results.edge_eliminated == 0:
                 break
         if fin or row > 40:
@@ -217,12 +227,18 @@ def lcc_roofline(scale: int, device: int):
     peak, peak_kind = measured_peaks()
     ms = sum(p[0] for p in passes)
     by = sum(p[1] for p in passes)
+    touched = sum(p[4] for p in passes)
     achieved = by / (ms / 1e3) / 1e9 if ms else None
     out = {"bound": "hbm", "kernel": "lcc sweep (k_lcc_check x2 + sweep 2)", "graph": f"rmat scale {scale} ef 16",
            "csr_entries": g.edge_count, "passes": len(passes), "ms_per_pass": ms / max(1, len(passes)),
-           "pass_ms": [round(p[0], 3) for p in passes], "gathered_per_pass": [p[3] for p in passes],
+           "pass_ms": [round(p[0], 3) for p in passes], "listed_per_pass": [p[2] for p in passes],
+           "gathered_per_pass": [p[3] for p in passes],
+           "bytes": "per checked-list entry 4 + 1/8 + 1/8 + 1 + ceil(k/8) B, + 1/8 B per eliminated entry",
            "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
-           "frac": achieved / peak if achieved else None, "traffic": profile_traffic("lcc")}
+           "frac": achieved / peak if achieved else None,
+           "achieved_touched": touched / (ms / 1e3) / 1e9 if ms else None,
+           "touched_bytes": "1/8 B per listed entry (live-target bit) + (4 + W) B per gathered entry",
+           "traffic": profile_traffic("lcc")}
     g.close()
     return out
 
