@@ -63,9 +63,9 @@ struct WarpShared {
   const uint32_t* src_adj;
   uint32_t src_n;
   uint32_t src_cached;
-  // ENUMERATION: the tail step iterates over the cached source entries
-  // instead of the bound vertex's list when that list has at least
-  // tail_swap times as many 32-entry chunks (0: never).
+  // ENUMERATION and exact walks: the tail step iterates over the cached
+  // source entries instead of the bound vertex's list when that list has at
+  // least tail_swap times as many 32-entry chunks (0: never).
   uint32_t tail_swap;
   // The step before the tail tests (candidate, cached source entry) pairs
   // one per lane instead of descending per candidate (0: never).
