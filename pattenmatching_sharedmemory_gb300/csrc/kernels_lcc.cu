@@ -790,11 +790,14 @@ __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState
   const uint32_t ee = __reduce_add_sync(kFull, tl.edge_elim);
   const uint32_t nm = __reduce_add_sync(kFull, tl.newly_modified);
   const uint32_t ga = __reduce_add_sync(kFull, tl.gathered);
+  // Listed entries: lane-per-vertex batches count per lane, the other paths
+  // on lane 0.
+  const uint32_t ls = __reduce_add_sync(kFull, tl.streamed);
   if (lane_id() == 0) {
     if (ee) atomicAdd(&ctr->edge_elim, static_cast<unsigned long long>(ee));
     if (nm) atomicAdd(&ctr->modified_total, static_cast<unsigned long long>(nm));
     if (ga) atomicAdd(&ctr->gathered, static_cast<unsigned long long>(ga));
-    if (tl.streamed) atomicAdd(&ctr->scanned, static_cast<unsigned long long>(tl.streamed));
+    if (ls) atomicAdd(&ctr->scanned, static_cast<unsigned long long>(ls));
   }
 }
 
