@@ -243,6 +243,42 @@ def lcc_roofline(scale: int, device: int):
     return out
 
 
+def poisson_stream(g, pm, tmpls, rate_qps: float, duration_s: float, slots: int, seed: int):
+    """Requests drawn from `tmpls` arriving as a Poisson process at
+    `rate_qps` for `duration_s` into one server; every arrival is admitted as
+    slots and memory free up.  Reports the completed rate and the per-request
+    latency (submit to result) percentiles."""
+    import random
+
+    rng = random.Random(seed)
+    with pm.Server(g, slots=slots) as srv:
+        for t in tmpls[:slots]:  # warm the slots (streams, captured loops)
+            tk = srv.submit(t)
+            srv.wait(tk)
+            srv.release(tk)
+        tickets = []
+        t0 = time.perf_counter()
+        next_t = t0
+        while True:
+            now = time.perf_counter()
+            if now - t0 >= duration_s:
+                break
+            if now < next_t:
+                time.sleep(min(next_t - now, 0.001))
+                continue
+            tickets.append(srv.submit(tmpls[rng.randrange(len(tmpls))]))
+            next_t += rng.expovariate(rate_qps)
+        results = [srv.wait(t) for t in tickets]
+        t1 = time.perf_counter()
+        for t in tickets:
+            srv.release(t)
+    lat = [r.latency_ms for r in results]
+    bad = sum(1 for r in results if r.status != pm.PM_SUCCESS)
+    return {"offered_qps": rate_qps, "requests": len(tickets), "failed": bad,
+            "completed_qps": len(tickets) / (t1 - t0) if t1 > t0 else None,
+            "latency_ms_p50": pct(lat, 0.5) if lat else None, "latency_ms_p99": pct(lat, 0.99) if lat else None}
+
+
 def small_stream(g, args, pm, torch):
     """Served vs one-at-a-time on a stream of small requests (35 triangles)."""
     tm = small_templates()
@@ -436,6 +472,14 @@ def run_gb300(args, w, rank, world):
         "gpu_launches": launches,
     }
     out["small_stream"] = small_stream(g, args, pm, torch)
+    # Poisson arrivals of the same 15 templates at 50 % and 90 % of the burst
+    # capacity measured above (extra figures: a failure here is reported, the
+    # main line stands).
+    try:
+        out["poisson"] = [poisson_stream(g, pm, tmpls, f * qps / world, 4.0, args.slots, seed=11 + i)
+                          for i, f in enumerate((0.5, 0.9))]
+    except Exception as e:  # noqa: BLE001
+        out["poisson"] = {"error": f"{type(e).__name__}: {e}"}
     if args.lcc_scale:
         out["lcc_roofline"] = lcc_roofline(args.lcc_scale, device)
     return out, g, tmpls
