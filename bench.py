@@ -2,51 +2,64 @@
 """Benchmark of the GB300 PruneJuice pipeline (one JSON line on rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--slots S] [--lcc-scale L]
+                    [--slots S] [--requests-per-step B] [--budget-ms D]
+    python bench.py --case c1|lcc|c4 [...]     one small fixed case (profiling)
 
-Graph: undirected RMAT scale 16 (65,536 vertices, edge factor 16, a/b/c =
-.57/.19/.19, seed 1, self-loops and duplicates removed), labels uniform over
-5 values (seed 1), resident on the GPU.  Stream: the 15 4-cycle templates
-with four distinct labels (every choice of 4 of the 5 labels in its 3 cyclic
-orders; labels 0,1,2,3 in that order is the classic single-query case).
-Every request runs the full reference pipeline: LCC0, LCC to a fixpoint, the
-CC constraint, LCC, exact ENUMERATION.
+Default workload (the served configuration): undirected RMAT scale 24
+(16,777,216 vertices, edge factor 16, a/b/c = .57/.19/.19, seed 1, ids
+permuted, self-loops and duplicates removed: 520,763,588 CSR entries), 32
+vertex labels drawn from Zipf(1.2) (seed 1), resident on the GPU.  Query
+stream: 2,000 seeded connected templates of 3-10 vertices, edge density
+0.3-0.6, labels drawn from the graph's Zipf(1.2) label distribution with
+repeats (templates.served_stream(2000, seed 24)).
 
-A step serves the whole stream: all 15 requests are submitted at once to a
-server with S slots (continuous batching, admission by device memory) and
-the step ends when the last one finished.  Before timing, pm_autotune picks
-the LCC degree classes and the enumeration slicing / count-memo size on
-probes of the stream (config.autotuned).
+A request runs the PruneJuice pruning pipeline of its template: LCC0, LCC to
+a fixpoint, every CC / PC / TDS constraint step, each followed by LCC to a
+fixpoint, on the reference's schedule (pm_query_prune /
+PM_SUBMIT_PRUNE_ONLY; exact match counting is timed on the RMAT-16 stream,
+key c1_stream).  Every request has a wall-clock budget of D ms from
+admission (pm_set_query_budget_ms): random templates over frequent labels
+make some constraint walks on this graph run for minutes, so a request
+either completes within D or ends with PM_E_TIMEOUT.  Timeouts are counted
+and reported, never dropped; `value` counts completed requests only.
 
-value      : served queries/s (host clock around the step, device
-             synchronised on both sides; the requests run on S streams).
-one_at_a_time: the same 15 templates run back to back through pm_query_run,
-             queries/s and latency p50/p99, measured in the same process.
-e2e        : served queries/s through the C ABI from host buffers: every
-             step uploads the CSR from pinned host memory (pm_graph_from_csr),
-             serves the stream and reads back every request's final state
-             (role sets, CSR-entry and vertex flags) and rows.
-roofline   : the dominant kernel class of a query run alone (by device
-             time): its algorithmic bytes over its CUDA-event time against
-             the measured HBM copy bandwidth.  Walker bytes: 16 B of CSR
-             offsets per hop plus, per tested CSR entry, 4 B neighbour id +
-             1/8 B edge bit + 1/8 B active bit + ceil(k/8) B neighbour roles.
-small_stream: served vs one-at-a-time on 35 small requests (the triangles
-             over the 5 labels, repeats allowed) on the same graph.
-lcc_roofline: LCC passes on RMAT scale L (default 22; 16 Zipf labels, the
-             two-cycle template on labels 0..5): per pass 1/8 B of edge bits
-             per listed CSR entry plus, per gathered entry, 4 B neighbour id
-             and the neighbour's packed word.
-cpu_baseline: the oracle restatement of the reference (all host cores) on a
-             bounded sample: each template's CC/ENUMERATION sources sampled
-             1 in --sample-stride and the time scaled back up.
---impl reference: that CPU estimate of the same stream as the reference arm.
-Multi-GPU: replicas only; every rank serves the stream on its own graph
-replica; value = all ranks' queries / slowest rank's time.
+A timed step serves B consecutive requests of the stream (step i: requests
+i*B .. i*B+B-1; warm-up steps use the stream's tail), all submitted at once
+to one long-lived server with S slots (continuous batching, admission by
+device memory); the step ends when the last finished.
+
+value        : completed requests per second over the timed steps (host
+               clock, device synchronised on both sides).
+one_at_a_time: the first requests of step 0 through pm_query_prune one
+               after another, same budget; `served_same_requests` is the
+               same requests served as one burst.
+poisson      : requests arriving as a Poisson process at 50 % and 90 % of
+               the served request rate: completed rate, p50/p99 latency.
+e2e          : through the C ABI from pinned host buffers: each step loads
+               the CSR with pm_graph_from_csr (host -> device), serves its
+               requests and reads back every request's result rows.
+roofline     : the dominant kernel class of requests run one at a time, its
+               algorithmic bytes over its device time against the measured
+               HBM copy bandwidth (walker bytes per hop: 16 B of offsets;
+               per tested CSR entry 4 B id + 1/8 B edge bit + 1/8 B active
+               bit + ceil(k/8) B roles).
+lcc_roofline : LCC passes of the two-cycle template (labels 0..5) on the same
+               graph: per pass 1/8 B edge bits per listed CSR entry plus 4 B
+               id and the neighbour's packed word per gathered entry.
+cpu_baseline : the oracle restatement on the host cores on a bounded sample
+               of the stream (requests 0, 100, 200, ...), whole requests,
+               reference budget, no extrapolation.
+--impl reference: the same restatement on the same seeded sample, one whole
+               request per step with the reference budget, on a graph the
+               oracle library generates (same generator source); it loads no
+               GPU library.
+Multi-GPU: replicas only; every rank serves the stream on its own replica;
+value = all ranks' completed requests / slowest rank's time.
 """
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import os
 import statistics
@@ -59,37 +72,49 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD = {"name": "rmat16_cycle4_stream15_served", "scale": 16, "ef": 16, "labels": ("uniform", 5, 1.0, 1),
-            "sample_stride": 256, "reference_stride": 512}
+C4 = {"name": "rmat24_zipf32_stream2000_prune_served", "scale": 24, "ef": 16, "abc": (0.57, 0.19, 0.19),
+      "graph_seed": 1, "labels": ("zipf", 32, 1.2, 1), "stream": 2000, "stream_seed": 24,
+      "template_vertices": (3, 10), "density": (0.3, 0.6), "reference_sample_stride": 100}
+C1 = {"name": "rmat16_cycle4_stream15_served", "scale": 16, "ef": 16, "labels": ("uniform", 5, 1.0, 1)}
+METRIC = ("completed queries/s served (continuous batching) vs one-at-a-time, PruneJuice pruning pipeline per "
+          "query, per-request budget")
 
 
-def stream_templates():
-    """The 15 distinct-label 4-cycles over labels 0..4."""
-    import itertools
-
-    from pattenmatching_sharedmemory_gb300 import templates as T
-
-    out = []
-    for a, b, c, d in itertools.combinations(range(5), 4):
-        for order in ([a, b, c, d], [a, b, d, c], [a, c, b, d]):
-            out.append(T.cycle(order))
-    return out
+def templates_module():
+    """templates.py loaded by path: plain numpy, no GPU library."""
+    spec = importlib.util.spec_from_file_location("pm_templates_bench",
+                                                  ROOT / "pattenmatching_sharedmemory_gb300" / "templates.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
-def small_templates():
-    """The 35 triangles over labels 0..4 (labels may repeat)."""
-    import itertools
-
-    from pattenmatching_sharedmemory_gb300 import templates as T
-
-    return [T.cycle(list(c)) for c in itertools.combinations_with_replacement(range(5), 3)]
+def c4_stream(T, n=None):
+    w = C4
+    return T.served_stream(n or w["stream"], n_labels=w["labels"][1], zipf_s=w["labels"][2], seed=w["stream_seed"],
+                           min_vertices=w["template_vertices"][0], max_vertices=w["template_vertices"][1],
+                           min_density=w["density"][0], max_density=w["density"][1])
 
 
-def make_graph(w):
-    import pattenmatching_sharedmemory_gb300 as pm
+def reference_sample(stream):
+    """The seeded 1 % sample both arms time on the CPU: requests 0, 100, ..."""
+    return [(i, stream[i]) for i in range(0, len(stream), C4["reference_sample_stride"])]
 
-    kind, n, s, seed = w["labels"]
-    return pm.Graph.rmat(w["scale"], w["ef"], 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels(kind, n, s, seed)
+
+def c4_config(args, vertices, entries):
+    w = C4
+    return {"workload": w["name"],
+            "graph": f"undirected rmat scale {w['scale']} ef {w['ef']} a/b/c {w['abc']} seed {w['graph_seed']}",
+            "vertices": vertices, "csr_entries": entries,
+            "labels": "32 labels, Zipf(1.2), seed 1",
+            "stream": f"{w['stream']} seeded templates (seed {w['stream_seed']}), 3-10 vertices, density 0.3-0.6, "
+                      "labels from the graph's label distribution (repeats allowed)",
+            "request": "PruneJuice pruning pipeline (LCC0, LCC fixpoints, CC/PC/TDS); counting: see c1_stream",
+            "budget_ms": args.budget_ms, "reference_budget_ms": args.reference_budget_ms,
+            "requests_per_step": args.requests_per_step, "slots": args.slots,
+            "reference_sample": f"requests i % {w['reference_sample_stride']} == 0 of the stream, one per step",
+            "l2": "inputs larger than L2 (2.1 GB CSR resident; no flush needed)",
+            "parallelism": "replicas (one per GPU)"}
 
 
 def measured_peaks():
@@ -98,18 +123,6 @@ def measured_peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
-
-
-def profile_traffic(kernel: str):
-    """dram bytes per launch recorded from an ncu capture (profiles/*.md)."""
-    for f in (ROOT / "profiles").glob("*.md"):
-        for line in f.read_text().splitlines():
-            if line.startswith(f"traffic_bytes_per_launch[{kernel}]:"):
-                try:
-                    return float(line.split(":", 1)[1].split()[0])
-                except ValueError:
-                    return None
-    return None
 
 
 class ClockSampler:
@@ -187,6 +200,8 @@ def word_bytes(k: int) -> int:
 
 
 def pct(xs, q):
+    if not xs:
+        return None
     xs = sorted(xs)
     return xs[min(len(xs) - 1, int(round(q * (len(xs) - 1))))]
 
@@ -200,15 +215,31 @@ def lcc_pass_bytes(listed: int, edges_eliminated: int, k: int) -> float:
     return listed * (4 + 0.125 + 0.125 + 1 + (k + 7) // 8) + edges_eliminated / 8
 
 
-def lcc_roofline(scale: int, device: int):
-    """LCC passes on a CSR larger than L2: algorithmic bytes / step time."""
-    import pattenmatching_sharedmemory_gb300 as pm
-    from pattenmatching_sharedmemory_gb300 import templates as T
+def walker_bytes(hops: int, tested: int, k: int) -> float:
+    """Algorithmic bytes of walker work: 16 B of CSR offsets per hop; per
+    tested CSR entry 4 B neighbour id, 1/8 B edge bit, 1/8 B active bit and
+    ceil(k/8) B of the neighbour's roles."""
+    return hops * 16 + tested * (4 + 0.25 + (k + 7) // 8)
 
-    g = pm.Graph.rmat(scale, 16, 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels("zipf", 16, 1.0, 1)
-    g.to_device(device)
+
+def outcome_summary(results, pm):
+    """Counts by status and latency percentiles (all requests / completed)."""
+    ok = [r for r in results if r.status == pm.PM_SUCCESS]
+    to = [r for r in results if r.status == pm.PM_E_TIMEOUT]
+    other = [r for r in results if r.status not in (pm.PM_SUCCESS, pm.PM_E_TIMEOUT)]
+    lat_all = [r.latency_ms for r in results]
+    lat_ok = [r.latency_ms for r in ok]
+    return {"requests": len(results), "completed": len(ok), "timed_out": len(to), "failed": len(other),
+            "failed_statuses": sorted({int(r.status) for r in other}),
+            "latency_ms_p50": pct(lat_all, 0.5), "latency_ms_p99": pct(lat_all, 0.99),
+            "completed_latency_ms_p50": pct(lat_ok, 0.5), "completed_latency_ms_p99": pct(lat_ok, 0.99)}
+
+
+def lcc_roofline(g, pm, T, device):
+    """LCC passes of the two-cycle template on a CSR larger than L2."""
+    k = 6
     q = pm.Query(g, pattern=T.two_cycles_sharing_edge([0, 1, 2, 3, 4, 5]))
-    wb = word_bytes(6)
+    wb = word_bytes(k)
     passes = []
     row = 0
     while True:
@@ -217,7 +248,7 @@ def lcc_roofline(scale: int, device: int):
         listed, gathered = q.step_walk_stats(row)
         row += 1
         if name == "LCC":
-            passes.append((rec.step_ms, lcc_pass_bytes(listed, rec.results.edge_eliminated, 6), listed, gathered,
+            passes.append((rec.step_ms, lcc_pass_bytes(listed, rec.results.edge_eliminated, k), listed, gathered,
                            listed / 8 + gathered * (4 + wb)))
             if rec.results.vertex_eliminated == 0 and rec.results.edge_eliminated == 0:
                 break
@@ -229,22 +260,21 @@ def lcc_roofline(scale: int, device: int):
     by = sum(p[1] for p in passes)
     touched = sum(p[4] for p in passes)
     achieved = by / (ms / 1e3) / 1e9 if ms else None
-    out = {"bound": "hbm", "kernel": "lcc sweep (k_lcc_check x2 + sweep 2)", "graph": f"rmat scale {scale} ef 16",
-           "csr_entries": g.edge_count, "passes": len(passes), "ms_per_pass": ms / max(1, len(passes)),
-           "pass_ms": [round(p[0], 3) for p in passes], "listed_per_pass": [p[2] for p in passes],
-           "gathered_per_pass": [p[3] for p in passes],
-           "bytes": "per checked-list entry 4 + 1/8 + 1/8 + 1 + ceil(k/8) B, + 1/8 B per eliminated entry",
-           "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
-           "frac": achieved / peak if achieved else None,
-           "achieved_touched": touched / (ms / 1e3) / 1e9 if ms else None,
-           "touched_bytes": "1/8 B per listed entry (live-target bit) + (4 + W) B per gathered entry",
-           "traffic": profile_traffic("lcc")}
-    g.close()
-    return out
+    return {"bound": "hbm", "kernel": "lcc sweep (k_lcc_check x2 + sweep 2)", "graph": "the served graph (rmat 24)",
+            "template": "two 4-cycles sharing an edge, labels 0..5", "csr_entries": g.edge_count,
+            "passes": len(passes), "ms_per_pass": ms / max(1, len(passes)),
+            "pass_ms": [round(p[0], 3) for p in passes], "listed_per_pass": [p[2] for p in passes],
+            "gathered_per_pass": [p[3] for p in passes],
+            "bytes": "per checked-list entry 4 + 1/8 + 1/8 + 1 + ceil(k/8) B, + 1/8 B per eliminated entry",
+            "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None,
+            "achieved_touched": touched / (ms / 1e3) / 1e9 if ms else None,
+            "touched_bytes": "1/8 B per listed entry (live-target bit) + (4 + W) B per gathered entry",
+            "traffic": None}
 
 
-def poisson_stream(g, pm, tmpls, rate_qps: float, duration_s: float, slots: int, seed: int):
-    """Requests drawn from `tmpls` arriving as a Poisson process at
+def poisson_stream(g, pm, tmpls, rate_qps: float, duration_s: float, slots: int, seed: int, prune_only=False):
+    """Requests drawn in order from `tmpls` arriving as a Poisson process at
     `rate_qps` for `duration_s` into one server; every arrival is admitted as
     slots and memory free up.  Reports the completed rate and the per-request
     latency (submit to result) percentiles."""
@@ -253,12 +283,13 @@ def poisson_stream(g, pm, tmpls, rate_qps: float, duration_s: float, slots: int,
     rng = random.Random(seed)
     with pm.Server(g, slots=slots) as srv:
         for t in tmpls[:slots]:  # warm the slots (streams, captured loops)
-            tk = srv.submit(t)
+            tk = srv.submit(t) if not prune_only else srv.submit(t, prune_only=True)
             srv.wait(tk)
             srv.release(tk)
         tickets = []
         t0 = time.perf_counter()
         next_t = t0
+        i = 0
         while True:
             now = time.perf_counter()
             if now - t0 >= duration_s:
@@ -266,309 +297,411 @@ def poisson_stream(g, pm, tmpls, rate_qps: float, duration_s: float, slots: int,
             if now < next_t:
                 time.sleep(min(next_t - now, 0.001))
                 continue
-            tickets.append(srv.submit(tmpls[rng.randrange(len(tmpls))]))
+            tm = tmpls[i % len(tmpls)]
+            i += 1
+            tickets.append(srv.submit(tm) if not prune_only else srv.submit(tm, prune_only=True))
             next_t += rng.expovariate(rate_qps)
         results = [srv.wait(t) for t in tickets]
         t1 = time.perf_counter()
         for t in tickets:
             srv.release(t)
-    lat = [r.latency_ms for r in results]
-    bad = sum(1 for r in results if r.status != pm.PM_SUCCESS)
-    return {"offered_qps": rate_qps, "requests": len(tickets), "failed": bad,
-            "completed_qps": len(tickets) / (t1 - t0) if t1 > t0 else None,
-            "latency_ms_p50": pct(lat, 0.5) if lat else None, "latency_ms_p99": pct(lat, 0.99) if lat else None}
+    out = {"offered_qps": rate_qps, "seconds": t1 - t0}
+    out.update(outcome_summary(results, pm))
+    out["completed_qps"] = out["completed"] / (t1 - t0) if t1 > t0 else None
+    return out
 
 
-def small_stream(g, args, pm, torch):
-    """Served vs one-at-a-time on a stream of small requests (35 triangles)."""
-    tm = small_templates()
-    reps = max(1, args.steps)
-    served_lat, seq_lat = [], []
-    counts = None
-    # One long-lived server, warmed up once, serves every timed burst.
-    with pm.Server(g, slots=args.slots) as srv:
-        for _ in range(max(1, args.warmup)):
-            [srv.wait(srv.submit(t)) for t in tm]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            rs = [srv.wait(x) for x in [srv.submit(t) for t in tm]]
-            served_lat += [r.latency_ms for r in rs]
-            counts = [int(r.match_count) for r in rs]
-        torch.cuda.synchronize()
-        served = len(tm) * reps / (time.perf_counter() - t0)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        seq_counts = []
-        for t in tm:
-            t1 = time.perf_counter()
-            q = pm.Query(g, pattern=t)
-            q.run()
-            seq_counts.append(q.match_count)
-            q.close()
-            seq_lat.append((time.perf_counter() - t1) * 1e3)
-    torch.cuda.synchronize()
-    seq = len(tm) * reps / (time.perf_counter() - t0)
-    if seq_counts != counts:
-        raise RuntimeError("small stream: served and one-at-a-time counts differ")
-    return {"templates": "35 triangles over labels 0..4 (repeats allowed)", "requests_per_step": len(tm),
-            "served": served, "one_at_a_time": seq, "unit": "queries/s", "speedup": served / seq,
-            "latency_ms_p50": pct(served_lat, 0.5), "latency_ms_p99": pct(served_lat, 0.99),
-            "one_at_a_time_latency_ms_p50": pct(seq_lat, 0.5), "one_at_a_time_latency_ms_p99": pct(seq_lat, 0.99)}
+# ---- the served workload on the GPU -----------------------------------------
+
+def serve_burst(srv, pm, tmpls, prune_only=True):
+    tickets = [srv.submit(t, prune_only=prune_only) for t in tmpls]
+    results = [srv.wait(t) for t in tickets]
+    for t in tickets:
+        srv.release(t)
+    return results
 
 
-def run_gb300(args, w, rank, world):
+def one_at_a_time(g, pm, tmpls, prune_only=True):
+    """Requests run back to back through pm_query_prune (or pm_query_run);
+    returns (seconds, statuses, latencies, per-class ms, per-class bytes)."""
     import torch
 
-    import pattenmatching_sharedmemory_gb300 as pm
+    statuses, lat = [], []
+    cls_ms, cls_bytes = {}, {}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for tm in tmpls:
+        t1 = time.perf_counter()
+        q = pm.Query(g, pattern=tm)
+        try:
+            recs = q.prune() if prune_only else q.run()
+            statuses.append(pm.PM_SUCCESS)
+            for i, r in enumerate(recs[:-1]):
+                c = kernel_class(pm.STEP_NAMES[r.step])
+                cls_ms[c] = cls_ms.get(c, 0.0) + r.step_ms
+                scanned, hops = q.step_walk_stats(i)
+                if c in ("walk", "enumerate"):
+                    cls_bytes[c] = cls_bytes.get(c, 0.0) + walker_bytes(hops, scanned, tm.n)
+                elif c == "lcc" and pm.STEP_NAMES[r.step] == "LCC":
+                    cls_bytes[c] = cls_bytes.get(c, 0.0) + lcc_pass_bytes(scanned, r.results.edge_eliminated, tm.n)
+        except pm.PmError as e:
+            statuses.append(e.code)
+        q.close()
+        lat.append((time.perf_counter() - t1) * 1e3)
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, statuses, lat, cls_ms, cls_bytes
+
+
+def run_c4(args, rank, world, pm, T):
+    import torch
 
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
-    pm._check(pm.lib.pm_set_lcc_graph(args.lcc_graph))
-    g = make_graph(w)
+    w = C4
+    kind, n_labels, s, lseed = w["labels"]
+    t_gen = time.perf_counter()
+    g = pm.Graph.rmat(w["scale"], w["ef"], *w["abc"], seed=w["graph_seed"], permute=True)
+    g.assign_labels(kind, n_labels, s, lseed)
     g.to_device(device)
-    tmpls = stream_templates()
-    n = len(tmpls)
-    # Autotuner (outside the timed region): degree classes and enumeration
-    # settings timed on probes of both streams, fastest kept in force.
-    t_tune = time.perf_counter()
-    tuned = pm.autotune(g, tmpls + small_templates(), max_per_group=4)
-    tuned["seconds"] = round(time.perf_counter() - t_tune, 2)
-    k_word = 1  # ceil(k/8) B of neighbour roles for the 4-vertex templates
+    gen_s = time.perf_counter() - t_gen
+    stream = c4_stream(T)
+    B = args.requests_per_step
+    pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
 
-    def serve_burst(srv, export=False):
-        tickets = [srv.submit(t, export_state=export) for t in tmpls]
-        results = [srv.wait(t) for t in tickets]
-        states = [srv.export(t) for t in tickets] if export else None
-        rows = [srv.records(t) for t in tickets] if export else None
-        for t in tickets:
-            srv.release(t)
-        bad = [r.status for r in results if r.status != pm.PM_SUCCESS]
-        if bad:
-            raise RuntimeError(f"served requests failed: {bad}")
-        return results, states, rows
-
-    def serve_stream(graph, export=False):
-        with pm.Server(graph, slots=args.slots) as srv:
-            return serve_burst(srv, export)
-
-    # The served measurement uses one long-lived server (created and warmed
-    # up outside the timed region), as a serving process would.
     server = pm.Server(g, slots=args.slots)
-    for _ in range(args.warmup):
-        serve_burst(server)
+    tail = len(stream) - B * args.warmup
+    for i in range(args.warmup):  # warm-up on the stream's tail
+        serve_burst(server, pm, stream[tail + i * B: tail + (i + 1) * B])
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = int(pm.lib.pm_kernel_launches())
-    # The CSR (7.3 MB) fits in the 129 MB L2: every timed step is preceded,
-    # outside its timed interval, by a 512 MB write that flushes L2.
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{device}")
-    served_s = 0.0
-    served_lat = []
-    counts = None
+    served_s, step_s = 0.0, []
+    results = []
     with ClockSampler(device) as clocks:
-        for _ in range(args.steps):
-            flush.fill_(1)
+        for i in range(args.steps):
+            lo = (i * B) % len(stream)
+            batch = stream[lo:lo + B]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            results, _, _ = serve_burst(server)
+            rs = serve_burst(server, pm, batch)
             torch.cuda.synchronize()
-            served_s += time.perf_counter() - t0
-            served_lat += [r.latency_ms for r in results]
-            counts = [int(r.match_count) for r in results]
+            dt = time.perf_counter() - t0
+            served_s += dt
+            step_s.append(dt)
+            results += rs
     launches = int(pm.lib.pm_kernel_launches()) - launches0
-    server.close()
+    served = outcome_summary(results, pm)
     served_max = max_over_ranks(served_s, world, f"cuda:{device}")
+    completed_qps = replica_throughput(served["completed"], world, served_max)
 
-    # One at a time: the same stream through pm_query_run, back to back.
-    seq_s = 0.0
-    seq_lat = []
-    per_class_ms, per_class_bytes, per_class_launch = {}, {}, {}
-    seq_counts = []
-    for _ in range(max(1, args.steps // 2)):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        seq_counts = []
-        t0 = time.perf_counter()
-        for tm in tmpls:
-            t1 = time.perf_counter()
-            q = pm.Query(g, pattern=tm)
-            recs = q.run()
-            seq_lat.append((time.perf_counter() - t1) * 1e3)
-            seq_counts.append(q.match_count)
-            for i, r in enumerate(recs[:-1]):
-                c = kernel_class(pm.STEP_NAMES[r.step])
-                per_class_ms[c] = per_class_ms.get(c, 0.0) + r.step_ms
-                per_class_launch[c] = per_class_launch.get(c, 0) + 1
-                scanned, hops = q.step_walk_stats(i)
-                if c in ("walk", "enumerate"):
-                    b = hops * 16 + scanned * (4 + 0.25 + k_word)
-                    per_class_bytes[c] = per_class_bytes.get(c, 0.0) + b
-            q.close()
-        torch.cuda.synchronize()
-        seq_s += time.perf_counter() - t0
-    seq_steps = max(1, args.steps // 2)
-    del flush
-    if seq_counts != counts:
-        raise RuntimeError("served and one-at-a-time match counts differ")
+    # One at a time vs served on the same requests (the first of step 0).
+    same = stream[:args.same_requests]
+    seq_s, seq_st, seq_lat, cls_ms, cls_bytes = one_at_a_time(g, pm, same)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    same_served = serve_burst(server, pm, same)
+    torch.cuda.synchronize()
+    same_served_s = time.perf_counter() - t0
+    seq_done = sum(1 for x in seq_st if x == pm.PM_SUCCESS)
+    same_done = sum(1 for r in same_served if r.status == pm.PM_SUCCESS)
+    server.close()
 
-    # e2e: host buffers through the C ABI, results read back.
+    # Poisson arrivals at 50 % and 90 % of the served request rate.
+    req_rate = len(results) / served_s
+    poisson = []
+    try:
+        for j, f in enumerate((0.5, 0.9)):
+            start = (args.steps * B + j * 997) % len(stream)
+            seq = stream[start:] + stream[:start]
+            poisson.append(poisson_stream(g, pm, seq, f * req_rate, args.poisson_seconds, args.slots,
+                                          seed=11 + j, prune_only=True))
+    except Exception as e:  # noqa: BLE001  (extra figures; the main line stands)
+        poisson = {"error": f"{type(e).__name__}: {e}"}
+
+    # e2e: the CSR from pinned host memory through pm_graph_from_csr each
+    # step, then the step's requests through the server, rows read back.
     off, adj, lab = g.host_csr()
     pin_off = torch.from_numpy(off.copy()).pin_memory()
     pin_adj = torch.from_numpy(adj.copy()).pin_memory()
     pin_lab = torch.from_numpy(lab.copy()).pin_memory()
-    h2d = pin_off.numel() * 8 + pin_adj.numel() * 4 + pin_lab.numel() * 8 + sum(
-        t.offsets.nbytes + t.adj.nbytes + t.labels.nbytes for t in tmpls)
-    d2h = n * (g.vertex_count * (8 + 1) + g.edge_count)
+    e2e_steps = max(1, args.e2e_steps)
+    e2e_done, h2d, d2h = 0, 0, 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps)):
+    for i in range(e2e_steps):
+        batch = stream[(i * B) % len(stream):(i * B) % len(stream) + B]
         ge = pm.Graph.from_csr(pin_off.numpy(), pin_adj.numpy(), pin_lab.numpy(), device=device)
-        _, states, rows = serve_stream(ge, export=True)
-        d2h_rows = sum(len(r) for r in rows) * 80
+        with pm.Server(ge, slots=args.slots) as srv:
+            tickets = [srv.submit(t, prune_only=True) for t in batch]
+            rs = [srv.wait(t) for t in tickets]
+            rows = [srv.records(t) if r.status == pm.PM_SUCCESS else [] for t, r in zip(tickets, rs)]
+            for t in tickets:
+                srv.release(t)
         ge.close()
+        e2e_done += sum(1 for r in rs if r.status == pm.PM_SUCCESS)
+        h2d += pin_off.numel() * 8 + pin_adj.numel() * 4 + pin_lab.numel() * 8 + sum(
+            t.offsets.nbytes + t.adj.nbytes + t.labels.nbytes for t in batch)
+        d2h += sum(len(r) for r in rows) * 80 + len(rs) * 64
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_qps = replica_throughput(n * max(1, args.steps), world, max_over_ranks(e2e_s, world, f"cuda:{device}"))
+    e2e_qps = replica_throughput(e2e_done, world, max_over_ranks(e2e_s, world, f"cuda:{device}"))
 
-    dom = max(per_class_ms, key=per_class_ms.get)
     peak, peak_kind = measured_peaks()
-    achieved = None
-    if dom in per_class_bytes and per_class_ms[dom] > 0:
-        achieved = per_class_bytes[dom] / (per_class_ms[dom] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_source": peak_kind,
-                "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": profile_traffic(dom),
-                "steps_timed": per_class_launch.get(dom, 0),
-                "kernel_ms_per_query": per_class_ms[dom] / (n * seq_steps),
-                "note": "one query alone; latency-bound depth-first walk; bytes are the per-hop algorithmic bytes"}
-    qps = replica_throughput(n * args.steps, world, served_max)
-    seq_qps = n * seq_steps / seq_s
+    dom = max(cls_ms, key=cls_ms.get) if cls_ms else "lcc"
+    achieved = cls_bytes.get(dom, 0.0) / (cls_ms[dom] / 1e3) / 1e9 if cls_ms.get(dom) else None
+    roofline = {"bound": "hbm", "kernel": {"walk": "k_walk (CC/PC/TDS)", "lcc": "LCC sweeps",
+                                           "enumerate": "k_enumerate"}.get(dom, dom),
+                "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None,
+                "device_ms_by_class": {k: round(v, 3) for k, v in cls_ms.items()},
+                "requests": len(same),
+                "note": "requests run one at a time; walker bytes per hop and tested entry (latency-bound "
+                        "depth-first walks); ncu DRAM traffic of the same kernels is in profiles/"}
+    seq_qps = seq_done / seq_s if seq_s else None
+    same_qps = same_done / same_served_s if same_served_s else None
     out = {
-        "metric": "queries/s served (continuous batching) vs one-at-a-time, full PruneJuice pipeline per query",
-        "value": qps, "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": served_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32/u64 integer and bitwise",
-        "data": "synthetic (seeded RMAT + labels; reference datasets absent)",
-        "config": {"workload": w["name"], "graph": f"rmat scale {w['scale']} ef {w['ef']}",
-                   "vertices": g.vertex_count, "csr_entries": g.edge_count, "labels": list(w["labels"]),
-                   "templates": "15 distinct-label 4-cycles over labels 0..4", "requests_per_step": n,
-                   "slots": args.slots, "arrival": "all requests of a step submitted at once",
-                   "server": "one long-lived server across the timed steps (e2e: one per step, new graph upload)",
-                   "autotuned": tuned,
-                   "lcc_fixpoint": ("one CUDA graph launch per fixpoint (conditional WHILE node over a pass)"
-                                    if args.lcc_graph else "host-driven, one launch sequence per pass"),
-                   "match_counts": counts, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every timed step (512 MB write outside the timed interval)"},
-        "latency_ms": {"p50": pct(served_lat, 0.5), "p99": pct(served_lat, 0.99)},
-        "one_at_a_time": {"value": seq_qps, "unit": "queries/s", "latency_ms_p50": pct(seq_lat, 0.5),
-                          "latency_ms_p99": pct(seq_lat, 0.99)},
-        "speedup_vs_one_at_a_time": qps / world / seq_qps,
-        "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h + d2h_rows},
+        "metric": METRIC, "value": completed_qps, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": served_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 integer and bitwise",
+        "data": "synthetic (seeded RMAT + Zipf labels + seeded template stream; reference datasets absent)",
+        "config": c4_config(args, g.vertex_count, g.edge_count),
+        "served": dict(served, requests_per_s=replica_throughput(len(results), world, served_max),
+                       step_seconds_p50=pct(step_s, 0.5), step_seconds_max=max(step_s)),
+        "latency_ms": {"p50": served["latency_ms_p50"], "p99": served["latency_ms_p99"],
+                       "completed_p50": served["completed_latency_ms_p50"],
+                       "completed_p99": served["completed_latency_ms_p99"]},
+        "one_at_a_time": {"value": seq_qps, "unit": "queries/s", "requests": len(same), "completed": seq_done,
+                          "timed_out": sum(1 for x in seq_st if x == pm.PM_E_TIMEOUT), "seconds": seq_s,
+                          "latency_ms_p50": pct(seq_lat, 0.5), "latency_ms_p99": pct(seq_lat, 0.99)},
+        "served_same_requests": {"value": same_qps, "unit": "queries/s", "requests": len(same),
+                                 "completed": same_done, "seconds": same_served_s,
+                                 "timed_out": sum(1 for r in same_served if r.status == pm.PM_E_TIMEOUT)},
+        "speedup_vs_one_at_a_time": (same_qps / seq_qps) if seq_qps and same_qps else None,
+        "poisson": poisson,
+        "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps, "completed": e2e_done,
+                "includes": "pm_graph_from_csr upload of the 2.1 GB CSR from pinned host memory per step"},
         "roofline": roofline,
-        "per_class_ms_per_query": {k: v / (n * seq_steps) for k, v in per_class_ms.items()},
         "clocks": clocks.summary(),
         "gpu_launches": launches,
+        "graph_generation_s": gen_s,
     }
-    out["small_stream"] = small_stream(g, args, pm, torch)
-    # Poisson arrivals of the same 15 templates at 50 % and 90 % of the burst
-    # capacity measured above (extra figures: a failure here is reported, the
-    # main line stands).
-    try:
-        out["poisson"] = [poisson_stream(g, pm, tmpls, f * qps / world, 4.0, args.slots, seed=11 + i)
-                          for i, f in enumerate((0.5, 0.9))]
-    except Exception as e:  # noqa: BLE001
-        out["poisson"] = {"error": f"{type(e).__name__}: {e}"}
-    if args.lcc_scale:
-        out["lcc_roofline"] = lcc_roofline(args.lcc_scale, device)
-    return out, g, tmpls
+    if args.lcc_roofline:
+        out["lcc_roofline"] = lcc_roofline(g, pm, T, device)
+    pm._check(pm.lib.pm_set_query_budget_ms(0.0))
+    return out, g, stream
 
 
-def cpu_estimate(g, tmpls, stride, threads):
-    """Oracle timing sample of the stream: per template, LCC-type steps in
-    full, CC/PC/TDS/ENUMERATION sources sampled 1/stride and scaled up.
-    Returns (seconds for the whole stream, info)."""
+def run_c1_stream(args, pm, T):
+    """The RMAT-16 stream of the 15 distinct-label 4-cycles, full pipeline
+    including exact ENUMERATION (6.2e7-8.4e7 matches each): served burst vs
+    one at a time, autotuned."""
+    import itertools
+
+    import torch
+
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    g = pm.Graph.rmat(16, 16, 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels("uniform", 5, 1.0, 1)
+    g.to_device(device)
+    tmpls = []
+    for a, b, c, d in itertools.combinations(range(5), 4):
+        for order in ([a, b, c, d], [a, b, d, c], [a, c, b, d]):
+            tmpls.append(T.cycle(order))
+    tuned = pm.autotune(g, tmpls, max_per_group=4)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+    reps = max(1, args.c1_steps)
+    with pm.Server(g, slots=8) as srv:
+        serve_burst(srv, pm, tmpls, prune_only=False)
+        served_s, lat, counts = 0.0, [], None
+        for _ in range(reps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rs = serve_burst(srv, pm, tmpls, prune_only=False)
+            torch.cuda.synchronize()
+            served_s += time.perf_counter() - t0
+            lat += [r.latency_ms for r in rs]
+            counts = [int(r.match_count) for r in rs]
+            if any(r.status != pm.PM_SUCCESS for r in rs):
+                raise RuntimeError("c1 stream: a request failed")
+    flush.fill_(1)
+    seq_s, st, seq_lat, cls_ms, cls_bytes = one_at_a_time(g, pm, tmpls, prune_only=False)
+    del flush
+    g.close()
+    n = len(tmpls)
+    peak, _ = measured_peaks()
+    enum_gbs = cls_bytes.get("enumerate", 0) / (cls_ms["enumerate"] / 1e3) / 1e9 if cls_ms.get("enumerate") else None
+    return {"workload": C1["name"], "graph": "rmat scale 16 ef 16, 5 uniform labels",
+            "templates": "15 distinct-label 4-cycles over labels 0..4, full pipeline with exact ENUMERATION",
+            "served": n * reps / served_s, "one_at_a_time": n / seq_s, "unit": "queries/s",
+            "speedup": (n * reps / served_s) / (n / seq_s), "latency_ms_p50": pct(lat, 0.5),
+            "latency_ms_p99": pct(lat, 0.99), "one_at_a_time_latency_ms_p50": pct(seq_lat, 0.5),
+            "match_counts": counts, "device_ms_per_query": {k: v / n for k, v in cls_ms.items()},
+            "enumerate_gbs": enum_gbs, "enumerate_frac": enum_gbs / peak if enum_gbs else None,
+            "autotuned": tuned, "l2": "flushed before every timed burst (512 MB write)"}
+
+
+# ---- the CPU side (oracle restatement) --------------------------------------
+
+def cpu_sample_run(off, adj, lab, sample, threads, budget_ms):
+    """Whole requests of the sample on the host cores, each with the
+    reference budget; returns per-request (index, outcome, seconds)."""
     from oracle import oracle
 
-    off, adj, lab = g.host_csr()
-    t0 = time.perf_counter()
-    est_ms = 0.0
-    for tm in tmpls:
-        r = oracle.run(off, adj, lab, tm.offsets, tm.adj, tm.labels, threads=threads, sample_stride=stride)
-        for row, ms in zip(r.rows, r.timings):
-            est_ms += ms * (stride if row[0] in ("CC", "PC", "TDS", "ENUMERATION") else 1)
-    return est_ms / 1e3, {"sample_wall_s": time.perf_counter() - t0, "stride": stride}
+    out = []
+    for i, p in sample:
+        t0 = time.perf_counter()
+        try:
+            oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=threads, nlcc_threads=threads,
+                          stop_before_enumeration=True, deadline_ms=budget_ms, want_state=False)
+            outcome = "completed"
+        except oracle.OracleTimeout:
+            outcome = "timed_out"
+        out.append((i, outcome, time.perf_counter() - t0))
+    return out
 
 
-def cpu_line(v, threads, stride, info, n):
-    return {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-            "sample": f"oracle restatement, {threads} threads, all {n} templates of the stream; "
-                      f"CC/PC/TDS/ENUMERATION sources sampled 1/{stride} and scaled x{stride}, LCC steps in "
-                      f"full; {info.get('sample_wall_s', 0):.1f} s per sampled stream"}
+def cpu_line(runs, threads, budget_ms, kind_note):
+    done = sum(1 for r in runs if r[1] == "completed")
+    secs = sum(r[2] for r in runs)
+    return {"value": done / secs if secs else 0.0, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"oracle restatement of the reference pipeline, {threads} threads, whole requests "
+                      f"{[r[0] for r in runs]} of the stream, budget {budget_ms:.0f} ms each (timeouts count "
+                      f"their time, not a completion); {done} of {len(runs)} completed in {secs:.1f} s; {kind_note}",
+            "requests": [{"request": r[0], "outcome": r[1], "seconds": round(r[2], 3)} for r in runs]}
+
+
+def run_reference(args):
+    """The reference arm: the oracle restatement on the host cores, one whole
+    request of the seeded 1 % sample per step, on a graph generated by the
+    oracle library; no GPU library is loaded."""
+    from oracle import oracle
+
+    T = templates_module()
+    threads = os.cpu_count() or 1
+    w = C4
+    kind, n_labels, s, lseed = w["labels"]
+    g = oracle.HostGraph(w["scale"], w["ef"], *w["abc"], seed=w["graph_seed"], permute=True, label_kind=kind,
+                         n_labels=n_labels, zipf_s=s, label_seed=lseed)
+    sample = reference_sample(c4_stream(T))
+    # Warm-up steps: the first sampled requests with a short budget.
+    cpu_sample_run(g.offsets, g.adj, g.labels, sample[:args.warmup], threads, min(1000.0, args.reference_budget_ms))
+    runs = []
+    for i in range(args.steps):
+        runs += cpu_sample_run(g.offsets, g.adj, g.labels, [sample[i % len(sample)]], threads,
+                               args.reference_budget_ms)
+    line = cpu_line(runs, threads, args.reference_budget_ms, "one request per step")
+    secs = sum(r[2] for r in runs)
+    out = {"impl": "reference", "metric": METRIC, "value": line["value"], "unit": "queries/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / max(1, args.steps) * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 integer and bitwise",
+           "data": "synthetic (seeded RMAT + Zipf labels + seeded template stream; reference datasets absent)",
+           "config": c4_config(args, g.vertex_count, g.edge_count), "cpu_baseline": line,
+           "e2e": {"value": line["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ---- single fixed cases for profiling ----------------------------------------
+
+def run_case(args):
+    """Small fixed cases for ncu: c1 (RMAT 16 4-cycle, full pipeline, N
+    queries), lcc (LCC0 and the LCC fixpoint of the two-cycle template on
+    RMAT --scale, 16 Zipf labels), c4 (the first --queries requests of the
+    served stream on RMAT --scale, pruning only).  One line per step."""
+    import pattenmatching_sharedmemory_gb300 as pm
+    from pattenmatching_sharedmemory_gb300 import templates as T
+
+    if args.case == "c1":
+        g = pm.Graph.rmat(16, 16, seed=1).assign_labels("uniform", 5, 1.0, 1).to_device(0)
+        for _ in range(args.queries):
+            q = pm.Query(g, pattern=T.cycle([0, 1, 2, 3]))
+            for r in q.run():
+                print(pm.STEP_NAMES[r.step], f"{r.step_ms:.3f} ms", r.results.enumeration)
+            q.close()
+        return
+    if args.case == "lcc":
+        g = pm.Graph.rmat(args.scale, 16, seed=1).assign_labels("zipf", 16, 1.0, 1).to_device(0)
+        q = pm.Query(g, pattern=T.two_cycles_sharing_edge([0, 1, 2, 3, 4, 5]))
+        row = 0
+        while True:
+            rec, fin = q.step()
+            name = pm.STEP_NAMES[rec.step]
+            listed, gathered = q.step_walk_stats(row)
+            row += 1
+            print(name, f"{rec.step_ms:.3f} ms", rec.results.vertex_eliminated, rec.results.edge_eliminated,
+                  f"listed={listed} gathered={gathered} active_v={rec.active_vertex}")
+            if (name == "LCC" and rec.results.vertex_eliminated == 0 and rec.results.edge_eliminated == 0) or fin:
+                break
+        return
+    kind, n_labels, s, lseed = C4["labels"]
+    g = pm.Graph.rmat(args.scale, 16, seed=1).assign_labels(kind, n_labels, s, lseed).to_device(0)
+    pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    for p in c4_stream(T)[:args.queries]:
+        q = pm.Query(g, pattern=p)
+        try:
+            rows = q.prune()
+            print(p.n, "ok", [(pm.STEP_NAMES[r.step], round(r.step_ms, 3)) for r in rows][:12])
+        except pm.PmError as e:
+            print(p.n, "error", e.code)
+        q.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--slots", type=int, default=8)
-    ap.add_argument("--lcc-scale", type=int, default=22)
-    ap.add_argument("--sample-stride", type=int, default=0)
+    ap.add_argument("--slots", type=int, default=16)
+    ap.add_argument("--requests-per-step", type=int, default=64)
+    ap.add_argument("--budget-ms", type=float, default=1000.0, help="per-request budget on the GPU")
+    ap.add_argument("--reference-budget-ms", type=float, default=6000.0, help="per-request budget on the CPU")
+    ap.add_argument("--same-requests", type=int, default=32)
+    ap.add_argument("--poisson-seconds", type=float, default=8.0)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--c1-steps", type=int, default=3)
+    ap.add_argument("--cpu-requests", type=int, default=2)
+    ap.add_argument("--lcc-roofline", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lcc-graph", type=int, default=1, choices=[0, 1],
-                    help="run each LCC fixpoint as one CUDA graph (1) or one host-driven launch sequence per pass (0)")
+    ap.add_argument("--no-c1", action="store_true")
+    ap.add_argument("--case", choices=["c1", "lcc", "c4"], default=None)
+    ap.add_argument("--queries", type=int, default=1)
+    ap.add_argument("--scale", type=int, default=22)
     args = ap.parse_args()
-    w = WORKLOAD
-    stride = args.sample_stride or w["sample_stride"]
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
-    threads = os.cpu_count() or 1
 
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        g = make_graph(w)  # host-only graph generation
-        tmpls = stream_templates()
-        n = len(tmpls)
-        stride = args.sample_stride or w["reference_stride"]
-        # Size the sample so the whole K + W run stays within ~3 minutes.
-        _, probe = cpu_estimate(g, tmpls, stride, threads)
-        target = max(1.0, 150.0 / max(1, args.steps + args.warmup))
-        if probe["sample_wall_s"] > target:
-            stride = int(stride * (probe["sample_wall_s"] / target + 1))
-        for _ in range(args.warmup):
-            cpu_estimate(g, tmpls, stride, threads)
-        times, info = [], {}
-        for _ in range(args.steps):
-            sec, info = cpu_estimate(g, tmpls, stride, threads)
-            times.append(sec)
-        per_stream = statistics.mean(times)
-        v = n / per_stream
-        out = {"impl": "reference",
-               "metric": "queries/s served (continuous batching) vs one-at-a-time, full PruneJuice pipeline per query",
-               "value": v, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": per_stream * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "u32/u64 integer and bitwise", "data": "synthetic (seeded RMAT + labels)",
-               "config": {"workload": w["name"], "graph": f"rmat scale {w['scale']} ef {w['ef']}",
-                          "templates": "15 distinct-label 4-cycles over labels 0..4", "requests_per_step": n},
-               "cpu_baseline": cpu_line(v, threads, stride, info, n),
-               "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(out))
+    if args.case:
+        run_case(args)
         return
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import pattenmatching_sharedmemory_gb300 as pm
+    from pattenmatching_sharedmemory_gb300 import templates as T
 
     if world > 1:
         import torch
 
         torch.distributed.init_process_group("nccl")
-    out, g, tmpls = run_gb300(args, w, rank, world)
+    out, g, stream = run_c4(args, rank, world, pm, T)
     if rank == 0:
+        if not args.no_c1:
+            try:
+                out["c1_stream"] = run_c1_stream(args, pm, T)
+            except Exception as e:  # noqa: BLE001  (extra figures; the main line stands)
+                out["c1_stream"] = {"error": f"{type(e).__name__}: {e}"}
         if not args.no_cpu_baseline:
-            sec, info = cpu_estimate(g, tmpls, stride, threads)
-            out["cpu_baseline"] = cpu_line(len(tmpls) / sec, threads, stride, info, len(tmpls))
+            threads = os.cpu_count() or 1
+            off, adj, lab = g.host_csr()
+            runs = cpu_sample_run(off, adj, lab, reference_sample(stream)[:args.cpu_requests], threads,
+                                  args.reference_budget_ms)
+            out["cpu_baseline"] = cpu_line(runs, threads, args.reference_budget_ms, "bounded sample")
         print(json.dumps(out))
+    g.close()
     if world > 1:
         import torch
 

@@ -155,6 +155,15 @@ pm_status_t pm_query_step(pm_query* q, pm_step_record* record, int* finished);
 pm_status_t pm_query_run(pm_query* q, pm_step_record* records, int32_t cap,
                          int32_t* n_records);
 
+/* The pruning half of the run loop: runPatternMatching
+ * (multiple_label_cpu.cc:113-184) stopped where MultipleLabelStep::
+ * getNextStep would enter ENUMERATION (multiple_label_step.cc:46-57), or at
+ * the iteration cap.  The last row written names the step that would run
+ * next (ENUMERATION), as the reference's final logResults row does.  A
+ * later pm_query_run continues from there (ENUMERATION and END). */
+pm_status_t pm_query_prune(pm_query* q, pm_step_record* records, int32_t cap,
+                           int32_t* n_records);
+
 /* Copies the pruned state back to caller-owned host buffers (any may be
  * NULL): candidate role bitmask per vertex (bit p = pattern vertex p, the
  * FixedBitmap<64> of multiple_label_common_cpu.h:49), active flag per CSR
@@ -199,8 +208,11 @@ typedef struct pm_server_config {
   uint64_t memory_budget; /* device bytes for admitted queries; 0 = 90% of free memory */
 } pm_server_config;
 
-/* pm_server_submit flag: keep the final state for pm_server_export. */
+/* pm_server_submit flags: keep the final state for pm_server_export;
+ * run the pruning pipeline only (as pm_query_prune: no ENUMERATION, match
+ * count 0). */
 #define PM_SUBMIT_EXPORT_STATE 1u
+#define PM_SUBMIT_PRUNE_ONLY 2u
 
 typedef struct pm_request_result {
   int32_t status;          /* PM_SUCCESS, or the request's error code */
@@ -246,6 +258,12 @@ pm_status_t pm_server_records(pm_server* s, uint64_t ticket, pm_step_record* rec
 pm_status_t pm_server_export(pm_server* s, uint64_t ticket, uint64_t* cand_masks,
                              uint8_t* edge_active, uint8_t* vertex_active);
 
+/* Cancels a request: a queued one ends at once, a running one before its
+ * next step (the step in flight finishes first); both end with
+ * PM_E_CANCELLED.  A finished request is left as it is.  The ticket stays
+ * valid until pm_server_release. */
+pm_status_t pm_server_cancel(pm_server* s, uint64_t ticket);
+
 /* Forgets a finished request (its rows and state). */
 pm_status_t pm_server_release(pm_server* s, uint64_t ticket);
 
@@ -268,6 +286,33 @@ typedef struct pm_template_csr {
 pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t slots,
                          uint64_t* match_counts, int32_t* statuses);
 
+/* Batched form (no counterpart in the reference, which runs one template per
+ * process, multiple_label_cpu.cc:113-184): the n templates run as one batch
+ * over graph g in lockstep rounds, each on the reference's schedule
+ * (multiple_label_step.cc:30-83).  The LCC0 steps and the LCC fixpoints of
+ * the batch's queries run as shared multi-query launches over per-query work
+ * lists (blocks of different queries walk the same CSR ranges together, so
+ * one HBM read of an adjacency range serves every query); their CC / PC /
+ * TDS / ENUMERATION steps run on per-query streams from a pool of host
+ * threads.  Each query's rows (timing columns aside), match count and state
+ * equal pm_query_run's on its own (pm_query_prune's with
+ * PM_SUBMIT_PRUNE_ONLY in flags).  pm_set_query_budget_ms bounds every query
+ * from the start of the run.  Returns PM_SUCCESS with per-query statuses in
+ * pm_fused_batch_result; the batch keeps every query's state until
+ * pm_fused_batch_destroy. */
+typedef struct pm_fused_batch pm_fused_batch;
+
+pm_status_t pm_fused_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t flags,
+                               pm_fused_batch** out);
+/* Query i's outcome: status, rows, match count, run_ms from the start of the
+ * run to its end, gpu_ms (sum of its step times), device bytes it holds. */
+pm_status_t pm_fused_batch_result(const pm_fused_batch* b, uint32_t i, pm_request_result* result);
+pm_status_t pm_fused_batch_records(const pm_fused_batch* b, uint32_t i, pm_step_record* records, int32_t cap,
+                                   int32_t* n_records);
+pm_status_t pm_fused_batch_export(const pm_fused_batch* b, uint32_t i, uint64_t* cand_masks,
+                                  uint8_t* edge_active, uint8_t* vertex_active);
+void pm_fused_batch_destroy(pm_fused_batch* b);
+
 /* Allocation-free ENUMERATION.  No counterpart in the reference: it serves
  * callers that cannot allocate device memory (code running inside a host
  * framework that owns every device allocation through its own pool or arena,
@@ -288,10 +333,15 @@ pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t
  * __device__ array that every GPU loading this library holds until the
  * process exits.  The first call on a device (with that device current)
  * resolves the array's address with cudaGetSymbolAddress; make that first
- * call before any stream capture begins.  Every call reuses the array and
- * clears what must start at zero; calls that overlap on the GPU (other
- * streams or host threads at the same time) race on it and must be
- * serialised by the caller.
+ * call before any stream capture begins.  The resolved address is kept for
+ * the life of the process, so a process that resets the device
+ * (cudaDeviceReset) must not call this entry point on it again.  Every call
+ * reuses the array and clears what must start at zero; calls that overlap
+ * on the GPU (other streams or host threads at the same time) race on it
+ * and must be serialised by the caller.  Each call reads the walker's
+ * counters back to the host after every round, to decide whether sources
+ * must be re-run with larger tables, and synchronises `stream` before it
+ * returns.
  *
  * Limits: vertex_count <= 67108864 (PM_E_INVALID_ARG beyond), template of
  * at most 56 vertices (PM_E_PATTERN_TOO_LARGE), PM_E_OOM when one source's

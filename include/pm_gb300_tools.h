@@ -175,10 +175,43 @@ pm_status_t pm_set_pair_tail(int32_t enumeration, int32_t walks);
  * counterpart in the reference. */
 pm_status_t pm_set_enum_second_split(uint32_t entries);
 
-/* Time budget of one CC/PC/TDS or ENUMERATION kernel launch (default
- * 120000 ms).  A walk still running past it stops; the step then fails with
- * PM_E_TIMEOUT and the query's state is no longer meaningful. */
+/* Time budget of one CC/PC/TDS or ENUMERATION step (default 120000 ms):
+ * one absolute deadline, set when the step's first walker warp starts, bounds
+ * every launch and retry round of the step (and each pm_enumerate_noalloc
+ * call as a whole).  A walk still running past it stops; the step then fails
+ * with PM_E_TIMEOUT and the query's state is no longer meaningful.  The
+ * host-side work between launches is not interrupted, so a step can overrun
+ * the budget by that much. */
 pm_status_t pm_set_walk_budget_ms(double ms);
+
+/* Count-memo entries per warp in the first round of pm_enumerate_noalloc
+ * (power of two in [32, 65536], default 2048); each later round, which
+ * re-runs only the sources whose tables overflowed, has 4x more.  Smaller
+ * values make more sources overflow into later rounds; the count is the
+ * same.  Process-wide; set it while no such call runs. */
+pm_status_t pm_set_noalloc_table_entries(uint32_t entries);
+
+/* Rounds run by the calling thread's last pm_enumerate_noalloc call: 1 when
+ * every source fit its first-round tables, more when some were re-run. */
+uint32_t pm_noalloc_last_rounds(void);
+
+/* Wall-clock budget of every whole run: pm_query_run / pm_query_prune,
+ * served requests (from admission) and pm_batch_run templates (0 = none,
+ * the default).  Checked before every step; the remaining time also caps
+ * each walker step's device budget (pm_set_walk_budget_ms), so a request
+ * ends with PM_E_TIMEOUT soon after its budget runs out.  Process-wide. */
+pm_status_t pm_set_query_budget_ms(double ms);
+
+/* Host-side fault injection for tests: the n-th device buffer allocation
+ * the library makes from now on (0 = the next one) fails the way an
+ * out-of-memory cudaMalloc does, so the call in progress returns PM_E_OOM
+ * and frees what it held; -1 turns it off.  Nothing reaches the device.
+ * Process-wide. */
+pm_status_t pm_debug_fail_device_alloc_after(int64_t n);
+
+/* Statistics of a batched run: lockstep rounds, and shared LCC phases
+ * (multi-query LCC0 launches and fused fixpoints) it issued. */
+pm_status_t pm_fused_batch_stats(const pm_fused_batch* b, uint64_t* rounds, uint64_t* shared_lcc_phases);
 
 /* Compiles a template (no device needed) and writes the reference-format
  * constraint dump, as pm_query_dump_constraints does. */

@@ -31,7 +31,15 @@ class _Record(ctypes.Structure):
                 ("total_vertex", ctypes.c_uint64), ("active_edge", ctypes.c_uint64), ("total_edge", ctypes.c_uint64)]
 
 
+class _Options(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("nlcc_threads", ctypes.c_int32),
+                ("stop_before_enumeration", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("sample_stride", ctypes.c_int64), ("enum_sample_stride", ctypes.c_int64),
+                ("deadline_ms", ctypes.c_double)]
+
+
 STEP_NAMES = {0: "START", 1: "END", 2: "LCC0", 3: "LCC", 4: "CC", 5: "PC", 6: "TDS", 7: "ENUMERATION"}
+TIMEOUT = -7
 
 _lib = None
 
@@ -49,6 +57,24 @@ def _load():
                                 ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int64, P(_Record),
                                 ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_uint64), P(ctypes.c_uint8),
                                 P(ctypes.c_uint8)]
+        lib.pmo_run_ex.restype = ctypes.c_int
+        lib.pmo_run_ex.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                   ctypes.c_uint32, P(_Options), P(_Record), ctypes.c_int32, P(ctypes.c_int32),
+                                   P(ctypes.c_uint64), P(ctypes.c_uint8), P(ctypes.c_uint8)]
+        lib.pmo_generate_graph.restype = ctypes.c_int
+        lib.pmo_generate_graph.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64,
+                                           P(ctypes.c_void_p)]
+        lib.pmo_graph_csr.restype = ctypes.c_int
+        lib.pmo_graph_csr.argtypes = [ctypes.c_void_p, P(ctypes.c_uint32), P(ctypes.c_uint64), P(P(ctypes.c_uint64)),
+                                      P(P(ctypes.c_uint32)), P(P(ctypes.c_uint64))]
+        lib.pmo_graph_free.restype = None
+        lib.pmo_graph_free.argtypes = [ctypes.c_void_p]
+        lib.pmo_enumeration_start_role.restype = ctypes.c_int
+        lib.pmo_enumeration_start_role.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                                   ctypes.c_uint32]
         lib.pmo_dump_constraints.restype = ctypes.c_int
         lib.pmo_dump_constraints.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
                                              ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
@@ -108,9 +134,105 @@ def run(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, stop
     return res
 
 
+class OracleTimeout(RuntimeError):
+    """The run passed its wall-clock deadline (run_ex deadline_ms)."""
+
+
+def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, nlcc_threads: int = 1,
+           stop_before_enumeration: bool = False, sample_stride: int = 1, enum_sample_stride: int = 1,
+           deadline_ms: float = 0.0, want_state: bool = True) -> OracleResult:
+    """run() with separate thread counts for the LCC sweeps (deterministic in
+    any order) and for the CC/PC/TDS/ENUMERATION source loops (1 = the
+    canonical order of the alreadyMatched shortcut), an ENUMERATION-only
+    source sample (enum_sample_stride > 1: the count over sources
+    v % stride == 0, pruning unchanged) and a wall-clock deadline (raises
+    OracleTimeout past it)."""
+    lib = _load()
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ad = np.ascontiguousarray(adj, np.uint32)
+    lab = np.ascontiguousarray(labels, np.uint64)
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    V, E, k = len(off) - 1, len(ad), len(po) - 1
+    cap = 1100
+    recs = (_Record * cap)()
+    n = ctypes.c_int32()
+    cand = np.zeros(V, np.uint64) if want_state else None
+    eact = np.zeros(E, np.uint8) if want_state else None
+    vact = np.zeros(V, np.uint8) if want_state else None
+    opt = _Options(threads, nlcc_threads, int(stop_before_enumeration), 0, sample_stride, enum_sample_stride,
+                   deadline_ms)
+    st = lib.pmo_run_ex(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), V, E,
+                        _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k,
+                        ctypes.byref(opt), recs, cap, ctypes.byref(n),
+                        _p(cand, ctypes.c_uint64) if want_state else None,
+                        _p(eact, ctypes.c_uint8) if want_state else None,
+                        _p(vact, ctypes.c_uint8) if want_state else None)
+    if st == TIMEOUT:
+        raise OracleTimeout(f"oracle run passed its {deadline_ms:.0f} ms deadline")
+    if st != 0:
+        raise RuntimeError(f"oracle failed with status {st}")
+    rows = [row_tuple(recs[i]) for i in range(n.value)]
+    res = OracleResult(rows, cand, eact, vact)
+    res.timings = [recs[i].step_ms for i in range(n.value)]
+    return res
+
+
+class HostGraph:
+    """A seeded RMAT graph generated inside the oracle library (the
+    product's generator source compiled in), so a caller gets the bench
+    graph without loading the product library.  offsets / adj / labels are
+    numpy views valid while this object lives."""
+
+    def __init__(self, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+                 seed: int = 1, permute: bool = True, label_kind: str = "uniform", n_labels: int = 5,
+                 zipf_s: float = 1.0, label_seed: int = 1):
+        lib = _load()
+        kind = {"uniform": 0, "zipf": 1, "degree": 2}[label_kind]
+        h = ctypes.c_void_p()
+        st = lib.pmo_generate_graph(scale, edge_factor, a, b, c, seed, int(permute), kind, n_labels, zipf_s,
+                                    label_seed, ctypes.byref(h))
+        if st != 0:
+            raise RuntimeError(f"oracle graph generation failed with status {st}")
+        self._h = h
+        V, E = ctypes.c_uint32(), ctypes.c_uint64()
+        o, a_, l = ctypes.POINTER(ctypes.c_uint64)(), ctypes.POINTER(ctypes.c_uint32)(), \
+            ctypes.POINTER(ctypes.c_uint64)()
+        lib.pmo_graph_csr(h, ctypes.byref(V), ctypes.byref(E), ctypes.byref(o), ctypes.byref(a_), ctypes.byref(l))
+        self.vertex_count, self.edge_count = V.value, E.value
+        self.offsets = np.ctypeslib.as_array(o, shape=(V.value + 1,))
+        self.adj = np.ctypeslib.as_array(a_, shape=(E.value,)) if E.value else np.zeros(0, np.uint32)
+        self.labels = np.ctypeslib.as_array(l, shape=(V.value,)) if V.value else np.zeros(0, np.uint64)
+
+    def close(self):
+        if self._h:
+            _load().pmo_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def row_tuple(r) -> tuple:
     return (STEP_NAMES[r.step], r.vertex_eliminated, r.active_vertex, r.total_vertex, r.edge_eliminated,
             r.active_edge, r.total_edge, r.match_eliminated, r.enumeration)
+
+
+def enumeration_start_role(p_offsets, p_adj, p_labels) -> int:
+    """The template vertex whose holders are ENUMERATION's sources."""
+    lib = _load()
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    r = lib.pmo_enumeration_start_role(_p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64),
+                                       len(po) - 1)
+    if r < 0:
+        raise RuntimeError(f"no enumeration walk (status {r})")
+    return r
 
 
 def dump_constraints(p_offsets, p_adj, p_labels) -> str:

@@ -14,6 +14,7 @@
 // (constraints.cc), itself pinned against the reference's log.totem dumps.
 #include <omp.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstdint>
 #include <cstring>
@@ -22,10 +23,24 @@
 #include <vector>
 
 #include "../pattenmatching_sharedmemory_gb300/csrc/constraints.h"
+#include "../pattenmatching_sharedmemory_gb300/csrc/generators.h"
 
 using namespace pmgb;
 
 namespace {
+
+// Wall-clock limit of one run (bounded CPU-baseline samples): the loops and
+// walks poll it and unwind once it passed; the run then reports a timeout.
+std::atomic<bool> g_expired{false};
+std::chrono::steady_clock::time_point g_deadline;
+bool g_has_deadline = false;
+thread_local uint32_t t_poll = 0;
+inline bool expired() {
+  if (!g_has_deadline) return false;
+  if ((++t_poll & 1023u) == 0 && std::chrono::steady_clock::now() > g_deadline)
+    g_expired.store(true, std::memory_order_relaxed);
+  return g_expired.load(std::memory_order_relaxed);
+}
 
 struct PairHashO {
   size_t operator()(const std::pair<uint32_t, uint32_t>& x) const {
@@ -55,17 +70,20 @@ struct State {
   std::vector<uint8_t> active, modified, scheduled, edge_active;
   std::vector<uint64_t> cand, matched, unmatch;
   uint64_t active_vertices, active_edges;
-  bool parallel;
+  bool parallel;       // LCC0 / LCC sweeps (deterministic in any order)
+  bool nlcc_parallel;  // CC / PC / TDS / ENUMERATION source loops
   int64_t sample_stride = 1;  // timing samples: NLCC / ENUMERATION sources v % stride == 0
+  int64_t enum_stride = 1;    // ENUMERATION only: sources v % enum_stride == 0
   bool sampled(int64_t v) const { return sample_stride <= 1 || v % sample_stride == 0; }
+  bool enum_sampled(int64_t v) const { return sampled(v) && (enum_stride <= 1 || v % enum_stride == 0); }
   void mark_matched(uint32_t v, uint32_t p) {
-    if (parallel)
+    if (nlcc_parallel)
       __atomic_fetch_or(&matched[v], uint64_t(1) << p, __ATOMIC_RELAXED);
     else
       matched[v] |= uint64_t(1) << p;
   }
   bool is_matched(uint32_t v, uint32_t p) const {
-    uint64_t w = parallel ? __atomic_load_n(&matched[v], __ATOMIC_RELAXED) : matched[v];
+    uint64_t w = nlcc_parallel ? __atomic_load_n(&matched[v], __ATOMIC_RELAXED) : matched[v];
     return w >> p & 1;
   }
   bool has(uint32_t v, uint32_t p) const { return cand[v] >> p & 1; }
@@ -139,7 +157,7 @@ Results step_lcc(State& s, const QueryConstraints& qc) {
 #pragma omp parallel for reduction(+ : ee) if (s.parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v] || !s.scheduled[v]) continue;
+    if (!s.active[v] || !s.scheduled[v] || expired()) continue;
     uint64_t nbr_set = 0;
     for (uint32_t p = 0; p < s.k; ++p)
       if (s.has(v, p)) nbr_set |= qc.local[p].neighbor_mask;
@@ -215,6 +233,7 @@ Results step_lcc(State& s, const QueryConstraints& qc) {
 // with the next template vertex id, and never rolled back within one source.
 bool cc_walk(State& s, const CycleConstraint& c, EdgeMemo& memo, uint32_t source, uint32_t cur, size_t start,
              size_t remaining) {
+  if (expired()) return false;
   const size_t L = c.length();
   if (remaining == 1) {
     for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
@@ -249,10 +268,10 @@ bool cc_walk(State& s, const CycleConstraint& c, EdgeMemo& memo, uint32_t source
 Results step_cc(State& s, const CycleConstraint& c) {
   Results r;
   EdgeMemo memo;
-#pragma omp parallel for private(memo) if (s.parallel)
+#pragma omp parallel for private(memo) if (s.nlcc_parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v] || !s.sampled(vi)) continue;
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
     bool changed = false;
     for (size_t pos = 0; pos < c.length(); ++pos) {
       uint32_t role = c.ids[pos];
@@ -273,6 +292,7 @@ Results step_cc(State& s, const CycleConstraint& c) {
 // PC walk (multiple_label_pc_cpu.tpp:12-81).
 bool pc_walk(State& s, const PathConstraint& pc, bool reverse, EdgeMemo& memo, uint32_t source, uint32_t cur,
              size_t remaining) {
+  if (expired()) return false;
   const size_t L = pc.length();
   const size_t cur_pos = reverse ? remaining : (L - remaining - 1);
   const size_t next_pos = reverse ? remaining - 1 : (L - remaining);
@@ -309,10 +329,10 @@ Results step_pc(State& s, const PathConstraint& pc) {
   Results r;
   EdgeMemo memo;
   const size_t L = pc.length();
-#pragma omp parallel for private(memo) if (s.parallel)
+#pragma omp parallel for private(memo) if (s.nlcc_parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v] || !s.sampled(vi)) continue;
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
     if (s.lab[v] != pc.initial_label) continue;
     bool changed = false;
     for (int end = 0; end < 2; ++end) {
@@ -341,6 +361,7 @@ struct TdsMemo {
 
 bool tds_walk(State& s, const Walk& w, TdsMemo& m, uint32_t source, uint32_t cur, size_t pos) {
   if (pos == w.length()) return true;
+  if (expired()) return false;
   const int move = w.moves[pos];
   if (move == kVertexNoStore || move == kVertexStore) {
     const uint32_t cur_role = w.ids[pos - 1];
@@ -397,10 +418,10 @@ bool tds_walk(State& s, const Walk& w, TdsMemo& m, uint32_t source, uint32_t cur
 Results step_tds(State& s, const TemplateConstraint& t) {
   Results r;
   TdsMemo m;
-#pragma omp parallel for private(m) if (s.parallel)
+#pragma omp parallel for private(m) if (s.nlcc_parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v] || !s.sampled(vi)) continue;
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
     bool changed = false;
     for (const auto& kv : t.walks) {
       uint32_t role = kv.first;
@@ -426,6 +447,7 @@ Results step_tds(State& s, const TemplateConstraint& t) {
 // embeddings following the walk; CHECK follows only the first matching entry.
 uint64_t enum_walk(const State& s, const Walk& w, std::vector<uint32_t>& history, uint32_t cur, size_t pos) {
   if (pos == w.length()) return 1;
+  if (expired()) return 0;
   const int move = w.moves[pos];
   uint64_t count = 0;
   if (move == kVertexNoStore || move == kVertexStore) {
@@ -469,10 +491,10 @@ Results step_enumeration(State& s, const TemplateConstraint& t) {
   const Walk& w = first->second;
   uint64_t total = 0;
   std::vector<uint32_t> history;
-#pragma omp parallel for reduction(+ : total) private(history) schedule(dynamic, 1000) if (s.parallel)
+#pragma omp parallel for reduction(+ : total) private(history) schedule(dynamic, 1000) if (s.nlcc_parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
     uint32_t v = static_cast<uint32_t>(vi);
-    if (!s.active[v] || !s.sampled(vi)) continue;
+    if (!s.active[v] || !s.enum_sampled(vi) || expired()) continue;
     if (!s.has(v, start_role)) continue;
     history.clear();
     history.push_back(v);
@@ -499,10 +521,48 @@ extern "C" {
 // Outputs (any may be NULL): step records (as pm_step_record), final role
 // sets, per-CSR-entry and per-vertex active flags, the matched count.
 // Returns 0, or a negative status on bad input.
+// Options of pmo_run_ex beyond pmo_run's.
+struct pmo_options {
+  int32_t threads;                  // LCC0 / LCC threads (deterministic in any order)
+  int32_t nlcc_threads;             // CC / PC / TDS / ENUMERATION threads; 1 = canonical order
+  int32_t stop_before_enumeration;  // 1 = end when the schedule reaches ENUMERATION
+  int32_t pad;
+  int64_t sample_stride;            // >1: CC/PC/TDS/ENUMERATION sources v % stride == 0 only
+  int64_t enum_sample_stride;       // >1: ENUMERATION sources v % stride == 0 only (a
+                                    // per-source sampled count; pruning unchanged)
+  double deadline_ms;               // >0: wall-clock limit; the run returns -7 past it
+};
+
+int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+               const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k,
+               const pmo_options* opt, pm_step_record* records, int32_t cap, int32_t* n_records, uint64_t* cand_out,
+               uint8_t* edge_active_out, uint8_t* vertex_active_out);
+
 int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
             const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k, int threads,
             int stop_before_enumeration, int64_t sample_stride, pm_step_record* records, int32_t cap,
             int32_t* n_records, uint64_t* cand_out, uint8_t* edge_active_out, uint8_t* vertex_active_out) {
+  pmo_options o{};
+  o.threads = threads;
+  o.nlcc_threads = threads;
+  o.stop_before_enumeration = stop_before_enumeration;
+  o.sample_stride = sample_stride;
+  return pmo_run_ex(off, adj, lab, V, E, p_off, p_adj, p_lab, k, &o, records, cap, n_records, cand_out,
+                    edge_active_out, vertex_active_out);
+}
+
+int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+               const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k,
+               const pmo_options* opt, pm_step_record* records, int32_t cap, int32_t* n_records, uint64_t* cand_out,
+               uint8_t* edge_active_out, uint8_t* vertex_active_out) {
+  const int threads = opt->threads;
+  const int stop_before_enumeration = opt->stop_before_enumeration;
+  const int64_t sample_stride = opt->sample_stride;
+  g_expired.store(false);
+  g_has_deadline = opt->deadline_ms > 0;
+  if (g_has_deadline)
+    g_deadline = std::chrono::steady_clock::now() +
+                 std::chrono::microseconds(static_cast<int64_t>(opt->deadline_ms * 1000.0));
   try {
     PatternGraph pg;
     pg.n = k;
@@ -518,8 +578,11 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
     s.E = E;
     s.k = k;
     s.parallel = threads > 1;
+    s.nlcc_parallel = opt->nlcc_threads > 1;
     s.sample_stride = sample_stride;
-    if (threads >= 1) omp_set_num_threads(threads);
+    s.enum_stride = opt->enum_sample_stride;
+    const int max_threads = threads > opt->nlcc_threads ? threads : opt->nlcc_threads;
+    if (max_threads >= 1) omp_set_num_threads(max_threads);
     s.active.assign(V, 1);
     s.modified.assign(V, 0);
     s.scheduled.assign(V, 1);
@@ -592,6 +655,10 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
         default: res = Results(); break;
       }
       double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (g_expired.load()) {
+        g_has_deadline = false;
+        return PM_E_TIMEOUT;
+      }
       emit(step + PM_STEP_START, ms, res);
       int next = advance(step);
       finished = (step == ENUM);
@@ -599,17 +666,69 @@ int pmo_run(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint3
       ++iteration;
     }
     // Final row: logResults(iteration, true) with cleared results and the
-    // name of the step the machine would run next (END after ENUMERATION).
-    emit(finished || step == ENUM ? PM_STEP_END : step, 0.0, Results());
+    // name of the step the machine would run next (END after ENUMERATION,
+    // multiple_label_cpu.cc:177-181; ENUMERATION when the run stopped before
+    // it).
+    emit(finished ? PM_STEP_END : step + PM_STEP_START, 0.0, Results());
     if (n_records) *n_records = n;
     if (cand_out) memcpy(cand_out, s.cand.data(), sizeof(uint64_t) * V);
     if (edge_active_out) memcpy(edge_active_out, s.edge_active.data(), E);
     if (vertex_active_out) memcpy(vertex_active_out, s.active.data(), V);
+    g_has_deadline = false;
+    return 0;
+  } catch (const PmError& e) {
+    g_has_deadline = false;
+    return e.code;
+  }
+}
+
+// The start role of the enumeration walk (walkMap.cbegin()->first,
+// multiple_label_enumeration_cpu.tpp:126-174): ENUMERATION's sources are the
+// active vertices holding it.
+int pmo_enumeration_start_role(const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k) {
+  try {
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    const QueryConstraints qc = compile_constraints(pg);
+    if (qc.enumeration.walks.empty()) return -1;
+    return static_cast<int>(qc.enumeration.walks.cbegin()->first);
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
+// Seeded synthetic graph for callers that must not load the product library
+// (the CPU baseline's graph): the same generator source, compiled into this
+// library.  Returns an owning handle; pmo_graph_csr exposes its CSR.
+int pmo_generate_graph(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed,
+                       int32_t permute, int32_t label_kind, uint32_t n_labels, double zipf_s, uint64_t label_seed,
+                       void** out) {
+  try {
+    auto* g = new HostGraph(generate_rmat(scale, edge_factor, a, b, c, seed, permute != 0));
+    if (n_labels) assign_labels(*g, label_kind, n_labels, zipf_s, label_seed);
+    else g->labels.assign(g->vertex_count, 0);
+    *out = g;
     return 0;
   } catch (const PmError& e) {
     return e.code;
   }
 }
+
+int pmo_graph_csr(void* h, uint32_t* V, uint64_t* E, const uint64_t** off, const uint32_t** adj,
+                  const uint64_t** lab) {
+  auto* g = static_cast<HostGraph*>(h);
+  *V = g->vertex_count;
+  *E = g->edge_count;
+  *off = g->offsets.data();
+  *adj = g->adj.data();
+  *lab = g->labels.data();
+  return 0;
+}
+
+void pmo_graph_free(void* h) { delete static_cast<HostGraph*>(h); }
 
 // Compiles a template and returns the reference-format constraint dump
 // (for pinning the template compiler against log.totem).

@@ -10,7 +10,6 @@ from __future__ import annotations
 
 import ctypes
 import os
-from dataclasses import dataclass
 from pathlib import Path
 
 import numpy as np
@@ -91,6 +90,7 @@ class TuneResult(ctypes.Structure):
 
 
 PM_SUBMIT_EXPORT_STATE = 1
+PM_SUBMIT_PRUNE_ONLY = 2
 
 
 class StepRecord(ctypes.Structure):
@@ -144,6 +144,10 @@ def _load_library() -> ctypes.CDLL:
                                                        P(ctypes.c_size_t)]),
         "pm_query_step": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), P(ctypes.c_int)]),
         "pm_query_run": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), ctypes.c_int32, P(ctypes.c_int32)]),
+        "pm_query_prune": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), ctypes.c_int32, P(ctypes.c_int32)]),
+        "pm_set_query_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
+        "pm_debug_fail_device_alloc_after": (ctypes.c_int32, [ctypes.c_int64]),
+        "pm_server_cancel": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64]),
         "pm_query_export": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u8p, c_u8p]),
         "pm_query_write_outputs": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p]),
         "pm_query_match_count": (ctypes.c_int32, [ctypes.c_void_p, c_u64p]),
@@ -157,6 +161,8 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_set_noalloc_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
+        "pm_noalloc_last_rounds": (ctypes.c_uint32, []),
         "pm_set_lcc_graph": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_enum_tail_swap": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_walk_tail_swap": (ctypes.c_int32, [ctypes.c_uint32]),
@@ -186,6 +192,14 @@ def _load_library() -> ctypes.CDLL:
         "pm_server_destroy": (None, [ctypes.c_void_p]),
         "pm_batch_run": (ctypes.c_int32, [ctypes.c_void_p, P(TemplateCsr), ctypes.c_uint32, ctypes.c_uint32,
                                           c_u64p, P(ctypes.c_int32)]),
+        "pm_fused_batch_run": (ctypes.c_int32, [ctypes.c_void_p, P(TemplateCsr), ctypes.c_uint32, ctypes.c_uint32,
+                                                P(ctypes.c_void_p)]),
+        "pm_fused_batch_result": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, P(RequestResult)]),
+        "pm_fused_batch_records": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, P(StepRecord), ctypes.c_int32,
+                                                    P(ctypes.c_int32)]),
+        "pm_fused_batch_export": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, c_u64p, c_u8p, c_u8p]),
+        "pm_fused_batch_stats": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u64p]),
+        "pm_fused_batch_destroy": (None, [ctypes.c_void_p]),
         # Device buffers (d_*) and the stream are passed as raw addresses.
         "pm_enumerate_noalloc": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                                   ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
@@ -200,6 +214,8 @@ def _load_library() -> ctypes.CDLL:
 
 
 lib = _load_library()
+
+from .templates import Pattern  # noqa: E402  (pure numpy; re-exported here)
 
 
 def _check(status: int) -> None:
@@ -309,56 +325,6 @@ class Graph:
             pass
 
 
-@dataclass
-class Pattern:
-    """A template graph in CSR form with per-vertex labels."""
-
-    offsets: np.ndarray
-    adj: np.ndarray
-    labels: np.ndarray
-
-    @property
-    def n(self) -> int:
-        return len(self.offsets) - 1
-
-    @classmethod
-    def from_edges(cls, n: int, edges, labels) -> "Pattern":
-        """Undirected template from an edge list (both directions stored, sorted)."""
-        nbrs = [set() for _ in range(n)]
-        for u, v in edges:
-            nbrs[u].add(v)
-            nbrs[v].add(u)
-        off = np.zeros(n + 1, np.uint64)
-        adj = []
-        for u in range(n):
-            adj.extend(sorted(nbrs[u]))
-            off[u + 1] = len(adj)
-        return cls(off, np.asarray(adj, np.uint32), np.asarray(labels, np.uint64))
-
-    def dump_constraints(self) -> str:
-        """Reference-format constraint dump (log.totem) of this template."""
-        off = np.ascontiguousarray(self.offsets, np.uint64)
-        adj = np.ascontiguousarray(self.adj, np.uint32)
-        lab = np.ascontiguousarray(self.labels, np.uint64)
-        args = (_ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32), _ptr(lab, ctypes.c_uint64), self.n, len(adj))
-        need = ctypes.c_size_t()
-        _check(lib.pm_template_dump_constraints(*args, None, 0, ctypes.byref(need)))
-        buf = ctypes.create_string_buffer(need.value)
-        _check(lib.pm_template_dump_constraints(*args, buf, need.value, None))
-        return buf.value.decode()
-
-    def write(self, directory) -> None:
-        """Writes pattern_edge (TOTEM text) and pattern_vertex_data."""
-        d = Path(directory)
-        d.mkdir(parents=True, exist_ok=True)
-        lines = [f"#Nodes:{self.n}", f"#Edges:{len(self.adj)}", "#Undirected"]
-        for u in range(self.n):
-            for e in range(int(self.offsets[u]), int(self.offsets[u + 1])):
-                lines.append(f"{u} {int(self.adj[e])}")
-        (d / "pattern_edge").write_text("\n".join(lines) + "\n")
-        (d / "pattern_vertex_data").write_text("".join(f"{u} {int(self.labels[u])}\n" for u in range(self.n)))
-
-
 class Query:
     """One template over a resident graph: constraint generation, GPU pruning
     steps and the reference's step schedule (MultipleLabelCpu)."""
@@ -401,6 +367,14 @@ class Query:
         recs = (StepRecord * cap)()
         n = ctypes.c_int32()
         _check(lib.pm_query_run(self._h, recs, cap, ctypes.byref(n)))
+        return [recs[i] for i in range(min(n.value, cap))]
+
+    def prune(self) -> list[StepRecord]:
+        """pm_query_prune: the pipeline up to (not including) ENUMERATION."""
+        cap = 1100
+        recs = (StepRecord * cap)()
+        n = ctypes.c_int32()
+        _check(lib.pm_query_prune(self._h, recs, cap, ctypes.byref(n)))
         return [recs[i] for i in range(min(n.value, cap))]
 
     def export(self):
@@ -468,12 +442,12 @@ class Server:
         cfg = ServerConfig(slots, memory_budget)
         _check(lib.pm_server_create(graph._h, ctypes.byref(cfg), ctypes.byref(self._h)))
 
-    def submit(self, pattern: Pattern, export_state: bool = False) -> int:
+    def submit(self, pattern: Pattern, export_state: bool = False, prune_only: bool = False) -> int:
         off = np.ascontiguousarray(pattern.offsets, np.uint64)
         adj = np.ascontiguousarray(pattern.adj, np.uint32)
         lab = np.ascontiguousarray(pattern.labels, np.uint64)
         t = ctypes.c_uint64()
-        flags = PM_SUBMIT_EXPORT_STATE if export_state else 0
+        flags = (PM_SUBMIT_EXPORT_STATE if export_state else 0) | (PM_SUBMIT_PRUNE_ONLY if prune_only else 0)
         _check(lib.pm_server_submit(self._h, _ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32),
                                     _ptr(lab, ctypes.c_uint64), pattern.n, len(adj), flags, ctypes.byref(t)))
         return t.value
@@ -504,6 +478,11 @@ class Server:
         _check(lib.pm_server_export(self._h, ticket, _ptr(cand, ctypes.c_uint64), _ptr(eact, ctypes.c_uint8),
                                     _ptr(vact, ctypes.c_uint8)))
         return cand, eact, vact
+
+    def cancel(self, ticket: int) -> None:
+        """pm_server_cancel: a queued request ends at once, a running one
+        before its next step (status PM_E_CANCELLED)."""
+        _check(lib.pm_server_cancel(self._h, ticket))
 
     def release(self, ticket: int) -> None:
         _check(lib.pm_server_release(self._h, ticket))
@@ -570,6 +549,64 @@ def batch_run(graph: Graph, patterns, slots: int = 4):
     _check(lib.pm_batch_run(graph._h, arr, len(patterns), slots, _ptr(counts, ctypes.c_uint64),
                             _ptr(statuses, ctypes.c_int32)))
     return counts, statuses
+
+
+class FusedBatch:
+    """pm_fused_batch_run: the templates run as one batch in lockstep rounds,
+    their LCC work in shared multi-query launches; per-query results equal
+    each template run on its own."""
+
+    def __init__(self, graph: Graph, patterns, prune_only: bool = False):
+        self.graph = graph
+        self.n = len(patterns)
+        arr, keep = _template_array(patterns)
+        self._h = ctypes.c_void_p()
+        flags = PM_SUBMIT_PRUNE_ONLY if prune_only else 0
+        _check(lib.pm_fused_batch_run(graph._h, arr, len(patterns), flags, ctypes.byref(self._h)))
+        del keep
+
+    def result(self, i: int) -> RequestResult:
+        r = RequestResult()
+        _check(lib.pm_fused_batch_result(self._h, i, ctypes.byref(r)))
+        return r
+
+    def records(self, i: int) -> list[StepRecord]:
+        n = ctypes.c_int32()
+        _check(lib.pm_fused_batch_records(self._h, i, None, 0, ctypes.byref(n)))
+        recs = (StepRecord * max(n.value, 1))()
+        _check(lib.pm_fused_batch_records(self._h, i, recs, n.value, ctypes.byref(n)))
+        return [recs[j] for j in range(n.value)]
+
+    def export(self, i: int):
+        V, E = self.graph.vertex_count, self.graph.edge_count
+        cand = np.zeros(V, np.uint64)
+        eact = np.zeros(E, np.uint8)
+        vact = np.zeros(V, np.uint8)
+        _check(lib.pm_fused_batch_export(self._h, i, _ptr(cand, ctypes.c_uint64), _ptr(eact, ctypes.c_uint8),
+                                         _ptr(vact, ctypes.c_uint8)))
+        return cand, eact, vact
+
+    def stats(self) -> dict:
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib.pm_fused_batch_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return {"rounds": a.value, "shared_lcc_phases": b.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib.pm_fused_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def version() -> str:

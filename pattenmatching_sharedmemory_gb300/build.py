@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels_lcc.cu", "kernels_walk.cu"]
 CC_SOURCES = ["totem_io.cc", "constraints.cc", "walk_compile.cc", "generators.cc", "engine.cc", "server.cc",
-              "autotune.cc", "capi.cc"]
+              "fused_batch.cc", "autotune.cc", "capi.cc"]
 
 
 def _sources() -> tuple[list[Path], list[Path]]:

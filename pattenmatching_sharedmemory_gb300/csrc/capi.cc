@@ -7,6 +7,7 @@
 #include "engine.h"
 #include "generators.h"
 #include "autotune.h"
+#include "fused_batch.h"
 #include "server.h"
 #include "totem_io.h"
 
@@ -18,6 +19,10 @@ struct pm_graph {
 struct pm_query {
   QueryImpl impl;
 };
+struct pm_fused_batch {
+  std::unique_ptr<pmgb::FusedBatch> impl;
+};
+
 struct pm_server {
   std::unique_ptr<Server> impl;
 };
@@ -203,6 +208,9 @@ pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets, con
                                      const uint64_t* p_labels, uint32_t p_vertex_count, uint64_t p_edge_count,
                                      pm_query** out) {
   PM_REQUIRE(g && p_offsets && out, "null argument");
+  PM_REQUIRE(p_offsets[0] == 0, "pattern offsets must start at 0");
+  for (uint32_t i = 0; i < p_vertex_count; ++i)
+    PM_REQUIRE(p_offsets[i] <= p_offsets[i + 1], "pattern offsets must not decrease");
   PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
   for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
   return guarded([&]() -> pm_status_t {
@@ -262,6 +270,38 @@ pm_status_t pm_query_run(pm_query* q, pm_step_record* records, int32_t cap, int3
     if (n_records) *n_records = n;
     return PM_SUCCESS;
   });
+}
+
+pm_status_t pm_query_prune(pm_query* q, pm_step_record* records, int32_t cap, int32_t* n_records) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    struct Restore {
+      QueryImpl& q;
+      ~Restore() { q.stop_before_enumeration = false; }
+    } restore{q->impl};
+    q->impl.stop_before_enumeration = true;
+    q->impl.run_all();
+    int32_t n = 0;
+    for (const auto& r : q->impl.records) {
+      if (records && n < cap) records[n] = r;
+      ++n;
+    }
+    if (records && n < cap) records[n] = q->impl.final_record();
+    ++n;
+    if (n_records) *n_records = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_debug_fail_device_alloc_after(int64_t n) {
+  set_fail_alloc_after(n);
+  return PM_SUCCESS;
+}
+
+pm_status_t pm_set_query_budget_ms(double ms) {
+  PM_REQUIRE(ms >= 0, "budget must not be negative");
+  set_query_budget_ms(ms);
+  return PM_SUCCESS;
 }
 
 pm_status_t pm_query_export(const pm_query* q, uint64_t* cand_masks, uint8_t* edge_active, uint8_t* vertex_active) {
@@ -349,6 +389,15 @@ pm_status_t pm_set_enum_table_entries(uint32_t entries) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_noalloc_table_entries(uint32_t entries) {
+  PM_REQUIRE(entries >= 32 && entries <= (1u << 16) && !(entries & (entries - 1)),
+             "entries must be a power of two in [32, 65536]");
+  set_noalloc_table_entries(entries);
+  return PM_SUCCESS;
+}
+
+uint32_t pm_noalloc_last_rounds(void) { return noalloc_last_rounds(); }
+
 pm_status_t pm_set_enum_tail_swap(uint32_t ratio) {
   set_enum_tail_swap(ratio);
   return PM_SUCCESS;
@@ -404,6 +453,9 @@ pm_status_t pm_template_dump_constraints(const uint64_t* p_offsets, const uint32
                                          uint32_t p_vertex_count, uint64_t p_edge_count, char* buf, size_t cap,
                                          size_t* needed) {
   PM_REQUIRE(p_offsets && (p_adj || p_edge_count == 0), "null argument");
+  PM_REQUIRE(p_offsets[0] == 0, "pattern offsets must start at 0");
+  for (uint32_t i = 0; i < p_vertex_count; ++i)
+    PM_REQUIRE(p_offsets[i] <= p_offsets[i + 1], "pattern offsets must not decrease");
   PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
   for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
   return guarded([&]() -> pm_status_t {
@@ -445,6 +497,9 @@ namespace {
 PatternGraph pattern_from_csr(const uint64_t* p_offsets, const uint32_t* p_adj, const uint64_t* p_labels,
                               uint32_t p_vertex_count, uint64_t p_edge_count) {
   if (!p_offsets || (!p_adj && p_edge_count)) throw PmError{PM_E_INVALID_ARG, "null template buffer"};
+  if (p_offsets[0] != 0) throw PmError{PM_E_INVALID_ARG, "pattern offsets must start at 0"};
+  for (uint32_t i = 0; i < p_vertex_count; ++i)
+    if (p_offsets[i] > p_offsets[i + 1]) throw PmError{PM_E_INVALID_ARG, "pattern offsets must not decrease"};
   if (p_offsets[p_vertex_count] != p_edge_count)
     throw PmError{PM_E_INVALID_ARG, "pattern offsets do not end at the edge count"};
   for (uint64_t e = 0; e < p_edge_count; ++e)
@@ -555,6 +610,14 @@ pm_status_t pm_server_export(pm_server* s, uint64_t ticket, uint64_t* cand_masks
     if (cand_masks && !r->cand.empty()) memcpy(cand_masks, r->cand.data(), r->cand.size() * 8);
     if (edge_active && !r->eact.empty()) memcpy(edge_active, r->eact.data(), r->eact.size());
     if (vertex_active && !r->vact.empty()) memcpy(vertex_active, r->vact.data(), r->vact.size());
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_server_cancel(pm_server* s, uint64_t ticket) {
+  PM_REQUIRE(s, "server is NULL");
+  return guarded([&]() -> pm_status_t {
+    s->impl->cancel(ticket);
     return PM_SUCCESS;
   });
 }
@@ -671,6 +734,9 @@ pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_ad
   if (p_vertex_count == 0 || p_vertex_count > 56)
     return fail(PM_E_PATTERN_TOO_LARGE, "pm_enumerate_noalloc: template of " + std::to_string(p_vertex_count) +
                                             " vertices; 1 to 56 supported (56-bit role masks)");
+  PM_REQUIRE(p_offsets[0] == 0, "pattern offsets must start at 0");
+  for (uint32_t i = 0; i < p_vertex_count; ++i)
+    PM_REQUIRE(p_offsets[i] <= p_offsets[i + 1], "pattern offsets must not decrease");
   PM_REQUIRE(p_offsets[p_vertex_count] == p_edge_count, "pattern offsets do not end at the edge count");
   for (uint64_t e = 0; e < p_edge_count; ++e) PM_REQUIRE(p_adj[e] < p_vertex_count, "pattern edge out of range");
   return guarded([&]() -> pm_status_t {
@@ -689,5 +755,86 @@ pm_status_t pm_enumerate_noalloc(const uint64_t* d_offsets, const uint32_t* d_ad
     return PM_SUCCESS;
   });
 }
+
+
+// ---- batched form ---------------------------------------------------------
+pm_status_t pm_fused_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t n, uint32_t flags,
+                               pm_fused_batch** out) {
+  PM_REQUIRE(g && out && (templates || n == 0), "null argument");
+  return guarded([&]() -> pm_status_t {
+    std::vector<PatternGraph> ps;
+    ps.reserve(n);
+    for (uint32_t i = 0; i < n; ++i)
+      ps.push_back(pattern_from_csr(templates[i].offsets, templates[i].adj, templates[i].labels,
+                                    templates[i].vertex_count, templates[i].edge_count));
+    g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    auto* b = new pm_fused_batch();
+    try {
+      b->impl = std::make_unique<FusedBatch>(&g->impl, ps, (flags & PM_SUBMIT_PRUNE_ONLY) != 0);
+      b->impl->run();
+    } catch (...) {
+      delete b;
+      throw;
+    }
+    *out = b;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_fused_batch_result(const pm_fused_batch* b, uint32_t i, pm_request_result* result) {
+  PM_REQUIRE(b && result, "null argument");
+  PM_REQUIRE(i < b->impl->size(), "query index out of range");
+  return guarded([&]() -> pm_status_t {
+    FusedBatchItem& it = b->impl->item(i);
+    *result = pm_request_result{};
+    result->status = it.status;
+    result->n_records = static_cast<int32_t>(it.q->records.size() + 1);
+    result->match_count = it.q->match_count;
+    result->run_ms = it.run_ms;
+    result->latency_ms = it.run_ms;
+    result->gpu_ms = it.q->total_ms;
+    result->charged_bytes = it.q->device_bytes();
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_fused_batch_records(const pm_fused_batch* b, uint32_t i, pm_step_record* records, int32_t cap,
+                                   int32_t* n_records) {
+  PM_REQUIRE(b, "null argument");
+  PM_REQUIRE(i < b->impl->size(), "query index out of range");
+  return guarded([&]() -> pm_status_t {
+    QueryImpl& q = *b->impl->item(i).q;
+    int32_t n = 0;
+    for (const auto& r : q.records) {
+      if (records && n < cap) records[n] = r;
+      ++n;
+    }
+    if (records && n < cap) records[n] = q.final_record();
+    ++n;
+    if (n_records) *n_records = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_fused_batch_export(const pm_fused_batch* b, uint32_t i, uint64_t* cand_masks, uint8_t* edge_active,
+                                  uint8_t* vertex_active) {
+  PM_REQUIRE(b, "null argument");
+  PM_REQUIRE(i < b->impl->size(), "query index out of range");
+  return guarded([&]() -> pm_status_t {
+    FusedBatchItem& it = b->impl->item(i);
+    if (it.status != PM_SUCCESS) return fail(it.status, "query failed: " + it.error);
+    it.q->export_state(cand_masks, edge_active, vertex_active);
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_fused_batch_stats(const pm_fused_batch* b, uint64_t* rounds, uint64_t* shared_lcc_phases) {
+  PM_REQUIRE(b, "null argument");
+  if (rounds) *rounds = b->impl->rounds;
+  if (shared_lcc_phases) *shared_lcc_phases = b->impl->fused_lcc_passes;
+  return PM_SUCCESS;
+}
+
+void pm_fused_batch_destroy(pm_fused_batch* b) { delete b; }
 
 }  // extern "C"

@@ -145,10 +145,15 @@ struct StepCounters {
   unsigned long long scanned;    // walkers: CSR entries tested; LCC: entries of the checked lists
   unsigned long long descents;   // walkers: hops taken (states entered)
   unsigned long long gathered;   // LCC: entries whose neighbour word was read
+  // Walkers: absolute %globaltimer deadline of the step, 0 until the first
+  // warp of the step's first walker launch sets it (now + budget).  Every
+  // later warp, launch and retry round of the step uses the same value, so
+  // the budget bounds the whole step, not each launch or resident wave.
+  unsigned long long deadline_ns;
   unsigned long long modified_total;  // vertices with mod=1 since the last reset
-  unsigned long long pad[3];
+  unsigned long long pad[2];
 };
-constexpr int kStepCounterWords = 12;
+constexpr int kStepCounterWords = 13;
 
 // The LCC fixpoint loop as one CUDA graph (a conditional WHILE node over one
 // LCC pass): the tail of every pass appends its counters as a row, clears the

@@ -32,10 +32,22 @@ void DeviceBuffer::release() {
   bytes = 0;
 }
 
+namespace {
+// Host-side fault injection (pm_debug_fail_device_alloc_after): counts down
+// the library's device allocations; the one that reaches zero fails as an
+// out-of-memory cudaMalloc would.  -1 = off.
+std::atomic<int64_t> g_fail_alloc_countdown{-1};
+}  // namespace
+void set_fail_alloc_after(int64_t n) { g_fail_alloc_countdown.store(n < 0 ? -1 : n); }
+
 void DeviceBuffer::ensure(size_t n) {
   if (n <= bytes && ptr) return;
   release();
   if (n == 0) n = 16;
+  int64_t left = g_fail_alloc_countdown.load();
+  while (left >= 0 && !g_fail_alloc_countdown.compare_exchange_weak(left, left - 1)) {
+  }
+  if (left == 0) throw_cuda(cudaErrorMemoryAllocation, "injected device allocation failure");
   if (ordered)
     PM_CUDA(cudaMallocAsync(&ptr, n, stream));
   else
@@ -408,8 +420,8 @@ void QueryImpl::read_counters() {
   PM_CUDA(cudaMemcpyAsync(h_ctr, d_ctr.ptr, sizeof(StepCounters), cudaMemcpyDeviceToHost, stream));
   PM_CUDA(cudaStreamSynchronize(stream));
   if (h_ctr->error == kDeviceErrorTimeout)
-    throw PmError{PM_E_TIMEOUT, "a walker launch exceeded its time budget of " +
-                                    std::to_string(walk_budget_ns() / 1000000) + " ms"};
+    throw PmError{PM_E_TIMEOUT, "the step's walkers exceeded their time budget of " +
+                                    std::to_string(effective_walk_budget_ns() / 1000000) + " ms"};
   if (h_ctr->error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(h_ctr->error)};
 }
 
@@ -888,6 +900,13 @@ int QueryImpl::advance(int cur) {
 pm_step_record QueryImpl::run_step() {
   if (finished) return final_record();
   const int kind = step;
+  // No vertex holds a role: every step of the reference's schedule finds
+  // nothing (its loops visit active vertices only, and ENUMERATION counts
+  // 0), so the remaining rows are produced without touching the device.
+  if (active_vertices == 0) {
+    append_record(StepResult{}, kind, 0.0, 0, 0);
+    return records.back();
+  }
   if (kind == PM_STEP_CC || kind == PM_STEP_PC || kind == PM_STEP_TDS) reset_modified();
   ensure_hub_acc();
   clear_step_counters();
@@ -1122,6 +1141,152 @@ void QueryImpl::run_lcc_loop(int max_iterations) {
   }
 }
 
+// ---- batched form: many queries per launch ---------------------------------
+namespace {
+// Device copies of the listed queries' pointer blocks and an index list.
+struct BatchPtrs {
+  DeviceBuffer d_qs, d_active, d_out;
+  std::vector<QueryDevPtrs> h_qs;
+  std::vector<uint32_t> h_active;
+  StepCounters* h_out = nullptr;
+  explicit BatchPtrs(cudaStream_t s) {
+    for (DeviceBuffer* b : {&d_qs, &d_active, &d_out}) {
+      b->stream = s;
+      b->ordered = true;
+    }
+  }
+  ~BatchPtrs() {
+    if (h_out) cudaFreeHost(h_out);
+  }
+  void upload(const std::vector<QueryImpl*>& qs, cudaStream_t s) {
+    h_qs.clear();
+    for (QueryImpl* q : qs) h_qs.push_back(q->ptrs());
+    d_qs.ensure(sizeof(QueryDevPtrs) * h_qs.size());
+    d_active.ensure(4 * h_qs.size());
+    d_out.ensure(sizeof(StepCounters) * h_qs.size());
+    PM_CUDA(cudaMallocHost(&h_out, sizeof(StepCounters) * h_qs.size()));
+    PM_CUDA(cudaMemcpyAsync(d_qs.ptr, h_qs.data(), sizeof(QueryDevPtrs) * h_qs.size(), cudaMemcpyHostToDevice, s));
+  }
+  void set_active(const std::vector<uint32_t>& a, cudaStream_t s) {
+    h_active = a;
+    PM_CUDA(cudaMemcpyAsync(d_active.ptr, h_active.data(), 4 * h_active.size(), cudaMemcpyHostToDevice, s));
+  }
+};
+
+// Queries grouped by word type (the multi-query kernels are per type).
+std::vector<std::vector<QueryImpl*>> by_word_kind(const std::vector<QueryImpl*>& qs) {
+  std::vector<std::vector<QueryImpl*>> out;
+  for (QueryImpl* q : qs) {
+    auto it = std::find_if(out.begin(), out.end(), [&](const auto& v) { return v[0]->word_kind == q->word_kind; });
+    if (it == out.end())
+      out.push_back({q});
+    else
+      it->push_back(q);
+  }
+  return out;
+}
+
+void check_batch_counters(const StepCounters& c) {
+  if (c.error) throw PmError{PM_E_DEVICE, "device-side error status " + std::to_string(c.error)};
+}
+}  // namespace
+
+void QueryImpl::lcc0_batch(const std::vector<QueryImpl*>& all, cudaStream_t s) {
+  for (auto& qs : by_word_kind(all)) {
+    const GraphImpl* g = qs[0]->g;
+    for (QueryImpl* q : qs) {
+      if (q->g != g || q->step != PM_STEP_LCC0 || q->finished) throw PmError{PM_FAILURE, "lcc0_batch: bad query"};
+      q->ensure_hub_acc();
+      PM_CUDA(cudaStreamSynchronize(q->stream));
+    }
+    BatchPtrs b(s);
+    b.upload(qs, s);
+    std::vector<uint32_t> active(qs.size());
+    for (uint32_t i = 0; i < active.size(); ++i) active[i] = i;
+    b.set_active(active, s);
+    cudaEvent_t e0, e1;
+    PM_CUDA(cudaEventCreate(&e0));
+    PM_CUDA(cudaEventCreate(&e1));
+    const uint32_t n = static_cast<uint32_t>(qs.size());
+    launch_counters_multi(b.d_qs.as<QueryDevPtrs>(), b.d_active.as<uint32_t>(), n, nullptr, true, s);
+    PM_CUDA(cudaEventRecord(e0, s));
+    launch_lcc0_multi(g->dev(), qs[0]->word_kind, b.d_qs.as<QueryDevPtrs>(), b.d_active.as<uint32_t>(), n, s);
+    PM_CUDA(cudaEventRecord(e1, s));
+    launch_counters_multi(b.d_qs.as<QueryDevPtrs>(), b.d_active.as<uint32_t>(), n, b.d_out.as<StepCounters>(), false,
+                          s);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaMemcpyAsync(b.h_out, b.d_out.ptr, sizeof(StepCounters) * n, cudaMemcpyDeviceToHost, s));
+    PM_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (uint32_t i = 0; i < n; ++i) {
+      check_batch_counters(b.h_out[i]);
+      StepResult r;
+      r.vertex = b.h_out[i].vertex_elim;
+      r.match = b.h_out[i].match_elim;
+      qs[i]->append_record(r, PM_STEP_LCC0, ms, 0, 0);
+    }
+  }
+}
+
+void QueryImpl::lcc_fixpoint_batch(const std::vector<QueryImpl*>& all, cudaStream_t s) {
+  for (auto& qs : by_word_kind(all)) {
+    const GraphImpl* g = qs[0]->g;
+    for (QueryImpl* q : qs) {
+      if (q->g != g || q->step != PM_STEP_LCC || q->finished || q->active_vertices == 0)
+        throw PmError{PM_FAILURE, "lcc_fixpoint_batch: bad query"};
+      q->ensure_hub_acc();
+      PM_CUDA(cudaStreamSynchronize(q->stream));
+    }
+    BatchPtrs b(s);
+    b.upload(qs, s);
+    std::vector<uint32_t> active(qs.size());
+    for (uint32_t i = 0; i < active.size(); ++i) active[i] = i;
+    cudaEvent_t e0, e1;
+    PM_CUDA(cudaEventCreate(&e0));
+    PM_CUDA(cudaEventCreate(&e1));
+    try {
+      while (!active.empty()) {
+        const uint32_t n = static_cast<uint32_t>(active.size());
+        b.set_active(active, s);
+        const QueryDevPtrs* dq = b.d_qs.as<QueryDevPtrs>();
+        const uint32_t* da = b.d_active.as<uint32_t>();
+        launch_counters_multi(dq, da, n, nullptr, true, s);
+        PM_CUDA(cudaEventRecord(e0, s));
+        launch_lcc_pass_multi(g->dev(), qs[0]->word_kind, dq, da, n, s);
+        PM_CUDA(cudaEventRecord(e1, s));
+        launch_counters_multi(dq, da, n, b.d_out.as<StepCounters>(), false, s);
+        PM_CUDA(cudaGetLastError());
+        PM_CUDA(cudaMemcpyAsync(b.h_out, b.d_out.ptr, sizeof(StepCounters) * n, cudaMemcpyDeviceToHost, s));
+        PM_CUDA(cudaStreamSynchronize(s));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        std::vector<uint32_t> next;
+        for (uint32_t j = 0; j < n; ++j) {
+          const StepCounters& c = b.h_out[j];
+          check_batch_counters(c);
+          QueryImpl* q = qs[active[j]];
+          StepResult r;
+          r.vertex = c.vertex_elim;
+          r.edge = c.edge_elim;
+          r.match = c.match_elim;
+          q->append_record(r, PM_STEP_LCC, ms, c.scanned, c.gathered);
+          if (!q->finished && q->step == PM_STEP_LCC && q->active_vertices != 0) next.push_back(active[j]);
+        }
+        active.swap(next);
+      }
+    } catch (...) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+}
+
 double QueryImpl::elapsed_ms() {
   if (!first_recorded) return 0.0;
   PM_CUDA(cudaEventSynchronize(ev1));
@@ -1143,9 +1308,36 @@ pm_step_record QueryImpl::final_record() {
   return rec;
 }
 
+namespace {
+double g_query_budget_ms = 0;
+}  // namespace
+void set_query_budget_ms(double ms) { g_query_budget_ms = ms > 0 ? ms : 0; }
+double query_budget_ms() { return g_query_budget_ms; }
+
+void QueryImpl::check_request() {
+  if (cancel && cancel->load(std::memory_order_relaxed))
+    throw PmError{PM_E_CANCELLED, "request cancelled while running"};
+  if (has_deadline) {
+    const auto left = deadline - std::chrono::steady_clock::now();
+    const int64_t left_ns = std::chrono::duration_cast<std::chrono::nanoseconds>(left).count();
+    if (left_ns <= 0) throw PmError{PM_E_TIMEOUT, "the request's time budget ran out"};
+    set_thread_walk_budget_cap_ns(static_cast<uint64_t>(left_ns));
+  }
+}
+
 void QueryImpl::run_all(int max_iterations) {
+  if (!has_deadline && g_query_budget_ms > 0) {
+    has_deadline = true;
+    deadline = std::chrono::steady_clock::now() +
+               std::chrono::microseconds(static_cast<int64_t>(g_query_budget_ms * 1000.0));
+  }
+  struct CapReset {
+    ~CapReset() { set_thread_walk_budget_cap_ns(0); }
+  } cap_reset;
   while (!finished && iteration < max_iterations) {
-    if (step == PM_STEP_LCC && g_lcc_graph)
+    if (stop_before_enumeration && step == PM_STEP_ENUMERATION) break;
+    check_request();
+    if (step == PM_STEP_LCC && g_lcc_graph && active_vertices != 0)
       run_lcc_loop(max_iterations);
     else
       run_step();

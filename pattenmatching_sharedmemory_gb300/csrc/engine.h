@@ -1,5 +1,7 @@
 // Host engine: resident graph, per-query device state and the step machine.
 #pragma once
+#include <atomic>
+#include <chrono>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -130,6 +132,14 @@ struct QueryImpl {
   bool first_recorded = false;
   double elapsed_ms();
 
+  // Request controls, checked before every step: a deadline (its remaining
+  // time also caps each walker step's device budget), a cancel flag another
+  // thread may set, and a stop before ENUMERATION (pruning only).
+  bool has_deadline = false;
+  std::chrono::steady_clock::time_point deadline{};
+  const std::atomic<bool>* cancel = nullptr;
+  bool stop_before_enumeration = false;
+
   // statistics of the alreadyMatched emulation
   uint64_t exact_resolutions = 0, overflow_retries = 0;
   // per step: walker CSR entries tested and hops taken (0 for LCC steps)
@@ -147,6 +157,20 @@ struct QueryImpl {
   // Runs the current step and advances the machine; returns the row.
   pm_step_record run_step();
   void run_all(int max_iterations = 1000);
+  // Request checks made before every step of a whole run: cancel flag
+  // (PM_E_CANCELLED), deadline (PM_E_TIMEOUT); caps this host thread's
+  // walker budget at the time left.
+  void check_request();
+  // Batched form over queries of one graph, each at a step boundary with
+  // nothing in flight on its stream; `s` carries the fused launches.
+  // lcc0_batch: the LCC0 step of every listed query (all at LCC0), as
+  // multi-query launches.  lcc_fixpoint_batch: every listed query (all at
+  // LCC with active vertices) runs LCC passes until its own fixpoint (or the
+  // iteration cap); each pass of the batch is one multi-query launch
+  // sequence over the queries still iterating.  Rows and state are those of
+  // the queries' own steps.
+  static void lcc0_batch(const std::vector<QueryImpl*>& qs, cudaStream_t s);
+  static void lcc_fixpoint_batch(const std::vector<QueryImpl*>& qs, cudaStream_t s);
   pm_step_record final_record();
 
   void export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact);
@@ -205,6 +229,15 @@ uint32_t enum_table_entries();
 void set_lcc_graph(bool on);
 bool lcc_graph();
 uint64_t next_plan_epoch();
+
+// Fault injection on the host: the n-th device buffer allocation from now on
+// (0 = the next one) fails as an out-of-memory cudaMalloc would; -1 = off.
+void set_fail_alloc_after(int64_t n);
+
+// Wall-clock budget of every whole run (run_all: pm_query_run, served and
+// batched requests), from its start; 0 = none.  Process-wide.
+void set_query_budget_ms(double ms);
+double query_budget_ms();
 
 // Device bytes a query of a k-vertex template holds in its first walk
 // round (state, worklists, first walker pool); the admission charge.

@@ -1,0 +1,165 @@
+// Batched form: lockstep rounds with shared LCC launches (see fused_batch.h).
+#include "fused_batch.h"
+
+#include <algorithm>
+#include <chrono>
+
+namespace pmgb {
+
+FusedBatch::FusedBatch(GraphImpl* g, const std::vector<PatternGraph>& patterns, bool prune_only)
+    : g_(g), prune_only_(prune_only) {
+  if (!g_ || g_->device < 0) throw PmError{PM_E_INVALID_ARG, "the graph is not on a device"};
+  PM_CUDA(cudaSetDevice(g_->device));
+  PM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  items_.resize(patterns.size());
+  try {
+    for (size_t i = 0; i < patterns.size(); ++i) {
+      items_[i].q = std::make_unique<QueryImpl>();
+      items_[i].q->create(g_, patterns[i], nullptr);
+      items_[i].q->stop_before_enumeration = prune_only_;
+    }
+  } catch (...) {
+    items_.clear();
+    cudaStreamDestroy(stream_);
+    throw;
+  }
+  const size_t n_threads = std::min<size_t>(std::max<size_t>(patterns.size(), 1), 16);
+  for (size_t t = 0; t < n_threads; ++t)
+    workers_.emplace_back([this] {
+      if (cudaSetDevice(g_->device) != cudaSuccess) return;
+      uint64_t seen = 0;
+      while (true) {
+        std::function<void()> task;
+        {
+          std::unique_lock<std::mutex> lk(mu_);
+          cv_work_.wait(lk, [&] { return stop_ || (generation_ != seen && next_task_ < tasks_.size()); });
+          if (stop_) return;
+          task = tasks_[next_task_++];
+          if (next_task_ == tasks_.size()) seen = generation_;
+        }
+        task();
+        {
+          std::lock_guard<std::mutex> lk(mu_);
+          ++finished_tasks_;
+        }
+        cv_done_.notify_all();
+      }
+    });
+}
+
+FusedBatch::~FusedBatch() {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    stop_ = true;
+  }
+  cv_work_.notify_all();
+  for (auto& t : workers_) t.join();
+  items_.clear();  // queries free their stream-ordered buffers first
+  if (stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+}
+
+void FusedBatch::parallel_steps(const std::vector<size_t>& idx) {
+  if (idx.empty()) return;
+  std::vector<std::function<void()>> tasks;
+  for (size_t i : idx)
+    tasks.push_back([this, i] {
+      FusedBatchItem& it = items_[i];
+      try {
+        it.q->check_request();
+        it.q->run_step();
+      } catch (const PmError& e) {
+        it.status = e.code;
+        it.error = e.message;
+      } catch (const std::bad_alloc&) {
+        it.status = PM_E_OOM;
+        it.error = "host allocation failed";
+      } catch (const std::exception& e) {
+        it.status = PM_FAILURE;
+        it.error = e.what();
+      }
+      set_thread_walk_budget_cap_ns(0);
+    });
+  std::unique_lock<std::mutex> lk(mu_);
+  tasks_ = std::move(tasks);
+  next_task_ = 0;
+  finished_tasks_ = 0;
+  ++generation_;
+  cv_work_.notify_all();
+  cv_done_.wait(lk, [&] { return finished_tasks_ == tasks_.size(); });
+  tasks_.clear();
+}
+
+void FusedBatch::run() {
+  using Clock = std::chrono::steady_clock;
+  const auto t0 = Clock::now();
+  for (auto& it : items_) {
+    if (query_budget_ms() > 0) {
+      it.q->has_deadline = true;
+      it.q->deadline = t0 + std::chrono::microseconds(static_cast<int64_t>(query_budget_ms() * 1000.0));
+    }
+  }
+  auto mark_done = [&](FusedBatchItem& it) {
+    it.done = true;
+    it.run_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+  };
+  // Runs a shared LCC phase; a failure ends every query it covered.
+  auto shared_phase = [&](const std::vector<size_t>& idx, bool lcc0) {
+    std::vector<size_t> ok;
+    for (size_t i : idx) {
+      try {
+        items_[i].q->check_request();
+        ok.push_back(i);
+      } catch (const PmError& e) {
+        items_[i].status = e.code;
+        items_[i].error = e.message;
+        mark_done(items_[i]);
+      }
+    }
+    set_thread_walk_budget_cap_ns(0);
+    if (ok.empty()) return;
+    std::vector<QueryImpl*> qs;
+    for (size_t i : ok) qs.push_back(items_[i].q.get());
+    try {
+      if (lcc0)
+        QueryImpl::lcc0_batch(qs, stream_);
+      else
+        QueryImpl::lcc_fixpoint_batch(qs, stream_);
+      ++fused_lcc_passes;
+    } catch (const PmError& e) {
+      for (size_t i : ok) {
+        items_[i].status = e.code;
+        items_[i].error = e.message;
+        mark_done(items_[i]);
+      }
+    }
+  };
+  while (true) {
+    std::vector<size_t> at_lcc0, at_lcc, others;
+    for (size_t i = 0; i < items_.size(); ++i) {
+      FusedBatchItem& it = items_[i];
+      if (it.done) continue;
+      QueryImpl& q = *it.q;
+      if (it.status != PM_SUCCESS || q.finished || q.iteration >= 1000 ||
+          (prune_only_ && q.step == PM_STEP_ENUMERATION)) {
+        mark_done(it);
+        continue;
+      }
+      if (q.active_vertices != 0 && q.step == PM_STEP_LCC0)
+        at_lcc0.push_back(i);
+      else if (q.active_vertices != 0 && q.step == PM_STEP_LCC)
+        at_lcc.push_back(i);
+      else
+        others.push_back(i);
+    }
+    if (at_lcc0.empty() && at_lcc.empty() && others.empty()) break;
+    ++rounds;
+    shared_phase(at_lcc0, true);
+    shared_phase(at_lcc, false);
+    parallel_steps(others);
+  }
+}
+
+}  // namespace pmgb

@@ -67,6 +67,17 @@ uint64_t thread_launch_count();
 // Order-preserving compaction of the vertices that hold a role of
 // `start_mask`: wl[i] = i-th such vertex, wl_index[wl[i]] = i, *count = n.
 // block_counts needs ceil(V / 4096) + 1 entries.
+// Batched LCC (many queries of one graph in each launch): queries
+// active[0, nq) of the device array qs, all of word type word_kind.  LCC0 of
+// every listed query; one LCC pass (sweep 1 + sweep 2) of every listed query;
+// their per-step counters cleared (clear) or copied to out[0, nq).
+void launch_lcc0_multi(const DevGraph& g, int word_kind, const QueryDevPtrs* qs, const uint32_t* active, uint32_t nq,
+                       cudaStream_t s);
+void launch_lcc_pass_multi(const DevGraph& g, int word_kind, const QueryDevPtrs* qs, const uint32_t* active,
+                           uint32_t nq, cudaStream_t s);
+void launch_counters_multi(const QueryDevPtrs* qs, const uint32_t* active, uint32_t nq, StepCounters* out, bool clear,
+                           cudaStream_t s);
+
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_mask, uint32_t* wl,
                      uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
 
@@ -76,8 +87,9 @@ enum ItemStatus : uint8_t { kItemSkip = 0, kItemFail = 1, kItemSuccess = 2, kIte
 // StepCounters::error values written by kernels.
 constexpr unsigned long long kDeviceErrorTimeout = 2;
 
-// Time budget of one walker launch (ns of %globaltimer per warp); a warp
-// past it stops, marks its item kItemTimeout and sets kDeviceErrorTimeout.
+// Time budget of one walker step (ns of %globaltimer): the step's first warp
+// fixes the deadline in StepCounters::deadline_ns; a warp past it stops,
+// marks its item kItemTimeout and sets kDeviceErrorTimeout.
 void set_walk_budget_ns(uint64_t ns);
 // ENUMERATION tail step from the cached source's side when the bound
 // vertex's list has at least `ratio` times as many 32-entry chunks as the
@@ -103,6 +115,11 @@ uint32_t enum_second_split();
 void set_walk_tail_swap(uint32_t ratio);
 uint32_t walk_tail_swap();
 uint64_t walk_budget_ns();
+// Per host thread: caps the walker budget of the launches this thread issues
+// (a request's remaining time); 0 = no cap.
+void set_thread_walk_budget_cap_ns(uint64_t ns);
+// The budget this thread's next walker launch gets.
+uint64_t effective_walk_budget_ns();
 
 // Per-warp scratch for the walkers' memo tables.  The edge and hypothesis
 // tables reproduce the reference's memos and must hold every entry (a walk
@@ -201,6 +218,11 @@ void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uin
 // Throws PmError (PM_E_INVALID_ARG above noalloc_max_vertices(), PM_E_OOM
 // when one source's count memo outgrows the array, PM_E_TIMEOUT, PM_E_DEVICE).
 uint32_t noalloc_max_vertices();
+// Count-memo entries per warp in the first round of enumerate_noalloc
+// (power of two; each retry round has 4x more).  Default 2048.
+void set_noalloc_table_entries(uint32_t entries);
+// Rounds (1 + retry rounds) of the calling thread's last enumerate_noalloc.
+uint32_t noalloc_last_rounds();
 void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t* d_edge_active,
                        const WalkProgram& prog, uint32_t state_words, uint64_t* d_count, cudaStream_t s);
 

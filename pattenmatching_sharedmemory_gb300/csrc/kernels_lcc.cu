@@ -11,6 +11,8 @@
 // multiple_label_lcc_cpu.tpp:26-101); sweep 2 is a separate launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <atomic>
 
 #include "kernels.h"
@@ -754,10 +756,18 @@ __device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTabl
 // Sweep 1 in two launches with their own register budgets: kTiles false
 // runs the hub segments (single- and multi-segment hubs), kTiles true the
 // tiles of light vertices.
+// Warp `warp` of `n_warps` takes tasks warp, warp + n_warps, ...: the
+// launch's own warps for one query, or one query's share of the blocks of a
+// multi-query launch.
+__device__ __forceinline__ uint64_t grid_warp() {
+  return (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+}
+__device__ __forceinline__ uint64_t grid_warps() { return (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5; }
+
 template <class W, bool kTiles>
 __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState<W>& st,
                                                const QueryTables* __restrict__ qt, HubAcc* hub_acc,
-                                               StepCounters* ctr) {
+                                               StepCounters* ctr, const uint64_t warp, const uint64_t n_warps) {
   __shared__ LccTables t;
   __shared__ LccWarp s_lw[kLccWarps];
   load_lcc_tables(t, qt, qt->k);
@@ -769,8 +779,6 @@ __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState
   // warp checks the flagged ones.
   const uint64_t n_tiles = (static_cast<uint64_t>(g.V) + 31) / 32;
   const uint64_t n_tasks = kTiles ? (n_tiles + 31) / 32 : batched;
-  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   LccTally tl;
   for (uint64_t task = warp; task < n_tasks; task += n_warps) {
     if (kTiles) {
@@ -812,7 +820,7 @@ template <class W, bool kTiles>
 __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph g, DevState<W> st,
                                                                         const QueryTables* __restrict__ qt,
                                                                         HubAcc* hub_acc, StepCounters* ctr) {
-  lcc_check_body<W, kTiles>(g, st, qt, hub_acc, ctr);
+  lcc_check_body<W, kTiles>(g, st, qt, hub_acc, ctr, grid_warp(), grid_warps());
 }
 
 template <class W, bool kTiles>
@@ -825,9 +833,9 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_at(DevGr
     __shared__ DevState<W> s_st;
     if (threadIdx.x == 0) s_st = state_at<W>(a);
     __syncthreads();
-    lcc_check_body<W, kTiles>(g, s_st, a->tables, a->hub_acc, a->ctr);
+    lcc_check_body<W, kTiles>(g, s_st, a->tables, a->hub_acc, a->ctr, grid_warp(), grid_warps());
   } else {
-    lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr);
+    lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, grid_warp(), grid_warps());
   }
 }
 
@@ -963,13 +971,11 @@ __device__ void apply_tile(const DevGraph& g, const DevState<W>& st, uint64_t ti
 
 template <class W>
 __device__ __forceinline__ void apply_body(const DevGraph& g, const DevState<W>& st, HubAcc* hub_acc,
-                                           StepCounters* ctr) {
+                                           StepCounters* ctr, const uint64_t warp, const uint64_t n_warps) {
   const bool any_modified = *reinterpret_cast<volatile unsigned long long*>(&ctr->modified_total) != 0;
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
   const uint64_t n_tasks = batched + (static_cast<uint64_t>(g.V) + 31) / 32;
-  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   unsigned me = 0, ve = 0;
   for (uint64_t task = warp; task < n_tasks; task += n_warps) {
     if (task < heavy) {
@@ -991,12 +997,12 @@ __device__ __forceinline__ void apply_body(const DevGraph& g, const DevState<W>&
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_apply(DevGraph g, DevState<W> st, HubAcc* hub_acc, StepCounters* ctr) {
-  apply_body(g, st, hub_acc, ctr);
+  apply_body(g, st, hub_acc, ctr, grid_warp(), grid_warps());
 }
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_apply_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
-  apply_body(g, state_at<W>(a), a->hub_acc, a->ctr);
+  apply_body(g, state_at<W>(a), a->hub_acc, a->ctr, grid_warp(), grid_warps());
 }
 
 // ---- sweep 2 on symmetric graphs: schedule by change -------------------
@@ -1017,10 +1023,9 @@ __global__ void __launch_bounds__(kThreads) k_apply_at(DevGraph g, const QueryDe
 // step", sch[v] keeps such vertices that still hold a role, tile_sch
 // summarises sch per tile.
 template <class W>
-__device__ __forceinline__ void apply_changed_body(const DevGraph& g, const DevState<W>& st, StepCounters* ctr) {
+__device__ __forceinline__ void apply_changed_body(const DevGraph& g, const DevState<W>& st, StepCounters* ctr,
+                                                   const uint64_t warp, const uint64_t n_warps) {
   const unsigned lane = lane_id();
-  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   unsigned me = 0, ve = 0;
   for (uint64_t tile = warp * 32; tile < g.V; tile += n_warps * 32) {
     const uint64_t v = tile + lane;
@@ -1055,12 +1060,12 @@ __device__ __forceinline__ void apply_changed_body(const DevGraph& g, const DevS
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_apply_changed(DevGraph g, DevState<W> st, StepCounters* ctr) {
-  apply_changed_body(g, st, ctr);
+  apply_changed_body(g, st, ctr, grid_warp(), grid_warps());
 }
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_apply_changed_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
-  apply_changed_body(g, state_at<W>(a), a->ctr);
+  apply_changed_body(g, state_at<W>(a), a->ctr, grid_warp(), grid_warps());
 }
 
 // Marks every entry target of [b, e) as scheduled (one warp).
@@ -1077,13 +1082,12 @@ __device__ __forceinline__ void push_range(const DevGraph& g, const DevState<W>&
 // task layout of sweep 1 (hub segments, batches of 32 single-segment hubs,
 // tiles of 32 light vertices).
 template <class W>
-__device__ __forceinline__ void push_changed_body(const DevGraph& g, const DevState<W>& st) {
+__device__ __forceinline__ void push_changed_body(const DevGraph& g, const DevState<W>& st, const uint64_t warp,
+                                                  const uint64_t n_warps) {
   const unsigned lane = lane_id();
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
   const uint64_t n_tasks = batched + (static_cast<uint64_t>(g.V) + 31) / 32;
-  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t task = warp; task < n_tasks; task += n_warps) {
     if (task < heavy) {
       const uint4 sd = g.seg[task];
@@ -1117,12 +1121,121 @@ __device__ __forceinline__ void push_changed_body(const DevGraph& g, const DevSt
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_push_changed(DevGraph g, DevState<W> st) {
-  push_changed_body(g, st);
+  push_changed_body(g, st, grid_warp(), grid_warps());
 }
 
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_push_changed_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
-  push_changed_body(g, state_at<W>(a));
+  push_changed_body(g, state_at<W>(a), grid_warp(), grid_warps());
+}
+
+// ---- many queries in one launch (batched LCC fixpoints) -----------------
+//
+// A launch of nq x bpq blocks over the queries listed in active[0, nq): block
+// b works for query active[b % nq] as its virtual block b / nq of bpq, and
+// runs the same sweep body over that query's state and task list.  Blocks of
+// different queries with the same virtual index take the same tasks (the same
+// CSR ranges) at about the same time, so an adjacency range brought from HBM
+// for one query is served from L2 for the others; each query's counters,
+// hub accumulators and flags are its own, so its rows are those of its own
+// passes.
+struct MultiSlot {
+  uint32_t q;
+  uint64_t warp, n_warps;
+};
+__device__ __forceinline__ MultiSlot multi_slot(uint32_t nq) {
+  MultiSlot m;
+  const uint32_t bpq = gridDim.x / nq;
+  m.q = blockIdx.x % nq;
+  m.warp = (static_cast<uint64_t>(blockIdx.x / nq) * blockDim.x + threadIdx.x) >> 5;
+  m.n_warps = (static_cast<uint64_t>(bpq) * blockDim.x) >> 5;
+  return m;
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_lcc0_multi(DevGraph g, const QueryDevPtrs* __restrict__ qs,
+                                                         const uint32_t* __restrict__ active, uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  const QueryDevPtrs* a = qs + active[m.q];
+  const DevState<W> st = state_at<W>(a);
+  __shared__ uint64_t slot_roles[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) slot_roles[i] = a->tables->slot_roles[i];
+  __syncthreads();
+  unsigned long long me = 0, ve = 0;
+  const uint64_t stride = m.n_warps * 32;
+  for (uint64_t v = m.warp * 32 + lane_id(); v < g.V; v += stride) {
+    W w = st.vs[v];
+    uint64_t c = Pack<W>::cand(w);
+    if (!c) continue;
+    uint32_t sl = Pack<W>::slot(w);
+    uint64_t nc = c & slot_roles[sl];
+    if (nc != c) {
+      me += __popcll(c ^ nc);
+      st.vs[v] = Pack<W>::make(nc, sl);
+      if (!nc) ++ve;
+    }
+  }
+  me = __reduce_add_sync(kFull, static_cast<unsigned>(me));
+  ve = __reduce_add_sync(kFull, static_cast<unsigned>(ve));
+  if (lane_id() == 0) {
+    if (me) atomicAdd(&a->ctr->match_elim, me);
+    if (ve) atomicAdd(&a->ctr->vertex_elim, ve);
+  }
+}
+
+template <class W, bool kTiles>
+__global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_multi(DevGraph g,
+                                                                              const QueryDevPtrs* __restrict__ qs,
+                                                                              const uint32_t* __restrict__ active,
+                                                                              uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  const QueryDevPtrs* a = qs + active[m.q];
+  if constexpr (kTiles) {
+    __shared__ DevState<W> s_st;
+    if (threadIdx.x == 0) s_st = state_at<W>(a);
+    __syncthreads();
+    lcc_check_body<W, kTiles>(g, s_st, a->tables, a->hub_acc, a->ctr, m.warp, m.n_warps);
+  } else {
+    lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, m.warp, m.n_warps);
+  }
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_multi(DevGraph g, const QueryDevPtrs* __restrict__ qs,
+                                                          const uint32_t* __restrict__ active, uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  const QueryDevPtrs* a = qs + active[m.q];
+  apply_body(g, state_at<W>(a), a->hub_acc, a->ctr, m.warp, m.n_warps);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_apply_changed_multi(DevGraph g, const QueryDevPtrs* __restrict__ qs,
+                                                                  const uint32_t* __restrict__ active, uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  const QueryDevPtrs* a = qs + active[m.q];
+  apply_changed_body(g, state_at<W>(a), a->ctr, m.warp, m.n_warps);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_push_changed_multi(DevGraph g, const QueryDevPtrs* __restrict__ qs,
+                                                                 const uint32_t* __restrict__ active, uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  push_changed_body(g, state_at<W>(qs + active[m.q]), m.warp, m.n_warps);
+}
+
+// Per active query: clear the per-step counter words (clear != 0), or copy
+// its counters to out[i] (clear == 0).
+__global__ void k_counters_multi(const QueryDevPtrs* __restrict__ qs, const uint32_t* __restrict__ active,
+                                 uint32_t nq, StepCounters* out, int clear) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nq * 16u; i += gridDim.x * blockDim.x) {
+    const uint32_t q = i / 16, w = i % 16;
+    unsigned long long* words = reinterpret_cast<unsigned long long*>(qs[active[q]].ctr);
+    if (clear) {
+      if (w < static_cast<uint32_t>(kStepCounterWords)) words[w] = 0;
+    } else {
+      reinterpret_cast<unsigned long long*>(out + q)[w] = words[w];
+    }
+  }
 }
 
 // ---- worklist compaction ----------------------------------------------
@@ -1414,6 +1527,48 @@ void launch_lcc_pass_at(const DevGraph& g, int word_kind, const QueryDevPtrs* a,
   }
   const int grid2 = grid_for_tasks(sweep_tasks(g), 8);
   PM_DISPATCH_WORD(word_kind, k_apply_at<W><<<grid2, kThreads, 0, s>>>(g, a));
+}
+
+// Blocks of a multi-query launch: nq x (the single-query grid / nq, at
+// least one), so the whole launch keeps the single-query residency.
+inline int multi_grid(int single_grid, uint32_t nq) {
+  const int per = std::max(1, single_grid / static_cast<int>(nq));
+  return per * static_cast<int>(nq);
+}
+
+void launch_lcc0_multi(const DevGraph& g, int word_kind, const QueryDevPtrs* qs, const uint32_t* active, uint32_t nq,
+                       cudaStream_t s) {
+  if (!nq) return;
+  const int grid = multi_grid(device_sm_count() * 8, nq);
+  PM_DISPATCH_WORD(word_kind, k_lcc0_multi<W><<<grid, kThreads, 0, s>>>(g, qs, active, nq));
+}
+
+void launch_lcc_pass_multi(const DevGraph& g, int word_kind, const QueryDevPtrs* qs, const uint32_t* active,
+                           uint32_t nq, cudaStream_t s) {
+  if (!nq) return;
+  const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
+  if (hub_tasks) {
+    const int grid = multi_grid(grid_for_tasks(hub_tasks, 5), nq);
+    PM_DISPATCH_WORD(word_kind, k_lcc_check_multi<W, false><<<grid, kThreads, 0, s>>>(g, qs, active, nq));
+  }
+  const int grid = multi_grid(grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4), nq);
+  PM_DISPATCH_WORD(word_kind, k_lcc_check_multi<W, true><<<grid, kThreads, 0, s>>>(g, qs, active, nq));
+  if (g.symmetric) {
+    const int grid1 = multi_grid(grid_for_tiles(g.V, 8), nq);
+    PM_DISPATCH_WORD(word_kind, k_apply_changed_multi<W><<<grid1, kThreads, 0, s>>>(g, qs, active, nq));
+    const int grid2 = multi_grid(grid_for_tasks(sweep_tasks(g), 8), nq);
+    PM_DISPATCH_WORD(word_kind, k_push_changed_multi<W><<<grid2, kThreads, 0, s>>>(g, qs, active, nq));
+    return;
+  }
+  const int grid2 = multi_grid(grid_for_tasks(sweep_tasks(g), 8), nq);
+  PM_DISPATCH_WORD(word_kind, k_apply_multi<W><<<grid2, kThreads, 0, s>>>(g, qs, active, nq));
+}
+
+void launch_counters_multi(const QueryDevPtrs* qs, const uint32_t* active, uint32_t nq, StepCounters* out, bool clear,
+                           cudaStream_t s) {
+  if (!nq) return;
+  note_launch();
+  k_counters_multi<<<std::max(1u, (nq * 16 + 255) / 256), 256, 0, s>>>(qs, active, nq, out, clear ? 1 : 0);
 }
 
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, uint32_t* wl, uint32_t* wl_index,

@@ -197,6 +197,22 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
   return t;
 }
 
+// The step's deadline (StepCounters::deadline_ns), set once by the first
+// warp that gets here after the host cleared it; called by lane 0 and
+// broadcast to the warp.
+__device__ __forceinline__ uint64_t warp_step_deadline(StepCounters* ctr, uint64_t budget_ns) {
+  uint64_t d = 0;
+  if (lane_id() == 0) {
+    d = *reinterpret_cast<volatile unsigned long long*>(&ctr->deadline_ns);
+    if (d == 0) {
+      const unsigned long long want = global_timer_ns() + budget_ns;
+      const unsigned long long prev = atomicCAS(&ctr->deadline_ns, 0ull, want);
+      d = prev ? prev : want;
+    }
+  }
+  return __shfl_sync(0xFFFFFFFFu, d, 0);
+}
+
 // ---- per-warp memo tables -------------------------------------------------
 struct WarpMemo {
   uint4* edge;
@@ -816,7 +832,9 @@ __device__ uint8_t run_walk(const DevGraph& g, const DevState<W>& st, WarpShared
   // they never overflow and are never re-run without the restriction.
   const bool second = second_lo != 0 || second_hi != 0xFFFFFFFFu;
   const bool count_memo = kEnum && ws.prog->count_memo && ws.memo_on && !second;
-  uint32_t iters = 0;
+  // The deadline is read on the first iteration (so that launches of many
+  // short items stop too) and every 1024 iterations after it.
+  uint32_t iters = 1023;
   __syncwarp();
   if (lane == 0) {
     ws.f.bound[0] = source;
@@ -1019,9 +1037,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm - 2) k_walk(
   }
   bind_frames(ws, s_frames + wib * frame_bytes(w.frame_steps), w.frame_steps);
   const uint32_t gw = blockIdx.x * kWalkWarps + wib;
-  uint64_t deadline = 0;
-  if (lane == 0) deadline = global_timer_ns() + budget_ns;
-  deadline = __shfl_sync(kFull, deadline, 0);
+  const uint64_t deadline = warp_step_deadline(ctr, budget_ns);
   WarpMemo m = warp_memo(sc, gw);
   const uint64_t n_items =
       w.slices ? w.n_slices : w.retry_items ? w.n_retry : static_cast<uint64_t>(w.n_wl) * w.n_progs;
@@ -1237,9 +1253,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, kWalkBlocksPerSm) k_enumerate
     __syncthreads();
   }
   WarpMemo m = warp_memo(sc, gw);
-  uint64_t deadline = 0;
-  if (lane == 0) deadline = global_timer_ns() + budget_ns;
-  deadline = __shfl_sync(kFull, deadline, 0);
+  const uint64_t deadline = warp_step_deadline(ctr, budget_ns);
   const uint64_t n = items ? n_items : n_wl;
   unsigned long long leaves = 0;
   // The source cache serves only the tail CHECKs, whose candidates hold the
@@ -1337,6 +1351,13 @@ uint32_t enum_second_split() { return g_enum_second_split; }
 void set_walk_tail_swap(uint32_t ratio) { g_walk_tail_swap = ratio; }
 uint32_t walk_tail_swap() { return g_walk_tail_swap; }
 uint64_t walk_budget_ns() { return g_walk_budget_ns; }
+namespace {
+thread_local uint64_t t_walk_budget_cap_ns = 0;
+}  // namespace
+void set_thread_walk_budget_cap_ns(uint64_t ns) { t_walk_budget_cap_ns = ns; }
+uint64_t effective_walk_budget_ns() {
+  return t_walk_budget_cap_ns && t_walk_budget_cap_ns < g_walk_budget_ns ? t_walk_budget_cap_ns : g_walk_budget_ns;
+}
 
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {
   uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * kWalkBlocksPerSm;
@@ -1349,7 +1370,7 @@ void launch_walk(const DevGraph& g, const QueryDevPtrs& q, const WalkLaunch& w, 
   const uint32_t blocks = walk_grid_blocks(sc.n_warps);
   const size_t dyn = kWalkWarps * frame_bytes(w.frame_steps);
   PM_DISPATCH_WORD(q.word_kind, k_walk<W><<<blocks, kWalkWarps * 32, dyn, s>>>(g, state_of<W>(q), w, sc, q.ctr,
-                                                                               g_walk_budget_ns));
+                                                                               effective_walk_budget_ns()));
 }
 
 void launch_flag_rescue(const WalkLaunch& w, StepCounters* ctr, cudaStream_t s) {
@@ -1391,7 +1412,7 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
   const size_t dyn = kWalkWarps * frame_bytes(frame_steps);
   PM_DISPATCH_WORD(q.word_kind, k_enumerate<W><<<blocks, kWalkWarps * 32, dyn, s>>>(
                                     g, state_of<W>(q), prog, frame_steps, wl, n_wl, items, n_items, overflow, sc,
-                                    q.ctr, g_walk_budget_ns, g_enum_tail_swap, g_enum_count_memo,
+                                    q.ctr, effective_walk_budget_ns(), g_enum_tail_swap, g_enum_count_memo,
                                     g_enum_pair_tail, g_enum_second_split));
 }
 
@@ -1491,9 +1512,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
   m.state_cap = L.cap;
   m.state_stride = L.stride;
   m.epoch = L.epochs[gw];
-  uint64_t deadline = 0;
-  if (lane == 0) deadline = global_timer_ns() + budget_ns;
-  deadline = __shfl_sync(kFull, deadline, 0);
+  const uint64_t deadline = warp_step_deadline(L.ctr, budget_ns);
   unsigned long long leaves = 0;
   bool stop = false;
   while (!stop) {
@@ -1536,6 +1555,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_enumerate_noalloc(DevGraph 
 
 std::mutex g_noalloc_mutex;
 void* g_noalloc_base[128] = {};
+uint32_t g_noalloc_first_cap = 2048;  // count-memo entries per warp, round 0
+thread_local uint32_t t_noalloc_rounds = 0;  // rounds run by this thread's last call
 
 void noalloc_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw PmError{PM_E_DEVICE, std::string(what) + ": " + cudaGetErrorString(e)};
@@ -1543,7 +1564,11 @@ void noalloc_check(cudaError_t e, const char* what) {
 
 // Device address of the scratch array on the current device.  Resolved once
 // per device, by the first call made with that device current, with
-// cudaGetSymbolAddress; later calls reuse the cached address.
+// cudaGetSymbolAddress; later calls reuse the cached address.  The cache
+// lives as long as the process: after cudaDeviceReset (or anything else that
+// destroys the device's primary context) the cached address is stale, so a
+// process that resets a device must not call pm_enumerate_noalloc on it
+// again.
 unsigned char* noalloc_scratch_current() {
   int dev = 0;
   noalloc_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -1561,6 +1586,8 @@ unsigned char* noalloc_scratch_current() {
 }  // namespace
 
 uint32_t noalloc_max_vertices() { return kNoAllocMaxVertices; }
+void set_noalloc_table_entries(uint32_t entries) { g_noalloc_first_cap = entries; }
+uint32_t noalloc_last_rounds() { return t_noalloc_rounds; }
 
 void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t* d_edge_active,
                        const WalkProgram& prog, uint32_t state_words, uint64_t* d_count, cudaStream_t s) {
@@ -1582,8 +1609,10 @@ void enumerate_noalloc(const DevGraph& g, const uint64_t* d_cand, const uint32_t
   // among them) start every call at zero.
   noalloc_check(cudaMemsetAsync(L.ctr, 0, sizeof(StepCounters), s), "clear counters");
   StepCounters host_ctr{};
+  t_noalloc_rounds = 0;
   for (int round = 0;; ++round) {
-    const uint64_t cap = uint64_t(2048) << (2 * round);
+    t_noalloc_rounds = static_cast<uint32_t>(round) + 1;
+    const uint64_t cap = uint64_t(g_noalloc_first_cap) << (2 * round);
     uint64_t warps = kNoAllocTableBytes / (cap * L.stride * 4);
     warps = std::min<uint64_t>(warps, std::min<uint64_t>(kNoAllocMaxWarps,
                                                          uint64_t(device_sm_count()) * 8 * kWalkWarps));

@@ -83,6 +83,33 @@ void Server::release(uint64_t ticket) {
   requests_.erase(it);
 }
 
+int Server::cancel(uint64_t ticket) {
+  std::shared_ptr<ServeRequest> r;
+  int was = ServeRequest::kDone;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = requests_.find(ticket);
+    if (it == requests_.end()) throw PmError{PM_E_INVALID_ARG, "unknown ticket"};
+    r = it->second;
+    was = r->state;
+    if (r->state == ServeRequest::kQueued) {
+      queue_.erase(std::find(queue_.begin(), queue_.end(), r));
+      r->status = PM_E_CANCELLED;
+      r->error = "request cancelled before it was admitted";
+      r->state = ServeRequest::kDone;
+      r->t_admit = r->t_done = ServeRequest::Clock::now();
+      ++done_;
+    } else if (r->state == ServeRequest::kRunning) {
+      r->cancel.store(true);
+    }
+  }
+  if (was == ServeRequest::kQueued) {
+    cv_done_.notify_all();
+    cv_work_.notify_all();
+  }
+  return was;
+}
+
 ServerStats Server::stats() {
   std::lock_guard<std::mutex> lk(mu_);
   ServerStats s;
@@ -135,7 +162,15 @@ void Server::worker(uint32_t) {
     } else {
       try {
         QueryImpl q;
+        // The request's budget (pm_set_query_budget_ms) runs from admission,
+        // so template compilation and allocation count against it too.
+        if (query_budget_ms() > 0) {
+          q.has_deadline = true;
+          q.deadline = r->t_admit + std::chrono::microseconds(static_cast<int64_t>(query_budget_ms() * 1000.0));
+        }
         q.create(g_, r->pattern, stream, h_ctr, h_count);
+        q.cancel = &r->cancel;
+        q.stop_before_enumeration = (r->flags & kSubmitPruneOnly) != 0;
         q.run_all();
         r->records = q.records;
         r->records.push_back(q.final_record());

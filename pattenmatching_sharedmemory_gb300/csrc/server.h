@@ -26,6 +26,7 @@
 namespace pmgb {
 
 constexpr uint32_t kSubmitExportState = 1;  // keep the final state for export
+constexpr uint32_t kSubmitPruneOnly = 2;    // stop when the schedule reaches ENUMERATION
 
 struct ServeRequest {
   using Clock = std::chrono::steady_clock;
@@ -37,6 +38,7 @@ struct ServeRequest {
   uint64_t bytes = 0;  // device bytes charged at admission
   State state = kQueued;
   Clock::time_point t_submit, t_admit, t_done;
+  std::atomic<bool> cancel{false};  // set by Server::cancel while running
 
   int status = PM_SUCCESS;
   std::string error;
@@ -69,6 +71,10 @@ class Server {
   // true when done.
   bool wait(uint64_t ticket, double timeout_ms);
   void release(uint64_t ticket);
+  // A queued request is dropped (PM_E_CANCELLED); a running one stops before
+  // its next step (PM_E_CANCELLED); a finished one is left as it is.
+  // Returns the request's state when the call was made.
+  int cancel(uint64_t ticket);
   ServerStats stats();
 
  private:

@@ -93,8 +93,25 @@ def synthetic_cases(include_big: bool = True):
     add("scale12_tds", graph_params(12, kind="zipf", n_labels=8, s=1.0, label_seed=3),
         {"kind": "random", "n": 6, "density": 0.5, "label_n": 8, "zipf_s": 1.0, "seed": 77})
     if include_big:
-        add("c1_scale16_cycle4", graph_params(16), {"kind": "cycle", "labels": [0, 1, 2, 3]}, ref_threads=8,
-            timeout=3600, big=True)
+        add("c1_scale16_cycle4", graph_params(16), {"kind": "cycle", "labels": [0, 1, 2, 3]}, ref_threads=1,
+            timeout=14400, big=True)
+    return cases
+
+
+def stream15_cases():
+    """The served RMAT-16 stream: the 15 4-cycles with four distinct labels
+    of 0..4 (every 4-subset in its 3 cyclic orders), full pipeline.  The
+    reference runs them with several threads (hours of CPU at one thread);
+    for distinct labels no memo test can block a walk, so the outputs do not
+    depend on the thread count."""
+    import itertools
+
+    cases = []
+    for a, b, c, d in itertools.combinations(range(5), 4):
+        for order in ([a, b, c, d], [a, b, d, c], [a, c, b, d]):
+            cases.append({"name": "stream15_" + "".join(map(str, order)), "graph": graph_params(16),
+                          "pattern": {"kind": "cycle", "labels": list(order)}, "ref_threads": 5, "timeout": 7200,
+                          "big": True})
     return cases
 
 

@@ -36,7 +36,9 @@ import pattenmatching_sharedmemory_gb300 as pm  # noqa: E402
 from pattenmatching_sharedmemory_gb300 import templates as T  # noqa: E402
 from tests import cases as C  # noqa: E402
 
-REF_DATA = Path("/root/reference/data/patternmatching")
+# The reference checkout (read-only); PM_REFERENCE_DIR overrides the default.
+REF_ROOT = Path(os.environ.get("PM_REFERENCE_DIR", "/root/reference"))
+REF_DATA = REF_ROOT / "data" / "patternmatching"
 REF_BIN = ROOT / "oracle" / "_ref" / "patternmatching"
 
 
@@ -134,6 +136,30 @@ def synthetic(skip_big: bool, only_big: bool = False):
     (HERE / name).write_text(json.dumps(results, indent=1))
 
 
+def stream15():
+    """The RMAT-16 served stream's 15 4-cycles, one reference run each,
+    appended to stream15_rmat16.json as they finish (hours of CPU)."""
+    path = HERE / "stream15_rmat16.json"
+    results = json.loads(path.read_text()) if path.exists() else []
+    have = {r["name"] for r in results}
+    for case in C.stream15_cases():
+        if case["name"] in have:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            tmp = Path(tmp)
+            g = C.make_graph(case)
+            g.write_text(tmp / "g.totem", tmp / "labels.totem")
+            C.make_pattern(case).write(tmp / "pattern")
+            res = run_reference(tmp / "g.totem", tmp / "labels.totem", tmp / "pattern", tmp / "out",
+                                threads=case["ref_threads"], timeout=case["timeout"])
+        entry = dict(case)
+        entry.update({"rows": res["rows"], "vertex_sha256": sha(res["vertex"]), "graph_sha256": sha(res["graph"]),
+                      "last": res["last"]})
+        results.append(entry)
+        path.write_text(json.dumps(results, indent=1))
+        print(case["name"], res["rows"][-2][8], "matches", flush=True)
+
+
 def constraints():
     # A fixed tiny background graph: constraint generation ignores it.
     out = []
@@ -154,7 +180,7 @@ def constraints():
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-big", action="store_true", help="skip the scale-16 case (minutes of CPU)")
-    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big"])
+    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big", "stream15"])
     a = ap.parse_args()
     if not REF_BIN.exists():
         sys.exit("build the reference first: make -C oracle ref")
@@ -166,3 +192,5 @@ if __name__ == "__main__":
         synthetic(True)
     if a.only in (None, "big") and not a.skip_big:
         synthetic(False, only_big=True)
+    if a.only == "stream15":
+        stream15()

@@ -82,3 +82,49 @@ def product_run(graph: pm.Graph, pattern=None, pattern_dir=None):
         res = (Path(tmp) / "results.totem").read_text()
     rows = [list(r.as_tuple()) for r in recs]
     return {"rows": rows, "vertex": vtx, "graph": grp, "last": last, "results": res, "query": q, "records": recs}
+
+
+def device_u64(a):
+    """A uint64 / uint32 numpy array as a CUDA tensor (same bytes)."""
+    import torch
+
+    signed = {np.dtype(np.uint64): np.int64, np.dtype(np.uint32): np.int32}[a.dtype]
+    return torch.from_numpy(np.ascontiguousarray(a).view(signed)).to("cuda:0")
+
+
+def edge_bits(eact: np.ndarray) -> np.ndarray:
+    """Per-CSR-entry flags -> one bit per entry, bit e % 32 of word e // 32."""
+    b = np.packbits(eact.astype(np.uint8) != 0, bitorder="little")
+    buf = np.zeros(max((len(eact) + 31) // 32, 1) * 4, np.uint8)
+    buf[:len(b)] = b
+    return buf.view("<u4").astype(np.uint32)
+
+
+def sampled_count_gpu(graph, pattern, cand, eact, start_role: int, stride: int) -> int:
+    """ENUMERATION count over the sources v % stride == 0 only: the pruned
+    state with the start role cleared on every other vertex, counted by
+    pm_enumerate_noalloc (the start role is bound at the walk's first step
+    only, so this is the per-source sum over the sampled sources)."""
+    import ctypes
+
+    import torch
+
+    off, adj, _ = graph.host_csr()
+    c = cand.copy()
+    keep = (np.arange(len(c)) % stride) == 0
+    c[~keep] &= ~np.uint64(1 << start_role)
+    d_off, d_adj = device_u64(off.copy()), device_u64(adj.copy())
+    d_cand, d_eact = device_u64(c), device_u64(edge_bits(eact))
+    d_count = torch.zeros(1, dtype=torch.int64, device="cuda:0")
+    po = np.ascontiguousarray(pattern.offsets, np.uint64)
+    pa = np.ascontiguousarray(pattern.adj, np.uint32)
+    pl = np.ascontiguousarray(pattern.labels, np.uint64)
+    st = pm.lib.pm_enumerate_noalloc(d_off.data_ptr(), d_adj.data_ptr(), graph.vertex_count, graph.edge_count, 1,
+                                     d_cand.data_ptr(), d_eact.data_ptr(),
+                                     po.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                     pa.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                     pl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), pattern.n, len(pa),
+                                     d_count.data_ptr(), None)
+    if st != pm.PM_SUCCESS:
+        raise pm.PmError(st, pm.lib.pm_last_error().decode())
+    return int(d_count.item())

@@ -57,9 +57,10 @@ def test_poisson_stream_reports_rates_and_percentiles():
         def release(self, ticket):
             released.append(ticket)
 
-    pm = types.SimpleNamespace(PM_SUCCESS=0, Server=Server)
+    pm = types.SimpleNamespace(PM_SUCCESS=0, PM_E_TIMEOUT=-7, Server=Server)
     lo = b.poisson_stream(None, pm, list(range(15)), 40.0, 0.4, 4, seed=3)
     hi = b.poisson_stream(None, pm, list(range(15)), 400.0, 0.4, 4, seed=4)
     assert hi["requests"] > lo["requests"] > 0
-    assert lo["failed"] == 0 and lo["latency_ms_p99"] >= lo["latency_ms_p50"]
+    assert lo["failed"] == 0 and lo["timed_out"] == 0 and lo["completed"] == lo["requests"]
+    assert lo["latency_ms_p99"] >= lo["latency_ms_p50"]
     assert len(released) == lo["requests"] + hi["requests"] + 8  # + the warm-up requests

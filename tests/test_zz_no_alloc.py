@@ -136,3 +136,22 @@ def test_noalloc_rejects_beyond_limits(states):
     st2.p_lab = np.ascontiguousarray(big.labels, np.uint64)
     assert st2.call(d_count) == pm.PM_E_PATTERN_TOO_LARGE
     assert int(d_count.item()) == 0
+
+
+def test_noalloc_retry_rounds(states):
+    """Tiny first-round tables make sources overflow, so later rounds re-run
+    them from the bitmap of overflowed sources with 4x larger tables (and
+    the two bitmaps swap roles between rounds); the count must not change."""
+    import torch
+
+    d_count = torch.empty(1, dtype=torch.int64, device="cuda:0")
+    assert pm.lib.pm_set_noalloc_table_entries(32) == pm.PM_SUCCESS
+    try:
+        for name in ("cycle5_distinct", "cycle4_distinct", "cycle5_distinct"):
+            assert _count(states[name], d_count) == states[name].expected
+            assert pm.lib.pm_noalloc_last_rounds() >= 2, name
+    finally:
+        assert pm.lib.pm_set_noalloc_table_entries(2048) == pm.PM_SUCCESS
+    assert _count(states["cycle4_distinct"], d_count) == states["cycle4_distinct"].expected
+    assert pm.lib.pm_noalloc_last_rounds() == 1
+    assert pm.lib.pm_set_noalloc_table_entries(48) == pm.PM_E_INVALID_ARG
