@@ -24,9 +24,10 @@ either completes within D or ends with PM_E_TIMEOUT.  Timeouts are counted
 and reported, never dropped; `value` counts completed requests only.
 
 A timed step serves B consecutive requests of the stream (step i: requests
-i*B .. i*B+B-1; warm-up steps use the stream's tail), all submitted at once
-to one long-lived server with S slots (continuous batching, admission by
-device memory); the step ends when the last finished.
+i*B .. i*B+B-1, so the default 20 steps of 100 serve the whole stream;
+warm-up steps serve another seeded stream), all submitted at once to one
+long-lived server with S slots (continuous batching, admission by device
+memory); the step ends when the last finished.
 
 value        : completed requests per second over the timed steps (host
                clock, device synchronised on both sides).
@@ -43,6 +44,10 @@ roofline     : the dominant kernel class of requests run one at a time, its
                HBM copy bandwidth (walker bytes per hop: 16 B of offsets;
                per tested CSR entry 4 B id + 1/8 B edge bit + 1/8 B active
                bit + ceil(k/8) B roles).
+c3_batch     : the batched configuration: 64 seeded 3-8-vertex templates on
+               RMAT scale 22, pruning only, same budget, as one fused batch
+               (LCC work of all queries in shared launches), one server burst
+               and one at a time.
 lcc_roofline : LCC passes of the two-cycle template (labels 0..5) on the same
                graph: per pass 1/8 B edge bits per listed CSR entry plus 4 B
                id and the neighbour's packed word per gathered entry.
@@ -369,9 +374,13 @@ def run_c4(args, rank, world, pm, T):
     pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
 
     server = pm.Server(g, slots=args.slots)
-    tail = len(stream) - B * args.warmup
-    for i in range(args.warmup):  # warm-up on the stream's tail
-        serve_burst(server, pm, stream[tail + i * B: tail + (i + 1) * B])
+    # Warm-up steps serve requests of another seeded stream of the same kind.
+    warm = T.served_stream(B * args.warmup, n_labels=w["labels"][1], zipf_s=w["labels"][2],
+                           seed=w["stream_seed"] + 1, min_vertices=w["template_vertices"][0],
+                           max_vertices=w["template_vertices"][1], min_density=w["density"][0],
+                           max_density=w["density"][1])
+    for i in range(args.warmup):
+        serve_burst(server, pm, warm[i * B:(i + 1) * B])
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -491,6 +500,62 @@ def run_c4(args, rank, world, pm, T):
         out["lcc_roofline"] = lcc_roofline(g, pm, T, device)
     pm._check(pm.lib.pm_set_query_budget_ms(0.0))
     return out, g, stream
+
+
+def run_c3_batch(args, pm, T):
+    """The batched configuration: 64 seeded templates of 3-8 vertices on
+    RMAT scale 22 (16 Zipf(1.0) labels), pruning pipeline, same per-query
+    budget: one fused batch (shared LCC launches, pm_fused_batch_run) vs one
+    server burst vs one at a time."""
+    import torch
+
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    g = pm.Graph.rmat(22, 16, 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels("zipf", 16, 1.0, 1)
+    g.to_device(device)
+    tmpls = T.served_stream(64, n_labels=16, zipf_s=1.0, seed=3, min_vertices=3, max_vertices=8)
+    pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    try:
+        with pm.FusedBatch(g, tmpls[:8], prune_only=True):  # warm-up
+            pass
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with pm.FusedBatch(g, tmpls, prune_only=True) as b:
+            torch.cuda.synchronize()
+            fused_s = time.perf_counter() - t0
+            fused = [b.result(i) for i in range(len(tmpls))]
+            stats = b.stats()
+            fused_rows = [[r.as_tuple() for r in b.records(i)] for i in range(len(tmpls))]
+        with pm.Server(g, slots=args.slots) as srv:
+            serve_burst(srv, pm, tmpls[:8])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            served = serve_burst(srv, pm, tmpls)
+            torch.cuda.synchronize()
+            served_s = time.perf_counter() - t0
+        seq_s, seq_st, _, _, _ = one_at_a_time(g, pm, tmpls)
+    finally:
+        pm._check(pm.lib.pm_set_query_budget_ms(0.0))
+    # Completed queries of the fused batch against their runs alone.
+    same = 0
+    for i, r in enumerate(fused):
+        if r.status != pm.PM_SUCCESS or seq_st[i] != pm.PM_SUCCESS:
+            continue
+        q = pm.Query(g, pattern=tmpls[i])
+        same += [x.as_tuple() for x in q.prune()] == fused_rows[i]
+        q.close()
+    g.close()
+    n_f = sum(1 for r in fused if r.status == pm.PM_SUCCESS)
+    n_s = sum(1 for r in served if r.status == pm.PM_SUCCESS)
+    n_q = sum(1 for x in seq_st if x == pm.PM_SUCCESS)
+    return {"workload": "rmat22_zipf16_64_templates_prune_batched",
+            "graph": "rmat scale 22 ef 16, 16 labels Zipf(1.0)",
+            "templates": "64 seeded templates (seed 3), 3-8 vertices, density 0.3-0.6, labels from the graph's "
+                         "distribution", "budget_ms": args.budget_ms, "unit": "queries/s",
+            "fused_batch": n_f / fused_s, "fused_completed": n_f, "fused_seconds": fused_s, "fused_stats": stats,
+            "served_burst": n_s / served_s, "served_completed": n_s,
+            "one_at_a_time": n_q / seq_s, "one_at_a_time_completed": n_q,
+            "fused_vs_one_at_a_time": (n_f / fused_s) / (n_q / seq_s) if n_q else None,
+            "fused_rows_equal_alone": f"{same} of the queries completed in both"}
 
 
 def run_c1_stream(args, pm, T):
@@ -654,10 +719,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--slots", type=int, default=16)
-    ap.add_argument("--requests-per-step", type=int, default=64)
-    ap.add_argument("--budget-ms", type=float, default=1000.0, help="per-request budget on the GPU")
+    ap.add_argument("--requests-per-step", type=int, default=100)
+    ap.add_argument("--budget-ms", type=float, default=250.0, help="per-request budget on the GPU")
     ap.add_argument("--reference-budget-ms", type=float, default=6000.0, help="per-request budget on the CPU")
-    ap.add_argument("--same-requests", type=int, default=32)
+    ap.add_argument("--same-requests", type=int, default=64)
     ap.add_argument("--poisson-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--c1-steps", type=int, default=3)
@@ -665,6 +730,7 @@ def main():
     ap.add_argument("--lcc-roofline", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c1", action="store_true")
+    ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--case", choices=["c1", "lcc", "c4"], default=None)
     ap.add_argument("--queries", type=int, default=1)
     ap.add_argument("--scale", type=int, default=22)
@@ -689,6 +755,11 @@ def main():
         torch.distributed.init_process_group("nccl")
     out, g, stream = run_c4(args, rank, world, pm, T)
     if rank == 0:
+        if not args.no_c3:
+            try:
+                out["c3_batch"] = run_c3_batch(args, pm, T)
+            except Exception as e:  # noqa: BLE001  (extra figures; the main line stands)
+                out["c3_batch"] = {"error": f"{type(e).__name__}: {e}"}
         if not args.no_c1:
             try:
                 out["c1_stream"] = run_c1_stream(args, pm, T)

@@ -164,6 +164,30 @@ pm_status_t pm_query_run(pm_query* q, pm_step_record* records, int32_t cap,
 pm_status_t pm_query_prune(pm_query* q, pm_step_record* records, int32_t cap,
                            int32_t* n_records);
 
+/* The embeddings ENUMERATION counts, listed — the reference's
+ * writeEnumeration (multiple_label_enumeration_cpu.tpp:15-35, compiled out
+ * there): each match is the graph vertices bound by the enumeration walk's
+ * vertex moves, in walk order (historyIndexVector), *per_match of them (the
+ * template size).  Runs the pruning first when the query has not reached
+ * ENUMERATION.  Writes up to cap matches to `matches` (cap x *per_match
+ * uint32), in no particular order; *n_matches receives the total, which is
+ * the ENUMERATION count (0 when the run ended at the iteration cap before
+ * ENUMERATION). */
+pm_status_t pm_query_list_matches(pm_query* q, uint32_t* matches, uint64_t cap, uint32_t* per_match,
+                                  uint64_t* n_matches);
+
+/* The same as text at `path`, the reference's format (each vertex followed
+ * by ';', one match per line), at most max_matches lines. */
+pm_status_t pm_query_write_matches(pm_query* q, const char* path, uint64_t max_matches, uint64_t* n_written);
+
+/* The pruned subgraph as a CSR over the original vertex ids: the CSR
+ * entries printActiveGraph prints (active entries between active vertices,
+ * multiple_label_cpu.cc:270-284), in CSR order.  offsets[V + 1] (may be
+ * NULL); adj receives the entries when cap is at least their number
+ * (*n_entries), else PM_E_INVALID_ARG with *n_entries set. */
+pm_status_t pm_query_export_subgraph(pm_query* q, uint64_t* offsets, uint32_t* adj, uint64_t cap,
+                                     uint64_t* n_entries);
+
 /* Copies the pruned state back to caller-owned host buffers (any may be
  * NULL): candidate role bitmask per vertex (bit p = pattern vertex p, the
  * FixedBitmap<64> of multiple_label_common_cpu.h:49), active flag per CSR

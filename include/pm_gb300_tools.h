@@ -25,6 +25,21 @@ pm_status_t pm_graph_generate_rmat(int32_t scale, int32_t edge_factor, double a,
  * 2 = correlated with degree rank.  Must precede device residency. */
 pm_status_t pm_graph_assign_labels(pm_graph* g, int32_t kind, uint32_t n_labels, double zipf_s, uint64_t seed);
 
+/* Graph ingestion tools, the TOTEM generator's ALTER commands
+ * (src/generator/totem_generator.cc): host-side, on a graph not yet on a
+ * device (the new graphs are host-only until pm_graph_to_device).
+ * UNDIRECTED (:631-680): a new graph in which every CSR entry u -> v of g
+ * gives u -> v and v -> u (duplicates kept; each list holds its entries in
+ * reverse order of appearance, as the generator's edgelist_to_graph builds
+ * it, :92-125).  SORT_NEIGHBOURS (:764-770): every list of g sorted
+ * ascending, in place.  SORT_VERTICES (:682-748): a new graph with ids
+ * renumbered by ascending degree (ties: ascending old id — the reference's
+ * parallel sort leaves their order unspecified); old_to_new (V entries,
+ * may be NULL) receives the renumbering.  Labels stay with their vertices. */
+pm_status_t pm_graph_make_undirected(const pm_graph* g, pm_graph** out);
+pm_status_t pm_graph_sort_neighbours(pm_graph* g);
+pm_status_t pm_graph_sort_vertices_by_degree(const pm_graph* g, pm_graph** out, uint32_t* old_to_new);
+
 /* Library-owned host CSR of g (valid until pm_graph_destroy). */
 pm_status_t pm_graph_host_csr(const pm_graph* g, const uint64_t** offsets, const uint32_t** adj,
                               const uint64_t** labels);

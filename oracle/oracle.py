@@ -72,6 +72,10 @@ def _load():
                                       P(P(ctypes.c_uint32)), P(P(ctypes.c_uint64))]
         lib.pmo_graph_free.restype = None
         lib.pmo_graph_free.argtypes = [ctypes.c_void_p]
+        lib.pmo_list_matches.restype = ctypes.c_int
+        lib.pmo_list_matches.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64), ctypes.c_uint32,
+                                         ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                         ctypes.c_uint32, P(ctypes.c_uint32), ctypes.c_uint64, P(ctypes.c_uint64)]
         lib.pmo_enumeration_start_role.restype = ctypes.c_int
         lib.pmo_enumeration_start_role.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
                                                    ctypes.c_uint32]
@@ -220,6 +224,29 @@ class HostGraph:
 def row_tuple(r) -> tuple:
     return (STEP_NAMES[r.step], r.vertex_eliminated, r.active_vertex, r.total_vertex, r.edge_eliminated,
             r.active_edge, r.total_edge, r.match_eliminated, r.enumeration)
+
+
+def list_matches(offsets, adj, labels, p_offsets, p_adj, p_labels, cap: int = 1 << 20):
+    """(matches as an (n, k) uint32 array of at most cap rows, total count):
+    the embeddings ENUMERATION counts, each as the vertices bound by the
+    enumeration walk's vertex moves in walk order."""
+    lib = _load()
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ad = np.ascontiguousarray(adj, np.uint32)
+    lab = np.ascontiguousarray(labels, np.uint64)
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    k = len(po) - 1
+    out = np.zeros(cap * k, np.uint32)
+    n = ctypes.c_uint64()
+    st = lib.pmo_list_matches(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64),
+                              len(off) - 1, len(ad), _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32),
+                              _p(pl, ctypes.c_uint64), k, _p(out, ctypes.c_uint32), cap, ctypes.byref(n))
+    if st != 0:
+        raise RuntimeError(f"oracle listing failed with status {st}")
+    rows = min(n.value, cap)
+    return out[:rows * k].reshape(rows, k), n.value
 
 
 def enumeration_start_role(p_offsets, p_adj, p_labels) -> int:

@@ -682,6 +682,95 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
   }
 }
 
+// The embeddings ENUMERATION counts, listed: the reference's
+// writeEnumeration (multiple_label_enumeration_cpu.tpp:15-35, compiled out
+// there) writes historyIndexVector, the graph vertices bound by the walk's
+// vertex moves in walk order.  Runs the pipeline to the ENUMERATION step
+// (one thread, the canonical order), then lists up to cap matches of k
+// vertices each into out; *n_matches receives the total.
+namespace {
+void enum_list(const State& s, const Walk& w, std::vector<uint32_t>& history, uint32_t cur, size_t pos,
+               std::vector<uint32_t>& out, uint64_t cap, uint64_t& n) {
+  if (pos == w.length()) {
+    if (n < cap) out.insert(out.end(), history.begin(), history.end());
+    ++n;
+    return;
+  }
+  const int move = w.moves[pos];
+  if (move == kVertexNoStore || move == kVertexStore) {
+    const uint32_t next_role = w.ids[pos];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb] || !s.has(nb, next_role)) continue;
+      bool seen = false;
+      for (uint32_t h : history)
+        if (h == nb) seen = true;
+      if (seen) continue;
+      history.push_back(nb);
+      enum_list(s, w, history, nb, pos + 1, out, cap, n);
+      history.pop_back();
+    }
+  } else if (move == kCheck) {
+    const uint32_t target = history[w.back[pos]];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb] || nb != target) continue;
+      enum_list(s, w, history, cur, pos + 1, out, cap, n);
+      return;
+    }
+  } else {
+    enum_list(s, w, history, history[w.back[pos]], pos + 1, out, cap, n);
+  }
+}
+}  // namespace
+
+int pmo_list_matches(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+                     const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k,
+                     uint32_t* out, uint64_t cap, uint64_t* n_matches) {
+  try {
+    // Pruned state: run the pipeline up to ENUMERATION.
+    std::vector<uint64_t> cand(V);
+    std::vector<uint8_t> eact(E), vact(V);
+    int32_t n_rec = 0;
+    const int st = pmo_run(off, adj, lab, V, E, p_off, p_adj, p_lab, k, 1, 1, 1, nullptr, 0, &n_rec, cand.data(),
+                           eact.data(), vact.data());
+    if (st != 0) return st;
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    const QueryConstraints qc = compile_constraints(pg);
+    State s;
+    s.off = off;
+    s.adj = adj;
+    s.lab = lab;
+    s.V = V;
+    s.E = E;
+    s.k = k;
+    s.parallel = s.nlcc_parallel = false;
+    s.active = vact;
+    s.edge_active = eact;
+    s.cand = cand;
+    auto first = qc.enumeration.walks.cbegin();
+    const uint32_t start_role = first->first;
+    std::vector<uint32_t> list, history;
+    uint64_t n = 0;
+    for (uint32_t v = 0; v < V; ++v) {
+      if (!s.active[v] || !s.has(v, start_role)) continue;
+      history.assign(1, v);
+      enum_list(s, first->second, history, v, 1, list, cap, n);
+    }
+    if (out && !list.empty()) memcpy(out, list.data(), 4 * list.size());
+    if (n_matches) *n_matches = n;
+    return 0;
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
 // The start role of the enumeration walk (walkMap.cbegin()->first,
 // multiple_label_enumeration_cpu.tpp:126-174): ENUMERATION's sources are the
 // active vertices holding it.

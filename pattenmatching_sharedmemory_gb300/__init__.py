@@ -132,6 +132,9 @@ def _load_library() -> ctypes.CDLL:
         "pm_graph_assign_labels": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32,
                                                     ctypes.c_double, ctypes.c_uint64]),
         "pm_graph_host_csr": (ctypes.c_int32, [ctypes.c_void_p, P(c_u64p), P(c_u32p), P(c_u64p)]),
+        "pm_graph_make_undirected": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_void_p)]),
+        "pm_graph_sort_neighbours": (ctypes.c_int32, [ctypes.c_void_p]),
+        "pm_graph_sort_vertices_by_degree": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_void_p), c_u32p]),
         "pm_graph_to_device": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32]),
         "pm_graph_write_text": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
         "pm_graph_set_hub_plan": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
@@ -146,6 +149,9 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_run": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), ctypes.c_int32, P(ctypes.c_int32)]),
         "pm_query_prune": (ctypes.c_int32, [ctypes.c_void_p, P(StepRecord), ctypes.c_int32, P(ctypes.c_int32)]),
         "pm_set_query_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
+        "pm_query_list_matches": (ctypes.c_int32, [ctypes.c_void_p, c_u32p, ctypes.c_uint64, c_u32p, c_u64p]),
+        "pm_query_write_matches": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint64, c_u64p]),
+        "pm_query_export_subgraph": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, ctypes.c_uint64, c_u64p]),
         "pm_debug_fail_device_alloc_after": (ctypes.c_int32, [ctypes.c_int64]),
         "pm_server_cancel": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64]),
         "pm_query_export": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u8p, c_u8p]),
@@ -307,6 +313,25 @@ class Graph:
         lab = np.ctypeslib.as_array(l, shape=(V,)) if V and l else np.zeros(V, np.uint64)
         return off, adj, lab
 
+    def undirected(self) -> "Graph":
+        """The generator's UNDIRECTED command: a new host graph with every
+        entry in both directions (duplicates kept)."""
+        h = ctypes.c_void_p()
+        _check(lib.pm_graph_make_undirected(self._h, ctypes.byref(h)))
+        return Graph(h)
+
+    def sort_neighbours(self) -> "Graph":
+        """The generator's SORT_NEIGHBOURS command, in place."""
+        _check(lib.pm_graph_sort_neighbours(self._h))
+        return self
+
+    def sorted_by_degree(self):
+        """The generator's SORT_VERTICES command: (new host graph, old_to_new)."""
+        h = ctypes.c_void_p()
+        m = np.zeros(max(self.vertex_count, 1), np.uint32)
+        _check(lib.pm_graph_sort_vertices_by_degree(self._h, ctypes.byref(h), _ptr(m, ctypes.c_uint32)))
+        return Graph(h), m[:self.vertex_count]
+
     def write_text(self, graph_path, labels_path=None) -> None:
         _check(lib.pm_graph_write_text(self._h, _enc(graph_path), _enc(labels_path)))
 
@@ -333,6 +358,7 @@ class Query:
                  load_pattern_labels: bool = True):
         self.graph = graph
         self._h = ctypes.c_void_p()
+        self._k = None if pattern is None else pattern.n
         if pattern_dir is not None:
             d = str(pattern_dir)
             _check(lib.pm_query_create(graph._h, _enc(d), int(load_pattern_labels), ctypes.byref(self._h)))
@@ -385,6 +411,35 @@ class Query:
         _check(lib.pm_query_export(self._h, _ptr(cand, ctypes.c_uint64), _ptr(eact, ctypes.c_uint8),
                                    _ptr(vact, ctypes.c_uint8)))
         return cand, eact, vact
+
+    def list_matches(self, cap: int = 1 << 20):
+        """pm_query_list_matches: (matches as an (n, k) uint32 array, at most
+        cap rows; total count)."""
+        per, n = ctypes.c_uint32(), ctypes.c_uint64()
+        k = self._k
+        if k is None:  # template from files: ask for the match width first
+            _check(lib.pm_query_list_matches(self._h, None, 0, ctypes.byref(per), ctypes.byref(n)))
+            k = per.value
+        buf = np.zeros(max(cap, 1) * max(k, 1), np.uint32)
+        _check(lib.pm_query_list_matches(self._h, _ptr(buf, ctypes.c_uint32), cap, ctypes.byref(per),
+                                         ctypes.byref(n)))
+        rows = min(n.value, cap)
+        return buf[:rows * per.value].reshape(rows, per.value), n.value
+
+    def write_matches(self, path, max_matches: int = 1 << 20) -> int:
+        n = ctypes.c_uint64()
+        _check(lib.pm_query_write_matches(self._h, _enc(path), max_matches, ctypes.byref(n)))
+        return n.value
+
+    def export_subgraph(self):
+        """pm_query_export_subgraph: (offsets[V + 1], adj) of the pruned subgraph."""
+        V = self.graph.vertex_count
+        off = np.zeros(V + 1, np.uint64)
+        n = ctypes.c_uint64()
+        _check(lib.pm_query_export_subgraph(self._h, _ptr(off, ctypes.c_uint64), None, 0, ctypes.byref(n)))
+        adj = np.zeros(max(n.value, 1), np.uint32)
+        _check(lib.pm_query_export_subgraph(self._h, None, _ptr(adj, ctypes.c_uint32), n.value, ctypes.byref(n)))
+        return off, adj[:n.value]
 
     def write_outputs(self, out_dir) -> None:
         _check(lib.pm_query_write_outputs(self._h, _enc(out_dir)))

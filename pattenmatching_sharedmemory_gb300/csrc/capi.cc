@@ -160,6 +160,50 @@ pm_status_t pm_graph_assign_labels(pm_graph* g, int32_t kind, uint32_t n_labels,
   });
 }
 
+pm_status_t pm_graph_make_undirected(const pm_graph* g, pm_graph** out) {
+  PM_REQUIRE(g && out, "null argument");
+  return guarded([&]() -> pm_status_t {
+    auto* n = new pm_graph();
+    try {
+      n->impl.host = make_undirected(g->impl.host);
+      n->impl.finalize_host();
+    } catch (...) {
+      delete n;
+      throw;
+    }
+    *out = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_sort_neighbours(pm_graph* g) {
+  PM_REQUIRE(g, "graph is NULL");
+  PM_REQUIRE(g->impl.device < 0, "sort the graph before it moves to a device");
+  return guarded([&]() -> pm_status_t {
+    sort_neighbours(g->impl.host);
+    g->impl.finalize_host();
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_graph_sort_vertices_by_degree(const pm_graph* g, pm_graph** out, uint32_t* old_to_new) {
+  PM_REQUIRE(g && out, "null argument");
+  return guarded([&]() -> pm_status_t {
+    auto* n = new pm_graph();
+    try {
+      std::vector<uint32_t> map;
+      n->impl.host = sort_vertices_by_degree(g->impl.host, &map);
+      n->impl.finalize_host();
+      if (old_to_new && !map.empty()) std::memcpy(old_to_new, map.data(), 4 * map.size());
+    } catch (...) {
+      delete n;
+      throw;
+    }
+    *out = n;
+    return PM_SUCCESS;
+  });
+}
+
 pm_status_t pm_graph_host_csr(const pm_graph* g, const uint64_t** offsets, const uint32_t** adj,
                               const uint64_t** labels) {
   PM_REQUIRE(g, "graph is NULL");
@@ -296,6 +340,51 @@ pm_status_t pm_query_prune(pm_query* q, pm_step_record* records, int32_t cap, in
 pm_status_t pm_debug_fail_device_alloc_after(int64_t n) {
   set_fail_alloc_after(n);
   return PM_SUCCESS;
+}
+
+pm_status_t pm_query_list_matches(pm_query* q, uint32_t* matches, uint64_t cap, uint32_t* per_match,
+                                  uint64_t* n_matches) {
+  PM_REQUIRE(q, "query is NULL");
+  PM_REQUIRE(matches || cap == 0, "null match buffer");
+  return guarded([&]() -> pm_status_t {
+    const uint64_t n = q->impl.list_matches(matches, cap, per_match);
+    if (n_matches) *n_matches = n;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_write_matches(pm_query* q, const char* path, uint64_t max_matches, uint64_t* n_written) {
+  PM_REQUIRE(q && path, "null argument");
+  return guarded([&]() -> pm_status_t {
+    uint32_t k = 0;
+    std::vector<uint32_t> buf(static_cast<size_t>(std::min<uint64_t>(max_matches, 1ull << 28)) *
+                              std::max<uint32_t>(q->impl.k, 1));
+    const uint64_t total = q->impl.list_matches(buf.data(), max_matches, &k);
+    const uint64_t rows = std::min(total, max_matches);
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(PM_E_IO, std::string("cannot open ") + path);
+    // The reference's text form: each bound vertex followed by ';', one
+    // match per line (multiple_label_enumeration_cpu.tpp:27-33).
+    for (uint64_t r = 0; r < rows; ++r) {
+      for (uint32_t j = 0; j < k; ++j) std::fprintf(f, "%u;", buf[r * k + j]);
+      std::fputc('\n', f);
+    }
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) return fail(PM_E_IO, std::string("cannot write ") + path);
+    if (n_written) *n_written = rows;
+    return PM_SUCCESS;
+  });
+}
+
+pm_status_t pm_query_export_subgraph(pm_query* q, uint64_t* offsets, uint32_t* adj, uint64_t cap,
+                                     uint64_t* n_entries) {
+  PM_REQUIRE(q, "query is NULL");
+  return guarded([&]() -> pm_status_t {
+    const uint64_t n = q->impl.export_subgraph(offsets, adj, cap);
+    if (n_entries) *n_entries = n;
+    if (adj && cap < n) return fail(PM_E_INVALID_ARG, "adjacency buffer holds fewer entries than the subgraph");
+    return PM_SUCCESS;
+  });
 }
 
 pm_status_t pm_set_query_budget_ms(double ms) {

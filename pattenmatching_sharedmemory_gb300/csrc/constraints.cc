@@ -5,6 +5,7 @@
 
 #include <deque>
 #include <sstream>
+#include <unordered_set>
 
 namespace pmgb {
 namespace {
@@ -15,6 +16,18 @@ bool contains(const std::vector<T>& v, const T& x) {
     if (y == x) return true;
   return false;
 }
+
+// Membership of generated constraints by their identifying ids, so that
+// deduplication stays linear in the number found (dense templates yield
+// thousands of cycles, each found once per rotation and direction); `out`
+// keeps the order of first discovery, as the reference's list does.
+struct IdsHash {
+  size_t operator()(const std::vector<uint32_t>& v) const {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ v.size();
+    for (uint32_t x : v) h = (h ^ x) * 0x100000001B3ull;
+    return static_cast<size_t>(h ^ (h >> 29));
+  }
+};
 
 // --- local constraints: generate_constraint_local.cc:12-33 --------------
 std::vector<LocalConstraint> gen_local(const PatternGraph& p) {
@@ -73,11 +86,12 @@ struct CycleSearch {
   std::vector<uint32_t> hist;
   std::vector<label_t> hist_labels;
   uint64_t visited = 0;
+  std::unordered_set<std::vector<uint32_t>, IdsHash> seen;  // ids of out's entries
   void dfs(uint32_t source, uint32_t cur, size_t remaining) {
     if (remaining == 0) {
       if (source != cur) return;
       CycleConstraint c = make_cycle(hist, hist_labels);
-      if (!contains(out, c)) out.push_back(c);
+      if (seen.insert(c.ids).second) out.push_back(std::move(c));
       return;
     }
     for (uint64_t e = p.offsets[cur]; e < p.offsets[cur + 1]; ++e) {
@@ -96,7 +110,7 @@ struct CycleSearch {
 
 std::vector<CycleConstraint> gen_cycles(const PatternGraph& p) {
   std::vector<CycleConstraint> out;
-  CycleSearch s{p, out, {}, {}, 0};
+  CycleSearch s{p, out, {}, {}, 0, {}};
   for (uint32_t v = 0; v < p.n; ++v) {
     s.hist.push_back(v);
     s.hist_labels.push_back(p.labels[v]);
@@ -131,10 +145,13 @@ struct PathSearch {
   std::vector<uint32_t> hist;
   std::vector<label_t> hist_labels;
   uint64_t visited = 0;
+  // ids of out's entries (a path's initial label is its first vertex's
+  // label, so the ids identify it)
+  std::unordered_set<std::vector<uint32_t>, IdsHash> seen;
   void dfs(uint32_t source, uint32_t cur, size_t depth) {
     if (depth >= 2 && p.labels[source] == p.labels[cur] && source != cur) {
       PathConstraint pc = make_path(hist, hist_labels);
-      if (!contains(out, pc)) out.push_back(pc);
+      if (seen.insert(pc.ids).second) out.push_back(std::move(pc));
       return;
     }
     for (uint64_t e = p.offsets[cur]; e < p.offsets[cur + 1]; ++e) {
@@ -153,7 +170,7 @@ struct PathSearch {
 
 std::vector<PathConstraint> gen_paths(const PatternGraph& p) {
   std::vector<PathConstraint> out;
-  PathSearch s{p, out, {}, {}, 0};
+  PathSearch s{p, out, {}, {}, 0, {}};
   for (uint32_t v = 0; v < p.n; ++v) {
     s.hist.push_back(v);
     s.hist_labels.push_back(p.labels[v]);

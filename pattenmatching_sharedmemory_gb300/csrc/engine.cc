@@ -1363,6 +1363,75 @@ void QueryImpl::export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact) {
   PM_CUDA(cudaStreamSynchronize(stream));
 }
 
+uint64_t QueryImpl::list_matches(uint32_t* out, uint64_t cap, uint32_t* per_match) {
+  if (!finished && step != PM_STEP_ENUMERATION) {
+    struct Restore {
+      QueryImpl& q;
+      ~Restore() { q.stop_before_enumeration = false; }
+    } restore{*this};
+    stop_before_enumeration = true;
+    run_all();
+  }
+  const WalkProgram& p = enumeration.cc.programs[0];
+  if (per_match) *per_match = p.n_hist;
+  // The run ended at the iteration cap before ENUMERATION: nothing counted.
+  const bool counted = step == PM_STEP_ENUMERATION ||
+                       std::any_of(records.begin(), records.end(),
+                                   [](const pm_step_record& r) { return r.step == PM_STEP_ENUMERATION; });
+  if (!counted || active_vertices == 0) return 0;
+  const uint32_t n_wl = build_worklist(uint64_t(1) << p.start_role);
+  if (!n_wl) return 0;
+  DeviceBuffer d_out, d_cnt;
+  for (DeviceBuffer* b : {&d_out, &d_cnt}) {
+    b->stream = stream;
+    b->ordered = true;
+  }
+  d_out.ensure(4ull * p.n_hist * std::max<uint64_t>(cap, 1));
+  d_cnt.ensure(2 * sizeof(unsigned long long));
+  PM_CUDA(cudaMemsetAsync(d_cnt.ptr, 0, 2 * sizeof(unsigned long long), stream));
+  clear_step_counters();
+  launch_enum_list(g->dev(), ptrs(), d_progs.as<WalkProgram>() + enumeration.prog_offset, d_wl.as<uint32_t>(), n_wl,
+                   d_out.as<uint32_t>(), cap, d_cnt.as<unsigned long long>(), stream);
+  PM_CUDA(cudaGetLastError());
+  unsigned long long cnt[2] = {0, 0};
+  PM_CUDA(cudaMemcpyAsync(cnt, d_cnt.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, stream));
+  read_counters();  // synchronises; a timeout or device error throws
+  const uint64_t rows = std::min<uint64_t>(cnt[1], cap);
+  if (out && rows) {
+    PM_CUDA(cudaMemcpyAsync(out, d_out.ptr, 4ull * p.n_hist * rows, cudaMemcpyDeviceToHost, stream));
+    PM_CUDA(cudaStreamSynchronize(stream));
+  }
+  return cnt[1];
+}
+
+uint64_t QueryImpl::export_subgraph(uint64_t* offsets, uint32_t* adj, uint64_t cap) {
+  const uint64_t V = g->host.vertex_count;
+  DeviceBuffer d_counts, d_off, d_adj;
+  for (DeviceBuffer* b : {&d_counts, &d_off, &d_adj}) {
+    b->stream = stream;
+    b->ordered = true;
+  }
+  d_counts.ensure(8 * std::max<uint64_t>(V, 1));
+  launch_subgraph(g->dev(), ptrs(), nullptr, d_counts.as<uint64_t>(), nullptr, stream);
+  PM_CUDA(cudaGetLastError());
+  std::vector<uint64_t> off(V + 1, 0);
+  if (V) PM_CUDA(cudaMemcpyAsync(off.data() + 1, d_counts.ptr, 8 * V, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  for (uint64_t v = 0; v < V; ++v) off[v + 1] += off[v];
+  const uint64_t total = off[V];
+  if (offsets) std::memcpy(offsets, off.data(), 8 * (V + 1));
+  if (adj && total && cap >= total) {
+    d_off.ensure(8 * (V + 1));
+    d_adj.ensure(4 * total);
+    PM_CUDA(cudaMemcpyAsync(d_off.ptr, off.data(), 8 * (V + 1), cudaMemcpyHostToDevice, stream));
+    launch_subgraph(g->dev(), ptrs(), d_off.as<uint64_t>(), nullptr, d_adj.as<uint32_t>(), stream);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaMemcpyAsync(adj, d_adj.ptr, 4 * total, cudaMemcpyDeviceToHost, stream));
+    PM_CUDA(cudaStreamSynchronize(stream));
+  }
+  return total;
+}
+
 namespace {
 void make_dirs(const std::string& path) {
   std::string cur;

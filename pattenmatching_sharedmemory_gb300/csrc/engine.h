@@ -177,6 +177,14 @@ struct QueryImpl {
   // Every device buffer the query owns.
   std::vector<DeviceBuffer*> buffers();
   void write_outputs(const std::string& dir);
+  // The embeddings ENUMERATION counts (the pruning runs first when the query
+  // has not reached ENUMERATION yet): up to cap of them, n_hist vertex ids
+  // each in walk order, into out; returns the total (the ENUMERATION count;
+  // 0 when the run ends at the iteration cap before ENUMERATION).
+  uint64_t list_matches(uint32_t* out, uint64_t cap, uint32_t* per_match);
+  // The pruned subgraph in CSR form over the original ids: offsets[V + 1],
+  // and up to cap entries into adj; returns the entry count.
+  uint64_t export_subgraph(uint64_t* offsets, uint32_t* adj, uint64_t cap);
 
  private:
   void reset_modified();

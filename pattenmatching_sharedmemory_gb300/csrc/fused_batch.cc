@@ -1,4 +1,5 @@
-// Batched form: lockstep rounds with shared LCC launches (see fused_batch.h).
+// Batched form: shared LCC launches, per-query walker steps on a host pool
+// (see fused_batch.h).
 #include "fused_batch.h"
 
 #include <algorithm>
@@ -12,6 +13,7 @@ FusedBatch::FusedBatch(GraphImpl* g, const std::vector<PatternGraph>& patterns, 
   PM_CUDA(cudaSetDevice(g_->device));
   PM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   items_.resize(patterns.size());
+  running_.assign(patterns.size(), 0);
   try {
     for (size_t i = 0; i < patterns.size(); ++i) {
       items_[i].q = std::make_unique<QueryImpl>();
@@ -24,27 +26,7 @@ FusedBatch::FusedBatch(GraphImpl* g, const std::vector<PatternGraph>& patterns, 
     throw;
   }
   const size_t n_threads = std::min<size_t>(std::max<size_t>(patterns.size(), 1), 16);
-  for (size_t t = 0; t < n_threads; ++t)
-    workers_.emplace_back([this] {
-      if (cudaSetDevice(g_->device) != cudaSuccess) return;
-      uint64_t seen = 0;
-      while (true) {
-        std::function<void()> task;
-        {
-          std::unique_lock<std::mutex> lk(mu_);
-          cv_work_.wait(lk, [&] { return stop_ || (generation_ != seen && next_task_ < tasks_.size()); });
-          if (stop_) return;
-          task = tasks_[next_task_++];
-          if (next_task_ == tasks_.size()) seen = generation_;
-        }
-        task();
-        {
-          std::lock_guard<std::mutex> lk(mu_);
-          ++finished_tasks_;
-        }
-        cv_done_.notify_all();
-      }
-    });
+  for (size_t t = 0; t < n_threads; ++t) workers_.emplace_back(&FusedBatch::worker, this);
 }
 
 FusedBatch::~FusedBatch() {
@@ -61,35 +43,40 @@ FusedBatch::~FusedBatch() {
   }
 }
 
-void FusedBatch::parallel_steps(const std::vector<size_t>& idx) {
-  if (idx.empty()) return;
-  std::vector<std::function<void()>> tasks;
-  for (size_t i : idx)
-    tasks.push_back([this, i] {
-      FusedBatchItem& it = items_[i];
-      try {
-        it.q->check_request();
-        it.q->run_step();
-      } catch (const PmError& e) {
-        it.status = e.code;
-        it.error = e.message;
-      } catch (const std::bad_alloc&) {
-        it.status = PM_E_OOM;
-        it.error = "host allocation failed";
-      } catch (const std::exception& e) {
-        it.status = PM_FAILURE;
-        it.error = e.what();
-      }
-      set_thread_walk_budget_cap_ns(0);
-    });
-  std::unique_lock<std::mutex> lk(mu_);
-  tasks_ = std::move(tasks);
-  next_task_ = 0;
-  finished_tasks_ = 0;
-  ++generation_;
-  cv_work_.notify_all();
-  cv_done_.wait(lk, [&] { return finished_tasks_ == tasks_.size(); });
-  tasks_.clear();
+// Runs the next step of the queries the coordinator queues, one at a time.
+void FusedBatch::worker() {
+  if (cudaSetDevice(g_->device) != cudaSuccess) return;
+  while (true) {
+    size_t i = 0;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_work_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+      if (stop_) return;
+      i = queue_.back();
+      queue_.pop_back();
+    }
+    FusedBatchItem& it = items_[i];
+    try {
+      it.q->check_request();
+      it.q->run_step();
+    } catch (const PmError& e) {
+      it.status = e.code;
+      it.error = e.message;
+    } catch (const std::bad_alloc&) {
+      it.status = PM_E_OOM;
+      it.error = "host allocation failed";
+    } catch (const std::exception& e) {
+      it.status = PM_FAILURE;
+      it.error = e.what();
+    }
+    set_thread_walk_budget_cap_ns(0);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      running_[i] = 0;
+      ++finished_steps_;
+    }
+    cv_done_.notify_all();
+  }
 }
 
 void FusedBatch::run() {
@@ -105,7 +92,7 @@ void FusedBatch::run() {
     it.done = true;
     it.run_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
   };
-  // Runs a shared LCC phase; a failure ends every query it covered.
+  // A shared LCC phase on this thread; a failure ends every query it covered.
   auto shared_phase = [&](const std::vector<size_t>& idx, bool lcc0) {
     std::vector<size_t> ok;
     for (size_t i : idx) {
@@ -136,11 +123,18 @@ void FusedBatch::run() {
       }
     }
   };
+  std::unique_lock<std::mutex> lk(mu_);
   while (true) {
+    // Queries between steps (not on a worker) and what they need next.
     std::vector<size_t> at_lcc0, at_lcc, others;
+    size_t busy = 0;
     for (size_t i = 0; i < items_.size(); ++i) {
       FusedBatchItem& it = items_[i];
       if (it.done) continue;
+      if (running_[i]) {
+        ++busy;
+        continue;
+      }
       QueryImpl& q = *it.q;
       if (it.status != PM_SUCCESS || q.finished || q.iteration >= 1000 ||
           (prune_only_ && q.step == PM_STEP_ENUMERATION)) {
@@ -154,11 +148,24 @@ void FusedBatch::run() {
       else
         others.push_back(i);
     }
-    if (at_lcc0.empty() && at_lcc.empty() && others.empty()) break;
+    if (!busy && at_lcc0.empty() && at_lcc.empty() && others.empty()) break;
     ++rounds;
-    shared_phase(at_lcc0, true);
-    shared_phase(at_lcc, false);
-    parallel_steps(others);
+    for (size_t i : others) {
+      running_[i] = 1;
+      queue_.push_back(i);
+    }
+    if (!others.empty()) cv_work_.notify_all();
+    if (!at_lcc0.empty() || !at_lcc.empty()) {
+      // The shared phases run while workers keep stepping other queries.
+      lk.unlock();
+      shared_phase(at_lcc0, true);
+      shared_phase(at_lcc, false);
+      lk.lock();
+      continue;
+    }
+    // Nothing for this thread: wait for a worker to finish a step.
+    finished_steps_ = 0;
+    cv_done_.wait(lk, [&] { return finished_steps_ != 0; });
   }
 }
 

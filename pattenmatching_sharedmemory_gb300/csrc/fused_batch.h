@@ -1,20 +1,21 @@
-// Batched form: many template queries over one resident graph advanced in
-// lockstep rounds, with the LCC work of all of them in shared launches.
+// Batched form: many template queries over one resident graph, with the LCC
+// work of all of them in shared launches.
 //
 // The reference runs one template per process (MultipleLabelCpu::
 // runPatternMatching, multiple_label_cpu.cc:113-184); each query here keeps
-// that schedule (multiple_label_step.cc:30-83) on its own state.  A round
-// advances every unfinished query by at least one step:
-//   1. the queries at LCC0 run it together (one multi-query launch);
-//   2. the queries at LCC run their fixpoints together: each pass is one
-//      multi-query launch sequence over the queries still iterating, whose
-//      blocks of different queries walk the same CSR ranges at the same time
-//      (one HBM read of an adjacency range serves every query in the batch);
-//   3. every other query runs its next step (CC / PC / TDS / ENUMERATION, or
-//      any step of a query whose graph state is empty) on its own stream,
-//      from a pool of host threads, so their walker launches overlap.
-// Results are those of each query run alone: the same rows (timing columns
-// aside), state and match count.
+// that schedule (multiple_label_step.cc:30-83) on its own state.  A
+// coordinator thread repeatedly takes the queries that are between steps:
+//   - those whose next step is LCC0, or an LCC fixpoint, run it together:
+//     one multi-query launch (LCC0), or one multi-query launch sequence per
+//     pass over the queries still iterating (LCC), whose blocks of different
+//     queries walk the same CSR ranges at the same time, so one HBM read of
+//     an adjacency range serves every query in the group;
+//   - every other query's next step (CC / PC / TDS / ENUMERATION, or any
+//     step of a query whose graph state is empty) goes to a pool of host
+//     threads and runs on the query's own stream, overlapping the walker
+//     launches of other queries and the shared LCC launches.
+// No query waits for another's walker step.  Results are those of each query
+// run alone: the same rows (timing columns aside), state and match count.
 #pragma once
 #include <condition_variable>
 #include <functional>
@@ -50,23 +51,23 @@ class FusedBatch {
   void run();
   size_t size() const { return items_.size(); }
   FusedBatchItem& item(size_t i) { return items_.at(i); }
-  // Rounds run and shared LCC launches issued (statistics).
+  // Coordinator passes and shared LCC phases issued (statistics).
   uint64_t rounds = 0, fused_lcc_passes = 0;
 
  private:
-  void parallel_steps(const std::vector<size_t>& idx);
+  void worker();
 
   GraphImpl* g_;
   bool prune_only_;
   std::vector<FusedBatchItem> items_;
+  std::vector<uint8_t> running_;  // a step of the query is on a worker
   cudaStream_t stream_ = nullptr;
-  // host thread pool for step 3
+  // host thread pool for the per-query steps
   std::vector<std::thread> workers_;
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
-  std::vector<std::function<void()>> tasks_;
-  size_t next_task_ = 0, finished_tasks_ = 0;
-  uint64_t generation_ = 0;
+  std::vector<size_t> queue_;     // queries whose next step a worker should run
+  size_t finished_steps_ = 0;     // steps finished since the coordinator last looked
   bool stop_ = false;
 };
 

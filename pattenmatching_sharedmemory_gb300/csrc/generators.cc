@@ -196,4 +196,89 @@ void assign_labels(HostGraph& g, int kind, uint32_t n_labels, double s, uint64_t
   }
 }
 
+// ---- graph ingestion tools (the TOTEM generator's ALTER commands,
+// src/generator/totem_generator.cc) ------------------------------------------
+
+namespace {
+// CSR from an edge list the way the generator's edgelist_to_graph does it
+// (totem_generator.cc:92-125): per-vertex degree counts, then each entry is
+// placed at the last free position of its source's list, so a list holds
+// its entries in reverse order of appearance.
+HostGraph csr_from_edgelist(const std::vector<uint32_t>& src, const std::vector<uint32_t>& dst, uint32_t V,
+                            bool directed) {
+  HostGraph g;
+  g.vertex_count = V;
+  g.directed = directed;
+  g.offsets.assign(static_cast<size_t>(V) + 1, 0);
+  std::vector<uint64_t> fill(V, 0);
+  for (uint32_t u : src) ++fill[u];
+  for (uint32_t v = 0; v < V; ++v) g.offsets[v + 1] = g.offsets[v] + fill[v];
+  g.edge_count = g.offsets[V];
+  g.adj.resize(g.edge_count);
+  for (size_t i = 0; i < src.size(); ++i) g.adj[g.offsets[src[i]] + --fill[src[i]]] = dst[i];
+  return g;
+}
+}  // namespace
+
+// UNDIRECTED (alter_undirected_handler, totem_generator.cc:631-680): every
+// CSR entry u -> v contributes u -> v and v -> u, in CSR order; duplicates
+// are kept.  Labels are carried over.
+HostGraph make_undirected(const HostGraph& in) {
+  std::vector<uint32_t> src, dst;
+  src.reserve(2 * in.edge_count);
+  dst.reserve(2 * in.edge_count);
+  for (uint32_t v = 0; v < in.vertex_count; ++v)
+    for (uint64_t e = in.offsets[v]; e < in.offsets[v + 1]; ++e) {
+      src.push_back(v);
+      dst.push_back(in.adj[e]);
+      src.push_back(in.adj[e]);
+      dst.push_back(v);
+    }
+  HostGraph g = csr_from_edgelist(src, dst, in.vertex_count, false);
+  g.labels = in.labels;
+  g.valued = in.valued;
+  return g;
+}
+
+// SORT_NEIGHBOURS (alter_sort_neighbours_handler, totem_generator.cc:764-770,
+// graph_sort_nbrs ascending): every adjacency list sorted by id, in place.
+void sort_neighbours(HostGraph& g) {
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < static_cast<int64_t>(g.vertex_count); ++v)
+    std::sort(g.adj.begin() + static_cast<int64_t>(g.offsets[v]), g.adj.begin() + static_cast<int64_t>(g.offsets[v + 1]));
+}
+
+// SORT_VERTICES (alter_sort_vertices_handler, totem_generator.cc:682-748):
+// vertex ids renumbered in ascending order of degree, then the edge list
+// (old CSR order, both ends renamed) rebuilt as edgelist_to_graph does.  The
+// reference sorts with a parallel sort, which leaves the order of equal
+// degrees unspecified; here ties keep ascending old ids (a stable sort).
+// Labels move with their vertices; old_to_new receives the renumbering.
+HostGraph sort_vertices_by_degree(const HostGraph& in, std::vector<uint32_t>* old_to_new) {
+  const uint32_t V = in.vertex_count;
+  std::vector<uint32_t> order(V);
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+    return in.offsets[a + 1] - in.offsets[a] < in.offsets[b + 1] - in.offsets[b];
+  });
+  std::vector<uint32_t> map(V);
+  for (uint32_t i = 0; i < V; ++i) map[order[i]] = i;
+  std::vector<uint32_t> src, dst;
+  src.reserve(in.edge_count);
+  dst.reserve(in.edge_count);
+  for (uint32_t v = 0; v < V; ++v)
+    for (uint64_t e = in.offsets[v]; e < in.offsets[v + 1]; ++e) {
+      src.push_back(map[v]);
+      dst.push_back(map[in.adj[e]]);
+    }
+  HostGraph g = csr_from_edgelist(src, dst, V, in.directed);
+  if (!in.labels.empty()) {
+    g.labels.assign(V, 0);
+    for (uint32_t v = 0; v < V; ++v) g.labels[map[v]] = in.labels[v];
+  }
+  g.valued = in.valued;
+  if (old_to_new) *old_to_new = std::move(map);
+  return g;
+}
+
 }  // namespace pmgb

@@ -13,4 +13,10 @@ HostGraph generate_rmat(int scale, int edge_factor, double a, double b, double c
 // Assigns labels 0..n_labels-1 to every vertex.
 void assign_labels(HostGraph& g, int kind, uint32_t n_labels, double s, uint64_t seed);
 
+// Graph ingestion tools: the TOTEM generator's UNDIRECTED, SORT_NEIGHBOURS
+// and SORT_VERTICES commands (see generators.cc).
+HostGraph make_undirected(const HostGraph& in);
+void sort_neighbours(HostGraph& g);
+HostGraph sort_vertices_by_degree(const HostGraph& in, std::vector<uint32_t>* old_to_new);
+
 }  // namespace pmgb

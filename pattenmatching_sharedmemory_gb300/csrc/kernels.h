@@ -205,6 +205,20 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
                       const uint32_t* wl, uint32_t n_wl, const uint4* items, uint32_t n_items, uint4* overflow,
                       const WalkScratch& scratch, cudaStream_t s);
 
+// Lists the embeddings of the ENUMERATION program `prog` from every
+// worklist source: each completed walk takes slot counters[1]++ and, below
+// cap, writes its n_hist history vertices to out[slot * n_hist ...];
+// counters[0] is the work counter (both start at 0).  Stops with
+// kDeviceErrorTimeout in q.ctr past the walker budget.
+void launch_enum_list(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
+                      uint32_t n_wl, uint32_t* out, uint64_t cap, unsigned long long* counters, cudaStream_t s);
+
+// The pruned subgraph (active CSR entries between active vertices): with
+// out_adj null, counts[v] = such entries of v; else writes them to
+// out_adj[out_off[v] ...] in CSR order.
+void launch_subgraph(const DevGraph& g, const QueryDevPtrs& q, const uint64_t* out_off, uint64_t* counts,
+                     uint32_t* out_adj, cudaStream_t s);
+
 // Export of the pruned state.
 void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,
                    cudaStream_t s);

@@ -1416,6 +1416,225 @@ void launch_enumerate(const DevGraph& g, const QueryDevPtrs& q, const WalkProgra
                                     g_enum_pair_tail, g_enum_second_split));
 }
 
+// ---- match listing --------------------------------------------------------
+//
+// The embeddings ENUMERATION counts, written out: the reference's
+// writeEnumeration (multiple_label_enumeration_cpu.tpp:15-35) records
+// historyIndexVector, the graph vertices bound by the walk's vertex moves in
+// walk order.  One warp per source of the start role, depth-first over the
+// enumeration program with the reference's semantics
+// (enumeration_cpu.tpp:39-118): a VERTEX step binds an active neighbour
+// behind an active CSR entry that holds the step's role and is not yet in
+// the history (embeddings are injective), 32 entries tested per round; a
+// CHECK step needs an active entry to the history vertex it names; a MOVE
+// step continues from a history vertex.  Each completed walk takes a slot
+// (counters[1]); slots below `cap` are written.  No memo and no tail
+// shortcut: every leaf is visited, so counters[1] ends at the ENUMERATION
+// count.
+namespace {
+constexpr int kListWarps = 4;
+
+template <class W>
+__global__ void __launch_bounds__(kListWarps * 32) k_enum_list(DevGraph g, DevState<W> st,
+                                                               const WalkProgram* __restrict__ prog_in,
+                                                               const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                                               uint32_t* out, uint64_t cap,
+                                                               unsigned long long* counters, uint64_t budget_ns,
+                                                               StepCounters* ctr) {
+  __shared__ WalkProgram prog;
+  __shared__ uint8_t s_hidx[kMaxWalkSteps];  // VERTEX step -> history index
+  __shared__ uint64_t s_pos[kListWarps][kMaxWalkSteps], s_end[kListWarps][kMaxWalkSteps],
+      s_base[kListWarps][kMaxWalkSteps];
+  __shared__ uint32_t s_mask[kListWarps][kMaxWalkSteps];
+  __shared__ uint32_t s_hist[kListWarps][64];
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(prog_in);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&prog);
+    for (uint32_t i = threadIdx.x; i < sizeof(WalkProgram) / 4; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint8_t h = 1;
+    for (int d = 1; d < prog.n_steps; ++d)
+      if (prog.steps[d].kind == kStepVertex || prog.steps[d].kind == kStepFinal) s_hidx[d] = h++;
+  }
+  __syncthreads();
+  const unsigned lane = lane_id();
+  const unsigned wib = threadIdx.x >> 5;
+  uint64_t* pos = s_pos[wib];
+  uint64_t* end = s_end[wib];
+  uint64_t* base = s_base[wib];
+  uint32_t* mask = s_mask[wib];
+  uint32_t* hist = s_hist[wib];
+  const uint64_t deadline = warp_step_deadline(ctr, budget_ns);
+  const int n_steps = prog.n_steps;
+  const uint32_t nh = prog.n_hist;
+  uint32_t iters = 0;
+  while (true) {
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(&counters[0], 1ull);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= n_wl) return;
+    const uint32_t v = wl[item];
+    if (lane == 0) hist[0] = v;
+    uint32_t cur = v;
+    int d = 1;
+    bool entering = true;
+    __syncwarp();
+    while (d > 0) {
+      if ((++iters & 63u) == 0) {
+        uint64_t now = 0;
+        if (lane == 0) now = global_timer_ns();
+        now = __shfl_sync(kFull, now, 0);
+        if (now > deadline) {
+          if (lane == 0) atomicMax(&ctr->error, kDeviceErrorTimeout);
+          return;
+        }
+      }
+      if (d == n_steps) {  // a completed walk
+        unsigned long long slot = 0;
+        if (lane == 0) slot = atomicAdd(&counters[1], 1ull);
+        slot = __shfl_sync(kFull, slot, 0);
+        if (slot < cap)
+          for (uint32_t j = lane; j < nh; j += 32) out[slot * nh + j] = hist[j];
+        --d;
+        entering = false;
+        __syncwarp();
+        continue;
+      }
+      const WalkStep sp = prog.steps[d];
+      if (sp.kind == kStepVertex || sp.kind == kStepFinal) {
+        if (entering) {
+          if (lane == 0) {
+            pos[d] = g.off[cur];
+            end[d] = g.off[cur + 1];
+            mask[d] = 0;
+          }
+          __syncwarp();
+        }
+        const uint32_t hi = s_hidx[d];
+        bool moved = false;
+        while (!moved) {
+          const uint32_t m = mask[d];
+          if (m) {
+            const uint32_t j = __ffs(m) - 1;
+            const uint32_t w = g.adj[base[d] + j];
+            __syncwarp();
+            if (lane == 0) {
+              mask[d] = m & (m - 1);
+              hist[hi] = w;
+            }
+            __syncwarp();
+            cur = w;
+            ++d;
+            entering = true;
+            moved = true;
+          } else if (pos[d] >= end[d]) {
+            --d;
+            entering = false;
+            moved = true;
+          } else {
+            const uint64_t b = pos[d], e = b + lane;
+            bool ok = false;
+            if (e < end[d] && edge_active(st.eact, e)) {
+              const uint32_t nb = g.adj[e];
+              const uint64_t cw = Pack<W>::cand(st.vs[nb]);
+              ok = cw != 0 && ((cw >> sp.role) & 1) && !(sp.kind == kStepFinal && nb == hist[0]);
+              for (uint32_t h = 0; ok && h < hi; ++h)
+                if (hist[h] == nb) ok = false;
+            }
+            const unsigned bm = __ballot_sync(kFull, ok);
+            __syncwarp();
+            if (lane == 0) {
+              base[d] = b;
+              pos[d] = b + 32;
+              mask[d] = bm;
+            }
+            __syncwarp();
+          }
+        }
+      } else if (sp.kind == kStepCheck) {
+        if (!entering) {
+          --d;
+          continue;
+        }
+        const uint32_t target = hist[sp.hist];
+        const uint64_t b = g.off[cur], e_end = g.off[cur + 1];
+        bool found = false;
+        if (Pack<W>::cand(st.vs[target]) != 0)
+          for (uint64_t c = b; c < e_end && !found; c += 32) {
+            const uint64_t e = c + lane;
+            const bool hit = e < e_end && g.adj[e] == target && edge_active(st.eact, e);
+            found = __any_sync(kFull, hit);
+          }
+        if (found) {
+          ++d;
+        } else {
+          --d;
+          entering = false;
+        }
+      } else {  // MOVE
+        if (!entering) {
+          --d;
+          continue;
+        }
+        cur = hist[sp.hist];
+        ++d;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void launch_enum_list(const DevGraph& g, const QueryDevPtrs& q, const WalkProgram* prog, const uint32_t* wl,
+                      uint32_t n_wl, uint32_t* out, uint64_t cap, unsigned long long* counters, cudaStream_t s) {
+  const uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * 8;
+  PM_DISPATCH_WORD(q.word_kind, k_enum_list<W><<<blocks, kListWarps * 32, 0, s>>>(
+                                    g, state_of<W>(q), prog, wl, n_wl, out, cap, counters,
+                                    effective_walk_budget_ns(), q.ctr));
+}
+
+namespace {
+// ---- pruned subgraph export ---------------------------------------------------
+// The reference's printActiveGraph (multiple_label_cpu.cc:270-284) prints a
+// CSR entry when it is active and both its vertices are active.  Pass 1
+// counts such entries per vertex (warp per vertex), the host scans, pass 2
+// writes them in CSR order.
+template <class W>
+__global__ void __launch_bounds__(256) k_subgraph(DevGraph g, DevState<W> st, const uint64_t* __restrict__ out_off,
+                                                  uint64_t* counts, uint32_t* out_adj) {
+  const unsigned lane = lane_id();
+  const uint64_t warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t v = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; v < g.V; v += warps) {
+    const bool va = Pack<W>::cand(st.vs[v]) != 0;
+    uint64_t n = 0;
+    const uint64_t b = g.off[v], e = g.off[v + 1];
+    uint64_t w = out_off ? out_off[v] : 0;
+    for (uint64_t c = b; va && c < e; c += 32) {
+      const uint64_t x = c + lane;
+      uint32_t nb = 0;
+      bool keep = false;
+      if (x < e && edge_active(st.eact, x)) {
+        nb = g.adj[x];
+        keep = Pack<W>::cand(st.vs[nb]) != 0;
+      }
+      const unsigned km = __ballot_sync(kFull, keep);
+      if (out_adj && keep) out_adj[w + __popc(km & ((1u << lane) - 1))] = nb;
+      w += __popc(km);
+      n += __popc(km);
+    }
+    if (!out_adj && lane == 0) counts[v] = n;
+  }
+}
+}  // namespace
+
+void launch_subgraph(const DevGraph& g, const QueryDevPtrs& q, const uint64_t* out_off, uint64_t* counts,
+                     uint32_t* out_adj, cudaStream_t s) {
+  const int grid = device_sm_count() * 8;
+  PM_DISPATCH_WORD(q.word_kind, k_subgraph<W><<<grid, 256, 0, s>>>(g, state_of<W>(q), out_off, counts, out_adj));
+}
+
 }  // namespace pmgb
 
 // ===========================================================================

@@ -67,10 +67,10 @@ def test_state_matches_oracle(case):
     off, adj, lab = g.host_csr()
     ref = oracle.run(off, adj, lab, p.offsets, p.adj, p.labels, threads=1, stop_before_enumeration=True)
     q = pm.Query(g, pattern=p)
-    recs = q.run()
-    rows = [r.as_tuple() for r in recs]
-    assert rows[-2][0] == "ENUMERATION" and ref.rows[-1][0] == "END"
-    assert rows[:-2] == ref.rows[:-1]
+    rows = [r.as_tuple() for r in q.prune()]
+    # Both stop where the schedule would enter ENUMERATION; the last row names it.
+    assert rows[-1][0] == "ENUMERATION"
+    assert rows == ref.rows
     cand, eact, vact = q.export()
     assert np.array_equal(cand, ref.cand)
     assert np.array_equal(eact, ref.eact)
@@ -327,3 +327,22 @@ def test_lcc_graph_alternating_graphs_one_thread():
         for c, g in zip(cases, graphs):
             rows = _rows_and_state(g, C.make_pattern(c))[1]
             assert rows == [tuple(r) for r in c["rows"]], c["name"]
+
+
+@pytest.mark.parametrize("name,rescues,overflows", [("random_10", 1, 1), ("random_11", 1, 1), ("random_15", 1, 1),
+                                                     ("k4_rep_s8", 0, 1), ("random_03", 1, 0)])
+def test_rescue_replay_and_overflow_reruns_run(name, rescues, overflows):
+    """Golden cases that reach the two rare paths: the host replay of the
+    reference's alreadyMatched shortcut (a failing walk that an earlier
+    success marked, multiple_label_cc_cpu.tpp:107) and the re-run of walks
+    whose memo tables overflowed.  The statistics prove the paths ran; the
+    rows prove they kept the reference's results."""
+    case = next(c for c in SYNTH if c["name"] == name)
+    g = C.make_graph(case)
+    q = pm.Query(g, pattern=C.make_pattern(case))
+    rows = [list(r.as_tuple()) for r in q.run()]
+    st = q.stats()
+    q.close()
+    assert rows == case["rows"]
+    assert st["exact_resolutions"] >= rescues
+    assert st["overflow_retries"] >= overflows
