@@ -558,6 +558,94 @@ def run_c3_batch(args, pm, T):
             "fused_rows_equal_alone": f"{same} of the queries completed in both"}
 
 
+def run_c5(args, pm, T):
+    """The large served configuration (run with --workload c5): undirected
+    RMAT scale 26 (67,108,864 vertices, ~2.1e9 CSR entries), 64 labels whose
+    probability follows degree rank; a seeded mixed stream of 10-vertex
+    templates with repeated labels (template-driven search) and 4-cycles,
+    pruning only, same per-request budget; served burst vs one at a time, and
+    a seeded 2 % sample (requests 0, 1, 100, 101, ...: both kinds of
+    template) checked row for row and state for state against the oracle
+    (LCC sweeps on every host core, constraint walks in the canonical
+    one-thread order, a deadline per request)."""
+    import torch
+
+    from oracle import oracle
+
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    t_gen = time.perf_counter()
+    g = pm.Graph.rmat(26, 16, 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels("degree", 64, 1.0, 1)
+    g.to_device(device)
+    gen_s = time.perf_counter() - t_gen
+    n = args.c5_requests
+    tens = T.served_stream(n, n_labels=16, zipf_s=1.0, seed=26, min_vertices=10, max_vertices=10)
+    tmpls = []
+    for i in range(n):
+        if i % 2 == 0:
+            tmpls.append(tens[i])
+        else:
+            r = T.Rng(1000 + i)
+            labels = []
+            while len(labels) < 4:
+                x = r.below(16)
+                if x not in labels:
+                    labels.append(x)
+            tmpls.append(T.cycle(labels))
+    pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    sample = list(range(0, n, 100)) + list(range(1, n, 100))
+    try:
+        with pm.Server(g, slots=args.slots) as srv:
+            serve_burst(srv, pm, tmpls[:4])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            served = serve_burst(srv, pm, tmpls)
+            torch.cuda.synchronize()
+            served_s = time.perf_counter() - t0
+        seq_s, seq_st, _, cls_ms, _ = one_at_a_time(g, pm, tmpls[:args.same_requests])
+        off, adj, lab = g.host_csr()
+        threads = os.cpu_count() or 1
+        checked, cpu_timeouts, gpu_timeouts, mismatches = [], 0, 0, []
+        for i in sample:
+            q = pm.Query(g, pattern=tmpls[i])
+            try:
+                rows = [r.as_tuple() for r in q.prune()]
+                cand, eact, vact = q.export()
+            except pm.PmError:
+                gpu_timeouts += 1
+                q.close()
+                continue
+            q.close()
+            try:
+                ref = oracle.run_ex(off, adj, lab, tmpls[i].offsets, tmpls[i].adj, tmpls[i].labels, threads=threads,
+                                    nlcc_threads=1, stop_before_enumeration=True, deadline_ms=args.c5_oracle_ms)
+            except oracle.OracleTimeout:
+                cpu_timeouts += 1
+                continue
+            same = (rows == ref.rows and bool((cand == ref.cand).all()) and bool((eact == ref.eact).all())
+                    and bool((vact == ref.vact).all()))
+            checked.append(i)
+            if not same:
+                mismatches.append(i)
+    finally:
+        pm._check(pm.lib.pm_set_query_budget_ms(0.0))
+    edges = g.edge_count
+    g.close()
+    out = outcome_summary(served, pm)
+    n_q = sum(1 for x in seq_st if x == pm.PM_SUCCESS)
+    return {"workload": "rmat26_degree64_mixed_prune_served",
+            "graph": "undirected rmat scale 26 ef 16, 64 labels correlated with degree rank",
+            "csr_entries": edges, "graph_generation_s": gen_s,
+            "templates": f"{n} seeded: 10-vertex templates with repeated labels (seed 26) and 4-cycles with distinct "
+                         "labels, alternating", "budget_ms": args.budget_ms, "unit": "queries/s",
+            "served": out["completed"] / served_s, "served_outcomes": out,
+            "one_at_a_time": n_q / seq_s if seq_s else None, "one_at_a_time_requests": args.same_requests,
+            "one_at_a_time_completed": n_q, "device_ms_by_class": {k: round(v, 3) for k, v in cls_ms.items()},
+            "parity_sample": {"requests": sample, "checked": checked, "mismatches": mismatches,
+                              "gpu_timeouts": gpu_timeouts, "oracle_timeouts": cpu_timeouts,
+                              "oracle_deadline_ms": args.c5_oracle_ms}}
+
+
 def run_c1_stream(args, pm, T):
     """The RMAT-16 stream of the 15 distinct-label 4-cycles, full pipeline
     including exact ENUMERATION (6.2e7-8.4e7 matches each): served burst vs
@@ -731,6 +819,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c1", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--workload", choices=["c4", "c5"], default="c4",
+                    help="c5: the RMAT-26 mixed stream with its oracle sample (its own JSON line)")
+    ap.add_argument("--c5-requests", type=int, default=200)
+    ap.add_argument("--c5-oracle-ms", type=float, default=60000.0)
     ap.add_argument("--case", choices=["c1", "lcc", "c4"], default=None)
     ap.add_argument("--queries", type=int, default=1)
     ap.add_argument("--scale", type=int, default=22)
@@ -753,6 +845,10 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
+    if args.workload == "c5":
+        if rank == 0:
+            print(json.dumps(run_c5(args, pm, T)))
+        return
     out, g, stream = run_c4(args, rank, world, pm, T)
     if rank == 0:
         if not args.no_c3:

@@ -133,6 +133,27 @@ pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets,
                                      uint32_t p_vertex_count,
                                      uint64_t p_edge_count, pm_query** out);
 
+/* The reference's article drivers (src/patternmatching/test_article,
+ * CMakeLists.txt:12-33) run the same schedule with other CC / PC / TDS
+ * walks: strict walks bind no graph vertex twice and keep no memo
+ * (multiple_label_test, the *_strict_cpu.tpp files, optimization_none);
+ * backtrack walks skip a (vertex, template vertex) pair the source's walk
+ * already visited (CC, PC) or keep only the hypothesis memo (TDS) (the
+ * *_backtrack_cpu.tpp files, optimization_all: work aggregation, early
+ * termination, multiple validation).  Their TDS steps advance through the
+ * template constraints, and their schedule ends with END where the
+ * reference's would enter ENUMERATION (test_optimization_multiple_label_
+ * step.cc:46-58).  pm_query_create_variant* builds such a query
+ * (PM_NLCC_REFERENCE gives pm_query_create's). */
+#define PM_NLCC_REFERENCE 0
+#define PM_NLCC_STRICT 1
+#define PM_NLCC_BACKTRACK 2
+pm_status_t pm_query_create_variant(pm_graph* g, const char* pattern_dir, int load_pattern_labels,
+                                    int32_t variant, pm_query** out);
+pm_status_t pm_query_create_variant_from_csr(pm_graph* g, const uint64_t* p_offsets, const uint32_t* p_adj,
+                                             const uint64_t* p_labels, uint32_t p_vertex_count,
+                                             uint64_t p_edge_count, int32_t variant, pm_query** out);
+
 /* Number of cycle / path / template constraints
  * (MultipleLabelStep::initStep{Cc,Pc,Tds}, multiple_label_step.cc:12-25). */
 pm_status_t pm_query_constraint_counts(const pm_query* q, int32_t* n_cycle,
@@ -320,8 +341,11 @@ pm_status_t pm_batch_run(pm_graph* g, const pm_template_csr* templates, uint32_t
  * TDS / ENUMERATION steps run on per-query streams from a pool of host
  * threads.  Each query's rows (timing columns aside), match count and state
  * equal pm_query_run's on its own (pm_query_prune's with
- * PM_SUBMIT_PRUNE_ONLY in flags).  pm_set_query_budget_ms bounds every query
- * from the start of the run.  Returns PM_SUCCESS with per-query statuses in
+ * PM_SUBMIT_PRUNE_ONLY in flags).  At most 16 queries are in flight at a
+ * time (one per host worker); the others enter in order as queries finish,
+ * and pm_set_query_budget_ms bounds every query from when it enters.  Each
+ * worker's walker launches take its share of the GPU.  Returns PM_SUCCESS
+ * with per-query statuses in
  * pm_fused_batch_result; the batch keeps every query's state until
  * pm_fused_batch_destroy. */
 typedef struct pm_fused_batch pm_fused_batch;

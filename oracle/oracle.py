@@ -33,9 +33,9 @@ class _Record(ctypes.Structure):
 
 class _Options(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("nlcc_threads", ctypes.c_int32),
-                ("stop_before_enumeration", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("stop_before_enumeration", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("sample_stride", ctypes.c_int64), ("enum_sample_stride", ctypes.c_int64),
-                ("deadline_ms", ctypes.c_double)]
+                ("deadline_ms", ctypes.c_double), ("max_steps", ctypes.c_int64)]
 
 
 STEP_NAMES = {0: "START", 1: "END", 2: "LCC0", 3: "LCC", 4: "CC", 5: "PC", 6: "TDS", 7: "ENUMERATION"}
@@ -76,6 +76,11 @@ def _load():
         lib.pmo_list_matches.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64), ctypes.c_uint32,
                                          ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
                                          ctypes.c_uint32, P(ctypes.c_uint32), ctypes.c_uint64, P(ctypes.c_uint64)]
+        lib.pmo_enumerate_state.restype = ctypes.c_int
+        lib.pmo_enumerate_state.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                            ctypes.c_uint32, ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32),
+                                            P(ctypes.c_uint64), ctypes.c_uint32, P(ctypes.c_uint64),
+                                            P(ctypes.c_uint8), ctypes.c_int64, ctypes.c_int, P(ctypes.c_uint64)]
         lib.pmo_enumeration_start_role.restype = ctypes.c_int
         lib.pmo_enumeration_start_role.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
                                                    ctypes.c_uint32]
@@ -144,13 +149,15 @@ class OracleTimeout(RuntimeError):
 
 def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, nlcc_threads: int = 1,
            stop_before_enumeration: bool = False, sample_stride: int = 1, enum_sample_stride: int = 1,
-           deadline_ms: float = 0.0, want_state: bool = True) -> OracleResult:
+           deadline_ms: float = 0.0, want_state: bool = True, variant: int = 0,
+           max_steps: int = 0) -> OracleResult:
     """run() with separate thread counts for the LCC sweeps (deterministic in
     any order) and for the CC/PC/TDS/ENUMERATION source loops (1 = the
     canonical order of the alreadyMatched shortcut), an ENUMERATION-only
     source sample (enum_sample_stride > 1: the count over sources
     v % stride == 0, pruning unchanged) and a wall-clock deadline (raises
-    OracleTimeout past it)."""
+    OracleTimeout past it).  variant 1 / 2: the reference's article drivers
+    with strict / backtrack constraint walks (pruning only, END row)."""
     lib = _load()
     off = np.ascontiguousarray(offsets, np.uint64)
     ad = np.ascontiguousarray(adj, np.uint32)
@@ -165,8 +172,8 @@ def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, n
     cand = np.zeros(V, np.uint64) if want_state else None
     eact = np.zeros(E, np.uint8) if want_state else None
     vact = np.zeros(V, np.uint8) if want_state else None
-    opt = _Options(threads, nlcc_threads, int(stop_before_enumeration), 0, sample_stride, enum_sample_stride,
-                   deadline_ms)
+    opt = _Options(threads, nlcc_threads, int(stop_before_enumeration), variant, sample_stride, enum_sample_stride,
+                   deadline_ms, max_steps)
     st = lib.pmo_run_ex(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), V, E,
                         _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k,
                         ctypes.byref(opt), recs, cap, ctypes.byref(n),
@@ -247,6 +254,29 @@ def list_matches(offsets, adj, labels, p_offsets, p_adj, p_labels, cap: int = 1 
         raise RuntimeError(f"oracle listing failed with status {st}")
     rows = min(n.value, cap)
     return out[:rows * k].reshape(rows, k), n.value
+
+
+def enumerate_state(offsets, adj, labels, p_offsets, p_adj, p_labels, cand, eact, stride: int = 1,
+                    threads: int = 1) -> int:
+    """ENUMERATION over a given pruned state (role masks, per-CSR-entry
+    flags), counting only sources v % stride == 0."""
+    lib = _load()
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ad = np.ascontiguousarray(adj, np.uint32)
+    lab = np.ascontiguousarray(labels, np.uint64)
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    c = np.ascontiguousarray(cand, np.uint64)
+    e = np.ascontiguousarray(eact, np.uint8)
+    n = ctypes.c_uint64()
+    st = lib.pmo_enumerate_state(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64),
+                                 len(off) - 1, len(ad), _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32),
+                                 _p(pl, ctypes.c_uint64), len(po) - 1, _p(c, ctypes.c_uint64), _p(e, ctypes.c_uint8),
+                                 stride, threads, ctypes.byref(n))
+    if st != 0:
+        raise RuntimeError(f"oracle enumeration failed with status {st}")
+    return n.value
 
 
 def enumeration_start_role(p_offsets, p_adj, p_labels) -> int:

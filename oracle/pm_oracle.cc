@@ -92,7 +92,11 @@ struct State {
 // Second sweep shared by the CC, PC and TDS steps (multiple_label_cc_cpu.tpp:134-173,
 // pc :150-186, tds :203-241): apply the roles to unmatch, deactivate empty
 // vertices, and reschedule modified vertices and their neighbours.
-void apply_unmatch(State& s, Results& r) {
+// keep_schedule: the article drivers' CC/PC/TDS variants
+// (multiple_label_test/*_{strict,backtrack}_cpu.tpp) leave a vertex's
+// schedule flag as it was when no active entry leads to a modified vertex,
+// instead of clearing it.
+void apply_unmatch(State& s, Results& r, bool keep_schedule = false) {
   uint64_t ve = 0, me = 0;
 #pragma omp parallel for reduction(+ : ve, me) if (s.parallel)
   for (int64_t vi = 0; vi < s.V; ++vi) {
@@ -116,7 +120,7 @@ void apply_unmatch(State& s, Results& r) {
         sched = true;
         break;
       }
-      s.scheduled[v] = sched;
+      if (sched || !keep_schedule) s.scheduled[v] = sched;
     }
   }
   s.active_vertices -= ve;
@@ -443,6 +447,253 @@ Results step_tds(State& s, const TemplateConstraint& t) {
   return r;
 }
 
+// ---- the article drivers' NLCC variants (test_article/CMakeLists.txt:12-33)
+// Strict (multiple_label_test/*_strict_cpu.tpp): walks bind no vertex twice
+// (isInVector over the history, source included) and keep no memo.
+// Backtrack (*_backtrack_cpu.tpp, built with work aggregation, early
+// termination and multiple validation): CC and PC skip a (vertex, template
+// vertex) pair already visited by the source's walk; TDS keeps only the
+// hypothesis memo.  Every success marks alreadyMatched as the regular walks do.
+bool in_history(const std::vector<uint32_t>& h, uint32_t v) {
+  for (uint32_t x : h)
+    if (x == v) return true;
+  return false;
+}
+
+// cc_strict_cpu.tpp:13-64
+bool cc_strict_walk(State& s, const CycleConstraint& c, std::vector<uint32_t>& hist, uint32_t source, uint32_t cur,
+                    size_t start, size_t remaining) {
+  if (expired()) return false;
+  const size_t L = c.length();
+  if (remaining == 1) {
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w]) continue;
+      if (w == source) return true;
+    }
+    return false;
+  }
+  const uint32_t next_role = c.ids[(start + L - (remaining - 1)) % L];
+  for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+    if (!s.edge_active[e]) continue;
+    uint32_t w = s.adj[e];
+    if (!s.active[w] || !s.has(w, next_role) || in_history(hist, w)) continue;
+    hist.push_back(w);
+    if (cc_strict_walk(s, c, hist, source, w, start, remaining - 1)) {
+      s.mark_matched(w, next_role);
+      return true;
+    }
+    hist.pop_back();
+  }
+  return false;
+}
+
+// cc_backtrack_cpu.tpp:13-78 (early termination, multiple validation)
+bool cc_backtrack_walk(State& s, const CycleConstraint& c, std::unordered_map<uint32_t, uint64_t>& seen,
+                       uint32_t source, uint32_t cur, size_t start, size_t remaining) {
+  if (expired()) return false;
+  const size_t L = c.length();
+  if (remaining == 1) {
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w]) continue;
+      if (w == source) return true;
+    }
+    return false;
+  }
+  const uint32_t next_role = c.ids[(start + L - (remaining - 1)) % L];
+  for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+    if (!s.edge_active[e]) continue;
+    uint32_t w = s.adj[e];
+    if (!s.active[w] || !s.has(w, next_role)) continue;
+    auto it = seen.find(w);
+    if (it != seen.end() && (it->second >> next_role & 1)) continue;
+    seen[w] |= uint64_t(1) << next_role;
+    if (cc_backtrack_walk(s, c, seen, source, w, start, remaining - 1)) {
+      s.mark_matched(w, next_role);
+      return true;
+    }
+  }
+  return false;
+}
+
+// CC step of either variant (cc_strict_cpu.tpp:72-178, cc_backtrack_cpu.tpp:86-190).
+Results step_cc_variant(State& s, const CycleConstraint& c, int variant) {
+  Results r;
+  std::vector<uint32_t> hist;
+  std::unordered_map<uint32_t, uint64_t> seen;
+#pragma omp parallel for private(hist, seen) if (s.nlcc_parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
+    bool changed = false;
+    for (size_t pos = 0; pos < c.length(); ++pos) {
+      uint32_t role = c.ids[pos];
+      if (!s.has(v, role) || s.is_matched(v, role)) continue;
+      bool ok;
+      if (variant == 1) {
+        hist.assign(1, v);
+        ok = cc_strict_walk(s, c, hist, v, v, pos, c.length());
+      } else {
+        seen.clear();
+        ok = cc_backtrack_walk(s, c, seen, v, v, pos, c.length());
+      }
+      if (!ok) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r, true);
+  return r;
+}
+
+// pc_strict_cpu.tpp:12-76 / pc_backtrack_cpu.tpp:12-78
+bool pc_variant_walk(State& s, const PathConstraint& pc, bool reverse, int variant, std::vector<uint32_t>& hist,
+                     std::unordered_map<uint32_t, uint64_t>& seen, uint32_t source, uint32_t cur, size_t remaining) {
+  if (expired()) return false;
+  const size_t L = pc.length();
+  const uint32_t next_role = pc.ids[reverse ? remaining - 1 : (L - remaining)];
+  auto blocked = [&](uint32_t w) {
+    if (variant == 1) return in_history(hist, w);
+    auto it = seen.find(w);
+    return it != seen.end() && (it->second >> next_role & 1) != 0;
+  };
+  if (remaining == 1) {
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t w = s.adj[e];
+      if (!s.active[w] || !s.has(w, next_role) || blocked(w)) continue;
+      if (source != w) {
+        s.mark_matched(w, next_role);
+        return true;
+      }
+    }
+    return false;
+  }
+  for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+    if (!s.edge_active[e]) continue;
+    uint32_t w = s.adj[e];
+    if (!s.active[w] || !s.has(w, next_role) || blocked(w)) continue;
+    if (variant == 1)
+      hist.push_back(w);
+    else
+      seen[w] |= uint64_t(1) << next_role;
+    if (pc_variant_walk(s, pc, reverse, variant, hist, seen, source, w, remaining - 1)) return true;
+    if (variant == 1) hist.pop_back();
+  }
+  return false;
+}
+
+// PC step of either variant (pc_strict_cpu.tpp:78-189).
+Results step_pc_variant(State& s, const PathConstraint& pc, int variant) {
+  Results r;
+  std::vector<uint32_t> hist;
+  std::unordered_map<uint32_t, uint64_t> seen;
+  const size_t L = pc.length();
+#pragma omp parallel for private(hist, seen) if (s.nlcc_parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
+    if (s.lab[v] != pc.initial_label) continue;
+    bool changed = false;
+    for (int end = 0; end < 2; ++end) {
+      uint32_t role = end == 0 ? pc.ids[0] : pc.ids[L - 1];
+      if (!s.has(v, role) || s.is_matched(v, role)) continue;
+      hist.assign(1, v);
+      seen.clear();
+      if (!pc_variant_walk(s, pc, end == 1, variant, hist, seen, v, v, L - 1)) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r, true);
+  return r;
+}
+
+// tds_strict_cpu.tpp:12-98 (history injective, no memo) and
+// tds_backtrack_cpu.tpp:12-116 (hypothesis memo only).
+bool tds_variant_walk(State& s, const Walk& w, int variant, TdsMemo& m, uint32_t source, uint32_t cur, size_t pos) {
+  if (pos == w.length()) return true;
+  if (expired()) return false;
+  const int move = w.moves[pos];
+  if (move == kVertexNoStore || move == kVertexStore) {
+    const uint32_t next_role = w.ids[pos];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb] || !s.has(nb, next_role)) continue;
+      if (variant == 1) {
+        if (in_history(m.history, nb)) continue;
+      } else {
+        auto hv = m.hyp.find(nb);
+        if (hv != m.hyp.end()) {
+          auto hr = hv->second.find(next_role);
+          if (hr != hv->second.end()) {
+            bool seen = false;
+            for (const auto& h : hr->second)
+              if (h == m.stored) seen = true;
+            if (seen) continue;
+          }
+        }
+        if (move == kVertexStore) m.stored.push_back(nb);
+        m.hyp[nb][next_role].push_back(m.stored);
+      }
+      m.history.push_back(nb);
+      if (tds_variant_walk(s, w, variant, m, source, nb, pos + 1)) {
+        s.mark_matched(nb, next_role);
+        return true;
+      }
+      m.history.pop_back();
+      if (variant != 1 && move == kVertexStore) m.stored.pop_back();
+    }
+  } else if (move == kCheck) {
+    const uint32_t target = m.history[w.back[pos]];
+    for (uint64_t e = s.off[cur]; e < s.off[cur + 1]; ++e) {
+      if (!s.edge_active[e]) continue;
+      uint32_t nb = s.adj[e];
+      if (!s.active[nb] || nb != target) continue;
+      if (tds_variant_walk(s, w, variant, m, source, cur, pos + 1)) return true;
+    }
+  } else {
+    if (tds_variant_walk(s, w, variant, m, source, m.history[w.back[pos]], pos + 1)) return true;
+  }
+  return false;
+}
+
+// TDS step of either variant (tds_strict_cpu.tpp:100-195); unlike the
+// regular TDS step the drivers advance to the next template constraint.
+Results step_tds_variant(State& s, const TemplateConstraint& t, int variant) {
+  Results r;
+  TdsMemo m;
+#pragma omp parallel for private(m) if (s.nlcc_parallel)
+  for (int64_t vi = 0; vi < s.V; ++vi) {
+    uint32_t v = static_cast<uint32_t>(vi);
+    if (!s.active[v] || !s.sampled(vi) || expired()) continue;
+    bool changed = false;
+    for (const auto& kv : t.walks) {
+      uint32_t role = kv.first;
+      if (!s.has(v, role) || s.is_matched(v, role)) continue;
+      m.hyp.clear();
+      m.edges.clear();
+      m.history.assign(1, v);
+      m.stored.clear();
+      if (!tds_variant_walk(s, kv.second, variant, m, v, v, 1)) {
+        s.unmatch[v] |= uint64_t(1) << role;
+        changed = true;
+      }
+    }
+    if (changed) s.modified[v] = 1;
+  }
+  apply_unmatch(s, r, true);
+  return r;
+}
+
 // ENUMERATION walk (multiple_label_enumeration_cpu.tpp:39-118): injective
 // embeddings following the walk; CHECK follows only the first matching entry.
 uint64_t enum_walk(const State& s, const Walk& w, std::vector<uint32_t>& history, uint32_t cur, size_t pos) {
@@ -526,11 +777,14 @@ struct pmo_options {
   int32_t threads;                  // LCC0 / LCC threads (deterministic in any order)
   int32_t nlcc_threads;             // CC / PC / TDS / ENUMERATION threads; 1 = canonical order
   int32_t stop_before_enumeration;  // 1 = end when the schedule reaches ENUMERATION
-  int32_t pad;
+  int32_t variant;                  // 0 = the reference's walks; 1 = strict, 2 = backtrack
+                                    // (the article drivers: TDS steps advance through
+                                    // the template constraints, END instead of ENUMERATION)
   int64_t sample_stride;            // >1: CC/PC/TDS/ENUMERATION sources v % stride == 0 only
   int64_t enum_sample_stride;       // >1: ENUMERATION sources v % stride == 0 only (a
                                     // per-source sampled count; pruning unchanged)
   double deadline_ms;               // >0: wall-clock limit; the run returns -7 past it
+  int64_t max_steps;                // >0: stop after that many steps (the last row names the next)
 };
 
 int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
@@ -607,7 +861,7 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
           if (next_cc < qc.cycles.size()) return CC;
           if (next_pc < qc.paths.size()) return PC;
           if (next_tds < qc.templates.size()) return TDS;
-          return ENUM;
+          return opt->variant ? END : ENUM;
         case CC: ++next_cc; return LCC;
         case PC: ++next_pc; return LCC;
         case TDS: ++next_tds; return LCC;
@@ -641,16 +895,20 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
     while (!finished && iteration < 1000) {
       if (step == CC || step == PC || step == TDS) std::fill(s.modified.begin(), s.modified.end(), 0);
       if (step == ENUM && stop_before_enumeration) break;
+      if (opt->max_steps > 0 && n >= opt->max_steps) break;
       auto t0 = std::chrono::steady_clock::now();
       switch (step) {
         case LCC0: res = step_lcc0(s, qc); break;
         case LCC: res = step_lcc(s, qc); break;
-        case CC: res = step_cc(s, qc.cycles[next_cc]); break;
-        case PC: res = step_pc(s, qc.paths[next_pc]); break;
+        case CC: res = opt->variant ? step_cc_variant(s, qc.cycles[next_cc], opt->variant)
+                                    : step_cc(s, qc.cycles[next_cc]); break;
+        case PC: res = opt->variant ? step_pc_variant(s, qc.paths[next_pc], opt->variant)
+                                    : step_pc(s, qc.paths[next_pc]); break;
         // MultipleLabelTdsCpu::compute never advances its constraint
         // iterator (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and
         // pc :186), so every TDS step checks template constraint 0.
-        case TDS: res = step_tds(s, qc.templates[0]); break;
+        case TDS: res = opt->variant ? step_tds_variant(s, qc.templates[next_tds], opt->variant)
+                                     : step_tds(s, qc.templates[0]); break;
         case ENUM: res = step_enumeration(s, qc.enumeration); break;
         default: res = Results(); break;
       }
@@ -661,7 +919,7 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
       }
       emit(step + PM_STEP_START, ms, res);
       int next = advance(step);
-      finished = (step == ENUM);
+      finished = (step == ENUM) || next == END;
       step = next;
       ++iteration;
     }
@@ -765,6 +1023,41 @@ int pmo_list_matches(const uint64_t* off, const uint32_t* adj, const uint64_t* l
     }
     if (out && !list.empty()) memcpy(out, list.data(), 4 * list.size());
     if (n_matches) *n_matches = n;
+    return 0;
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
+// ENUMERATION (multiple_label_enumeration_cpu.tpp:126-174) over a given
+// pruned state (role masks, CSR-entry flags; active = any role), counting
+// only sources v % stride == 0: a per-source sampled count.
+int pmo_enumerate_state(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+                        const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k,
+                        const uint64_t* cand, const uint8_t* eact, int64_t stride, int threads, uint64_t* count) {
+  try {
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    const QueryConstraints qc = compile_constraints(pg);
+    State s;
+    s.off = off;
+    s.adj = adj;
+    s.lab = lab;
+    s.V = V;
+    s.E = E;
+    s.k = k;
+    s.parallel = false;
+    s.nlcc_parallel = threads > 1;
+    if (threads >= 1) omp_set_num_threads(threads);
+    s.cand.assign(cand, cand + V);
+    s.edge_active.assign(eact, eact + E);
+    s.active.resize(V);
+    for (uint32_t v = 0; v < V; ++v) s.active[v] = cand[v] != 0;
+    s.enum_stride = stride;
+    *count = step_enumeration(s, qc.enumeration).enumeration;
     return 0;
   } catch (const PmError& e) {
     return e.code;

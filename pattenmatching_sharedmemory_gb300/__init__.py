@@ -141,6 +141,11 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_create": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_void_p)]),
         "pm_query_create_from_csr": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, c_u64p, ctypes.c_uint32,
                                                       ctypes.c_uint64, P(ctypes.c_void_p)]),
+        "pm_query_create_variant": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int32,
+                                                     P(ctypes.c_void_p)]),
+        "pm_query_create_variant_from_csr": (ctypes.c_int32, [ctypes.c_void_p, c_u64p, c_u32p, c_u64p,
+                                                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32,
+                                                              P(ctypes.c_void_p)]),
         "pm_query_constraint_counts": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32),
                                                         P(ctypes.c_int32)]),
         "pm_query_dump_constraints": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
@@ -354,21 +359,27 @@ class Query:
     """One template over a resident graph: constraint generation, GPU pruning
     steps and the reference's step schedule (MultipleLabelCpu)."""
 
+    VARIANTS = {None: 0, "reference": 0, "strict": 1, "backtrack": 2}
+
     def __init__(self, graph: Graph, pattern_dir=None, pattern: Pattern | None = None,
-                 load_pattern_labels: bool = True):
+                 load_pattern_labels: bool = True, variant: str | None = None):
+        """variant: None / "reference" (the reference's walks), or the article
+        drivers' "strict" / "backtrack" walks (pm_query_create_variant*)."""
         self.graph = graph
         self._h = ctypes.c_void_p()
         self._k = None if pattern is None else pattern.n
+        v = self.VARIANTS[variant]
         if pattern_dir is not None:
             d = str(pattern_dir)
-            _check(lib.pm_query_create(graph._h, _enc(d), int(load_pattern_labels), ctypes.byref(self._h)))
+            _check(lib.pm_query_create_variant(graph._h, _enc(d), int(load_pattern_labels), v, ctypes.byref(self._h)))
         else:
             p = pattern
             off = np.ascontiguousarray(p.offsets, np.uint64)
             adj = np.ascontiguousarray(p.adj, np.uint32)
             lab = np.ascontiguousarray(p.labels, np.uint64)
-            _check(lib.pm_query_create_from_csr(graph._h, _ptr(off, ctypes.c_uint64), _ptr(adj, ctypes.c_uint32),
-                                                _ptr(lab, ctypes.c_uint64), p.n, len(adj), ctypes.byref(self._h)))
+            _check(lib.pm_query_create_variant_from_csr(graph._h, _ptr(off, ctypes.c_uint64),
+                                                        _ptr(adj, ctypes.c_uint32), _ptr(lab, ctypes.c_uint64), p.n,
+                                                        len(adj), v, ctypes.byref(self._h)))
 
     def constraint_counts(self):
         a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

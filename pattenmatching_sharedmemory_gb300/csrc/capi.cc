@@ -230,10 +230,11 @@ pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const
   });
 }
 
-static pm_status_t create_query(pm_graph* g, const PatternGraph& p, pm_query** out) {
+static pm_status_t create_query(pm_graph* g, const PatternGraph& p, pm_query** out, int variant = 0) {
   auto* q = new pm_query();
   try {
     g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
+    q->impl.nlcc_variant = variant;
     q->impl.create(&g->impl, p, nullptr);
   } catch (...) {
     delete q;
@@ -265,6 +266,15 @@ pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets, con
     p.labels = p_labels ? std::vector<uint64_t>(p_labels, p_labels + p_vertex_count)
                         : std::vector<uint64_t>(p_vertex_count, 0);
     return create_query(g, p, out);
+  });
+}
+
+pm_status_t pm_query_create_variant(pm_graph* g, const char* pattern_dir, int load_pattern_labels, int32_t variant,
+                                    pm_query** out) {
+  PM_REQUIRE(g && pattern_dir && out, "null argument");
+  PM_REQUIRE(variant >= PM_NLCC_REFERENCE && variant <= PM_NLCC_BACKTRACK, "unknown walk variant");
+  return guarded([&]() -> pm_status_t {
+    return create_query(g, load_pattern(pattern_dir, load_pattern_labels != 0), out, variant);
   });
 }
 
@@ -925,5 +935,16 @@ pm_status_t pm_fused_batch_stats(const pm_fused_batch* b, uint64_t* rounds, uint
 }
 
 void pm_fused_batch_destroy(pm_fused_batch* b) { delete b; }
+
+pm_status_t pm_query_create_variant_from_csr(pm_graph* g, const uint64_t* p_offsets, const uint32_t* p_adj,
+                                             const uint64_t* p_labels, uint32_t p_vertex_count,
+                                             uint64_t p_edge_count, int32_t variant, pm_query** out) {
+  PM_REQUIRE(g && out, "null argument");
+  PM_REQUIRE(variant >= PM_NLCC_REFERENCE && variant <= PM_NLCC_BACKTRACK, "unknown walk variant");
+  return guarded([&]() -> pm_status_t {
+    return create_query(g, pattern_from_csr(p_offsets, p_adj, p_labels, p_vertex_count, p_edge_count), out,
+                        variant);
+  });
+}
 
 }  // extern "C"

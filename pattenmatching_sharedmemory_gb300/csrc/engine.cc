@@ -298,9 +298,11 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, 
   pattern = p;
   k = p.n;
   qc = compile_constraints(p);
-  for (const auto& c : qc.cycles) cycles.push_back(make_device_constraint(compile_cycle(c, p.labels)));
-  for (const auto& pc : qc.paths) paths.push_back(make_device_constraint(compile_path(pc, p.labels)));
-  for (const auto& t : qc.templates) templates.push_back(make_device_constraint(compile_template(t, p.labels)));
+  for (const auto& c : qc.cycles)
+    cycles.push_back(make_device_constraint(compile_cycle(c, p.labels, nlcc_variant)));
+  for (const auto& pc : qc.paths) paths.push_back(make_device_constraint(compile_path(pc, p.labels, nlcc_variant)));
+  for (const auto& t : qc.templates)
+    templates.push_back(make_device_constraint(compile_template(t, p.labels, nlcc_variant)));
   enumeration = make_device_constraint(compile_enumeration(qc.enumeration, p.labels));
   word_kind = word_kind_for(k);
 
@@ -889,7 +891,9 @@ int QueryImpl::advance(int cur) {
       if (next_cc < cycles.size()) return PM_STEP_CC;
       if (next_pc < paths.size()) return PM_STEP_PC;
       if (next_tds < templates.size()) return PM_STEP_TDS;
-      return PM_STEP_ENUMERATION;
+      // The article drivers end their schedule here
+      // (test_optimization_multiple_label_step.cc:46-58).
+      return nlcc_variant ? PM_STEP_END : PM_STEP_ENUMERATION;
     case PM_STEP_CC: ++next_cc; return PM_STEP_LCC;
     case PM_STEP_PC: ++next_pc; return PM_STEP_LCC;
     case PM_STEP_TDS: ++next_tds; return PM_STEP_LCC;
@@ -924,7 +928,8 @@ pm_step_record QueryImpl::run_step() {
     // The reference's TDS step never advances its constraint iterator
     // (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and pc :186):
     // each of the n_template TDS steps checks template constraint 0.
-    case PM_STEP_TDS: r = step_nlcc(templates[0]); break;
+    // The article drivers' TDS steps do advance (tds_strict_cpu.tpp:192).
+    case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? next_tds : 0]); break;
     case PM_STEP_ENUMERATION: r = step_enumeration(); break;
     default: break;
   }
@@ -968,7 +973,7 @@ void QueryImpl::append_record(const StepResult& r_in, int kind, double ms, uint6
   records.push_back(rec);
   walk_stats.emplace_back(scanned, second);
   step = advance(kind);
-  if (kind == PM_STEP_ENUMERATION) finished = true;
+  if (kind == PM_STEP_ENUMERATION || step == PM_STEP_END) finished = true;
   ++iteration;
   if (iteration >= 1000) finished = true;
 }

@@ -135,6 +135,10 @@ struct QueryImpl {
   // Request controls, checked before every step: a deadline (its remaining
   // time also caps each walker step's device budget), a cancel flag another
   // thread may set, and a stop before ENUMERATION (pruning only).
+  // CC / PC / TDS walk semantics (NlccVariant, walk_compile.h); set before
+  // create().  The article drivers' variants also advance through the
+  // template constraints and end with END where the reference would count.
+  int nlcc_variant = 0;
   bool has_deadline = false;
   std::chrono::steady_clock::time_point deadline{};
   const std::atomic<bool>* cancel = nullptr;

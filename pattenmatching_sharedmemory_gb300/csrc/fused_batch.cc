@@ -26,6 +26,7 @@ FusedBatch::FusedBatch(GraphImpl* g, const std::vector<PatternGraph>& patterns, 
     throw;
   }
   const size_t n_threads = std::min<size_t>(std::max<size_t>(patterns.size(), 1), 16);
+  n_workers_ = static_cast<uint32_t>(n_threads);
   for (size_t t = 0; t < n_threads; ++t) workers_.emplace_back(&FusedBatch::worker, this);
 }
 
@@ -46,6 +47,7 @@ FusedBatch::~FusedBatch() {
 // Runs the next step of the queries the coordinator queues, one at a time.
 void FusedBatch::worker() {
   if (cudaSetDevice(g_->device) != cudaSuccess) return;
+  set_thread_walk_grid_share(n_workers_);
   while (true) {
     size_t i = 0;
     {
@@ -82,12 +84,22 @@ void FusedBatch::worker() {
 void FusedBatch::run() {
   using Clock = std::chrono::steady_clock;
   const auto t0 = Clock::now();
-  for (auto& it : items_) {
-    if (query_budget_ms() > 0) {
-      it.q->has_deadline = true;
-      it.q->deadline = t0 + std::chrono::microseconds(static_cast<int64_t>(query_budget_ms() * 1000.0));
+  // At most one query per worker is in flight; the others wait their turn,
+  // and a query's budget (query_budget_ms) starts when it enters.
+  const size_t window = std::max<size_t>(n_workers_, 1);
+  size_t entered = 0;
+  auto enter = [&]() {
+    while (entered < items_.size()) {
+      size_t in_flight = 0;
+      for (size_t i = 0; i < entered; ++i) in_flight += items_[i].done ? 0 : 1;
+      if (in_flight >= window) break;
+      FusedBatchItem& it = items_[entered++];
+      if (query_budget_ms() > 0) {
+        it.q->has_deadline = true;
+        it.q->deadline = Clock::now() + std::chrono::microseconds(static_cast<int64_t>(query_budget_ms() * 1000.0));
+      }
     }
-  }
+  };
   auto mark_done = [&](FusedBatchItem& it) {
     it.done = true;
     it.run_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
@@ -125,10 +137,11 @@ void FusedBatch::run() {
   };
   std::unique_lock<std::mutex> lk(mu_);
   while (true) {
+    enter();
     // Queries between steps (not on a worker) and what they need next.
     std::vector<size_t> at_lcc0, at_lcc, others;
     size_t busy = 0;
-    for (size_t i = 0; i < items_.size(); ++i) {
+    for (size_t i = 0; i < entered; ++i) {
       FusedBatchItem& it = items_[i];
       if (it.done) continue;
       if (running_[i]) {
@@ -148,7 +161,10 @@ void FusedBatch::run() {
       else
         others.push_back(i);
     }
-    if (!busy && at_lcc0.empty() && at_lcc.empty() && others.empty()) break;
+    if (!busy && at_lcc0.empty() && at_lcc.empty() && others.empty()) {
+      if (entered < items_.size()) continue;  // the next queries enter
+      break;
+    }
     ++rounds;
     for (size_t i : others) {
       running_[i] = 1;

@@ -46,8 +46,10 @@ class FusedBatch {
   FusedBatch(const FusedBatch&) = delete;
   FusedBatch& operator=(const FusedBatch&) = delete;
 
-  // Runs every query to its end (or failure).  A per-query budget
-  // (query_budget_ms) runs from the start of this call.
+  // Runs every query to its end (or failure).  At most one query per host
+  // worker (16 at most) is in flight at a time, the others enter in order as
+  // queries finish; a per-query budget (query_budget_ms) runs from when the
+  // query enters.
   void run();
   size_t size() const { return items_.size(); }
   FusedBatchItem& item(size_t i) { return items_.at(i); }
@@ -64,6 +66,7 @@ class FusedBatch {
   cudaStream_t stream_ = nullptr;
   // host thread pool for the per-query steps
   std::vector<std::thread> workers_;
+  uint32_t n_workers_ = 1;  // the walker grid share of each worker
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
   std::vector<size_t> queue_;     // queries whose next step a worker should run

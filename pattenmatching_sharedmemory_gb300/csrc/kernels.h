@@ -192,6 +192,10 @@ void launch_apply_failures(const DevGraph& g, const QueryDevPtrs& q, const WalkL
 void launch_collect_overflow(const WalkLaunch& w, uint32_t* list, StepCounters* ctr, cudaStream_t s);
 // Blocks of the persistent walker for a scratch pool of n_warps warps.
 uint32_t walk_grid_blocks(uint32_t n_warps_available);
+// Per host thread: walker launches (and walker pools sized after them) take
+// 1/share of the GPU's resident walker blocks (at least one block per SM):
+// a server slot among `share` slots.  1 = the whole GPU (default).
+void set_thread_walk_grid_share(uint32_t share);
 constexpr uint32_t kWalkWarpsPerBlock = 4;
 void launch_apply_unmatch_list(const DevGraph& g, const QueryDevPtrs& q, const uint32_t* vertices, const uint64_t* roles,
                                uint32_t n, cudaStream_t s);

@@ -471,7 +471,7 @@ __device__ bool load_chunk(const DevGraph& g, const DevState<W>& st, WarpShared&
     ok = role_of(st, nb, s.role);
   }
   if (s.kind == kStepFinal) ok = ok && nb != source;
-  if (kEnum && ok) {
+  if ((kEnum || ws.prog->injective) && ok) {
     for (int h = 0; h < ws.prog->n_hist && ws.prog->hist_step[h] < d; ++h)
       if (ws.f.bound[ws.prog->hist_step[h]] == nb) ok = false;
   }
@@ -1359,8 +1359,20 @@ uint64_t effective_walk_budget_ns() {
   return t_walk_budget_cap_ns && t_walk_budget_cap_ns < g_walk_budget_ns ? t_walk_budget_cap_ns : g_walk_budget_ns;
 }
 
+namespace {
+thread_local uint32_t t_walk_grid_share = 1;  // this thread's walker launches get 1/share of the GPU
+}  // namespace
+void set_thread_walk_grid_share(uint32_t share) { t_walk_grid_share = share ? share : 1; }
+
 uint32_t walk_grid_blocks(uint32_t n_warps_available) {
   uint32_t blocks = static_cast<uint32_t>(device_sm_count()) * kWalkBlocksPerSm;
+  // A share of the resident blocks (at least two per SM's worth of SMs /
+  // share): persistent walker grids of concurrent requests then sit on the
+  // GPU side by side instead of the first one taking every SM until it ends.
+  if (t_walk_grid_share > 1) {
+    const uint32_t floor_blocks = static_cast<uint32_t>(device_sm_count());
+    blocks = std::max(blocks / t_walk_grid_share, floor_blocks);
+  }
   if (blocks * kWalkWarps > n_warps_available) blocks = n_warps_available / kWalkWarps;
   return blocks ? blocks : 1;
 }

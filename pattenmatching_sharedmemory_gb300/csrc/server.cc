@@ -135,6 +135,10 @@ void Server::worker(uint32_t) {
   StepCounters* h_ctr = nullptr;
   uint32_t* h_count = nullptr;
   std::string err;
+  // Each slot's walker launches take its share of the GPU, so that requests
+  // running side by side overlap instead of queueing behind the first
+  // persistent walker grid (speed only).
+  set_thread_walk_grid_share(walk_share_ ? walk_share_ : slots_);
   if (cudaSetDevice(g_->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMallocHost(&h_ctr, sizeof(StepCounters)) != cudaSuccess ||

@@ -84,6 +84,7 @@ class Server {
   GraphImpl* g_;
   uint32_t slots_;
   uint64_t budget_;
+  uint32_t walk_share_ = 0;  // walker grid share of a slot (0: one per slot)
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
   std::deque<std::shared_ptr<ServeRequest>> queue_;

@@ -88,7 +88,11 @@ void analyze(WalkProgram& p, const std::vector<label_t>& role_label) {
       const int h = s.hist;
       if (h > 0 && p.hist_step[h] < d) refs[d] |= uint64_t(1) << h;
     }
-  bool exact = p.family != kFamilyEnum;
+  // Injective (strict) walks: the subtree below a hop depends on every
+  // vertex bound so far, and the tail shortcuts of exact programs do not
+  // test injectivity, so such programs are walked as non-exact ones with
+  // the whole history in their state key.
+  bool exact = p.family != kFamilyEnum && !p.injective;
   for (int d = 1; d < n && exact; ++d) {
     const WalkStep& s = p.steps[d];
     if (s.kind == kStepVertex && s.blocker >= 0) exact = false;
@@ -103,8 +107,11 @@ void analyze(WalkProgram& p, const std::vector<label_t>& role_label) {
   p.max_refs = 0;
   for (int d = 1; d < n; ++d) {
     uint64_t key = 0;
-    if (p.steps[d].kind == kStepVertex) {
+    if (p.steps[d].kind == kStepVertex || (p.injective && p.steps[d].kind == kStepFinal)) {
       key = refs[d];
+      if (p.injective)
+        for (int h = 1; h < p.n_hist; ++h)
+          if (p.hist_step[h] < d) key |= uint64_t(1) << h;
       if (!exact)
         for (int h = 1; h < p.n_hist; ++h)
           if (p.hist_step[h] < d && p.steps[p.hist_step[h]].store) key |= uint64_t(1) << h;
@@ -152,7 +159,7 @@ void finalize(CompiledConstraint& cc) {
 
 }  // namespace
 
-CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label) {
+CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label, int variant) {
   CompiledConstraint cc;
   cc.family = kFamilyCC;
   const int L = static_cast<int>(c.length());
@@ -173,7 +180,11 @@ CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<lab
     close.hist = 0;
     close.blocker = -1;
     p.steps[L] = close;
-    resolve_blockers(p, test);
+    p.injective = variant == kNlccStrict;
+    // The reference's edge memo; the backtrack walks' (vertex, template
+    // vertex) memo never blocks a walk that could still succeed, so it is
+    // the state memo of exact programs.
+    if (variant == kNlccReference) resolve_blockers(p, test);
     analyze(p, role_label);
     cc.programs.push_back(p);
   }
@@ -181,7 +192,7 @@ CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<lab
   return cc;
 }
 
-CompiledConstraint compile_path(const PathConstraint& pc, const std::vector<label_t>& role_label) {
+CompiledConstraint compile_path(const PathConstraint& pc, const std::vector<label_t>& role_label, int variant) {
   CompiledConstraint cc;
   cc.family = kFamilyPC;
   const int L = static_cast<int>(pc.length());
@@ -202,7 +213,8 @@ CompiledConstraint compile_path(const PathConstraint& pc, const std::vector<labe
     fin.mark = 1;
     p.steps[L - 1] = fin;
     add_history(p, L - 1);
-    resolve_blockers(p, test);
+    p.injective = variant == kNlccStrict;
+    if (variant == kNlccReference) resolve_blockers(p, test);
     analyze(p, role_label);
     cc.programs.push_back(p);
   }
@@ -212,7 +224,7 @@ CompiledConstraint compile_path(const PathConstraint& pc, const std::vector<labe
 
 namespace {
 WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family,
-                              const std::vector<label_t>& role_label) {
+                              const std::vector<label_t>& role_label, int variant = kNlccReference) {
   WalkProgram p = empty_program(family, static_cast<uint8_t>(start_role));
   const int n = static_cast<int>(w.length());
   check_length(n);
@@ -224,8 +236,9 @@ WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family
       WalkStep s = vertex_step(static_cast<uint8_t>(w.ids[d]));
       if (family == kFamilyTDS) {
         s.mark = 1;
-        s.store = m == kVertexStore;
-        s.hyp = m == kVertexNoStore;
+        // Strict walks keep no hypothesis memo (and so no stored vertices).
+        s.store = variant != kNlccStrict && m == kVertexStore;
+        s.hyp = variant != kNlccStrict && m == kVertexNoStore;
         test[d] = static_cast<int>(w.ids[d - 1]);
       }
       p.steps[d] = s;
@@ -240,17 +253,19 @@ WalkProgram program_from_walk(const Walk& w, uint32_t start_role, uint8_t family
       p.steps[d] = s;
     }
   }
-  if (family == kFamilyTDS) resolve_blockers(p, test);
+  p.injective = family == kFamilyTDS && variant == kNlccStrict;
+  if (family == kFamilyTDS && variant == kNlccReference) resolve_blockers(p, test);
   analyze(p, role_label);
   return p;
 }
 }  // namespace
 
-CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label) {
+CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label,
+                                    int variant) {
   CompiledConstraint cc;
   cc.family = kFamilyTDS;
   for (const auto& kv : t.walks)
-    cc.programs.push_back(program_from_walk(kv.second, kv.first, kFamilyTDS, role_label));
+    cc.programs.push_back(program_from_walk(kv.second, kv.first, kFamilyTDS, role_label, variant));
   finalize(cc);
   return cc;
 }

@@ -20,12 +20,23 @@ struct CompiledConstraint {
   uint32_t max_hyp_words = 0;         // key words of the reference's hypothesis memo
 };
 
+// Walk semantics of the CC / PC / TDS steps: the reference's walks with their
+// edge memo (and TDS hypothesis memo), or the article drivers' variants
+// (test_article/CMakeLists.txt:12-33): strict walks bind no vertex twice and
+// keep no memo (multiple_label_test/*_strict_cpu.tpp); backtrack walks skip
+// a (vertex, template vertex) pair the source's walk already visited (CC,
+// PC) or keep only the hypothesis memo (TDS) (*_backtrack_cpu.tpp).
+enum NlccVariant : int { kNlccReference = 0, kNlccStrict = 1, kNlccBacktrack = 2 };
+
 // CC: one program per cycle position (multiple_label_cc_cpu.tpp:94-129).
-CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label);
+CompiledConstraint compile_cycle(const CycleConstraint& c, const std::vector<label_t>& role_label,
+                                 int variant = kNlccReference);
 // PC: forward from ids[0], then backward from ids[L-1] (pc :104-142).
-CompiledConstraint compile_path(const PathConstraint& p, const std::vector<label_t>& role_label);
+CompiledConstraint compile_path(const PathConstraint& p, const std::vector<label_t>& role_label,
+                                int variant = kNlccReference);
 // TDS: one program per walkMap entry, in walkMap order (tds :153-195).
-CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label);
+CompiledConstraint compile_template(const TemplateConstraint& t, const std::vector<label_t>& role_label,
+                                    int variant = kNlccReference);
 // ENUMERATION: the first walkMap entry (enumeration :133-135).
 CompiledConstraint compile_enumeration(const TemplateConstraint& t, const std::vector<label_t>& role_label);
 

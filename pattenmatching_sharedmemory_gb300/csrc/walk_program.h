@@ -91,7 +91,9 @@ struct WalkProgram {
   uint8_t max_refs;      // largest popcount of state_refs
   uint8_t tail_from;     // first step of the trailing CHECK-only suffix
   uint8_t count_memo;    // ENUMERATION: subtree counts may be memoized
-  uint8_t pad[5];
+  uint8_t injective;     // CC/PC/TDS: no vertex bound twice (the article
+                         // drivers' strict walks); ENUMERATION always is
+  uint8_t pad[4];
   uint8_t hist_step[kMaxWalkSteps];   // history index -> step index
   uint8_t store_step[kMaxWalkSteps];  // i-th store step
   uint64_t state_refs[kMaxWalkSteps]; // history indices (>0) keyed by the

@@ -42,7 +42,7 @@ REF_DATA = REF_ROOT / "data" / "patternmatching"
 REF_BIN = ROOT / "oracle" / "_ref" / "patternmatching"
 
 
-def run_reference(graph, labels, pattern_dir, out_dir, threads=1, timeout=600):
+def run_reference(graph, labels, pattern_dir, out_dir, threads=1, timeout=600, binary=None):
     out_dir = Path(out_dir)
     if out_dir.exists():
         shutil.rmtree(out_dir)
@@ -50,7 +50,7 @@ def run_reference(graph, labels, pattern_dir, out_dir, threads=1, timeout=600):
     if os.path.exists(bin_path):
         os.remove(bin_path)
     env = dict(os.environ, PM_REF_THREADS=str(threads))
-    cmd = [str(REF_BIN), "-i", str(graph), "-b", bin_path, "-v", str(labels), "-p", str(pattern_dir).rstrip("/") + "/",
+    cmd = [str(binary or REF_BIN), "-i", str(graph), "-b", bin_path, "-v", str(labels), "-p", str(pattern_dir).rstrip("/") + "/",
            "-o", str(out_dir) + "/"]
     subprocess.run(cmd, env=env, check=True, timeout=timeout, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return parse_outputs(out_dir)
@@ -160,6 +160,41 @@ def stream15():
         print(case["name"], res["rows"][-2][8], "matches", flush=True)
 
 
+def article():
+    """The article drivers' strict and backtrack variants
+    (oracle/_ref/patternmatching_{strict,backtrack}, test_article/
+    CMakeLists.txt:12-33) on the bundled fixtures and the small synthetic
+    cases: rows and sha256 of the final vertex / graph files."""
+    out = []
+    cases = [("fixture_" + t, None, t) for t in ["test_1", "test_2", "test_3", "test_4"]]
+    cases += [(c["name"], c, None) for c in C.synthetic_cases(include_big=False)
+              if c["name"] not in ("scale12_cycle4",)]
+    for name, case, fixture in cases:
+        for variant in ("strict", "backtrack"):
+            binary = ROOT / "oracle" / "_ref" / f"patternmatching_{variant}"
+            with tempfile.TemporaryDirectory() as tmp:
+                tmp = Path(tmp)
+                if fixture:
+                    d = HERE / "data" / fixture
+                    graph, labels, pdir = d / "graph.totem", d / "vertex_data" / "graph_vertex_data.totem", \
+                        d / "pattern_1"
+                else:
+                    g = C.make_graph(case)
+                    g.write_text(tmp / "g.totem", tmp / "labels.totem")
+                    C.make_pattern(case).write(tmp / "pattern")
+                    graph, labels, pdir = tmp / "g.totem", tmp / "labels.totem", tmp / "pattern"
+                try:
+                    res = run_reference(graph, labels, pdir, tmp / "out", binary=binary, timeout=300)
+                except subprocess.TimeoutExpired:
+                    print("timeout", name, variant)
+                    continue
+            out.append({"name": name, "variant": variant, "fixture": fixture, "case": case, "rows": res["rows"],
+                        "vertex_sha256": sha(res["vertex"]), "graph_sha256": sha(res["graph"]),
+                        "last": res["last"]})
+            print(name, variant, res["rows"][-1], flush=True)
+    (HERE / "article_variants.json").write_text(json.dumps(out, indent=1))
+
+
 def constraints():
     # A fixed tiny background graph: constraint generation ignores it.
     out = []
@@ -180,7 +215,7 @@ def constraints():
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-big", action="store_true", help="skip the scale-16 case (minutes of CPU)")
-    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big", "stream15"])
+    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big", "stream15", "article"])
     a = ap.parse_args()
     if not REF_BIN.exists():
         sys.exit("build the reference first: make -C oracle ref")
@@ -194,3 +229,5 @@ if __name__ == "__main__":
         synthetic(False, only_big=True)
     if a.only == "stream15":
         stream15()
+    if a.only == "article":
+        article()

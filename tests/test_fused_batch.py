@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 SYNTH = {c["name"]: c for c in pmtest.load_synthetic_golden()}
 MIX = ["c1_scale10_cycle4", "triangle_rep_s9", "path4_rep_s9", "fixture3_s9", "k4_rep_s8", "two_cycles_s10",
-       "scale12_tds", "cycle4_rep_s9", "star_s9", "fixture4_s10", "path_rep_s9", "cycle5_s10"]
+       "scale12_tds", "cycle4_rep_s9", "star_s9", "fixture1_s10_zipf", "path_rep_s9", "cycle5_s10"]
 
 
 def _patterns():

