@@ -592,10 +592,10 @@ def run_c5(args, pm, T):
                 if x not in labels:
                     labels.append(x)
             tmpls.append(T.cycle(labels))
-    pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    pm._check(pm.lib.pm_set_query_budget_ms(args.c5_budget_ms))
     sample = list(range(0, n, 100)) + list(range(1, n, 100))
     try:
-        with pm.Server(g, slots=args.slots) as srv:
+        with pm.Server(g, slots=args.c5_slots) as srv:
             serve_burst(srv, pm, tmpls[:4])
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -616,9 +616,15 @@ def run_c5(args, pm, T):
                 q.close()
                 continue
             q.close()
+            # Distinct template labels: no memo test can block a walk, so the
+            # alreadyMatched shortcut changes no outcome and the oracle's
+            # walks may use every core; repeated labels keep the canonical
+            # one-thread order.
+            distinct = len(set(int(x) for x in tmpls[i].labels)) == len(tmpls[i].labels)
             try:
                 ref = oracle.run_ex(off, adj, lab, tmpls[i].offsets, tmpls[i].adj, tmpls[i].labels, threads=threads,
-                                    nlcc_threads=1, stop_before_enumeration=True, deadline_ms=args.c5_oracle_ms)
+                                    nlcc_threads=threads if distinct else 1, stop_before_enumeration=True,
+                                    deadline_ms=args.c5_oracle_ms)
             except oracle.OracleTimeout:
                 cpu_timeouts += 1
                 continue
@@ -637,7 +643,8 @@ def run_c5(args, pm, T):
             "graph": "undirected rmat scale 26 ef 16, 64 labels correlated with degree rank",
             "csr_entries": edges, "graph_generation_s": gen_s,
             "templates": f"{n} seeded: 10-vertex templates with repeated labels (seed 26) and 4-cycles with distinct "
-                         "labels, alternating", "budget_ms": args.budget_ms, "unit": "queries/s",
+                         "labels, alternating", "budget_ms": args.c5_budget_ms, "slots": args.c5_slots,
+            "unit": "queries/s",
             "served": out["completed"] / served_s, "served_outcomes": out,
             "one_at_a_time": n_q / seq_s if seq_s else None, "one_at_a_time_requests": args.same_requests,
             "one_at_a_time_completed": n_q, "device_ms_by_class": {k: round(v, 3) for k, v in cls_ms.items()},
@@ -822,7 +829,9 @@ def main():
     ap.add_argument("--workload", choices=["c4", "c5"], default="c4",
                     help="c5: the RMAT-26 mixed stream with its oracle sample (its own JSON line)")
     ap.add_argument("--c5-requests", type=int, default=200)
-    ap.add_argument("--c5-oracle-ms", type=float, default=60000.0)
+    ap.add_argument("--c5-oracle-ms", type=float, default=180000.0)
+    ap.add_argument("--c5-budget-ms", type=float, default=1000.0, help="per-request GPU budget of the scale-26 runs")
+    ap.add_argument("--c5-slots", type=int, default=8)
     ap.add_argument("--case", choices=["c1", "lcc", "c4"], default=None)
     ap.add_argument("--queries", type=int, default=1)
     ap.add_argument("--scale", type=int, default=22)

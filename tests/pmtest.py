@@ -100,10 +100,10 @@ def edge_bits(eact: np.ndarray) -> np.ndarray:
     return buf.view("<u4").astype(np.uint32)
 
 
-def sampled_count_gpu(graph, pattern, cand, eact, start_role: int, stride: int) -> int:
-    """ENUMERATION count over the sources v % stride == 0 only: the pruned
-    state with the start role cleared on every other vertex, counted by
-    pm_enumerate_noalloc (the start role is bound at the walk's first step
+def sampled_count_gpu(graph, pattern, cand, eact, start_role: int, stride: int, residue: int = 0) -> int:
+    """ENUMERATION count over the sources v % stride == residue only: the
+    pruned state with the start role cleared on every other vertex, counted
+    by pm_enumerate_noalloc (the start role is bound at the walk's first step
     only, so this is the per-source sum over the sampled sources)."""
     import ctypes
 
@@ -111,7 +111,7 @@ def sampled_count_gpu(graph, pattern, cand, eact, start_role: int, stride: int) 
 
     off, adj, _ = graph.host_csr()
     c = cand.copy()
-    keep = (np.arange(len(c)) % stride) == 0
+    keep = (np.arange(len(c)) % stride) == residue
     c[~keep] &= ~np.uint64(1 << start_role)
     d_off, d_adj = device_u64(off.copy()), device_u64(adj.copy())
     d_cand, d_eact = device_u64(c), device_u64(edge_bits(eact))

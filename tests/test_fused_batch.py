@@ -27,11 +27,15 @@ MIX = ["c1_scale10_cycle4", "triangle_rep_s9", "path4_rep_s9", "fixture3_s9", "k
 
 def _patterns():
     ps = [C.make_pattern(SYNTH[n]) for n in MIX]
-    # wider word types: a 12-vertex template (32-bit words) and a 26-vertex
-    # path (64-bit words) whose last label no vertex carries, so its roles
-    # fall one layer per LCC pass until the state is empty
-    ps.append(T.random_template(12, 0.3, T.zipf_weights(8, 1.0), seed=5))
-    ps.append(pm.Pattern.from_edges(26, [(i, i + 1) for i in range(25)], [i % 8 for i in range(25)] + [9]))
+    # wider word types: a 12-vertex template (32-bit words: a 4-cycle and a
+    # tail of 8) and a 26-vertex path (64-bit words), each with distinct
+    # labels of which the last ones no vertex carries, so their roles fall
+    # one layer per LCC pass until the state is empty.  (Templates of that
+    # size with repeated labels make template-driven searches that run for
+    # minutes on this graph, in the reference's walks and on the GPU alike.)
+    ps.append(pm.Pattern.from_edges(12, [(0, 1), (1, 2), (2, 3), (3, 0)] + [(i, i + 1) for i in range(3, 11)],
+                                    list(range(8)) + [20, 21, 22, 23]))
+    ps.append(pm.Pattern.from_edges(26, [(i, i + 1) for i in range(25)], list(range(8)) + list(range(20, 38))))
     # a template whose labels no vertex carries: the state empties at LCC0
     ps.append(T.cycle([50, 51, 52]))
     return ps
