@@ -137,6 +137,16 @@ pm_status_t pm_set_enum_table_entries(uint32_t entries);
  * counterpart in the reference. */
 pm_status_t pm_set_lcc_graph(int32_t enabled);
 
+/* The first LCC pass after LCC0 reads one byte per CSR entry, the label of
+ * the entry's target (built once with the graph's device copy when the graph
+ * has at most 256 distinct labels: E bytes of device memory), instead of
+ * loading the target id and gathering its role word: after LCC0 every
+ * vertex holds exactly the roles of its label, so the byte determines the
+ * word.  Rows, counts and state are those of the gathering pass.  enabled =
+ * 0 turns it off (default 1).  Process-wide; speed only.  No counterpart in
+ * the reference (lcc :26-101 reads the neighbour's state every pass). */
+pm_status_t pm_set_lcc_label_stream(int32_t enabled);
+
 /* ENUMERATION's last VERTEX step before the closing CHECKs (e.g. the fourth
  * vertex of a 4-cycle, checked against the source): on symmetric graphs,
  * when the source's list is cached (at most 256 entries) and the current

@@ -175,6 +175,7 @@ def _load_library() -> ctypes.CDLL:
         "pm_set_noalloc_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_noalloc_last_rounds": (ctypes.c_uint32, []),
         "pm_set_lcc_graph": (ctypes.c_int32, [ctypes.c_int32]),
+        "pm_set_lcc_label_stream": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_enum_tail_swap": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_walk_tail_swap": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_enum_count_memo": (ctypes.c_int32, [ctypes.c_int32]),

@@ -533,6 +533,11 @@ pm_status_t pm_set_lcc_graph(int32_t enabled) {
   return PM_SUCCESS;
 }
 
+pm_status_t pm_set_lcc_label_stream(int32_t enabled) {
+  set_lcc_label_stream(enabled != 0);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_set_walk_budget_ms(double ms) {
   PM_REQUIRE(ms > 0, "budget must be positive");
   set_walk_budget_ns(static_cast<uint64_t>(ms * 1e6));

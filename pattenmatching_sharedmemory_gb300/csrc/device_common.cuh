@@ -98,6 +98,10 @@ struct DevGraph {
   const uint4* __restrict__ seg;   // [n_seg] {vertex, segment index, segments, accumulator}
   // Every CSR entry u -> w has its reverse w -> u (lists strictly increasing).
   int symmetric;
+  // Label of each CSR entry's target (dense label id, lab[adj[e]]), one byte
+  // per entry; null when the graph has more than 256 distinct labels.  The
+  // first LCC pass after LCC0 reads it instead of gathering neighbour words.
+  const uint8_t* __restrict__ nlab;
 };
 
 // Per-query accumulator of a hub with several segments.  Zero between
@@ -126,6 +130,10 @@ struct DevState {
   // holding a role and scheduled (hubs under the current plan count as
   // scheduled), so LCC sweep 1 can skip the tile.  Null: no summary.
   uint8_t* tile_sch;
+  // 1 for the first LCC pass after LCC0 when DevGraph::nlab exists: every
+  // vertex then holds exactly the roles of its label slot, so a neighbour's
+  // word follows from the entry's label byte (QueryTables::dense_slot).
+  uint32_t first;
 };
 
 // Device counters.  The first kStepCounterWords words are per step
@@ -184,6 +192,7 @@ struct QueryTables {
   uint64_t req_slots[64];        // slots with a required count for p
   uint8_t req[64][64];           // required neighbour count, [role][slot]
   uint64_t slot_roles[256];      // roles whose origin label has this slot
+  uint8_t dense_slot[256];       // slot of dense label ids 0..255
 };
 
 #ifdef __CUDACC__

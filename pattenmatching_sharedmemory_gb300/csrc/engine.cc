@@ -97,6 +97,12 @@ void GraphImpl::to_device(int dev) {
     PM_CUDA(cudaMemcpy(d_adj.ptr, host.adj.data(), sizeof(uint32_t) * host.edge_count, cudaMemcpyHostToDevice));
   if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
   device = dev;
+  if (host.edge_count && dense_values.size() <= 256) {
+    d_nlab.ensure(std::max<uint64_t>(host.edge_count, 16));
+    launch_build_entry_labels(this->dev(), d_nlab.as<uint8_t>(), nullptr);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaDeviceSynchronize());
+  }
   build_hub_plan(hub_degree, seg_entries);
   symmetric = false;
   if (sorted_unique && V) {
@@ -166,6 +172,7 @@ DevGraph GraphImpl::dev() const {
   g.n_acc = n_acc;
   g.seg = d_seg.as<uint4>();
   g.symmetric = symmetric ? 1 : 0;
+  g.nlab = d_nlab.as<uint8_t>();
   return g;
 }
 
@@ -271,9 +278,10 @@ QueryImpl::~QueryImpl() {
 }
 
 QueryDevPtrs QueryImpl::ptrs() const {
+  const uint32_t first = lcc_first_pending && g->d_nlab.ptr && lcc_label_stream() ? 1u : 0u;
   return QueryDevPtrs{word_kind, d_vs.ptr, d_eact.as<uint32_t>(), d_mod.as<uint8_t>(), d_sch.as<uint8_t>(),
                       d_unm.ptr, d_ctr.as<StepCounters>(), d_tables.as<QueryTables>(), d_hub_acc.as<HubAcc>(),
-                      d_lt.as<uint32_t>(), d_tile_sch.as<uint8_t>()};
+                      d_lt.as<uint32_t>(), d_tile_sch.as<uint8_t>(), first};
 }
 
 uint64_t QueryImpl::device_bytes() const {
@@ -331,6 +339,7 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, 
   }
   dense_to_slot.resize(std::max<size_t>(g->dense_values.size(), 1), 0xFF);
   for (size_t i = 0; i < g->dense_values.size(); ++i) dense_to_slot[i] = static_cast<uint8_t>(slot_of(g->dense_values[i]));
+  for (size_t i = 0; i < 256; ++i) tables.dense_slot[i] = i < dense_to_slot.size() ? dense_to_slot[i] : 0xFF;
 
   if (s) {
     stream = s;
@@ -431,6 +440,7 @@ StepResult QueryImpl::step_lcc0() {
   launch_lcc0(g->dev(), ptrs(), stream);
   PM_CUDA(cudaGetLastError());
   read_counters();
+  lcc_first_pending = true;
   StepResult r;
   r.vertex = h_ctr->vertex_elim;
   r.match = h_ctr->match_elim;
@@ -440,6 +450,7 @@ StepResult QueryImpl::step_lcc0() {
 StepResult QueryImpl::step_lcc() {
   launch_lcc_check(g->dev(), ptrs(), stream);
   launch_apply(g->dev(), ptrs(), stream);
+  lcc_first_pending = false;
   PM_CUDA(cudaGetLastError());
   read_counters();
   StepResult r;
@@ -1093,6 +1104,11 @@ thread_local LccLoopCache t_lcc_loops;
 uint64_t next_plan_epoch() { return g_plan_epochs.fetch_add(1, std::memory_order_relaxed) + 1; }
 void set_lcc_graph(bool on) { g_lcc_graph = on; }
 bool lcc_graph() { return g_lcc_graph; }
+namespace {
+std::atomic<bool> g_lcc_label_stream{true};
+}  // namespace
+void set_lcc_label_stream(bool on) { g_lcc_label_stream.store(on, std::memory_order_relaxed); }
+bool lcc_label_stream() { return g_lcc_label_stream.load(std::memory_order_relaxed); }
 
 void QueryImpl::run_lcc_loop(int max_iterations) {
   const int cap = std::min(max_iterations, 1000) - iteration;
@@ -1114,6 +1130,7 @@ void QueryImpl::run_lcc_loop(int max_iterations) {
     first_recorded = true;
   }
   PM_CUDA(cudaGraphLaunch(loop.exec, stream));
+  lcc_first_pending = false;  // the loop's first tail cleared the block's flag
   PM_CUDA(cudaEventRecord(ev1, stream));
   // Control block and the first rows in one read; the rest only if needed.
   constexpr size_t kFirstRows = 64;
@@ -1169,7 +1186,12 @@ struct BatchPtrs {
     d_qs.ensure(sizeof(QueryDevPtrs) * h_qs.size());
     d_active.ensure(4 * h_qs.size());
     d_out.ensure(sizeof(StepCounters) * h_qs.size());
-    PM_CUDA(cudaMallocHost(&h_out, sizeof(StepCounters) * h_qs.size()));
+    if (!h_out) PM_CUDA(cudaMallocHost(&h_out, sizeof(StepCounters) * h_qs.size()));
+    PM_CUDA(cudaMemcpyAsync(d_qs.ptr, h_qs.data(), sizeof(QueryDevPtrs) * h_qs.size(), cudaMemcpyHostToDevice, s));
+  }
+  // The same queries' pointer blocks again (their flags changed).
+  void refresh(const std::vector<QueryImpl*>& qs, cudaStream_t s) {
+    for (size_t i = 0; i < qs.size(); ++i) h_qs[i] = qs[i]->ptrs();
     PM_CUDA(cudaMemcpyAsync(d_qs.ptr, h_qs.data(), sizeof(QueryDevPtrs) * h_qs.size(), cudaMemcpyHostToDevice, s));
   }
   void set_active(const std::vector<uint32_t>& a, cudaStream_t s) {
@@ -1232,6 +1254,7 @@ void QueryImpl::lcc0_batch(const std::vector<QueryImpl*>& all, cudaStream_t s) {
       r.vertex = b.h_out[i].vertex_elim;
       r.match = b.h_out[i].match_elim;
       qs[i]->append_record(r, PM_STEP_LCC0, ms, 0, 0);
+      qs[i]->lcc_first_pending = true;
     }
   }
 }
@@ -1262,6 +1285,14 @@ void QueryImpl::lcc_fixpoint_batch(const std::vector<QueryImpl*>& all, cudaStrea
         PM_CUDA(cudaEventRecord(e0, s));
         launch_lcc_pass_multi(g->dev(), qs[0]->word_kind, dq, da, n, s);
         PM_CUDA(cudaEventRecord(e1, s));
+        // Passes after the first gather neighbour words: clear the flags in
+        // the device copies (stream-ordered after this pass's kernels).
+        bool any_first = false;
+        for (QueryImpl* q : qs) any_first |= q->lcc_first_pending;
+        if (any_first) {
+          for (QueryImpl* q : qs) q->lcc_first_pending = false;
+          b.refresh(qs, s);
+        }
         launch_counters_multi(dq, da, n, b.d_out.as<StepCounters>(), false, s);
         PM_CUDA(cudaGetLastError());
         PM_CUDA(cudaMemcpyAsync(b.h_out, b.d_out.ptr, sizeof(StepCounters) * n, cudaMemcpyDeviceToHost, s));

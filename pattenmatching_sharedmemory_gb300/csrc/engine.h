@@ -50,6 +50,9 @@ struct GraphImpl {
   bool symmetric = false;  // sorted_unique and every entry has its reverse (checked on the device)
   int device = -1;
   DeviceBuffer d_off, d_adj, d_lab;
+  // Target label byte per CSR entry (DevGraph::nlab), built with the device
+  // copy when the graph has at most 256 distinct labels.
+  DeviceBuffer d_nlab;
   // Degree classes of the LCC sweeps (DevGraph::hub_degree and segments).
   uint32_t hub_degree = kDefaultHubDegree, seg_entries = kDefaultSegEntries;
   uint32_t n_seg = 0, n_heavy = 0, n_acc = 0;
@@ -69,7 +72,7 @@ struct GraphImpl {
   void build_hub_plan(uint32_t hub_degree, uint32_t seg_entries);
   DevGraph dev() const;
   uint64_t device_bytes() const {
-    return d_off.bytes + d_adj.bytes + d_lab.bytes + d_seg.bytes;
+    return d_off.bytes + d_adj.bytes + d_lab.bytes + d_nlab.bytes + d_seg.bytes;
   }
 };
 
@@ -131,6 +134,9 @@ struct QueryImpl {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_first = nullptr;
   bool first_recorded = false;
   double elapsed_ms();
+  // Set by LCC0, cleared once an LCC pass ran: the next pass may read the
+  // graph's entry labels instead of gathering (DevState::first).
+  bool lcc_first_pending = false;
 
   // Request controls, checked before every step: a deadline (its remaining
   // time also caps each walker step's device budget), a cancel flag another
@@ -240,6 +246,9 @@ uint32_t enum_table_entries();
 // (default on); off: one host-driven launch sequence per pass.
 void set_lcc_graph(bool on);
 bool lcc_graph();
+// First LCC pass after LCC0 from the graph's entry labels (DevState::first).
+void set_lcc_label_stream(bool on);
+bool lcc_label_stream();
 uint64_t next_plan_epoch();
 
 // Fault injection on the host: the n-th device buffer allocation from now on

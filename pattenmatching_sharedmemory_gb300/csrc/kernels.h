@@ -27,6 +27,7 @@ struct QueryDevPtrs {
   HubAcc* hub_acc;  // [DevGraph::n_acc]
   uint32_t* lt;     // live-target bits (DevState::lt)
   uint8_t* tile_sch;  // DevState::tile_sch, ceil(V / 32) bytes
+  uint32_t first_pass;  // DevState::first (the captured loop's tail clears it)
 };
 
 // Launch geometry shared by all kernels (SM count of the current device).
@@ -46,6 +47,10 @@ void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* 
 // w -> u (adjacency lists must be strictly increasing).
 void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_t s);
 
+// nlab[e] = lab[adj[e]] (dense label ids below 256) for every CSR entry;
+// adj must be 16-byte aligned.
+void launch_build_entry_labels(const DevGraph& g, uint8_t* nlab, cudaStream_t s);
+
 // LCC0 (multiple_label_lcc0_cpu.tpp:15-87).
 void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 
@@ -56,7 +61,7 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 void launch_apply(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s);
 // Kernels of the captured LCC fixpoint loop (rows follow ctl in memory).
 void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s);
-void launch_lcc_loop_tail(const QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s);
+void launch_lcc_loop_tail(QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s);
 // One LCC pass with the query's pointers read from the device block `a`.
 void launch_lcc_pass_at(const DevGraph& g, int word_kind, const QueryDevPtrs* a, cudaStream_t s);
 // Adds launches that ran inside graphs (captured launches count once).

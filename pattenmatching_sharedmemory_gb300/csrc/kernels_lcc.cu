@@ -91,6 +91,22 @@ __global__ void __launch_bounds__(kThreads) k_check_symmetric(DevGraph g, uint32
   }
 }
 
+// Label byte of every CSR entry's target (DevGraph::nlab): four entries per
+// thread and step, the adj reads coalesced, the label reads gathered once
+// per graph.
+__global__ void __launch_bounds__(kThreads) k_build_entry_labels(DevGraph g, uint8_t* __restrict__ nlab) {
+  const uint64_t tid = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  const uint64_t quads = g.E / 4;
+  for (uint64_t i = tid; i < quads; i += stride) {
+    const uint4 a = reinterpret_cast<const uint4*>(g.adj)[i];
+    const uint32_t packed = (g.lab[a.x] & 0xFFu) | (g.lab[a.y] & 0xFFu) << 8 | (g.lab[a.z] & 0xFFu) << 16 |
+                            (g.lab[a.w] & 0xFFu) << 24;
+    reinterpret_cast<uint32_t*>(nlab)[i] = packed;
+  }
+  for (uint64_t e = quads * 4 + tid; e < g.E; e += stride) nlab[e] = static_cast<uint8_t>(g.lab[g.adj[e]]);
+}
+
 // ---- LCC0 ---------------------------------------------------------------
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_lcc0(DevGraph g, DevState<W> st, const QueryTables* __restrict__ qt,
@@ -144,6 +160,10 @@ struct LccTables {
   uint64_t need[64];
   uint8_t role_slot[64];
   uint8_t req[64][64];
+  // First pass after LCC0 (DevState::first): role set and slot of a vertex
+  // by its dense label id.
+  uint64_t lab_cand[256];
+  uint8_t lab_slot[256];
 };
 
 struct LccWarp {
@@ -162,7 +182,8 @@ __device__ __forceinline__ void set_ranks(LccWarp& lw, uint64_t slots, uint32_t 
   __syncwarp();
 }
 
-__device__ __forceinline__ void load_lcc_tables(LccTables& t, const QueryTables* __restrict__ qt, uint32_t k) {
+__device__ __forceinline__ void load_lcc_tables(LccTables& t, const QueryTables* __restrict__ qt, uint32_t k,
+                                                bool first) {
   for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) {
     t.nbr[i] = qt->nbr_mask[i];
     t.need[i] = qt->req_slots[i];
@@ -170,7 +191,24 @@ __device__ __forceinline__ void load_lcc_tables(LccTables& t, const QueryTables*
   }
   const uint32_t rows = k < 64 ? k : 64;
   for (uint32_t i = threadIdx.x; i < rows * 64; i += blockDim.x) t.req[i / 64][i % 64] = qt->req[i / 64][i % 64];
+  if (first) {
+    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
+      const uint8_t sl = qt->dense_slot[i];
+      t.lab_slot[i] = sl;
+      t.lab_cand[i] = qt->slot_roles[sl];
+    }
+  }
   __syncthreads();
+}
+
+// The neighbour word of CSR entry e as LCC sweep 1 sees it.  In the first
+// pass after LCC0 every vertex holds exactly the roles of its label slot
+// (LCC0 intersected the full role set with them, and sweep 1 changes no
+// role), so the entry's label byte gives the word without the dependent
+// adj -> vs gather; later passes gather.
+template <class W>
+__device__ __forceinline__ W label_word(const LccTables& t, uint32_t lb) {
+  return Pack<W>::make(t.lab_cand[lb], t.lab_slot[lb]);
 }
 
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -316,8 +354,12 @@ __device__ void lcc_vertex_warp(const DevGraph& g, const DevState<W>& st, const 
     const bool act = e < end && edge_active(st.eact, e);
     W ww = Pack<W>::zero();
     if (act) {
-      ww = st.vs[g.adj[e]];
-      ++tl.gathered;
+      if (st.first) {
+        ww = label_word<W>(t, g.nlab[e]);
+      } else {
+        ww = st.vs[g.adj[e]];
+        ++tl.gathered;
+      }
     }
     const uint64_t cw = Pack<W>::cand(ww);
     const bool live = act && cw != 0;
@@ -386,7 +428,7 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
       if (beg > lo) word &= ~0u << static_cast<uint32_t>(beg - lo);
       if (end < lo + 32) word &= (1u << static_cast<uint32_t>(end - lo)) - 1u;
     }
-    tl.gathered += __popc(word);
+    if (!st.first) tl.gathered += __popc(word);
     for (unsigned nz = __ballot_sync(kFull, word != 0); nz;) {
       uint32_t idx[kUnroll], bits[kUnroll];
 #pragma unroll
@@ -396,13 +438,23 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
         bits[u] = __shfl_sync(kFull, word, idx[u] & 31);
         if (idx[u] == 32) bits[u] = 0;
       }
-      uint32_t nb[kUnroll];
-#pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
-        nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
       W ww[kUnroll];
+      if (st.first) {
+        uint32_t lb[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+        for (int u = 0; u < kUnroll; ++u)
+          lb[u] = ((bits[u] >> lane) & 1u) ? g.nlab[((w0 + idx[u]) << 5) + lane] : 0u;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+          ww[u] = ((bits[u] >> lane) & 1u) ? label_word<W>(t, lb[u]) : Pack<W>::zero();
+      } else {
+        uint32_t nb[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+          nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+      }
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
         const bool in = (bits[u] >> lane) & 1u;
@@ -575,15 +627,22 @@ __device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTab
       bit[u] = in[u] ? static_cast<uint32_t>(__ffs(word) - 1) : 0u;
       word &= word - 1;
     }
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) nb[u] = in[u] ? g.adj[(w << 5) + bit[u]] : 0u;
     W ww[kUnroll];
+    if (st.first) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) ww[u] = in[u] ? st.vs[nb[u]] : Pack<W>::zero();
+      for (int u = 0; u < kUnroll; ++u) nb[u] = in[u] ? g.nlab[(w << 5) + bit[u]] : 0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) ww[u] = in[u] ? label_word<W>(t, nb[u]) : Pack<W>::zero();
+    } else {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) nb[u] = in[u] ? g.adj[(w << 5) + bit[u]] : 0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) ww[u] = in[u] ? st.vs[nb[u]] : Pack<W>::zero();
+    }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
       if (!in[u]) continue;
-      ++gathered;
+      gathered += !st.first;
       const uint64_t cw = Pack<W>::cand(ww[u]);
       const bool poss = (cw & ncs) != 0;
       if (!poss) {
@@ -715,18 +774,25 @@ __device__ void lcc_tile(const DevGraph& g, const DevState<W>& st, const LccTabl
       e[u] = shfl64(base, lo) + i;
     }
     uint32_t aw[kUnroll], nb[kUnroll];
+    const bool first = st.first;
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
       aw[u] = in[u] ? st.lt[e[u] >> 5] : 0u;
-      nb[u] = in[u] ? g.adj[e[u]] : 0u;
+      nb[u] = in[u] ? (first ? static_cast<uint32_t>(g.nlab[e[u]]) : g.adj[e[u]]) : 0u;
     }
     W ww[kUnroll];
+    if (first) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) ww[u] = ((aw[u] >> (e[u] & 31)) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+      for (int u = 0; u < kUnroll; ++u)
+        ww[u] = ((aw[u] >> (e[u] & 31)) & 1u) ? label_word<W>(t, nb[u]) : Pack<W>::zero();
+    } else {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) ww[u] = ((aw[u] >> (e[u] & 31)) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+    }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
       const bool act = (aw[u] >> (e[u] & 31)) & 1u;
-      tl.gathered += act;
+      tl.gathered += act && !first;
       const uint64_t cw = Pack<W>::cand(ww[u]);
       const uint64_t own_ncs = shfl64(ncs, own[u]);
       const bool live = cw != 0;  // entries outside lt gathered zero
@@ -770,7 +836,7 @@ __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState
                                                StepCounters* ctr, const uint64_t warp, const uint64_t n_warps) {
   __shared__ LccTables t;
   __shared__ LccWarp s_lw[kLccWarps];
-  load_lcc_tables(t, qt, qt->k);
+  load_lcc_tables(t, qt, qt->k, st.first != 0);
   LccWarp& lw = s_lw[threadIdx.x >> 5];
   const uint64_t heavy = g.n_heavy;
   const uint64_t batched = heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
@@ -813,7 +879,8 @@ __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState
 // instantiated graph serves every query that writes its block).
 template <class W>
 __device__ __forceinline__ DevState<W> state_at(const QueryDevPtrs* __restrict__ a) {
-  return DevState<W>{static_cast<W*>(a->vs), a->eact, a->mod, a->sch, static_cast<W*>(a->unm), a->lt, a->tile_sch};
+  return DevState<W>{static_cast<W*>(a->vs), a->eact, a->mod, a->sch, static_cast<W*>(a->unm), a->lt, a->tile_sch,
+                     a->first_pass};
 }
 
 template <class W, bool kTiles>
@@ -1266,10 +1333,11 @@ __global__ void k_lcc_loop_head(LccLoopCtl* ctl) {
 // max_passes passes ran.  The step counters start the next pass at zero.
 // rows holds kLccLoopMaxPasses rows and max_passes <= kLccLoopMaxPasses, so
 // the row index stays in bounds.
-__global__ void k_lcc_loop_tail(const QueryDevPtrs* __restrict__ a, LccLoopCtl* ctl, LccPassRow* rows,
+__global__ void k_lcc_loop_tail(QueryDevPtrs* __restrict__ a, LccLoopCtl* ctl, LccPassRow* rows,
                                 cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0) return;
   StepCounters* ctr = a->ctr;
+  a->first_pass = 0;  // later passes gather neighbour words
   const uint32_t i = ctl->passes;
   const uint32_t cap = min(ctl->max_passes, kLccLoopMaxPasses);
   LccPassRow r;
@@ -1398,7 +1466,8 @@ __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st,
 
 template <class W>
 DevState<W> state_of(const QueryDevPtrs& q) {
-  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt, q.tile_sch};
+  return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt, q.tile_sch,
+                     q.first_pass};
 }
 
 #define PM_DISPATCH_WORD(kind, ...)            \
@@ -1454,6 +1523,11 @@ void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_
   k_check_symmetric<<<device_sm_count() * 8, kThreads, 0, s>>>(g, asymmetric);
 }
 
+void launch_build_entry_labels(const DevGraph& g, uint8_t* nlab, cudaStream_t s) {
+  note_launch();
+  k_build_entry_labels<<<device_sm_count() * 8, kThreads, 0, s>>>(g, nlab);
+}
+
 void launch_lcc0(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) {
   const int grid = device_sm_count() * 8;
   PM_DISPATCH_WORD(q.word_kind, k_lcc0<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.ctr));
@@ -1503,7 +1577,7 @@ void launch_lcc_loop_head(LccLoopCtl* ctl, cudaStream_t s) {
   k_lcc_loop_head<<<1, 32, 0, s>>>(ctl);
 }
 
-void launch_lcc_loop_tail(const QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s) {
+void launch_lcc_loop_tail(QueryDevPtrs* a, LccLoopCtl* ctl, cudaGraphConditionalHandle h, cudaStream_t s) {
   note_launch();
   k_lcc_loop_tail<<<1, 32, 0, s>>>(a, ctl, reinterpret_cast<LccPassRow*>(ctl + 1), h);
 }

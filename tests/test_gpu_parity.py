@@ -302,6 +302,39 @@ def test_lcc_graph_equals_host_loop(name):
     assert cum == sorted(cum)
 
 
+@pytest.mark.parametrize("name", LCC_GRAPH_CASES)
+def test_lcc_label_stream_equals_gather(name):
+    """The first LCC pass after LCC0 from the entry label bytes gives the
+    rows, count and state of the pass that gathers neighbour words, through
+    the captured loop and the host-driven loop alike."""
+    case = next(c for c in SYNTH if c["name"] == name)
+    g = C.make_graph(case).to_device(0)
+    p = C.make_pattern(case)
+    pm._check(pm.lib.pm_set_lcc_label_stream(0))
+    try:
+        gather = _rows_and_state(g, p)
+    finally:
+        pm._check(pm.lib.pm_set_lcc_label_stream(1))
+    for graph_loop in (1, 0):
+        pm._check(pm.lib.pm_set_lcc_graph(graph_loop))
+        try:
+            label = _rows_and_state(g, p)
+        finally:
+            pm._check(pm.lib.pm_set_lcc_graph(1))
+        assert label[1] == gather[1] == [tuple(r) for r in case["rows"]]
+        assert label[2] == gather[2]
+        for a, b in zip(label[3:], gather[3:]):
+            assert np.array_equal(a, b)
+    # The first LCC row read no neighbour word; the gathering run's did.
+    first_lcc = next(i for i, r in enumerate(gather[1]) if r[0] == "LCC")
+    q = pm.Query(g, pattern=p)
+    q.step()
+    q.step()
+    assert q.step_walk_stats(first_lcc)[1] == 0
+    q.close()
+    g.close()
+
+
 def test_lcc_graph_follows_hub_plan_change():
     """A plan change between queries rebuilds the captured loop (its kernels
     bake the graph's segment table)."""
