@@ -809,14 +809,19 @@ def run_case(args):
     kind, n_labels, s, lseed = C4["labels"]
     g = pm.Graph.rmat(args.scale, 16, seed=1).assign_labels(kind, n_labels, s, lseed).to_device(0)
     pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    if args.walk_table:
+        pm._check(pm.lib.pm_set_walk_table_entries(args.walk_table))
+    done, t0 = 0, time.perf_counter()
     for p in c4_stream(T)[:args.queries]:
         q = pm.Query(g, pattern=p)
         try:
             rows = q.prune()
+            done += 1
             print(p.n, "ok", [(pm.STEP_NAMES[r.step], round(r.step_ms, 3)) for r in rows][:12])
         except pm.PmError as e:
             print(p.n, "error", e.code)
         q.close()
+    print(f"completed {done} of {args.queries} in {time.perf_counter() - t0:.3f} s")
 
 
 def main():
@@ -836,6 +841,7 @@ def main():
     ap.add_argument("--cpu-requests", type=int, default=2)
     ap.add_argument("--lcc-roofline", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--walk-table", type=int, default=0, help="--case c4: walker state-memo entries per warp")
     ap.add_argument("--no-label-stream", action="store_true",
                     help="--case lcc: first LCC pass gathers neighbour words instead of reading entry labels")
     ap.add_argument("--no-c1", action="store_true")

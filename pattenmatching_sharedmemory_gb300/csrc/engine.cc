@@ -191,7 +191,7 @@ void WalkPool::ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uin
   PM_CUDA(cudaMemsetAsync(hyp.ptr, 0, hyp.bytes, s));
   PM_CUDA(cudaMemsetAsync(state.ptr, 0, state.bytes, s));
   PM_CUDA(cudaMemsetAsync(epochs.ptr, 0, epochs.bytes, s));
-  sc.edge_tab = edge.as<uint4>();
+  sc.edge_tab = edge.as<uint32_t>();
   sc.hyp_tab = hyp.as<uint32_t>();
   sc.state_tab = state.as<uint32_t>();
   sc.epochs = epochs.as<uint32_t>();

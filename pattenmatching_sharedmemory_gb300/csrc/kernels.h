@@ -131,7 +131,7 @@ uint64_t effective_walk_budget_ns();
 // that fills them is re-run with larger tables); the state table is a
 // best-effort cache (state memo / count memo, see walk_program.h).
 struct WalkScratch {
-  uint4* edge_tab;       // n_warps * edge_cap entries {epoch, a, b, step}
+  uint32_t* edge_tab;    // per warp 4 * edge_cap words: columns tag, a, b, step
   uint32_t* hyp_tab;     // n_warps * hyp_cap * hyp_stride words
   uint32_t* state_tab;   // n_warps * state_cap * state_stride words
   uint32_t* epochs;      // n_warps

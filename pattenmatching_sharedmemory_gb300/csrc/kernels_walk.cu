@@ -215,27 +215,44 @@ __device__ __forceinline__ uint64_t warp_step_deadline(StepCounters* ctr, uint64
 
 // ---- per-warp memo tables -------------------------------------------------
 struct WarpMemo {
-  uint4* edge;
+  uint32_t* edge;
   uint32_t* hyp;
   uint32_t* state;
   uint32_t edge_cap, hyp_cap, hyp_stride, state_cap, state_stride;
-  uint32_t epoch;
+  uint32_t epoch;  // 1..65535
   uint32_t edge_n, hyp_n, state_n;
 };
+
+// Memo tables are open-addressing sets stored word-major (word w of slot s
+// at tab[w * cap + s]) whose first word is a tag: the walk's 16-bit epoch
+// in the high half and a 16-bit fingerprint of the key in the low half.
+// Zeroed memory and slots of older epochs are free, so a new walk only
+// bumps the epoch.  A lookup probes aligned windows of 32 slots, one lane
+// per slot: the tags of a window are one 128-byte line, and the other words
+// of a slot are read only where the whole tag matches (one live slot in
+// 65,536 by chance), so a probe costs one line, not one line per word.
+constexpr uint32_t kMaxEpoch = 0xFFFFu;
+
+__device__ __forceinline__ uint32_t memo_tag(uint32_t epoch, uint32_t h) {
+  return (epoch << 16) | (fmix32(h ^ 0x85ebca6bu) >> 16);
+}
 
 __device__ __forceinline__ uint32_t edge_hash(uint32_t a, uint32_t b, uint32_t step) {
   return fmix32(mix32(mix32(mix32(0x9747b28cu, a), b), step));
 }
 
-// True when (a, b, step) is present.
+// Edge memo slot words: {tag, a, b, step}.  True when (a, b, step) is
+// present.
 __device__ bool edge_memo_find(const WarpMemo& m, uint32_t a, uint32_t b, uint32_t step) {
   const unsigned lane = lane_id();
-  const uint32_t mask = m.edge_cap - 1;
+  const uint32_t cap = m.edge_cap, mask = cap - 1;
   const uint32_t h = edge_hash(a, b, step);
-  for (uint32_t probe = 0; probe < m.edge_cap; probe += 32) {
-    const uint4 ent = __ldcg(m.edge + ((h + probe + lane) & mask));
-    const bool live = ent.x == m.epoch;
-    const bool match = live && ent.y == a && ent.z == b && ent.w == step;
+  const uint32_t tag = memo_tag(m.epoch, h), base = h & mask & ~31u;
+  for (uint32_t probe = 0; probe < cap; probe += 32) {
+    const uint32_t* e = m.edge + ((base + probe + lane) & mask);
+    const uint32_t tg = __ldcg(e);
+    const bool live = (tg >> 16) == m.epoch;
+    const bool match = tg == tag && __ldcg(e + cap) == a && __ldcg(e + 2 * cap) == b && __ldcg(e + 3 * cap) == step;
     if (__any_sync(kFull, match)) return true;
     if (__any_sync(kFull, !live)) return false;
   }
@@ -245,17 +262,23 @@ __device__ bool edge_memo_find(const WarpMemo& m, uint32_t a, uint32_t b, uint32
 // Inserts (a, b, step) if absent; false on overflow.
 __device__ bool edge_memo_insert(WarpMemo& m, uint32_t a, uint32_t b, uint32_t step) {
   const unsigned lane = lane_id();
-  const uint32_t mask = m.edge_cap - 1;
+  const uint32_t cap = m.edge_cap, mask = cap - 1;
   const uint32_t h = edge_hash(a, b, step);
-  for (uint32_t probe = 0; probe < m.edge_cap; probe += 32) {
-    const uint32_t slot = (h + probe + lane) & mask;
-    const uint4 ent = __ldcg(m.edge + slot);
-    const bool live = ent.x == m.epoch;
-    const bool match = live && ent.y == a && ent.z == b && ent.w == step;
+  const uint32_t tag = memo_tag(m.epoch, h), base = h & mask & ~31u;
+  for (uint32_t probe = 0; probe < cap; probe += 32) {
+    uint32_t* e = m.edge + ((base + probe + lane) & mask);
+    const uint32_t tg = __ldcg(e);
+    const bool live = (tg >> 16) == m.epoch;
+    const bool match = tg == tag && __ldcg(e + cap) == a && __ldcg(e + 2 * cap) == b && __ldcg(e + 3 * cap) == step;
     if (__any_sync(kFull, match)) return true;
     const unsigned em = __ballot_sync(kFull, !live);
     if (em) {
-      if (lane == static_cast<unsigned>(__ffs(em) - 1)) __stcg(m.edge + slot, make_uint4(m.epoch, a, b, step));
+      if (lane == static_cast<unsigned>(__ffs(em) - 1)) {
+        __stcg(e + cap, a);
+        __stcg(e + 2 * cap, b);
+        __stcg(e + 3 * cap, step);
+        __stcg(e, tag);
+      }
       __syncwarp();
       return ++m.edge_n <= (m.edge_cap >> 1);
     }
@@ -297,32 +320,32 @@ __device__ __forceinline__ uint32_t tuple_hash(uint32_t nb, uint32_t step, const
   return fmix32(h);
 }
 
-// Open-addressing tuple table of `cap` entries, stored word-major: word w
-// of entry s at tab[w * cap + s], entry = {epoch, nb, step, key words padded
-// with 0xFFFFFFFF, [count lo, count hi]}.  Probes 32 consecutive slots per
-// round, so the epoch words of a probe are one 128-byte line and the key
-// words are read only where the epoch matches.  Returns the slot of a live
-// match, or ~0 with *empty_slot set to the first free slot (or ~0 when the
-// table has no free slot in reach).
+// Tuple table of `cap` slots, words {tag, nb, step, key words padded with
+// 0xFFFFFFFF, [count lo, count hi]} (see memo_tag).  Returns the slot of a
+// live match, or ~0 with *empty_slot set to the first free slot (~0 when the
+// table has no free slot in reach); *tag_out is the key's tag.
 __device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t key_words, uint32_t epoch, uint32_t nb,
-                               uint32_t step, const KeyTuple& t, uint32_t* empty_slot) {
+                               uint32_t step, const KeyTuple& t, uint32_t* empty_slot, uint32_t* tag_out) {
   const unsigned lane = lane_id();
   const uint32_t mask = cap - 1;
   const uint32_t h = tuple_hash(nb, step, t);
+  const uint32_t tag = memo_tag(epoch, h), base = h & mask & ~31u;
+  *tag_out = tag;
   for (uint32_t probe = 0; probe < cap; probe += 32) {
-    const uint32_t slot = (h + probe + lane) & mask;
+    const uint32_t slot = (base + probe + lane) & mask;
     const uint32_t* e = tab + slot;
-    const bool live = __ldcg(e) == epoch;
-    bool match = live && __ldcg(e + cap) == nb && __ldcg(e + 2 * cap) == step;
+    const uint32_t tg = __ldcg(e);
+    const bool live = (tg >> 16) == epoch;
+    bool match = tg == tag && __ldcg(e + cap) == nb && __ldcg(e + 2 * cap) == step;
     for (uint32_t i = 0; match && i < key_words; ++i) {
       const uint32_t want = static_cast<int>(i) < t.n ? t[i] : 0xFFFFFFFFu;
       if (__ldcg(e + static_cast<uint64_t>(3 + i) * cap) != want) match = false;
     }
     const unsigned mm = __ballot_sync(kFull, match);
-    if (mm) return (h + probe + __ffs(mm) - 1) & mask;
+    if (mm) return (base + probe + __ffs(mm) - 1) & mask;
     const unsigned em = __ballot_sync(kFull, !live);
     if (em) {
-      *empty_slot = (h + probe + __ffs(em) - 1) & mask;
+      *empty_slot = (base + probe + __ffs(em) - 1) & mask;
       return ~0u;
     }
   }
@@ -330,7 +353,7 @@ __device__ uint32_t tuple_find(const uint32_t* tab, uint32_t cap, uint32_t key_w
   return ~0u;
 }
 
-__device__ void tuple_write(uint32_t* tab, uint32_t cap, uint32_t key_words, uint32_t slot, uint32_t epoch,
+__device__ void tuple_write(uint32_t* tab, uint32_t cap, uint32_t key_words, uint32_t slot, uint32_t tag,
                             uint32_t nb, uint32_t step, const KeyTuple& t, bool with_count, unsigned long long count) {
   if (lane_id() == 0) {
     uint32_t* w = tab + slot;
@@ -342,7 +365,7 @@ __device__ void tuple_write(uint32_t* tab, uint32_t cap, uint32_t key_words, uin
       __stcg(w + static_cast<uint64_t>(3 + key_words) * cap, static_cast<uint32_t>(count));
       __stcg(w + static_cast<uint64_t>(4 + key_words) * cap, static_cast<uint32_t>(count >> 32));
     }
-    __stcg(w, epoch);
+    __stcg(w, tag);
   }
   __syncwarp();
 }
@@ -354,9 +377,10 @@ __device__ int hyp_memo(WarpMemo& m, uint32_t nb, uint32_t step, const WarpShare
   const KeyTuple t = stored_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.hyp_stride - 3;
-  if (tuple_find(m.hyp, m.hyp_cap, key_words, m.epoch, nb, step, t, &empty) != ~0u) return kFound;
+  uint32_t tag;
+  if (tuple_find(m.hyp, m.hyp_cap, key_words, m.epoch, nb, step, t, &empty, &tag) != ~0u) return kFound;
   if (empty == ~0u) return kOverflowHit;
-  tuple_write(m.hyp, m.hyp_cap, key_words, empty, m.epoch, nb, step, t, false, 0);
+  tuple_write(m.hyp, m.hyp_cap, key_words, empty, tag, nb, step, t, false, 0);
   return ++m.hyp_n <= (m.hyp_cap >> 1) ? kNone : kOverflowHit;
 }
 
@@ -368,9 +392,11 @@ __device__ int state_seen(WarpMemo& m, uint32_t nb, uint32_t step, const WarpSha
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step | kStateTag, t, &empty) != ~0u) return kFound;
+  uint32_t tag;
+  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step | kStateTag, t, &empty, &tag) != ~0u)
+    return kFound;
   if (empty == ~0u || m.state_n >= (m.state_cap >> 1)) return kOverflowHit;
-  tuple_write(m.state, m.state_cap, key_words, empty, m.epoch, nb, step | kStateTag, t, false, 0);
+  tuple_write(m.state, m.state_cap, key_words, empty, tag, nb, step | kStateTag, t, false, 0);
   ++m.state_n;
   return kNone;
 }
@@ -381,7 +407,8 @@ __device__ bool count_lookup(const WarpMemo& m, uint32_t nb, uint32_t step, cons
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  const uint32_t slot = tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty);
+  uint32_t tag;
+  const uint32_t slot = tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty, &tag);
   if (slot == ~0u) return false;
   const uint32_t* e = m.state + slot;
   *count = static_cast<unsigned long long>(__ldcg(e + static_cast<uint64_t>(3 + key_words) * m.state_cap)) |
@@ -396,9 +423,10 @@ __device__ bool count_store(WarpMemo& m, uint32_t nb, uint32_t step, const WarpS
   const KeyTuple t = state_key(ws, d);
   uint32_t empty = ~0u;
   const uint32_t key_words = m.state_stride - 5;
-  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty) != ~0u) return true;
+  uint32_t tag;
+  if (tuple_find(m.state, m.state_cap, key_words, m.epoch, nb, step, t, &empty, &tag) != ~0u) return true;
   if (empty == ~0u) return false;
-  tuple_write(m.state, m.state_cap, key_words, empty, m.epoch, nb, step, t, true, count);
+  tuple_write(m.state, m.state_cap, key_words, empty, tag, nb, step, t, true, count);
   ++m.state_n;
   return true;
 }
@@ -985,11 +1013,11 @@ __device__ __forceinline__ void load_program(WarpShared& ws, const WalkProgram* 
 
 __device__ __forceinline__ void next_epoch(WarpMemo& m) {
   ++m.epoch;
-  if (m.epoch == 0) {
-    // 2^32 walks on this warp: wipe the tables once and restart at 1.
-    for (uint32_t i = lane_id(); i < m.edge_cap; i += 32) m.edge[i] = make_uint4(0, 0, 0, 0);
-    for (uint64_t i = lane_id(); i < static_cast<uint64_t>(m.hyp_cap) * m.hyp_stride; i += 32) m.hyp[i] = 0;
-    for (uint64_t i = lane_id(); i < static_cast<uint64_t>(m.state_cap) * m.state_stride; i += 32) m.state[i] = 0;
+  if (m.epoch > kMaxEpoch || m.epoch == 0) {
+    // 65,535 walks on this warp: clear the tags once and restart at 1.
+    for (uint32_t i = lane_id(); i < m.edge_cap; i += 32) m.edge[i] = 0;
+    for (uint32_t i = lane_id(); i < m.hyp_cap; i += 32) m.hyp[i] = 0;
+    for (uint32_t i = lane_id(); i < m.state_cap; i += 32) m.state[i] = 0;
     __syncwarp();
     m.epoch = 1;
   }
@@ -1000,7 +1028,7 @@ __device__ __forceinline__ void next_epoch(WarpMemo& m) {
 
 __device__ __forceinline__ WarpMemo warp_memo(const WalkScratch& sc, uint32_t gw) {
   WarpMemo m;
-  m.edge = sc.edge_tab + static_cast<uint64_t>(gw) * sc.edge_cap;
+  m.edge = sc.edge_tab + static_cast<uint64_t>(gw) * sc.edge_cap * 4;
   m.hyp = sc.hyp_tab + static_cast<uint64_t>(gw) * sc.hyp_cap * sc.hyp_stride;
   m.state = sc.state_tab + static_cast<uint64_t>(gw) * sc.state_cap * sc.state_stride;
   m.edge_cap = sc.edge_cap;
