@@ -288,6 +288,7 @@ uint64_t QueryImpl::device_bytes() const {
   return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_tile_sch.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
          d_d2s.bytes + d_hub_acc.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
          d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes + d_slices.bytes +
+         d_slice_tiles.bytes +
          pool.bytes() + big_pool.bytes();
 }
 
@@ -296,7 +297,8 @@ std::vector<DeviceBuffer*> QueryImpl::buffers() {
           &d_tile_sch,
           &d_tables,      &d_d2s,       &d_hub_acc,   &d_progs,     &d_start_roles, &d_role_index,  &d_wl,
           &d_wl_index,    &d_blocks,    &d_count,     &d_status,    &d_marker,     &d_marks,       &d_list,
-          &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &pool.edge,   &pool.hyp,     &pool.state,    &pool.epochs,
+          &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &d_slice_tiles, &pool.edge, &pool.hyp,   &pool.state,
+          &pool.epochs,
           &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs};
 }
 
@@ -553,22 +555,20 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   bool sliced = dc.cc.exact && !record_marks && g_walk_presplit > 0 && g->sorted_unique;
   for (const WalkProgram& pr : dc.cc.programs)
     if (pr.n_steps < 2 || (pr.steps[1].kind != kStepVertex && pr.steps[1].kind != kStepFinal)) sliced = false;
-  std::vector<uint4> slices;
+  // The slices are listed on the device; only their number comes back.
+  uint64_t n_slices = 0;
   if (sliced) {
-    std::vector<uint32_t> wl(n_wl);
-    PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
+    d_slice_tiles.ensure(8 * (static_cast<uint64_t>(n_wl) / 4096 + 2));
+    unsigned long long* tiles = d_slice_tiles.as<unsigned long long>();
+    unsigned long long* total = tiles + static_cast<uint64_t>(n_wl) / 4096 + 1;
+    launch_slice_count(g->dev(), d_wl.as<uint32_t>(), n_wl, R, g_walk_presplit, tiles, total, stream);
+    PM_CUDA(cudaGetLastError());
+    unsigned long long total_h = 0;
+    PM_CUDA(cudaMemcpyAsync(&total_h, total, sizeof(total_h), cudaMemcpyDeviceToHost, stream));
     PM_CUDA(cudaStreamSynchronize(stream));
-    const std::vector<uint64_t>& off = g->host.offsets;
-    const uint64_t t = g_walk_presplit;
-    for (uint32_t pos = 0; pos < n_wl; ++pos) {
-      const uint64_t deg = off[wl[pos] + 1] - off[wl[pos]];
-      if (deg <= t) continue;
-      for (uint32_t r = 0; r < R; ++r)
-        for (uint64_t lo = 0; lo < deg; lo += t)
-          slices.push_back(make_uint4(pos * R + r, static_cast<uint32_t>(lo),
-                                      static_cast<uint32_t>(std::min(lo + t, deg)), 0));
-    }
-    sliced = !slices.empty();
+    n_slices = total_h;
+    if (n_slices >= 0xFFFFFFFFull) throw PmError{PM_E_DEVICE, "too many walker slices for 32-bit slice ids"};
+    sliced = n_slices != 0;
   }
   zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
   zero_field(d_ctr.ptr, offsetof(StepCounters, overflow), stream);
@@ -580,12 +580,13 @@ void QueryImpl::run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record
   launch_walk(g->dev(), ptrs(), w, pool.sc, stream);
   PM_CUDA(cudaGetLastError());
   if (sliced) {
-    d_slices.ensure(sizeof(uint4) * slices.size());
-    PM_CUDA(cudaMemcpyAsync(d_slices.ptr, slices.data(), sizeof(uint4) * slices.size(), cudaMemcpyHostToDevice,
-                            stream));
+    d_slices.ensure(sizeof(uint4) * n_slices);
+    launch_slice_write(g->dev(), d_wl.as<uint32_t>(), n_wl, R, g_walk_presplit,
+                       d_slice_tiles.as<unsigned long long>(), d_slices.as<uint4>(), stream);
+    PM_CUDA(cudaGetLastError());
     WalkLaunch ws = w;
     ws.slices = d_slices.as<uint4>();
-    ws.n_slices = static_cast<uint32_t>(slices.size());
+    ws.n_slices = static_cast<uint32_t>(n_slices);
     zero_field(d_ctr.ptr, offsetof(StepCounters, items), stream);
     launch_walk(g->dev(), ptrs(), ws, pool.sc, stream);
     PM_CUDA(cudaGetLastError());

@@ -83,6 +83,16 @@ void launch_lcc_pass_multi(const DevGraph& g, int word_kind, const QueryDevPtrs*
 void launch_counters_multi(const QueryDevPtrs* qs, const uint32_t* active, uint32_t nq, StepCounters* out, bool clear,
                            cudaStream_t s);
 
+// First-hop slices of the heavy items of an exact walk (worklist positions
+// whose vertex has more than t CSR entries): ceil(deg / t) slices per
+// program, {pos * R + r, lo, min(lo + t, deg), 0} in (pos, r, lo) order.
+// Count: per 4096-position tile counts (ceil(n_wl / 4096) words), scanned in
+// place, and the total in *total; write: the slices at the scanned offsets.
+void launch_slice_count(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t R, uint32_t t,
+                        unsigned long long* tile_counts, unsigned long long* total, cudaStream_t s);
+void launch_slice_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t R, uint32_t t,
+                        const unsigned long long* tile_offsets, uint4* slices, cudaStream_t s);
+
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_mask, uint32_t* wl,
                      uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
 

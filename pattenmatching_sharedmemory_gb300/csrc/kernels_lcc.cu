@@ -1449,6 +1449,117 @@ __global__ void __launch_bounds__(256) k_wl_write(DevGraph g, DevState<W> st, ui
   }
 }
 
+// ---- first-hop slices of heavy walker items ---------------------------------
+//
+// An exact walk program's item (worklist position pos, program r) whose
+// source has more than t CSR entries also runs as ceil(deg / t) slices of
+// its first hop, {pos * R + r, lo, min(lo + t, deg), 0}, listed in (pos, r,
+// lo) order: per-tile counts, one scan, then each tile writes its slices.
+__device__ __forceinline__ uint64_t slices_of(const DevGraph& g, const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                              uint64_t pos, uint32_t R, uint32_t t) {
+  if (pos >= n_wl) return 0;
+  const uint32_t v = wl[pos];
+  const uint64_t deg = g.off[v + 1] - g.off[v];
+  return deg > t ? static_cast<uint64_t>(R) * ((deg + t - 1) / t) : 0;
+}
+
+__global__ void __launch_bounds__(256) k_slice_count(DevGraph g, const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                                     uint32_t R, uint32_t t, unsigned long long* tile_counts) {
+  __shared__ unsigned long long s_cnt[8];
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileV;
+  unsigned long long c = 0;
+  for (int i = 0; i < kTileV / 256; ++i) c += slices_of(g, wl, n_wl, base + i * 256 + threadIdx.x, R, t);
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+  if (lane_id() == 0) s_cnt[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long x = 0;
+    for (int i = 0; i < 8; ++i) x += s_cnt[i];
+    tile_counts[blockIdx.x] = x;
+  }
+}
+
+// Exclusive scan of the n tile counts in one block (in place); *total gets
+// the sum.
+__global__ void __launch_bounds__(1024) k_slice_scan(unsigned long long* counts, uint32_t n,
+                                                     unsigned long long* total) {
+  __shared__ unsigned long long s_warp[32];
+  const uint32_t per = (n + 1023) / 1024;
+  const uint32_t b = threadIdx.x * per;
+  unsigned long long local = 0;
+  for (uint32_t i = 0; i < per; ++i)
+    if (b + i < n) local += counts[b + i];
+  unsigned long long x = local;
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(kFull, x, o);
+    if (lane >= static_cast<unsigned>(o)) x += y;
+  }
+  if (lane == 31) s_warp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long w = s_warp[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(kFull, w, o);
+      if (lane >= static_cast<unsigned>(o)) w += y;
+    }
+    s_warp[lane] = w;
+  }
+  __syncthreads();
+  unsigned long long excl = x - local + (wid ? s_warp[wid - 1] : 0);
+  for (uint32_t i = 0; i < per; ++i)
+    if (b + i < n) {
+      const unsigned long long c = counts[b + i];
+      counts[b + i] = excl;
+      excl += c;
+    }
+  if (threadIdx.x == 1023) *total = excl;
+}
+
+__global__ void __launch_bounds__(256) k_slice_write(DevGraph g, const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                                     uint32_t R, uint32_t t,
+                                                     const unsigned long long* __restrict__ tile_offsets,
+                                                     uint4* __restrict__ slices) {
+  __shared__ unsigned long long s_warp[8];
+  __shared__ unsigned long long s_base;
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileV;
+  if (threadIdx.x == 0) s_base = tile_offsets[blockIdx.x];
+  __syncthreads();
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  for (int i = 0; i < kTileV / 256; ++i) {
+    const uint64_t pos = base + i * 256 + threadIdx.x;
+    const unsigned long long c = slices_of(g, wl, n_wl, pos, R, t);
+    unsigned long long x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(kFull, x, o);
+      if (lane >= static_cast<unsigned>(o)) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    unsigned long long before = 0;
+    for (unsigned w = 0; w < wid; ++w) before += s_warp[w];
+    if (c) {
+      const uint32_t v = wl[pos];
+      const uint64_t deg = g.off[v + 1] - g.off[v];
+      const uint64_t per_prog = (deg + t - 1) / t;
+      uint64_t out = s_base + before + x - c;
+      for (uint32_t r = 0; r < R; ++r)
+        for (uint64_t k = 0; k < per_prog; ++k, ++out) {
+          const uint64_t lo = k * t, hi = lo + t < deg ? lo + t : deg;
+          slices[out] = make_uint4(static_cast<uint32_t>(pos * R + r), static_cast<uint32_t>(lo),
+                                   static_cast<uint32_t>(hi), 0u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long tot = 0;
+      for (int w = 0; w < 8; ++w) tot += s_warp[w];
+      s_base += tot;
+    }
+    __syncthreads();
+  }
+}
+
 // ---- export ---------------------------------------------------------------
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st, uint64_t* cand, uint8_t* vact,
@@ -1657,6 +1768,27 @@ void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t mask, ui
   k_wl_scan<<<1, 1024, 0, s>>>(block_counts, blocks, count);
   PM_DISPATCH_WORD(q.word_kind,
                    k_wl_write<W><<<blocks, 256, 0, s>>>(g, state_of<W>(q), mask, block_counts, wl, wl_index));
+}
+
+void launch_slice_count(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t R, uint32_t t,
+                        unsigned long long* tile_counts, unsigned long long* total, cudaStream_t s) {
+  const uint32_t tiles = (n_wl + kTileV - 1) / kTileV;
+  if (tiles == 0) {
+    cudaMemsetAsync(total, 0, sizeof(unsigned long long), s);
+    return;
+  }
+  note_launch();
+  k_slice_count<<<tiles, 256, 0, s>>>(g, wl, n_wl, R, t, tile_counts);
+  note_launch();
+  k_slice_scan<<<1, 1024, 0, s>>>(tile_counts, tiles, total);
+}
+
+void launch_slice_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t R, uint32_t t,
+                        const unsigned long long* tile_offsets, uint4* slices, cudaStream_t s) {
+  const uint32_t tiles = (n_wl + kTileV - 1) / kTileV;
+  if (tiles == 0) return;
+  note_launch();
+  k_slice_write<<<tiles, 256, 0, s>>>(g, wl, n_wl, R, t, tile_offsets, slices);
 }
 
 void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,
