@@ -288,7 +288,7 @@ uint64_t QueryImpl::device_bytes() const {
   return d_vs.bytes + d_eact.bytes + d_lt.bytes + d_tile_sch.bytes + d_mod.bytes + d_sch.bytes + d_unm.bytes + d_ctr.bytes + d_tables.bytes +
          d_d2s.bytes + d_hub_acc.bytes + d_progs.bytes + d_start_roles.bytes + d_role_index.bytes + d_wl.bytes + d_wl_index.bytes +
          d_blocks.bytes + d_count.bytes + d_status.bytes + d_marker.bytes + d_marks.bytes + d_list.bytes + d_slices.bytes +
-         d_slice_tiles.bytes +
+         d_slice_tiles.bytes + d_item_scratch.bytes +
          pool.bytes() + big_pool.bytes();
 }
 
@@ -297,7 +297,8 @@ std::vector<DeviceBuffer*> QueryImpl::buffers() {
           &d_tile_sch,
           &d_tables,      &d_d2s,       &d_hub_acc,   &d_progs,     &d_start_roles, &d_role_index,  &d_wl,
           &d_wl_index,    &d_blocks,    &d_count,     &d_status,    &d_marker,     &d_marks,       &d_list,
-          &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &d_slice_tiles, &pool.edge, &pool.hyp,   &pool.state,
+          &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &d_slice_tiles, &d_item_scratch, &pool.edge,
+          &pool.hyp,      &pool.state,
           &pool.epochs,
           &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs};
 }
@@ -766,59 +767,35 @@ StepResult QueryImpl::step_enumeration() {
     const uint32_t presplit = enum_presplit(p.count_memo != 0);
     if (splittable && presplit) {
       // Sources with more first-hop entries than `presplit` start as slices
-      // of that many entries, queued first (the longest work).
-      std::vector<uint32_t> wl(n_wl);
-      PM_CUDA(cudaMemcpyAsync(wl.data(), d_wl.ptr, sizeof(uint32_t) * n_wl, cudaMemcpyDeviceToHost, stream));
-      PM_CUDA(cudaStreamSynchronize(stream));
-      const uint64_t t = presplit;
-      // In sources of more than s2 entries, a first-hop vertex whose list has
-      // more than twice s2 entries takes its own items, one per s2-entry
-      // slice of its list at the second hop (exact when the second step also
-      // binds a new vertex; not when the tail starts at step 2, whose pair
-      // step at step 1 would read whole lists).  The other positions go in
-      // runs of at most t.
+      // of that many entries, queued first (the longest work).  In sources
+      // of more than s2 entries, a first-hop vertex whose list has more than
+      // twice s2 entries takes its own items, one per s2-entry slice of its
+      // list at the second hop (exact when the second step also binds a new
+      // vertex; not when the tail starts at step 2, whose pair step at step
+      // 1 would read whole lists).  The items are listed on the device
+      // (launch_enum_item_count / _write); only their number comes back.
       const uint64_t s2 = enum_second_split();
       const bool second_ok = s2 && p.n_steps > 2 &&
                              (p.steps[2].kind == kStepVertex || p.steps[2].kind == kStepFinal) && p.tail_from != 3;
-      const std::vector<uint32_t>& adj = g->host.adj;
-      for (uint32_t i = 0; i < n_wl; ++i) {
-        const uint64_t deg = off[wl[i] + 1] - off[wl[i]];
-        if (deg <= t) continue;
-        if (!second_ok || deg <= s2) {
-          for (uint64_t lo = 0; lo < deg; lo += t)
-            items.push_back(
-                make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(std::min(lo + t, deg)), 0));
-          continue;
-        }
-        const uint64_t base = off[wl[i]];
-        uint64_t run = 0;
-        for (uint64_t pos = 0; pos < deg; ++pos) {
-          const uint32_t v1 = adj[base + pos];
-          const uint64_t d1 = off[v1 + 1] - off[v1];
-          const bool hub = d1 > 2 * s2;
-          if ((hub || pos - run == t) && pos > run) {
-            items.push_back(make_uint4(i, static_cast<uint32_t>(run), static_cast<uint32_t>(pos), 0));
-            run = pos;
-          }
-          if (hub) {
-            const uint64_t n_sl = (d1 + s2 - 1) / s2;
-            for (uint64_t k = 0; k < n_sl; ++k)
-              items.push_back(make_uint4(i, static_cast<uint32_t>(pos), static_cast<uint32_t>(pos + 1),
-                                         static_cast<uint32_t>(k + 1)));
-            run = pos + 1;
-          }
-        }
-        if (deg > run)
-          items.push_back(make_uint4(i, static_cast<uint32_t>(run), static_cast<uint32_t>(deg), 0));
-      }
-      for (uint32_t i = 0; i < n_wl; ++i)
-        if (off[wl[i] + 1] - off[wl[i]] <= t) items.push_back(make_uint4(i, 0, 0xFFFFFFFFu, 0));
-      d_list.ensure(sizeof(uint4) * items.size());
-      d_list2.ensure(sizeof(uint4) * items.size());
-      PM_CUDA(cudaMemcpyAsync(d_list.ptr, items.data(), sizeof(uint4) * items.size(), cudaMemcpyHostToDevice,
+      const uint32_t s2_used = second_ok ? static_cast<uint32_t>(s2) : 0u;
+      d_item_scratch.ensure(8 * enum_item_scratch_words(n_wl));
+      unsigned long long* scratch = d_item_scratch.as<unsigned long long>();
+      launch_enum_item_count(g->dev(), d_wl.as<uint32_t>(), n_wl, presplit, s2_used, scratch, stream);
+      PM_CUDA(cudaGetLastError());
+      unsigned long long totals[3] = {0, 0, 0};
+      PM_CUDA(cudaMemcpyAsync(totals, enum_item_totals(scratch, n_wl), sizeof(totals), cudaMemcpyDeviceToHost,
                               stream));
+      PM_CUDA(cudaStreamSynchronize(stream));
+      const uint64_t n_items = totals[0] + totals[1];
+      if (totals[2] || n_items >= 0xFFFFFFFFull)
+        throw PmError{PM_E_DEVICE, "too many enumeration items for 32-bit item ids"};
+      d_list.ensure(sizeof(uint4) * std::max<uint64_t>(n_items, 1));
+      d_list2.ensure(sizeof(uint4) * std::max<uint64_t>(n_items, 1));
+      launch_enum_item_write(g->dev(), d_wl.as<uint32_t>(), n_wl, presplit, s2_used, scratch, d_list.as<uint4>(),
+                             stream);
+      PM_CUDA(cudaGetLastError());
       launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, d_list.as<uint4>(),
-                       static_cast<uint32_t>(items.size()), d_list2.as<uint4>(), pool.sc, stream);
+                       static_cast<uint32_t>(n_items), d_list2.as<uint4>(), pool.sc, stream);
     } else {
       d_list2.ensure(sizeof(uint4) * n_wl);
       launch_enumerate(g->dev(), ptrs(), prog, p.n_steps + 1u, d_wl.as<uint32_t>(), n_wl, nullptr, 0, d_list2.as<uint4>(), pool.sc,

@@ -117,6 +117,7 @@ struct QueryImpl {
   DeviceBuffer d_wl, d_wl_index, d_blocks, d_count, d_status, d_marker, d_marks, d_list, d_list2, d_apply_v,
       d_apply_r, d_slices;
   DeviceBuffer d_slice_tiles;  // per-tile slice counts / offsets and the total (launch_slice_count)
+  DeviceBuffer d_item_scratch;  // ENUMERATION item listing (launch_enum_item_count)
   StepCounters* h_ctr = nullptr;  // pinned
   uint32_t* h_count = nullptr;    // pinned
   bool own_host = true;           // h_ctr / h_count allocated here

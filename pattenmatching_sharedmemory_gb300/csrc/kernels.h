@@ -93,6 +93,22 @@ void launch_slice_count(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, ui
 void launch_slice_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t R, uint32_t t,
                         const unsigned long long* tile_offsets, uint4* slices, cudaStream_t s);
 
+// ENUMERATION's up-front items over the worklist's sources: a source with
+// more than t first-hop entries (heavy) takes items {i, lo, hi, 0} over runs
+// of at most t entries of its list; with s2 > 0 and more than s2 entries, a
+// first-hop position whose vertex has more than 2 * s2 entries closes the
+// run before it and takes ceil(d1 / s2) items {i, pos, pos + 1, k + 1}.
+// Heavy items first (worklist, then list order), then {i, 0, 2^32 - 1, 0}
+// per light source.  Count: enum_item_scratch_words(n_wl) u64 words of
+// scratch; afterwards enum_item_totals(scratch, n_wl) holds on the device
+// {heavy items, light items, overflow flag}.  Write: the items, at `items`.
+uint64_t enum_item_scratch_words(uint32_t n_wl);
+void launch_enum_item_count(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t t, uint32_t s2,
+                            unsigned long long* scratch, cudaStream_t s);
+const unsigned long long* enum_item_totals(const unsigned long long* scratch, uint32_t n_wl);
+void launch_enum_item_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t t, uint32_t s2,
+                            const unsigned long long* scratch, uint4* items, cudaStream_t s);
+
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_mask, uint32_t* wl,
                      uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
 

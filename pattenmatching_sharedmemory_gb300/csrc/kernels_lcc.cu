@@ -1560,6 +1560,149 @@ __global__ void __launch_bounds__(256) k_slice_write(DevGraph g, const uint32_t*
   }
 }
 
+// ---- ENUMERATION items --------------------------------------------------------
+//
+// Source i of the worklist with more than t first-hop entries (heavy) takes
+// items {i, lo, hi, 0} over runs of its list; with the second-hop split on
+// (s2 > 0) and more than s2 entries, a first-hop position whose vertex has
+// more than 2 * s2 entries ends the run before it and takes ceil(d1 / s2)
+// items {i, pos, pos + 1, k + 1} of its own, and the runs between such
+// positions are cut every t entries.  Heavy items come first, in worklist
+// and list order; then one item {i, 0, 2^32 - 1, 0} per light source.  A
+// warp per source: lane j tests position base + j, hubs are taken in order
+// from the ballot.
+
+struct EnumItemRule {
+  uint32_t t, s2;  // run length, second-hop slice length (0: off)
+};
+
+__device__ __forceinline__ uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+// Count (out == nullptr) or write the heavy items of source i (degree deg,
+// list at off[v]); returns the count.  Warp-uniform arguments.
+__device__ uint64_t enum_heavy_items(const DevGraph& g, uint32_t i, uint32_t v, uint64_t deg, EnumItemRule r,
+                                     uint4* out) {
+  const unsigned lane = lane_id();
+  if (r.s2 == 0 || deg <= r.s2) {
+    const uint64_t n = ceil_div(deg, r.t);
+    if (out)
+      for (uint64_t k = lane; k < n; k += 32) {
+        const uint64_t lo = k * r.t, hi = lo + r.t < deg ? lo + r.t : deg;
+        out[k] = make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(hi), 0u);
+      }
+    return n;
+  }
+  const uint64_t base = g.off[v];
+  uint64_t n = 0, a = 0;  // items so far, start of the current run
+  auto runs = [&](uint64_t b) {  // runs of [a, b)
+    if (b <= a) return;
+    const uint64_t m = ceil_div(b - a, r.t);
+    if (out)
+      for (uint64_t k = lane; k < m; k += 32) {
+        const uint64_t lo = a + k * r.t, hi = lo + r.t < b ? lo + r.t : b;
+        out[n + k] = make_uint4(i, static_cast<uint32_t>(lo), static_cast<uint32_t>(hi), 0u);
+      }
+    n += m;
+  };
+  for (uint64_t p0 = 0; p0 < deg; p0 += 32) {
+    const uint64_t pos = p0 + lane;
+    uint64_t d1 = 0;
+    if (pos < deg) {
+      const uint32_t w = g.adj[base + pos];
+      d1 = g.off[w + 1] - g.off[w];
+    }
+    const bool hub = pos < deg && d1 > 2ull * r.s2;
+    for (unsigned hm = __ballot_sync(kFull, hub); hm; hm &= hm - 1) {
+      const unsigned j = __ffs(hm) - 1;
+      const uint64_t hp = p0 + j;
+      const uint64_t hd = shfl64(d1, j);
+      runs(hp);
+      const uint64_t m = ceil_div(hd, r.s2);
+      if (out)
+        for (uint64_t k = lane; k < m; k += 32)
+          out[n + k] = make_uint4(i, static_cast<uint32_t>(hp), static_cast<uint32_t>(hp + 1),
+                                  static_cast<uint32_t>(k + 1));
+      n += m;
+      a = hp + 1;
+    }
+  }
+  runs(deg);
+  return n;
+}
+
+// Per source: heavy item count and light flag.
+__global__ void __launch_bounds__(256) k_enum_item_count(DevGraph g, const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                                         EnumItemRule r, uint32_t* __restrict__ heavy,
+                                                         uint32_t* __restrict__ light, uint32_t* overflow) {
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t i = grid_warp(); i < n_wl; i += n_warps) {
+    const uint32_t v = wl[i];
+    const uint64_t deg = g.off[v + 1] - g.off[v];
+    uint64_t h = 0;
+    if (deg > r.t) h = enum_heavy_items(g, static_cast<uint32_t>(i), v, deg, r, nullptr);
+    if (lane_id() == 0) {
+      if (h > 0xFFFFFFFFull) atomicOr(overflow, 1u);
+      heavy[i] = static_cast<uint32_t>(h);
+      light[i] = deg > r.t ? 0u : 1u;
+    }
+  }
+}
+
+// Exclusive scan of a u32 array in tiles of 4096: per element its offset
+// within the tile, per tile its sum (scanned afterwards by k_slice_scan).
+__global__ void __launch_bounds__(256) k_scan_tiles(const uint32_t* __restrict__ in, uint32_t n,
+                                                    unsigned long long* __restrict__ local,
+                                                    unsigned long long* __restrict__ tile_sums) {
+  __shared__ unsigned long long s_warp[8];
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileV + threadIdx.x * 16ull;
+  unsigned long long mine = 0;
+  uint32_t v[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    v[k] = base + k < n ? in[base + k] : 0u;
+    mine += v[k];
+  }
+  unsigned long long x = mine;
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(kFull, x, o);
+    if (lane >= static_cast<unsigned>(o)) x += y;
+  }
+  if (lane == 31) s_warp[wid] = x;
+  __syncthreads();
+  unsigned long long before = 0;
+  for (unsigned w = 0; w < wid; ++w) before += s_warp[w];
+  unsigned long long run = before + x - mine;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    if (base + k < n) local[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 255) tile_sums[blockIdx.x] = before + x;
+}
+
+__global__ void __launch_bounds__(256) k_enum_item_write(DevGraph g, const uint32_t* __restrict__ wl, uint32_t n_wl,
+                                                         EnumItemRule r, const uint32_t* __restrict__ light,
+                                                         const unsigned long long* __restrict__ heavy_local,
+                                                         const unsigned long long* __restrict__ heavy_tiles,
+                                                         const unsigned long long* __restrict__ light_local,
+                                                         const unsigned long long* __restrict__ light_tiles,
+                                                         const unsigned long long* __restrict__ heavy_total,
+                                                         uint4* __restrict__ items) {
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t i = grid_warp(); i < n_wl; i += n_warps) {
+    const uint32_t v = wl[i];
+    const uint64_t deg = g.off[v + 1] - g.off[v];
+    if (light[i]) {
+      if (lane_id() == 0)
+        items[*heavy_total + light_tiles[i / kTileV] + light_local[i]] =
+            make_uint4(static_cast<uint32_t>(i), 0u, 0xFFFFFFFFu, 0u);
+    } else {
+      enum_heavy_items(g, static_cast<uint32_t>(i), v, deg, r, items + heavy_tiles[i / kTileV] + heavy_local[i]);
+    }
+  }
+}
+
 // ---- export ---------------------------------------------------------------
 template <class W>
 __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st, uint64_t* cand, uint8_t* vact,
@@ -1789,6 +1932,64 @@ void launch_slice_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, ui
   if (tiles == 0) return;
   note_launch();
   k_slice_write<<<tiles, 256, 0, s>>>(g, wl, n_wl, R, t, tile_offsets, slices);
+}
+
+namespace {
+// Scratch layout of the ENUMERATION item listing (u64 words).
+struct EnumItemScratch {
+  uint32_t* heavy;
+  uint32_t* light;
+  unsigned long long *heavy_local, *light_local, *heavy_tiles, *light_tiles, *totals;
+  uint64_t tiles;
+  EnumItemScratch(unsigned long long* scratch, uint32_t n_wl) {
+    tiles = (static_cast<uint64_t>(n_wl) + kTileV - 1) / kTileV;
+    heavy = reinterpret_cast<uint32_t*>(scratch);
+    light = heavy + n_wl;
+    heavy_local = scratch + n_wl;
+    light_local = heavy_local + n_wl;
+    heavy_tiles = light_local + n_wl;
+    light_tiles = heavy_tiles + tiles;
+    totals = light_tiles + tiles;
+  }
+};
+}  // namespace
+
+uint64_t enum_item_scratch_words(uint32_t n_wl) {
+  const uint64_t tiles = (static_cast<uint64_t>(n_wl) + kTileV - 1) / kTileV;
+  return 3ull * n_wl + 2 * tiles + 3;
+}
+
+void launch_enum_item_count(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t t, uint32_t s2,
+                            unsigned long long* scratch, cudaStream_t s) {
+  const EnumItemScratch x(scratch, n_wl);
+  const EnumItemRule r{t, s2};
+  cudaMemsetAsync(x.totals, 0, 3 * sizeof(unsigned long long), s);
+  if (n_wl == 0) return;
+  note_launch();
+  k_enum_item_count<<<device_sm_count() * 8, 256, 0, s>>>(g, wl, n_wl, r, x.heavy, x.light,
+                                                            reinterpret_cast<uint32_t*>(x.totals + 2));
+  note_launch();
+  k_scan_tiles<<<static_cast<unsigned>(x.tiles), 256, 0, s>>>(x.heavy, n_wl, x.heavy_local, x.heavy_tiles);
+  note_launch();
+  k_scan_tiles<<<static_cast<unsigned>(x.tiles), 256, 0, s>>>(x.light, n_wl, x.light_local, x.light_tiles);
+  note_launch();
+  k_slice_scan<<<1, 1024, 0, s>>>(x.heavy_tiles, static_cast<uint32_t>(x.tiles), x.totals);
+  note_launch();
+  k_slice_scan<<<1, 1024, 0, s>>>(x.light_tiles, static_cast<uint32_t>(x.tiles), x.totals + 1);
+}
+
+const unsigned long long* enum_item_totals(const unsigned long long* scratch, uint32_t n_wl) {
+  return EnumItemScratch(const_cast<unsigned long long*>(scratch), n_wl).totals;
+}
+
+void launch_enum_item_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t t, uint32_t s2,
+                            const unsigned long long* scratch, uint4* items, cudaStream_t s) {
+  if (n_wl == 0) return;
+  const EnumItemScratch x(const_cast<unsigned long long*>(scratch), n_wl);
+  note_launch();
+  k_enum_item_write<<<device_sm_count() * 8, 256, 0, s>>>(g, wl, n_wl, EnumItemRule{t, s2}, x.light, x.heavy_local,
+                                                            x.heavy_tiles, x.light_local, x.light_tiles, x.totals,
+                                                            items);
 }
 
 void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uint8_t* vact, uint8_t* eact_bytes,
