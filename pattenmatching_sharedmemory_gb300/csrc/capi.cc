@@ -2,6 +2,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <exception>
+#include <thread>
 
 #include "../../include/pm_gb300_tools.h"
 #include "engine.h"
@@ -91,20 +93,43 @@ pm_status_t pm_graph_from_csr(const uint64_t* offsets, const uint32_t* adj, cons
                               uint32_t vertex_count, uint64_t edge_count, int device, pm_graph** out) {
   PM_REQUIRE(out && offsets && (adj || edge_count == 0), "null CSR buffer");
   PM_REQUIRE(offsets[vertex_count] == edge_count, "offsets[vertex_count] != edge_count");
-  for (uint32_t v = 0; v < vertex_count; ++v) PM_REQUIRE(offsets[v] <= offsets[v + 1], "offsets not monotone");
-  for (uint64_t e = 0; e < edge_count; ++e) PM_REQUIRE(adj[e] < vertex_count, "edge target out of range");
+  // One parallel pass checks the offsets, the targets and the list order.
+  const CsrScan scan = scan_csr(offsets, adj, vertex_count);
+  PM_REQUIRE(scan.monotone, "offsets not monotone");
+  PM_REQUIRE(scan.in_range, "edge target out of range");
   return guarded([&]() -> pm_status_t {
     auto* g = new pm_graph();
     try {
       HostGraph& h = g->impl.host;
       h.vertex_count = vertex_count;
       h.edge_count = edge_count;
-      h.offsets.assign(offsets, offsets + vertex_count + 1);
-      h.adj.assign(adj, adj + edge_count);
+      auto fill = [](auto& dst, const auto* src, uint64_t n) {
+        dst.resize(n);  // unwritten: the parallel copy touches each page first
+        auto* d = dst.data();
+        parallel_ranges(n, [&](uint64_t lo, uint64_t hi) { std::memcpy(d + lo, src + lo, sizeof(*d) * (hi - lo)); });
+      };
+      fill(h.offsets, offsets, uint64_t(vertex_count) + 1);
       h.valued = labels != nullptr;
-      if (labels) h.labels.assign(labels, labels + vertex_count);
-      g->impl.finalize_host();
-      if (device >= 0) g->impl.to_device(device);
+      if (labels) fill(h.labels, labels, vertex_count);
+      g->impl.finalize_host(&scan.sorted_unique);
+      // The host copy of the adjacency is filled while the device copy is
+      // made from the caller's buffer.
+      std::exception_ptr copy_err;
+      std::thread copier([&] {
+        try {
+          fill(h.adj, adj, edge_count);
+        } catch (...) {
+          copy_err = std::current_exception();
+        }
+      });
+      try {
+        if (device >= 0) g->impl.to_device(device, adj);
+      } catch (...) {
+        copier.join();
+        throw;
+      }
+      copier.join();
+      if (copy_err) std::rethrow_exception(copy_err);
     } catch (...) {
       delete g;
       throw;

@@ -9,6 +9,9 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <exception>
+#include <mutex>
+#include <thread>
 
 #include "totem_io.h"
 
@@ -56,27 +59,107 @@ void DeviceBuffer::ensure(size_t n) {
 }
 
 // ---- graph ------------------------------------------------------------------
-void GraphImpl::finalize_host() {
-  const uint32_t V = host.vertex_count;
-  if (host.labels.size() != V) host.labels.assign(V, 0);
-  dense_values = host.labels;
-  std::sort(dense_values.begin(), dense_values.end());
-  dense_values.erase(std::unique(dense_values.begin(), dense_values.end()), dense_values.end());
-  dense_ids.resize(V);
-  for (uint32_t v = 0; v < V; ++v)
-    dense_ids[v] = static_cast<uint32_t>(std::lower_bound(dense_values.begin(), dense_values.end(), host.labels[v]) -
-                                         dense_values.begin());
-  sorted_unique = true;
-  for (uint32_t v = 0; v < V && sorted_unique; ++v)
-    for (uint64_t e = host.offsets[v] + 1; e < host.offsets[v + 1]; ++e)
-      if (host.adj[e - 1] >= host.adj[e]) {
-        sorted_unique = false;
-        break;
+void parallel_ranges(uint64_t n, const std::function<void(uint64_t, uint64_t)>& f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const uint64_t T = std::min<uint64_t>(std::max(1u, hw), 32);
+  if (T == 1 || n < (uint64_t(1) << 16)) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> ts;
+  std::exception_ptr err;
+  std::mutex mu;
+  for (uint64_t t = 0; t < T; ++t) {
+    const uint64_t lo = n * t / T, hi = n * (t + 1) / T;
+    ts.emplace_back([&, lo, hi] {
+      try {
+        f(lo, hi);
+      } catch (...) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!err) err = std::current_exception();
       }
+    });
+  }
+  for (auto& t : ts) t.join();
+  if (err) std::rethrow_exception(err);
 }
 
-void GraphImpl::to_device(int dev) {
+CsrScan scan_csr(const uint64_t* offsets, const uint32_t* adj, uint32_t vertex_count) {
+  std::atomic<bool> mono{true}, range{true}, sorted{true};
+  parallel_ranges(vertex_count, [&](uint64_t lo, uint64_t hi) {
+    bool m = true, r = true, so = true;
+    for (uint64_t v = lo; v < hi; ++v) {
+      const uint64_t b = offsets[v], e = offsets[v + 1];
+      if (b > e) {
+        m = false;
+        continue;
+      }
+      for (uint64_t x = b; x < e; ++x) {
+        if (adj[x] >= vertex_count) r = false;
+        if (x > b && adj[x - 1] >= adj[x]) so = false;
+      }
+    }
+    if (!m) mono = false;
+    if (!r) range = false;
+    if (!so) sorted = false;
+  });
+  CsrScan c;
+  c.monotone = mono;
+  c.in_range = range;
+  c.sorted_unique = sorted;
+  return c;
+}
+
+void GraphImpl::finalize_host(const bool* sorted) {
+  const uint32_t V = host.vertex_count;
+  if (host.labels.size() != V) host.labels.assign(V, 0);
+  // Dense ids: the rank of each label among the distinct values.  Labels
+  // below 2^22 (the common case) go through a presence table, larger ones
+  // through a sorted copy.
+  label_t top = 0;
+  for (uint32_t v = 0; v < V; ++v) top = std::max(top, host.labels[v]);
+  dense_ids.resize(V);
+  if (top < (label_t(1) << 22)) {
+    std::vector<uint32_t> id(static_cast<size_t>(top) + 1, 0);
+    for (uint32_t v = 0; v < V; ++v) id[host.labels[v]] = 1;
+    dense_values.clear();
+    for (size_t x = 0; x < id.size(); ++x)
+      if (id[x]) {
+        id[x] = static_cast<uint32_t>(dense_values.size());
+        dense_values.push_back(static_cast<label_t>(x));
+      }
+    parallel_ranges(V, [&](uint64_t lo, uint64_t hi) {
+      for (uint64_t v = lo; v < hi; ++v) dense_ids[v] = id[host.labels[v]];
+    });
+  } else {
+    dense_values.assign(host.labels.begin(), host.labels.end());
+    std::sort(dense_values.begin(), dense_values.end());
+    dense_values.erase(std::unique(dense_values.begin(), dense_values.end()), dense_values.end());
+    parallel_ranges(V, [&](uint64_t lo, uint64_t hi) {
+      for (uint64_t v = lo; v < hi; ++v)
+        dense_ids[v] = static_cast<uint32_t>(
+            std::lower_bound(dense_values.begin(), dense_values.end(), host.labels[v]) - dense_values.begin());
+    });
+  }
+  if (sorted) {
+    sorted_unique = *sorted;
+  } else {
+    std::atomic<bool> ok{true};
+    parallel_ranges(V, [&](uint64_t lo, uint64_t hi) {
+      for (uint64_t v = lo; v < hi && ok.load(std::memory_order_relaxed); ++v)
+        for (uint64_t e = host.offsets[v] + 1; e < host.offsets[v + 1]; ++e)
+          if (host.adj[e - 1] >= host.adj[e]) {
+            ok = false;
+            break;
+          }
+    });
+    sorted_unique = ok;
+  }
+}
+
+void GraphImpl::to_device(int dev, const uint32_t* adj_src) {
   if (device == dev && d_off.ptr) return;
+  if (!adj_src) adj_src = host.adj.data();
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
     throw PmError{PM_E_NO_DEVICE, "no CUDA device available for the GB300 pruning kernels"};
@@ -94,7 +177,7 @@ void GraphImpl::to_device(int dev) {
   d_lab.ensure(sizeof(uint32_t) * std::max<uint32_t>(V, 1));
   PM_CUDA(cudaMemcpy(d_off.ptr, host.offsets.data(), sizeof(uint64_t) * (V + 1), cudaMemcpyHostToDevice));
   if (host.edge_count)
-    PM_CUDA(cudaMemcpy(d_adj.ptr, host.adj.data(), sizeof(uint32_t) * host.edge_count, cudaMemcpyHostToDevice));
+    PM_CUDA(cudaMemcpy(d_adj.ptr, adj_src, sizeof(uint32_t) * host.edge_count, cudaMemcpyHostToDevice));
   if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
   device = dev;
   if (host.edge_count && dense_values.size() <= 256) {
@@ -106,15 +189,15 @@ void GraphImpl::to_device(int dev) {
   build_hub_plan(hub_degree, seg_entries);
   symmetric = false;
   if (sorted_unique && V) {
-    uint32_t* d_flag = nullptr;
-    uint32_t asym = 0;
-    PM_CUDA(cudaMalloc(&d_flag, sizeof(uint32_t)));
-    PM_CUDA(cudaMemset(d_flag, 0, sizeof(uint32_t)));
-    launch_check_symmetric(this->dev(), d_flag, nullptr);
-    const cudaError_t e = cudaMemcpy(&asym, d_flag, sizeof(uint32_t), cudaMemcpyDeviceToHost);
-    cudaFree(d_flag);
+    unsigned long long* d_res = nullptr;
+    unsigned long long res[3] = {0, 0, 0};
+    PM_CUDA(cudaMalloc(&d_res, sizeof(res)));
+    PM_CUDA(cudaMemset(d_res, 0, sizeof(res)));
+    launch_check_symmetric(this->dev(), d_res, nullptr);
+    const cudaError_t e = cudaMemcpy(res, d_res, sizeof(res), cudaMemcpyDeviceToHost);
+    cudaFree(d_res);
     PM_CUDA(e);
-    symmetric = asym == 0;
+    symmetric = res[0] == 0 && res[1] == res[2];
   }
   plan_epoch = next_plan_epoch();
 }
@@ -227,9 +310,12 @@ PatternGraph load_pattern(const std::string& dir, bool load_labels) {
   if (load_labels && is_regular_file(dir + "pattern_vertex_data")) read_vertex_labels(dir + "pattern_vertex_data", pg);
   PatternGraph p;
   p.n = pg.vertex_count;
-  p.offsets = pg.offsets;
-  p.adj = pg.adj;
-  p.labels = pg.labels.empty() ? std::vector<uint64_t>(p.n, 0) : pg.labels;
+  p.offsets.assign(pg.offsets.begin(), pg.offsets.end());
+  p.adj.assign(pg.adj.begin(), pg.adj.end());
+  if (pg.labels.empty())
+    p.labels.assign(p.n, 0);
+  else
+    p.labels.assign(pg.labels.begin(), pg.labels.end());
   return p;
 }
 
@@ -761,7 +847,7 @@ StepResult QueryImpl::step_enumeration() {
     // Slicing the first hop is exact when that step binds a new vertex.
     const bool splittable =
         p.n_steps > 1 && (p.steps[1].kind == kStepVertex || p.steps[1].kind == kStepFinal);
-    const std::vector<uint64_t>& off = g->host.offsets;
+    const auto& off = g->host.offsets;
     std::vector<uint4> over, items;
     zero_field(d_ctr.ptr, offsetof(StepCounters, aux), stream);
     const uint32_t presplit = enum_presplit(p.count_memo != 0);

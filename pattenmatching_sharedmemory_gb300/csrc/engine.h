@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include <functional>
+
 #include "constraints.h"
 #include "kernels.h"
 #include "walk_compile.h"
@@ -65,8 +67,13 @@ struct GraphImpl {
   static constexpr uint32_t kDefaultHubDegree = 32;
   static constexpr uint32_t kDefaultSegEntries = 1024;
 
-  void finalize_host();  // dense labels, adjacency checks
-  void to_device(int device);
+  // Dense labels; sorted_unique from a scan of the lists, or from *sorted
+  // when the caller already checked them.
+  void finalize_host(const bool* sorted = nullptr);
+  // Device copy; adj_src (default: host.adj) is where the adjacency is read
+  // from, e.g. the caller's own, possibly pinned, buffer while host.adj is
+  // still being filled.
+  void to_device(int device, const uint32_t* adj_src = nullptr);
   // Hubs = vertices of more than hub_degree CSR entries, in segments of
   // seg_entries entries (device tables rebuilt; graph must be on a device).
   void build_hub_plan(uint32_t hub_degree, uint32_t seg_entries);
@@ -75,6 +82,17 @@ struct GraphImpl {
     return d_off.bytes + d_adj.bytes + d_lab.bytes + d_nlab.bytes + d_seg.bytes;
   }
 };
+
+// Runs f(lo, hi) over [0, n) in contiguous chunks on up to the host's
+// hardware threads (one chunk when n is small).
+void parallel_ranges(uint64_t n, const std::function<void(uint64_t, uint64_t)>& f);
+
+// One pass over a caller's CSR: offsets non-decreasing, every target below
+// vertex_count, every list strictly increasing.
+struct CsrScan {
+  bool monotone = true, in_range = true, sorted_unique = true;
+};
+CsrScan scan_csr(const uint64_t* offsets, const uint32_t* adj, uint32_t vertex_count);
 
 // Walker scratch pool (memo tables), sized on demand.
 struct WalkPool {

@@ -43,9 +43,10 @@ uint64_t launch_count();
 void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* dense_to_slot, uint64_t full_cand,
                        cudaStream_t s);
 
-// Sets *asymmetric to 1 when some CSR entry u -> w has no reverse entry
-// w -> u (adjacency lists must be strictly increasing).
-void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_t s);
+// Symmetry check of a graph whose adjacency lists are strictly increasing:
+// res[3] zeroed before; afterwards the graph is symmetric (every entry
+// u -> w has its reverse w -> u) iff res[0] == 0 and res[1] == res[2].
+void launch_check_symmetric(const DevGraph& g, unsigned long long* res, cudaStream_t s);
 
 // nlab[e] = lab[adj[e]] (dense label ids below 256) for every CSR entry;
 // adj must be 16-byte aligned.

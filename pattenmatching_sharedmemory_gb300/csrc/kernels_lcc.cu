@@ -59,35 +59,81 @@ __global__ void __launch_bounds__(kThreads) k_init_state(DevGraph g, DevState<W>
 }
 
 // ---- graph properties -------------------------------------------------------
-// Warp per vertex: every entry u -> w looks for u in w's sorted list.
-__global__ void __launch_bounds__(kThreads) k_check_symmetric(DevGraph g, uint32_t* asymmetric) {
+// Index of `target` in the strictly increasing list adj[lo, hi), or ~0:
+// interpolation steps (the ids of a list spread evenly in most graphs, so a
+// guess from the end values lands close) alternating with halvings (which
+// bound the steps by twice the binary search's), then a scan of the last
+// 16 entries.
+__device__ __forceinline__ uint64_t find_sorted(const uint32_t* __restrict__ adj, uint64_t lo, uint64_t hi,
+                                                uint32_t target) {
+  bool interp = true;
+  while (hi - lo > 16) {
+    const uint32_t a = adj[lo], b = adj[hi - 1];
+    if (target < a || target > b) return ~uint64_t(0);
+    uint64_t mid;
+    if (interp && b > a)
+      mid = lo + static_cast<uint64_t>(target - a) * (hi - 1 - lo) / (b - a);
+    else
+      mid = lo + ((hi - lo) >> 1);
+    interp = !interp;
+    const uint32_t x = adj[mid];
+    if (x == target) return mid;
+    if (x < target)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  for (; lo < hi; ++lo) {
+    const uint32_t x = adj[lo];
+    if (x == target) return lo;
+    if (x > target) break;
+  }
+  return ~uint64_t(0);
+}
+
+// Symmetry of a graph with strictly increasing lists: every entry u -> w
+// with u < w finds u in w's list, and the entries with u < w and u > w are
+// equally many (the reverses of the former are distinct entries of the
+// latter, so equal counts leave none without a reverse; self-loops are
+// their own).  res[0] = 1 when an entry has no reverse; res[1], res[2]
+// count the entries with u < w and u > w.  Warp per vertex, lane per entry.
+__global__ void __launch_bounds__(kThreads) k_check_symmetric(DevGraph g, unsigned long long* res) {
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long up = 0, down = 0;
   for (uint64_t u = warp; u < g.V; u += n_warps) {
-    if (*reinterpret_cast<volatile uint32_t*>(asymmetric)) return;
+    // Another warp found an entry without reverse: stop (warp-uniform read).
+    const unsigned found = lane == 0 ? (*reinterpret_cast<volatile unsigned long long*>(res) != 0) : 0u;
+    if (__shfl_sync(kFull, found, 0)) break;
     const uint64_t b = g.off[u], e = g.off[u + 1];
-    for (uint64_t x0 = b; x0 < e; x0 += 32) {
+    bool missing = false;
+    for (uint64_t x0 = b; x0 < e && !missing; x0 += 32) {
       const uint64_t x = x0 + lane;
-      bool missing = false;
+      bool miss = false;
       if (x < e) {
         const uint32_t w = g.adj[x];
-        uint64_t lo = g.off[w], hi = g.off[w + 1];
-        const uint64_t end = hi;
-        while (lo < hi) {
-          const uint64_t mid = lo + ((hi - lo) >> 1);
-          if (g.adj[mid] < u)
-            lo = mid + 1;
-          else
-            hi = mid;
+        if (u < w) {
+          ++up;
+          miss = find_sorted(g.adj, g.off[w], g.off[w + 1], static_cast<uint32_t>(u)) == ~uint64_t(0);
+        } else if (u > w) {
+          ++down;
         }
-        missing = !(lo < end && g.adj[lo] == u);
       }
-      if (__any_sync(kFull, missing)) {
-        if (lane == 0) atomicOr(asymmetric, 1u);
-        return;
-      }
+      missing = __any_sync(kFull, miss);
     }
+    if (missing) {
+      if (lane == 0) atomicOr(res, 1ull);
+      break;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    up += __shfl_xor_sync(kFull, up, o);
+    down += __shfl_xor_sync(kFull, down, o);
+  }
+  if (lane == 0) {
+    if (up) atomicAdd(res + 1, up);
+    if (down) atomicAdd(res + 2, down);
   }
 }
 
@@ -1772,9 +1818,9 @@ void launch_init_state(const DevGraph& g, const QueryDevPtrs& q, const uint8_t* 
   PM_DISPATCH_WORD(q.word_kind, k_init_state<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), d2s, full));
 }
 
-void launch_check_symmetric(const DevGraph& g, uint32_t* asymmetric, cudaStream_t s) {
+void launch_check_symmetric(const DevGraph& g, unsigned long long* res, cudaStream_t s) {
   note_launch();
-  k_check_symmetric<<<device_sm_count() * 8, kThreads, 0, s>>>(g, asymmetric);
+  k_check_symmetric<<<device_sm_count() * 8, kThreads, 0, s>>>(g, res);
 }
 
 void launch_build_entry_labels(const DevGraph& g, uint8_t* nlab, cudaStream_t s) {
