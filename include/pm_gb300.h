@@ -46,6 +46,9 @@ typedef int32_t pm_status_t;
 #define PM_E_CANCELLED (-10)        /* request cancelled before it finished   */
 #define PM_E_OOM (-11)              /* host or device allocation failed       */
 #define PM_E_BUSY (-12)             /* server queue full, retry later         */
+#define PM_E_STATISTICS (-13)       /* dynamic order: a graph statistic its
+                                       estimate reads is absent (the reference
+                                       throws std::out_of_range and aborts)  */
 
 /* Last error message of the calling host thread (never NULL). */
 const char* pm_last_error(void);
@@ -148,8 +151,40 @@ pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets,
 #define PM_NLCC_REFERENCE 0
 #define PM_NLCC_STRICT 1
 #define PM_NLCC_BACKTRACK 2
+/* Flags or-ed into `variant` (with PM_NLCC_STRICT or PM_NLCC_BACKTRACK): the
+ * article's constraint-order drivers (test_article/CMakeLists.txt:53-73,
+ * test_order_multiple_label_cpu.cc).  Their NLCC steps run each constraint
+ * once and drop it.
+ *   PM_ORDER_ENUMERATE      USE_ENUMERATE: the schedule ends in ENUMERATION
+ *                           (then END) instead of END.
+ *   PM_ORDER_EFFECTIVENESS  ORDER_USE_DYNAMIC: after every LCC fixpoint the
+ *                           graph statistics of the pruned graph are taken
+ *                           on the GPU (GraphStatCpu::compute,
+ *                           algorithms/graph_stat_cpu.tpp:42-80) and the
+ *                           remaining constraint with the largest estimated
+ *                           effectiveness (multiple_label_constraint_
+ *                           effectiveness.cc) runs next; the run starts with
+ *                           an empty row (step PM_STEP_START, written with
+ *                           an empty step name) and no LCC0, as the
+ *                           reference's driver does.  A statistic the
+ *                           estimate needs but the graph lacks ends the run
+ *                           with PM_E_STATISTICS.
+ *   PM_ORDER_EARLY_ENUMERATION  ENUMERATE_START_EARLY (threshold 0.01):
+ *                           ENUMERATION starts as soon as its estimated cost
+ *                           is at most the next constraint's, or the next
+ *                           constraint's effectiveness is at most 0.01. */
+#define PM_ORDER_ENUMERATE 0x100
+#define PM_ORDER_EFFECTIVENESS 0x200
+#define PM_ORDER_EARLY_ENUMERATION 0x400
 pm_status_t pm_query_create_variant(pm_graph* g, const char* pattern_dir, int load_pattern_labels,
                                     int32_t variant, pm_query** out);
+/* The order drivers' OpenMP thread count (process-wide, read when a query is
+ * created; default 1, the reference hard-codes 60 at
+ * test_order_multiple_label_cpu.cc:15): the graph statistics split the
+ * vertices into that many static-schedule blocks, each with its own
+ * never-reset neighbour-label accumulation (graph_stat_cpu.tpp:46-70), and
+ * the cost estimates divide by it. */
+pm_status_t pm_set_order_threads(int32_t threads);
 pm_status_t pm_query_create_variant_from_csr(pm_graph* g, const uint64_t* p_offsets, const uint32_t* p_adj,
                                              const uint64_t* p_labels, uint32_t p_vertex_count,
                                              uint64_t p_edge_count, int32_t variant, pm_query** out);
@@ -251,6 +286,11 @@ typedef struct pm_server pm_server;
 typedef struct pm_server_config {
   uint32_t slots;         /* queries on the GPU at once, >= 1 */
   uint64_t memory_budget; /* device bytes for admitted queries; 0 = 90% of free memory */
+  uint32_t walk_share;    /* each slot's walker launches use 1/walk_share of the
+                             GPU's resident walker blocks; 0 = 1/slots (requests
+                             that run into their budget leave room to the
+                             others), 1 = the whole GPU (requests that each fill
+                             the GPU, e.g. exact counting).  Speed only. */
 } pm_server_config;
 
 /* pm_server_submit flags: keep the final state for pm_server_export;

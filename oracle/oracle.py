@@ -35,11 +35,13 @@ class _Options(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("nlcc_threads", ctypes.c_int32),
                 ("stop_before_enumeration", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("sample_stride", ctypes.c_int64), ("enum_sample_stride", ctypes.c_int64),
-                ("deadline_ms", ctypes.c_double), ("max_steps", ctypes.c_int64)]
+                ("deadline_ms", ctypes.c_double), ("max_steps", ctypes.c_int64), ("order", ctypes.c_int32),
+                ("order_threads", ctypes.c_int32)]
 
 
 STEP_NAMES = {0: "START", 1: "END", 2: "LCC0", 3: "LCC", 4: "CC", 5: "PC", 6: "TDS", 7: "ENUMERATION"}
 TIMEOUT = -7
+STATISTICS = -13
 
 _lib = None
 
@@ -150,14 +152,17 @@ class OracleTimeout(RuntimeError):
 def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, nlcc_threads: int = 1,
            stop_before_enumeration: bool = False, sample_stride: int = 1, enum_sample_stride: int = 1,
            deadline_ms: float = 0.0, want_state: bool = True, variant: int = 0,
-           max_steps: int = 0) -> OracleResult:
+           max_steps: int = 0, order: int = 0, order_threads: int = 1) -> OracleResult:
     """run() with separate thread counts for the LCC sweeps (deterministic in
     any order) and for the CC/PC/TDS/ENUMERATION source loops (1 = the
     canonical order of the alreadyMatched shortcut), an ENUMERATION-only
     source sample (enum_sample_stride > 1: the count over sources
     v % stride == 0, pruning unchanged) and a wall-clock deadline (raises
     OracleTimeout past it).  variant 1 / 2: the reference's article drivers
-    with strict / backtrack constraint walks (pruning only, END row)."""
+    with strict / backtrack constraint walks (pruning only, END row).
+    order: PM_ORDER_* bits (the article's constraint-order drivers, with
+    variant 1 or 2), order_threads their OpenMP thread count; a run the
+    reference would abort on an absent graph statistic raises StatMissing."""
     lib = _load()
     off = np.ascontiguousarray(offsets, np.uint64)
     ad = np.ascontiguousarray(adj, np.uint32)
@@ -173,7 +178,7 @@ def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, n
     eact = np.zeros(E, np.uint8) if want_state else None
     vact = np.zeros(V, np.uint8) if want_state else None
     opt = _Options(threads, nlcc_threads, int(stop_before_enumeration), variant, sample_stride, enum_sample_stride,
-                   deadline_ms, max_steps)
+                   deadline_ms, max_steps, order, order_threads)
     st = lib.pmo_run_ex(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), V, E,
                         _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64), k,
                         ctypes.byref(opt), recs, cap, ctypes.byref(n),
@@ -182,12 +187,19 @@ def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, n
                         _p(vact, ctypes.c_uint8) if want_state else None)
     if st == TIMEOUT:
         raise OracleTimeout(f"oracle run passed its {deadline_ms:.0f} ms deadline")
+    if st == STATISTICS:
+        raise StatMissing("a graph statistic the dynamic order reads is absent")
     if st != 0:
         raise RuntimeError(f"oracle failed with status {st}")
     rows = [row_tuple(recs[i]) for i in range(n.value)]
     res = OracleResult(rows, cand, eact, vact)
     res.timings = [recs[i].step_ms for i in range(n.value)]
     return res
+
+
+class StatMissing(RuntimeError):
+    """The dynamic order read a graph statistic the pruned graph lacks (the
+    reference's order driver throws std::out_of_range there and aborts)."""
 
 
 class HostGraph:

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../pattenmatching_sharedmemory_gb300/csrc/constraints.h"
+#include "../pattenmatching_sharedmemory_gb300/csrc/effectiveness.h"
 #include "../pattenmatching_sharedmemory_gb300/csrc/generators.h"
 
 using namespace pmgb;
@@ -757,6 +758,64 @@ Results step_enumeration(State& s, const TemplateConstraint& t) {
 
 }  // namespace
 
+namespace {
+
+// GraphStatCpu::compute (src/patternmatching/algorithms/graph_stat_cpu.tpp:
+// 42-80) with `threads` OpenMP threads under the static schedule, run here
+// one thread block after the other: each block keeps one label -> count
+// accumulation that is never cleared between its vertices (the reference
+// declares it outside the vertex loop), and GraphStat::addAccumulation
+// (graph_stat.cc:103-114) counts a label-a vertex towards (a, b, i) when the
+// accumulated b count has reached i, for i up to the template's maximum.
+// The reference reads accumulationMaximumMap.at(a) once the accumulation
+// holds anything; a label a without template neighbours then throws
+// (PM_E_STATISTICS here).
+GraphStat oracle_graph_stat(const State& s, const AccumulationMaximum& am, uint32_t threads) {
+  const uint32_t S = am.slots;
+  GraphStat gs;
+  gs.slots = S;
+  gs.label_of_slot = am.label_of_slot;
+  gs.vertex_total.assign(S, 0);
+  gs.edge_total.assign(static_cast<size_t>(S) * S, 0);
+  gs.edge_outbound.assign(S, 0);
+  gs.at_least.assign(static_cast<size_t>(S) * S * GraphStat::kMaxAtLeast, 0);
+  auto slot = [&](uint64_t label) -> uint32_t {
+    for (uint32_t a = 0; a < S; ++a)
+      if (am.label_of_slot[a] == label) return a;
+    throw_stat_missing("active vertex without a template label");
+  };
+  const StaticPartition part(s.V, threads);
+  for (uint32_t t = 0; t < threads; ++t) {
+    std::vector<uint64_t> acc(S, 0);
+    bool any = false;
+    for (uint64_t v = part.begin(t); v < part.end(t); ++v) {
+      if (!s.active[v]) continue;
+      const uint32_t a = slot(s.lab[v]);
+      ++gs.vertex_total[a];
+      for (uint64_t e = s.off[v]; e < s.off[v + 1]; ++e) {
+        if (!s.edge_active[e]) continue;
+        const uint32_t w = s.adj[e];
+        if (!s.active[w]) continue;
+        const uint32_t b = slot(s.lab[w]);
+        ++gs.edge_total[a * S + b];
+        ++gs.edge_outbound[a];
+        ++acc[b];
+        any = true;
+      }
+      if (!any) continue;
+      if (!am.has_a[a]) throw_stat_missing("accumulationMaximumMap has no entry for an active label");
+      for (uint32_t b = 0; b < S; ++b) {
+        const uint32_t most = am.max[a * S + b];
+        for (uint32_t i = 1; i <= most; ++i)
+          if (acc[b] >= i) ++gs.at_least[(static_cast<size_t>(a) * S + b) * GraphStat::kMaxAtLeast + i];
+      }
+    }
+  }
+  return gs;
+}
+
+}  // namespace
+
 extern "C" {
 
 // Runs the reference pipeline (MultipleLabelCpu::runPatternMatching,
@@ -785,6 +844,10 @@ struct pmo_options {
                                     // per-source sampled count; pruning unchanged)
   double deadline_ms;               // >0: wall-clock limit; the run returns -7 past it
   int64_t max_steps;                // >0: stop after that many steps (the last row names the next)
+  int32_t order;                    // the article's order drivers (variants 1 / 2 only):
+                                    // PM_ORDER_* bits of pm_gb300.h
+  int32_t order_threads;            // their OpenMP thread count (statistics partition and
+                                    // cost divisor); 0 = 1
 };
 
 int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
@@ -852,7 +915,43 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
     int step = START;
     size_t next_cc = 0, next_pc = 0, next_tds = 0;
     Results res;
+    const int order = opt->variant ? opt->order : 0;
+    const bool dynamic = order & PM_ORDER_EFFECTIVENESS;
+    const bool use_enumerate = order & PM_ORDER_ENUMERATE;
+    const int order_threads = opt->order_threads > 0 ? opt->order_threads : 1;
+    const AccumulationMaximum am = accumulation_maximum(pg);
+    // The order drivers' NLCC steps erase the constraint they ran
+    // (multiple_label_test/*_cpu.tpp, e.g. cc_backtrack :192); the dynamic
+    // order picks by index among the remaining ones.
+    std::vector<size_t> rem_cc, rem_pc, rem_tds;
+    for (size_t i = 0; i < qc.cycles.size(); ++i) rem_cc.push_back(i);
+    for (size_t i = 0; i < qc.paths.size(); ++i) rem_pc.push_back(i);
+    for (size_t i = 0; i < qc.templates.size(); ++i) rem_tds.push_back(i);
+    size_t chosen = 0;
+    auto choose = [&]() -> int {
+      const GraphStat gs = oracle_graph_stat(s, am, static_cast<uint32_t>(order_threads));
+      std::vector<const CycleConstraint*> cs;
+      std::vector<const PathConstraint*> ps;
+      std::vector<const TemplateConstraint*> ts;
+      for (size_t i : rem_cc) cs.push_back(&qc.cycles[i]);
+      for (size_t i : rem_pc) ps.push_back(&qc.paths[i]);
+      for (size_t i : rem_tds) ts.push_back(&qc.templates[i]);
+      const OrderChoice c = choose_next_constraint(gs, cs, ps, ts, qc.enumeration, use_enumerate,
+                                                   order & PM_ORDER_EARLY_ENUMERATION, 0.01, order_threads);
+      chosen = c.index;
+      return c.kind - PM_STEP_START;
+    };
     auto advance = [&](int cur) -> int {
+      if (dynamic) {
+        switch (cur) {
+          case START: return LCC;
+          case LCC: return res.empty() ? choose() : LCC;
+          case CC: rem_cc.erase(rem_cc.begin() + chosen); return LCC;
+          case PC: rem_pc.erase(rem_pc.begin() + chosen); return LCC;
+          case TDS: rem_tds.erase(rem_tds.begin() + chosen); return LCC;
+          default: return END;
+        }
+      }
       switch (cur) {
         case START: return LCC0;
         case LCC0: return LCC;
@@ -861,13 +960,16 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
           if (next_cc < qc.cycles.size()) return CC;
           if (next_pc < qc.paths.size()) return PC;
           if (next_tds < qc.templates.size()) return TDS;
-          return opt->variant ? END : ENUM;
+          return opt->variant && !use_enumerate ? END : ENUM;
         case CC: ++next_cc; return LCC;
         case PC: ++next_pc; return LCC;
         case TDS: ++next_tds; return LCC;
         default: return END;
       }
     };
+    auto cc_index = [&]() { return dynamic ? rem_cc[chosen] : next_cc; };
+    auto pc_index = [&]() { return dynamic ? rem_pc[chosen] : next_pc; };
+    auto tds_index = [&]() { return dynamic ? rem_tds[chosen] : next_tds; };
     int32_t n = 0;
     double total_ms = 0;
     auto emit = [&](int kind, double ms, const Results& r) {
@@ -889,7 +991,12 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
       }
       ++n;
     };
-    step = advance(START);
+    // The dynamic order's driver never sets its first step
+    // (test_order_multiple_label_cpu.cc:128-130 skip getNextStep under
+    // ORDER_USE_DYNAMIC): its first iteration runs no step and logs a row
+    // with an empty step name (START here), then goes to LCC; LCC0 never
+    // runs.
+    step = dynamic ? START : advance(START);
     int iteration = 0;
     bool finished = false;
     while (!finished && iteration < 1000) {
@@ -900,14 +1007,14 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
       switch (step) {
         case LCC0: res = step_lcc0(s, qc); break;
         case LCC: res = step_lcc(s, qc); break;
-        case CC: res = opt->variant ? step_cc_variant(s, qc.cycles[next_cc], opt->variant)
+        case CC: res = opt->variant ? step_cc_variant(s, qc.cycles[cc_index()], opt->variant)
                                     : step_cc(s, qc.cycles[next_cc]); break;
-        case PC: res = opt->variant ? step_pc_variant(s, qc.paths[next_pc], opt->variant)
+        case PC: res = opt->variant ? step_pc_variant(s, qc.paths[pc_index()], opt->variant)
                                     : step_pc(s, qc.paths[next_pc]); break;
         // MultipleLabelTdsCpu::compute never advances its constraint
         // iterator (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and
         // pc :186), so every TDS step checks template constraint 0.
-        case TDS: res = opt->variant ? step_tds_variant(s, qc.templates[next_tds], opt->variant)
+        case TDS: res = opt->variant ? step_tds_variant(s, qc.templates[tds_index()], opt->variant)
                                      : step_tds(s, qc.templates[0]); break;
         case ENUM: res = step_enumeration(s, qc.enumeration); break;
         default: res = Results(); break;

@@ -33,6 +33,20 @@ PM_E_NO_DEVICE = -9
 PM_E_CANCELLED = -10
 PM_E_OOM = -11
 PM_E_BUSY = -12
+PM_E_STATISTICS = -13
+
+# Flags or-ed into a query's variant (pm_gb300.h): the article's
+# constraint-order drivers (test_article/CMakeLists.txt:53-73).
+PM_ORDER_ENUMERATE = 0x100
+PM_ORDER_EFFECTIVENESS = 0x200
+PM_ORDER_EARLY_ENUMERATION = 0x400
+# The reference's order binaries by name (order_intuitive is the backtrack
+# variant without flags).
+ORDER_DRIVERS = {"intuitive": 0, "enumerate_intuitive": PM_ORDER_ENUMERATE,
+                 "effectiveness": PM_ORDER_EFFECTIVENESS,
+                 "enumerate_effectiveness": PM_ORDER_EFFECTIVENESS | PM_ORDER_ENUMERATE,
+                 "enumerate_effectiveness_early": PM_ORDER_EFFECTIVENESS | PM_ORDER_ENUMERATE
+                 | PM_ORDER_EARLY_ENUMERATION}
 
 
 class PmError(RuntimeError):
@@ -49,7 +63,7 @@ class AlgoResults(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("slots", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+    _fields_ = [("slots", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64), ("walk_share", ctypes.c_uint32)]
 
 
 class RequestResult(ctypes.Structure):
@@ -170,6 +184,7 @@ def _load_library() -> ctypes.CDLL:
         "pm_kernel_launches": (ctypes.c_uint64, []),
         "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
+        "pm_set_order_threads": (ctypes.c_int32, [ctypes.c_int32]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_noalloc_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
@@ -363,13 +378,15 @@ class Query:
     VARIANTS = {None: 0, "reference": 0, "strict": 1, "backtrack": 2}
 
     def __init__(self, graph: Graph, pattern_dir=None, pattern: Pattern | None = None,
-                 load_pattern_labels: bool = True, variant: str | None = None):
+                 load_pattern_labels: bool = True, variant: str | None = None, order: int | str = 0):
         """variant: None / "reference" (the reference's walks), or the article
-        drivers' "strict" / "backtrack" walks (pm_query_create_variant*)."""
+        drivers' "strict" / "backtrack" walks (pm_query_create_variant*).
+        order: PM_ORDER_* flags, or an order driver's name (ORDER_DRIVERS), for
+        the article's constraint-order drivers (strict / backtrack walks)."""
         self.graph = graph
         self._h = ctypes.c_void_p()
         self._k = None if pattern is None else pattern.n
-        v = self.VARIANTS[variant]
+        v = self.VARIANTS[variant] | (ORDER_DRIVERS[order] if isinstance(order, str) else int(order))
         if pattern_dir is not None:
             d = str(pattern_dir)
             _check(lib.pm_query_create_variant(graph._h, _enc(d), int(load_pattern_labels), v, ctypes.byref(self._h)))
@@ -503,10 +520,12 @@ class Server:
     (pm_server_*): `slots` queries run on the GPU at once, admitted in FIFO
     order as slots and the device-memory budget allow."""
 
-    def __init__(self, graph: Graph, slots: int = 4, memory_budget: int = 0):
+    def __init__(self, graph: Graph, slots: int = 4, memory_budget: int = 0, walk_share: int = 0):
+        """walk_share: pm_server_config.walk_share (0: 1/slots of the GPU
+        per slot's walker launches, 1: the whole GPU)."""
         self.graph = graph
         self._h = ctypes.c_void_p()
-        cfg = ServerConfig(slots, memory_budget)
+        cfg = ServerConfig(slots, memory_budget, walk_share)
         _check(lib.pm_server_create(graph._h, ctypes.byref(cfg), ctypes.byref(self._h)))
 
     def submit(self, pattern: Pattern, export_state: bool = False, prune_only: bool = False) -> int:
@@ -674,6 +693,12 @@ class FusedBatch:
             self.close()
         except Exception:
             pass
+
+
+def set_order_threads(threads: int) -> None:
+    """The order drivers' thread count for queries created from now on
+    (pm_set_order_threads)."""
+    _check(lib.pm_set_order_threads(int(threads)))
 
 
 def version() -> str:

@@ -32,7 +32,8 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels_lcc.cu", "kernels_walk.cu"]
-CC_SOURCES = ["totem_io.cc", "constraints.cc", "walk_compile.cc", "generators.cc", "engine.cc", "server.cc",
+CC_SOURCES = ["totem_io.cc", "constraints.cc", "effectiveness.cc", "walk_compile.cc", "generators.cc", "engine.cc",
+              "server.cc",
               "fused_batch.cc", "autotune.cc", "capi.cc"]
 
 

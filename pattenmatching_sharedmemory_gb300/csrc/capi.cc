@@ -255,11 +255,15 @@ pm_status_t pm_graph_write_text(const pm_graph* g, const char* graph_path, const
   });
 }
 
+std::atomic<int> g_order_threads{1};
+
 static pm_status_t create_query(pm_graph* g, const PatternGraph& p, pm_query** out, int variant = 0) {
   auto* q = new pm_query();
   try {
     g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
-    q->impl.nlcc_variant = variant;
+    q->impl.nlcc_variant = variant & 0xFF;
+    q->impl.order = variant & ~0xFF;
+    q->impl.order_threads = g_order_threads.load();
     q->impl.create(&g->impl, p, nullptr);
   } catch (...) {
     delete q;
@@ -294,10 +298,27 @@ pm_status_t pm_query_create_from_csr(pm_graph* g, const uint64_t* p_offsets, con
   });
 }
 
+// Walk variant in the low byte, PM_ORDER_* flags above it; the order
+// drivers run the article's walks only.
+static bool valid_variant(int32_t variant) {
+  const int32_t walk = variant & 0xFF, order = variant & ~0xFF;
+  if (walk < PM_NLCC_REFERENCE || walk > PM_NLCC_BACKTRACK) return false;
+  if (order & ~(PM_ORDER_ENUMERATE | PM_ORDER_EFFECTIVENESS | PM_ORDER_EARLY_ENUMERATION)) return false;
+  if (order && walk == PM_NLCC_REFERENCE) return false;
+  if ((order & PM_ORDER_EARLY_ENUMERATION) && !(order & PM_ORDER_EFFECTIVENESS)) return false;
+  return true;
+}
+
+pm_status_t pm_set_order_threads(int32_t threads) {
+  PM_REQUIRE(threads >= 1, "thread count must be at least 1");
+  g_order_threads.store(threads);
+  return PM_SUCCESS;
+}
+
 pm_status_t pm_query_create_variant(pm_graph* g, const char* pattern_dir, int load_pattern_labels, int32_t variant,
                                     pm_query** out) {
   PM_REQUIRE(g && pattern_dir && out, "null argument");
-  PM_REQUIRE(variant >= PM_NLCC_REFERENCE && variant <= PM_NLCC_BACKTRACK, "unknown walk variant");
+  PM_REQUIRE(valid_variant(variant), "unknown walk variant or order flags");
   return guarded([&]() -> pm_status_t {
     return create_query(g, load_pattern(pattern_dir, load_pattern_labels != 0), out, variant);
   });
@@ -676,7 +697,7 @@ pm_status_t pm_server_create(pm_graph* g, const pm_server_config* config, pm_ser
     g->impl.to_device(g->impl.device >= 0 ? g->impl.device : 0);
     auto* s = new pm_server();
     try {
-      s->impl = std::make_unique<Server>(&g->impl, config->slots, config->memory_budget);
+      s->impl = std::make_unique<Server>(&g->impl, config->slots, config->memory_budget, config->walk_share);
     } catch (...) {
       delete s;
       throw;
@@ -970,7 +991,7 @@ pm_status_t pm_query_create_variant_from_csr(pm_graph* g, const uint64_t* p_offs
                                              const uint64_t* p_labels, uint32_t p_vertex_count,
                                              uint64_t p_edge_count, int32_t variant, pm_query** out) {
   PM_REQUIRE(g && out, "null argument");
-  PM_REQUIRE(variant >= PM_NLCC_REFERENCE && variant <= PM_NLCC_BACKTRACK, "unknown walk variant");
+  PM_REQUIRE(valid_variant(variant), "unknown walk variant or order flags");
   return guarded([&]() -> pm_status_t {
     return create_query(g, pattern_from_csr(p_offsets, p_adj, p_labels, p_vertex_count, p_edge_count), out,
                         variant);

@@ -386,7 +386,7 @@ std::vector<DeviceBuffer*> QueryImpl::buffers() {
           &d_list2,       &d_apply_v,   &d_apply_r,   &d_slices,    &d_slice_tiles, &d_item_scratch, &pool.edge,
           &pool.hyp,      &pool.state,
           &pool.epochs,
-          &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs};
+          &big_pool.edge, &big_pool.hyp, &big_pool.state, &big_pool.epochs, &d_stat, &d_stat_tab};
 }
 
 void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, StepCounters* ext_ctr,
@@ -503,7 +503,98 @@ void QueryImpl::create(GraphImpl* graph, const PatternGraph& p, cudaStream_t s, 
   PM_CUDA(cudaStreamSynchronize(stream));
   active_vertices = V;
   active_edges = E;
-  step = advance(PM_STEP_START);
+  for (size_t i = 0; i < cycles.size(); ++i) rem_cc.push_back(i);
+  for (size_t i = 0; i < paths.size(); ++i) rem_pc.push_back(i);
+  for (size_t i = 0; i < templates.size(); ++i) rem_tds.push_back(i);
+  if (order & PM_ORDER_EFFECTIVENESS) acc_max = accumulation_maximum(p);
+  // The dynamic order's driver never sets its first step
+  // (test_order_multiple_label_cpu.cc:128-130 call getNextStep only without
+  // ORDER_USE_DYNAMIC): its first iteration runs nothing and logs a row with
+  // an empty step name (START here), and LCC0 never runs.
+  step = (order & PM_ORDER_EFFECTIVENESS) ? PM_STEP_START : advance(PM_STEP_START);
+}
+
+size_t QueryImpl::cc_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? rem_cc[chosen] : next_cc; }
+size_t QueryImpl::pc_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? rem_pc[chosen] : next_pc; }
+size_t QueryImpl::tds_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? rem_tds[chosen] : next_tds; }
+
+GraphStat QueryImpl::graph_stat() {
+  const uint32_t S = acc_max.slots, S1 = S + 1;
+  const uint32_t T = static_cast<uint32_t>(std::max(order_threads, 1));
+  const uint64_t V = g->host.vertex_count;
+  // Host tables: accumulation maxima (column S: 1 for labels without
+  // template neighbours, whose accumulation the reference cannot look up)
+  // and the largest maximum of each column.
+  std::vector<uint8_t> max(static_cast<size_t>(S) * S1, 0);
+  std::vector<uint32_t> thr(S1, 0);
+  for (uint32_t a = 0; a < S; ++a) {
+    for (uint32_t b = 0; b < S; ++b)
+      max[a * S1 + b] = static_cast<uint8_t>(std::min<uint32_t>(acc_max.max[a * S + b], GraphStat::kMaxAtLeast - 1));
+    max[a * S1 + S] = acc_max.has_a[a] ? 0 : 1;
+    for (uint32_t b = 0; b < S1; ++b) thr[b] = std::max<uint32_t>(thr[b], max[a * S1 + b]);
+  }
+  const size_t n_vseg = static_cast<size_t>(T) * S, n_edges = static_cast<size_t>(S) * S,
+               n_at = static_cast<size_t>(S) * S1 * 64;
+  const size_t words = n_vseg + n_edges + n_at + 1;
+  d_stat.ensure(8 * words);
+  d_stat_tab.ensure(max.size() + 4 * thr.size() + 16);
+  uint8_t* tab = d_stat_tab.as<uint8_t>();
+  const size_t thr_off = (max.size() + 15) / 16 * 16;
+  PM_CUDA(cudaMemsetAsync(d_stat.ptr, 0, 8 * words, stream));
+  PM_CUDA(cudaMemcpyAsync(tab, max.data(), max.size(), cudaMemcpyHostToDevice, stream));
+  PM_CUDA(cudaMemcpyAsync(tab + thr_off, thr.data(), 4 * thr.size(), cudaMemcpyHostToDevice, stream));
+  unsigned long long* base = d_stat.as<unsigned long long>();
+  GraphStatDev p{};
+  p.slots = S;
+  p.blocks = T;
+  p.q = V / T;
+  p.r = V % T;
+  p.vseg = base;
+  p.edges = base + n_vseg;
+  p.at_least = base + n_vseg + n_edges;
+  p.bad = base + n_vseg + n_edges + n_at;
+  p.max = tab;
+  p.thr = reinterpret_cast<const uint32_t*>(tab + thr_off);
+  if (S) launch_graph_stat(g->dev(), ptrs(), p, stream);
+  PM_CUDA(cudaGetLastError());
+  std::vector<unsigned long long> h(words);
+  PM_CUDA(cudaMemcpyAsync(h.data(), d_stat.ptr, 8 * words, cudaMemcpyDeviceToHost, stream));
+  PM_CUDA(cudaStreamSynchronize(stream));
+  if (h[words - 1]) throw_stat_missing("an active vertex carries no template label");
+  GraphStat gs;
+  gs.slots = S;
+  gs.label_of_slot = acc_max.label_of_slot;
+  gs.vertex_total.assign(S, 0);
+  gs.edge_total.assign(h.begin() + n_vseg, h.begin() + n_vseg + n_edges);
+  gs.edge_outbound.assign(S, 0);
+  gs.at_least.assign(static_cast<size_t>(S) * S * GraphStat::kMaxAtLeast, 0);
+  for (uint32_t t = 0; t < T; ++t)
+    for (uint32_t a = 0; a < S; ++a) gs.vertex_total[a] += h[t * S + a];
+  for (uint32_t a = 0; a < S; ++a) {
+    for (uint32_t b = 0; b < S; ++b) gs.edge_outbound[a] += gs.edge_total[a * S + b];
+    for (uint32_t b = 0; b < S; ++b)
+      for (uint32_t i = 1; i < GraphStat::kMaxAtLeast; ++i)
+        gs.at_least[(a * S + b) * GraphStat::kMaxAtLeast + i] = h[n_vseg + n_edges + (a * S1 + b) * 64 + i];
+    // GraphStat::addAccumulation reads accumulationMaximumMap.at(a) as soon
+    // as a label-a vertex's accumulation holds anything.
+    if (!acc_max.has_a[a] && h[n_vseg + n_edges + (a * S1 + S) * 64 + 1])
+      throw_stat_missing("accumulationMaximumMap has no entry for an active label");
+  }
+  return gs;
+}
+
+int QueryImpl::choose_dynamic() {
+  const GraphStat gs = graph_stat();
+  std::vector<const CycleConstraint*> cs;
+  std::vector<const PathConstraint*> ps;
+  std::vector<const TemplateConstraint*> ts;
+  for (size_t i : rem_cc) cs.push_back(&qc.cycles[i]);
+  for (size_t i : rem_pc) ps.push_back(&qc.paths[i]);
+  for (size_t i : rem_tds) ts.push_back(&qc.templates[i]);
+  const OrderChoice c = choose_next_constraint(gs, cs, ps, ts, qc.enumeration, order & PM_ORDER_ENUMERATE,
+                                               order & PM_ORDER_EARLY_ENUMERATION, 0.01, std::max(order_threads, 1));
+  chosen = c.index;
+  return c.kind;
 }
 
 void QueryImpl::reset_modified() {
@@ -958,6 +1049,17 @@ StepResult QueryImpl::step_enumeration() {
 }
 
 int QueryImpl::advance(int cur) {
+  if (order & PM_ORDER_EFFECTIVENESS) {
+    // test_order_multiple_label_cpu.cc:177-300 (ORDER_USE_DYNAMIC).
+    switch (cur) {
+      case PM_STEP_START: return PM_STEP_LCC;
+      case PM_STEP_LCC: return last.empty() ? choose_dynamic() : PM_STEP_LCC;
+      case PM_STEP_CC: rem_cc.erase(rem_cc.begin() + chosen); return PM_STEP_LCC;
+      case PM_STEP_PC: rem_pc.erase(rem_pc.begin() + chosen); return PM_STEP_LCC;
+      case PM_STEP_TDS: rem_tds.erase(rem_tds.begin() + chosen); return PM_STEP_LCC;
+      default: return PM_STEP_END;
+    }
+  }
   switch (cur) {
     case PM_STEP_START: return PM_STEP_LCC0;
     case PM_STEP_LCC0: return PM_STEP_LCC;
@@ -967,8 +1069,10 @@ int QueryImpl::advance(int cur) {
       if (next_pc < paths.size()) return PM_STEP_PC;
       if (next_tds < templates.size()) return PM_STEP_TDS;
       // The article drivers end their schedule here
-      // (test_optimization_multiple_label_step.cc:46-58).
-      return nlcc_variant ? PM_STEP_END : PM_STEP_ENUMERATION;
+      // (test_optimization_multiple_label_step.cc:46-58), the order drivers
+      // built with USE_ENUMERATE count first (test_order_multiple_label_
+      // step.cc:52-61).
+      return nlcc_variant && !(order & PM_ORDER_ENUMERATE) ? PM_STEP_END : PM_STEP_ENUMERATION;
     case PM_STEP_CC: ++next_cc; return PM_STEP_LCC;
     case PM_STEP_PC: ++next_pc; return PM_STEP_LCC;
     case PM_STEP_TDS: ++next_tds; return PM_STEP_LCC;
@@ -979,6 +1083,11 @@ int QueryImpl::advance(int cur) {
 pm_step_record QueryImpl::run_step() {
   if (finished) return final_record();
   const int kind = step;
+  // The dynamic order's first iteration runs no step.
+  if (kind == PM_STEP_START) {
+    append_record(StepResult{}, kind, 0.0, 0, 0);
+    return records.back();
+  }
   // No vertex holds a role: every step of the reference's schedule finds
   // nothing (its loops visit active vertices only, and ENUMERATION counts
   // 0), so the remaining rows are produced without touching the device.
@@ -998,13 +1107,13 @@ pm_step_record QueryImpl::run_step() {
   switch (kind) {
     case PM_STEP_LCC0: r = step_lcc0(); break;
     case PM_STEP_LCC: r = step_lcc(); break;
-    case PM_STEP_CC: r = step_nlcc(cycles[next_cc]); break;
-    case PM_STEP_PC: r = step_nlcc(paths[next_pc]); break;
+    case PM_STEP_CC: r = step_nlcc(cycles[cc_index()]); break;
+    case PM_STEP_PC: r = step_nlcc(paths[pc_index()]); break;
     // The reference's TDS step never advances its constraint iterator
     // (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and pc :186):
     // each of the n_template TDS steps checks template constraint 0.
     // The article drivers' TDS steps do advance (tds_strict_cpu.tpp:192).
-    case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? next_tds : 0]); break;
+    case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? tds_index() : 0]); break;
     case PM_STEP_ENUMERATION: r = step_enumeration(); break;
     default: break;
   }
@@ -1566,7 +1675,9 @@ void QueryImpl::write_outputs(const std::string& dir_in) {
     char line[512];
     auto row = [&](const pm_step_record& r) {
       snprintf(line, sizeof(line), "%04d; %s; %.4f ; %.4f ; %llu; %llu; %llu; %llu; %llu; %llu; %llu; %llu\n",
-               r.iteration, step_name(r.step).c_str(), r.step_ms, r.cumulative_ms,
+               // The only START row is the dynamic order's first one, which
+               // the reference logs with an empty step name.
+               r.iteration, r.step == PM_STEP_START ? "" : step_name(r.step).c_str(), r.step_ms, r.cumulative_ms,
                (unsigned long long)r.results.vertex_eliminated, (unsigned long long)r.active_vertex,
                (unsigned long long)r.total_vertex, (unsigned long long)r.results.edge_eliminated,
                (unsigned long long)r.active_edge, (unsigned long long)r.total_edge,

@@ -11,6 +11,7 @@
 #include <functional>
 
 #include "constraints.h"
+#include "effectiveness.h"
 #include "kernels.h"
 #include "walk_compile.h"
 
@@ -165,6 +166,19 @@ struct QueryImpl {
   // create().  The article drivers' variants also advance through the
   // template constraints and end with END where the reference would count.
   int nlcc_variant = 0;
+  // The article's constraint-order drivers (PM_ORDER_* bits; variants 1 and
+  // 2 only), set before create().  order_threads is their OpenMP thread
+  // count: the static blocks of the graph statistics and the estimates'
+  // cost divisor.  Their NLCC steps drop the constraint they ran; the
+  // dynamic order picks `chosen` among the remaining ones (rem_*).
+  int order = 0;
+  int order_threads = 1;
+  std::vector<size_t> rem_cc, rem_pc, rem_tds;
+  size_t chosen = 0;
+  AccumulationMaximum acc_max;
+  DeviceBuffer d_stat, d_stat_tab;
+  // Graph statistics of the active graph on the device (GraphStatCpu).
+  GraphStat graph_stat();
   bool has_deadline = false;
   std::chrono::steady_clock::time_point deadline{};
   const std::atomic<bool>* cancel = nullptr;
@@ -230,6 +244,11 @@ struct QueryImpl {
   void run_walks(const DeviceConstraint& dc, uint32_t n_wl, bool record_marks);
   void resolve_exact(const DeviceConstraint& dc, uint32_t n_wl);
   int advance(int cur);
+  // The dynamic order's next step after an LCC fixpoint; sets `chosen`.
+  int choose_dynamic();
+  size_t cc_index() const;
+  size_t pc_index() const;
+  size_t tds_index() const;
   void ensure_hub_acc();
   // Runs LCC passes until the fixpoint (or max_iterations) in one graph
   // launch and appends one row per pass, as run_step would.

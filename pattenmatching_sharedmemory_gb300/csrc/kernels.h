@@ -110,6 +110,30 @@ const unsigned long long* enum_item_totals(const unsigned long long* scratch, ui
 void launch_enum_item_write(const DevGraph& g, const uint32_t* wl, uint32_t n_wl, uint32_t t, uint32_t s2,
                             const unsigned long long* scratch, uint4* items, cudaStream_t s);
 
+// Graph statistics of the dynamic constraint order (GraphStatCpu::compute,
+// algorithms/graph_stat_cpu.tpp:42-80) over the query's active graph, with
+// the vertices split into `blocks` static-schedule blocks of q or q + 1 ids
+// (the first r blocks one longer).  Outputs are zeroed by the caller:
+//   vseg[t * S + a]            active vertices of slot a in block t
+//   edges[a * S + b]           active CSR entries from slot a to slot b
+//   at_least[(a * (S + 1) + b) * 64 + i]  label-a vertices whose block's
+//                              running count of slot-b neighbours (b == S:
+//                              of any neighbour) has reached i, for i up to
+//                              max[a * (S + 1) + b]
+//   *bad                       set when an active vertex carries no slot
+// thr[b] = the largest max[. * (S + 1) + b] (0: column not needed).
+struct GraphStatDev {
+  uint32_t slots, blocks;
+  uint64_t q, r;
+  unsigned long long* vseg;
+  unsigned long long* edges;
+  unsigned long long* at_least;
+  unsigned long long* bad;
+  const uint8_t* max;
+  const uint32_t* thr;
+};
+void launch_graph_stat(const DevGraph& g, const QueryDevPtrs& q, const GraphStatDev& p, cudaStream_t s);
+
 void launch_worklist(const DevGraph& g, const QueryDevPtrs& q, uint64_t start_mask, uint32_t* wl,
                      uint32_t* wl_index, uint32_t* block_counts, uint32_t* count, cudaStream_t s);
 

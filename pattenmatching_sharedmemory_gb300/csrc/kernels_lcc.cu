@@ -1764,6 +1764,139 @@ __global__ void __launch_bounds__(kThreads) k_export(DevGraph g, DevState<W> st,
     for (uint64_t e = tid; e < g.E; e += stride) eact_bytes[e] = edge_active(st.eact, e);
 }
 
+// ---- graph statistics of the dynamic constraint order ---------------------
+// GraphStatCpu::compute (src/patternmatching/algorithms/graph_stat_cpu.tpp:
+// 42-80) over the active graph: active vertices per (partition block, label
+// slot), active CSR entries between active vertices per (slot, slot), and
+// the at-least counts of the reference's per-thread accumulation, which is
+// never cleared between the vertices of one thread's block: a label-a vertex
+// counts towards (a, b, i) when the running number of label-b neighbours of
+// the block's active vertices up to and including it has reached i.  That
+// running number only grows, so once it reaches the largest i any label
+// needs (at most 63) every later vertex of the block counts fully: one warp
+// per (block, b) scans from the block's start to that point and the rest of
+// the block is added from the per-block vertex counts.
+
+__device__ __forceinline__ uint32_t stat_block_of(uint64_t v, uint64_t q, uint64_t r) {
+  const uint64_t big = r * (q + 1);
+  return static_cast<uint32_t>(v < big ? v / (q + 1) : r + (v - big) / q);
+}
+
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_stat_counts(DevGraph g, const W* __restrict__ vs,
+                                                           const uint32_t* __restrict__ eact, GraphStatDev p) {
+  extern __shared__ uint32_t hist[];  // [S * S] entries between slots
+  const uint32_t S = p.slots;
+  for (uint32_t i = threadIdx.x; i < S * S; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  const uint32_t lane = lane_id();
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t tile = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; tile * 32 < g.V;
+       tile += nwarps) {
+    const uint64_t v = tile * 32 + lane;
+    uint32_t a = 0;
+    bool act = false;
+    if (v < g.V) {
+      const W w = vs[v];
+      act = Pack<W>::cand(w) != 0;
+      a = Pack<W>::slot(w);
+    }
+    if (act && a >= S) {
+      atomicOr(p.bad, 1ull);
+      act = false;
+    }
+    const unsigned am = __ballot_sync(kFull, act);
+    if (act) {
+      const uint32_t key = stat_block_of(v, p.q, p.r) * S + a;
+      const unsigned peers = __match_any_sync(am, key);
+      if (lane == static_cast<uint32_t>(__ffs(peers) - 1))
+        atomicAdd(p.vseg + key, static_cast<unsigned long long>(__popc(peers)));
+    }
+    for (unsigned todo = am; todo; todo &= todo - 1) {
+      const int src = __ffs(todo) - 1;
+      const uint64_t u = tile * 32 + src;
+      const uint32_t au = __shfl_sync(kFull, a, src);
+      const uint64_t hi = g.off[u + 1];
+      for (uint64_t e = g.off[u] + lane; e < hi; e += 32) {
+        if (!edge_active(eact, e)) continue;
+        const W ww = vs[g.adj[e]];
+        if (Pack<W>::cand(ww) == 0) continue;
+        const uint32_t b = Pack<W>::slot(ww);
+        if (b >= S) {
+          atomicOr(p.bad, 1ull);
+          continue;
+        }
+        atomicAdd(&hist[au * S + b], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < S * S; i += blockDim.x)
+    if (hist[i]) atomicAdd(p.edges + i, static_cast<unsigned long long>(hist[i]));
+}
+
+// One warp per (partition block t, neighbour slot b), b == S standing for
+// "any label" (the accumulation holds anything); needs k_stat_counts first.
+template <class W>
+__global__ void __launch_bounds__(kThreads) k_stat_accum(DevGraph g, const W* __restrict__ vs,
+                                                          const uint32_t* __restrict__ eact, GraphStatDev p) {
+  __shared__ uint32_t scanned_all[kWarpsPerBlock][64];
+  const uint32_t S = p.slots, S1 = S + 1;
+  const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= static_cast<uint64_t>(p.blocks) * S1) return;
+  const uint32_t t = static_cast<uint32_t>(warp / S1), b = static_cast<uint32_t>(warp % S1);
+  const uint32_t thr = p.thr[b];
+  if (thr == 0) return;
+  uint32_t* scanned = scanned_all[wib];
+  for (uint32_t a = lane; a < 64; a += 32) scanned[a] = 0;
+  __syncwarp();
+  const uint64_t begin = t * p.q + (t < p.r ? t : p.r), end = begin + p.q + (t < p.r ? 1 : 0);
+  uint64_t run = 0, pos = begin;
+  while (pos < end && run < thr) {
+    const uint64_t v = pos + lane;
+    uint32_t c = 0, a = S;
+    if (v < end) {
+      const W w = vs[v];
+      if (Pack<W>::cand(w) != 0 && Pack<W>::slot(w) < S) {
+        a = Pack<W>::slot(w);
+        const uint64_t hi = g.off[v + 1];
+        for (uint64_t e = g.off[v]; e < hi; ++e) {
+          if (!edge_active(eact, e)) continue;
+          const W ww = vs[g.adj[e]];
+          if (Pack<W>::cand(ww) == 0) continue;
+          if (b == S || Pack<W>::slot(ww) == b) ++c;
+        }
+      }
+    }
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t n = __shfl_up_sync(kFull, incl, d);
+      if (lane >= static_cast<uint32_t>(d)) incl += n;
+    }
+    if (a < S) {
+      const uint32_t most = p.max[a * S1 + b];
+      const uint64_t upto = run + incl < most ? run + incl : most;
+      for (uint32_t i = 1; i <= upto; ++i) atomicAdd(p.at_least + (static_cast<uint64_t>(a) * S1 + b) * 64 + i, 1ull);
+      atomicAdd(&scanned[a], 1u);
+    }
+    run += __shfl_sync(kFull, incl, 31);
+    pos += 32;
+  }
+  __syncwarp();
+  if (pos >= end) return;
+  // Every active vertex after `pos` in the block sees a running count of at
+  // least thr >= every maximum of this column.
+  for (uint32_t a = lane; a < S; a += 32) {
+    const uint32_t most = p.max[a * S1 + b];
+    if (!most) continue;
+    const unsigned long long rest = p.vseg[static_cast<uint64_t>(t) * S + a] - scanned[a];
+    if (!rest) continue;
+    for (uint32_t i = 1; i <= most; ++i) atomicAdd(p.at_least + (static_cast<uint64_t>(a) * S1 + b) * 64 + i, rest);
+  }
+}
+
 template <class W>
 DevState<W> state_of(const QueryDevPtrs& q) {
   return DevState<W>{static_cast<W*>(q.vs), q.eact, q.mod, q.sch, static_cast<W*>(q.unm), q.lt, q.tile_sch,
@@ -2042,6 +2175,16 @@ void launch_export(const DevGraph& g, const QueryDevPtrs& q, uint64_t* cand, uin
                    cudaStream_t s) {
   const int grid = device_sm_count() * 8;
   PM_DISPATCH_WORD(q.word_kind, k_export<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), cand, vact, eact_bytes));
+}
+
+void launch_graph_stat(const DevGraph& g, const QueryDevPtrs& q, const GraphStatDev& p, cudaStream_t s) {
+  const int grid = grid_for_tiles(g.V, 8);
+  const size_t shmem = sizeof(uint32_t) * p.slots * p.slots;
+  PM_DISPATCH_WORD(q.word_kind, k_stat_counts<W><<<grid, kThreads, shmem, s>>>(g, static_cast<const W*>(q.vs), q.eact,
+                                                                                p));
+  const uint64_t warps = static_cast<uint64_t>(p.blocks) * (p.slots + 1);
+  const int grid2 = static_cast<int>((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  PM_DISPATCH_WORD(q.word_kind, k_stat_accum<W><<<grid2, kThreads, 0, s>>>(g, static_cast<const W*>(q.vs), q.eact, p));
 }
 
 }  // namespace pmgb

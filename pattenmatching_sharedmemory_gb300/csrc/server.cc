@@ -5,7 +5,8 @@
 
 namespace pmgb {
 
-Server::Server(GraphImpl* graph, uint32_t slots, uint64_t budget) : g_(graph), slots_(slots), budget_(budget) {
+Server::Server(GraphImpl* graph, uint32_t slots, uint64_t budget, uint32_t walk_share)
+    : g_(graph), slots_(slots), budget_(budget), walk_share_(walk_share) {
   if (!g_ || g_->device < 0) throw PmError{PM_E_INVALID_ARG, "the graph is not on a device"};
   if (slots_ == 0) throw PmError{PM_E_INVALID_ARG, "a server needs at least one slot"};
   PM_CUDA(cudaSetDevice(g_->device));

@@ -58,7 +58,7 @@ struct ServerStats {
 class Server {
  public:
   // slots >= 1; budget 0 = 90 % of the device's free memory now.
-  Server(GraphImpl* graph, uint32_t slots, uint64_t budget);
+  Server(GraphImpl* graph, uint32_t slots, uint64_t budget, uint32_t walk_share = 0);
   ~Server();  // queued requests end with PM_E_CANCELLED; running ones finish
   Server(const Server&) = delete;
   Server& operator=(const Server&) = delete;

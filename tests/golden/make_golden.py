@@ -195,6 +195,61 @@ def article():
     (HERE / "article_variants.json").write_text(json.dumps(out, indent=1))
 
 
+ORDER_BINARIES = ("enumerate_intuitive", "effectiveness", "enumerate_effectiveness",
+                  "enumerate_effectiveness_early")
+
+
+def order():
+    """The article's constraint-order drivers (oracle/_ref/
+    patternmatching_order_*, test_article/CMakeLists.txt:53-73; backtrack
+    walks with all three optimisations) on the bundled fixtures and the small
+    synthetic cases, with one thread and, for a few cases, three (the graph
+    statistics and the cost estimate depend on the thread count).  A run the
+    reference ends by an uncaught exception (a graph statistic the estimate
+    reads is absent) is recorded with "aborted": true.  An empty step name
+    (the first row of the dynamic order) is recorded as "START"."""
+    out = []
+    cases = [("fixture_" + t, None, t) for t in ["test_1", "test_2", "test_3", "test_4"]]
+    cases += [(c["name"], c, None) for c in C.synthetic_cases(include_big=False)
+              if c["name"] not in ("scale12_cycle4",)]
+    for ci, (name, case, fixture) in enumerate(cases):
+        for binary_name in ORDER_BINARIES:
+            for threads in ((1, 3) if ci % 4 == 1 else (1,)):
+                binary = ROOT / "oracle" / "_ref" / f"patternmatching_order_{binary_name}"
+                with tempfile.TemporaryDirectory() as tmp:
+                    tmp = Path(tmp)
+                    if fixture:
+                        d = HERE / "data" / fixture
+                        graph, labels, pdir = d / "graph.totem", d / "vertex_data" / "graph_vertex_data.totem", \
+                            d / "pattern_1"
+                    else:
+                        g = C.make_graph(case)
+                        g.write_text(tmp / "g.totem", tmp / "labels.totem")
+                        C.make_pattern(case).write(tmp / "pattern")
+                        graph, labels, pdir = tmp / "g.totem", tmp / "labels.totem", tmp / "pattern"
+                    entry = {"name": name, "order": binary_name, "threads": threads, "fixture": fixture,
+                             "case": case}
+                    try:
+                        res = run_reference(graph, labels, pdir, tmp / "out", binary=binary, timeout=300,
+                                            threads=threads)
+                    except subprocess.TimeoutExpired:
+                        print("timeout", name, binary_name, flush=True)
+                        continue
+                    except subprocess.CalledProcessError as e:
+                        entry.update({"aborted": True, "returncode": e.returncode})
+                        out.append(entry)
+                        print(name, binary_name, threads, "aborted", e.returncode, flush=True)
+                        continue
+                for r in res["rows"]:
+                    if r[0] == "":
+                        r[0] = "START"
+                entry.update({"rows": res["rows"], "vertex_sha256": sha(res["vertex"]),
+                              "graph_sha256": sha(res["graph"]), "last": res["last"], "aborted": False})
+                out.append(entry)
+                print(name, binary_name, threads, len(res["rows"]), "rows", res["rows"][-2][0], flush=True)
+    (HERE / "order_variants.json").write_text(json.dumps(out, indent=1))
+
+
 def constraints():
     # A fixed tiny background graph: constraint generation ignores it.
     out = []
@@ -215,7 +270,7 @@ def constraints():
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-big", action="store_true", help="skip the scale-16 case (minutes of CPU)")
-    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big", "stream15", "article"])
+    ap.add_argument("--only", choices=["fixtures", "synthetic", "constraints", "big", "stream15", "article", "order"])
     a = ap.parse_args()
     if not REF_BIN.exists():
         sys.exit("build the reference first: make -C oracle ref")
@@ -231,3 +286,5 @@ if __name__ == "__main__":
         stream15()
     if a.only == "article":
         article()
+    if a.only == "order":
+        order()
