@@ -181,7 +181,9 @@ void GraphImpl::to_device(int dev, const uint32_t* adj_src) {
   if (V) PM_CUDA(cudaMemcpy(d_lab.ptr, dense_ids.data(), sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
   device = dev;
   if (host.edge_count && dense_values.size() <= 256) {
-    d_nlab.ensure(std::max<uint64_t>(host.edge_count, 16));
+    // Padded to whole 32-entry words plus one: LCC's first pass reads it in
+    // 16-byte loads that start below the edge count.
+    d_nlab.ensure((host.edge_count + 31) / 32 * 32 + 32);
     launch_build_entry_labels(this->dev(), d_nlab.as<uint8_t>(), nullptr);
     PM_CUDA(cudaGetLastError());
     PM_CUDA(cudaDeviceSynchronize());
