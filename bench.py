@@ -39,7 +39,8 @@ poisson      : requests arriving as a Poisson process at 50 % and 90 % of
 e2e          : through the C ABI from pinned host buffers: each step loads
                the CSR with pm_graph_from_csr (host -> device), serves its
                requests and reads back every request's result rows.
-roofline     : the dominant kernel class of requests run one at a time, its
+roofline     : the dominant kernel class of requests run one at a time
+               (timed-out requests count the step their deadline cut short), its
                algorithmic bytes over its device time against the measured
                HBM copy bandwidth (walker bytes per hop: 16 B of offsets;
                per tested CSR entry 4 B id + 1/8 B edge bit + 1/8 B active
@@ -359,6 +360,15 @@ def one_at_a_time(g, pm, tmpls, prune_only=True):
                     cls_bytes[c] = cls_bytes.get(c, 0.0) + lcc_pass_bytes(scanned, r.results.edge_eliminated, tm.n)
         except pm.PmError as e:
             statuses.append(e.code)
+            # A request that ran into its budget: the step its deadline cut
+            # short (walkers), with the entries they tested until then.
+            ab = q.aborted_step()
+            if ab is not None:
+                kind, ms, scanned, hops = ab
+                c = kernel_class(pm.STEP_NAMES[kind])
+                cls_ms[c] = cls_ms.get(c, 0.0) + ms
+                if c in ("walk", "enumerate"):
+                    cls_bytes[c] = cls_bytes.get(c, 0.0) + walker_bytes(hops, scanned, tm.n)
         q.close()
         lat.append((time.perf_counter() - t1) * 1e3)
     torch.cuda.synchronize()
@@ -641,6 +651,35 @@ def run_c5(args, pm, T):
             checked.append(i)
             if not same:
                 mismatches.append(i)
+        # Templates over the four least frequent labels, which both sides
+        # prune to a small remainder: a check past 2^31 CSR entries that the
+        # oracle finishes (a 4-cycle, and a 4-path whose end labels repeat).
+        import numpy as np
+
+        counts = np.bincount(lab.astype(np.int64), minlength=64)
+        present = [int(x) for x in np.argsort(counts, kind="stable") if counts[x] > 0]
+        r4 = present[:4]
+        rare = {"cycle4_rarest": T.cycle(r4),
+                "path4_rarest_repeated": pm.Pattern.from_edges(4, [(0, 1), (1, 2), (2, 3)], [r4[0], r4[1], r4[2], r4[0]])}
+        rare_checked, rare_mismatches = [], []
+        for name, tp in rare.items():
+            q = pm.Query(g, pattern=tp)
+            try:
+                rows = [r.as_tuple() for r in q.prune()]
+                cand, eact, vact = q.export()
+            except pm.PmError:
+                q.close()
+                continue
+            q.close()
+            try:
+                ref = oracle.run_ex(off, adj, lab, tp.offsets, tp.adj, tp.labels, threads=threads, nlcc_threads=1,
+                                    stop_before_enumeration=True, deadline_ms=args.c5_oracle_ms)
+            except oracle.OracleTimeout:
+                continue
+            rare_checked.append(name)
+            if not (rows == ref.rows and bool((cand == ref.cand).all()) and bool((eact == ref.eact).all())
+                    and bool((vact == ref.vact).all())):
+                rare_mismatches.append(name)
     finally:
         pm._check(pm.lib.pm_set_query_budget_ms(0.0))
     edges = g.edge_count
@@ -658,7 +697,9 @@ def run_c5(args, pm, T):
             "one_at_a_time_completed": n_q, "device_ms_by_class": {k: round(v, 3) for k, v in cls_ms.items()},
             "parity_sample": {"requests": sample, "checked": checked, "mismatches": mismatches,
                               "gpu_timeouts": gpu_timeouts, "oracle_timeouts": cpu_timeouts,
-                              "oracle_deadline_ms": args.c5_oracle_ms}}
+                              "oracle_deadline_ms": args.c5_oracle_ms},
+            "parity_rare_labels": {"labels": r4, "checked": rare_checked, "mismatches": rare_mismatches,
+                                   "compared": "rows, role sets, CSR-entry and vertex flags after pruning"}}
 
 
 def run_c1_stream(args, pm, T):
@@ -834,7 +875,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--slots", type=int, default=16)
+    ap.add_argument("--slots", type=int, default=32)
     ap.add_argument("--requests-per-step", type=int, default=100)
     ap.add_argument("--budget-ms", type=float, default=250.0, help="per-request budget on the GPU")
     ap.add_argument("--reference-budget-ms", type=float, default=6000.0, help="per-request budget on the CPU")

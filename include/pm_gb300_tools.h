@@ -255,6 +255,13 @@ pm_status_t pm_query_step_walk_stats(const pm_query* q, int32_t row, uint64_t* s
  * reference's alreadyMatched shortcut, and of memo-table overflow retries. */
 pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries);
 
+/* The step that ended a run with PM_E_TIMEOUT because its walkers passed
+ * their deadline (it has no result row): its kind, device time, and the CSR
+ * entries its walkers tested and hops they took until then (the counters of
+ * pm_query_step_walk_stats).  PM_FAILURE when no step was cut short. */
+pm_status_t pm_query_aborted_step(const pm_query* q, int32_t* step, double* step_ms, uint64_t* scanned,
+                                  uint64_t* hops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -185,6 +185,9 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_order_threads": (ctypes.c_int32, [ctypes.c_int32]),
+        "pm_query_aborted_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                                   ctypes.POINTER(ctypes.c_uint64)]),
         "pm_set_enum_split": (ctypes.c_int32, [ctypes.c_uint32, ctypes.c_uint32]),
         "pm_set_enum_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
         "pm_set_noalloc_table_entries": (ctypes.c_int32, [ctypes.c_uint32]),
@@ -496,6 +499,15 @@ class Query:
         ms = ctypes.c_double()
         _check(lib.pm_query_elapsed_ms(self._h, ctypes.byref(ms)))
         return ms.value
+
+    def aborted_step(self):
+        """(step kind, device ms, CSR entries tested, hops) of the step that
+        ended the run with PM_E_TIMEOUT (pm_query_aborted_step), or None."""
+        k, ms, a, b = ctypes.c_int32(), ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint64()
+        if lib.pm_query_aborted_step(self._h, ctypes.byref(k), ctypes.byref(ms), ctypes.byref(a),
+                                     ctypes.byref(b)) != PM_SUCCESS:
+            return None
+        return k.value, ms.value, a.value, b.value
 
     def step_walk_stats(self, row: int):
         """(CSR entries tested, hops taken) by the walkers of result row `row`."""

@@ -641,6 +641,17 @@ pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint6
   return PM_SUCCESS;
 }
 
+pm_status_t pm_query_aborted_step(const pm_query* q, int32_t* step, double* step_ms, uint64_t* scanned,
+                                  uint64_t* hops) {
+  PM_REQUIRE(q, "null argument");
+  if (q->impl.aborted_kind < 0) return fail(PM_FAILURE, "no step of this query was cut short");
+  if (step) *step = q->impl.aborted_kind;
+  if (step_ms) *step_ms = q->impl.aborted_ms;
+  if (scanned) *scanned = q->impl.aborted_scanned;
+  if (hops) *hops = q->impl.aborted_hops;
+  return PM_SUCCESS;
+}
+
 void pm_query_destroy(pm_query* q) { delete q; }
 
 namespace {

@@ -1106,6 +1106,7 @@ pm_step_record QueryImpl::run_step() {
     first_recorded = true;
   }
   StepResult r;
+  try {
   switch (kind) {
     case PM_STEP_LCC0: r = step_lcc0(); break;
     case PM_STEP_LCC: r = step_lcc(); break;
@@ -1118,6 +1119,19 @@ pm_step_record QueryImpl::run_step() {
     case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? tds_index() : 0]); break;
     case PM_STEP_ENUMERATION: r = step_enumeration(); break;
     default: break;
+  }
+  } catch (const PmError& e) {
+    if (e.code == PM_E_TIMEOUT) {
+      // The walkers' counters were read when the deadline was seen.
+      float ms = 0;
+      if (cudaEventRecord(ev1, stream) == cudaSuccess && cudaEventSynchronize(ev1) == cudaSuccess)
+        cudaEventElapsedTime(&ms, ev0, ev1);
+      aborted_kind = kind;
+      aborted_ms = ms;
+      aborted_scanned = h_ctr->scanned;
+      aborted_hops = h_ctr->descents;
+    }
+    throw;
   }
   PM_CUDA(cudaEventRecord(ev1, stream));
   PM_CUDA(cudaEventSynchronize(ev1));

@@ -186,6 +186,12 @@ struct QueryImpl {
 
   // statistics of the alreadyMatched emulation
   uint64_t exact_resolutions = 0, overflow_retries = 0;
+  // The step that ended the run with PM_E_TIMEOUT (its walkers passed their
+  // deadline): kind (-1: none), device time, walker CSR entries tested and
+  // hops taken until then.  It has no result row.
+  int aborted_kind = -1;
+  double aborted_ms = 0;
+  uint64_t aborted_scanned = 0, aborted_hops = 0;
   // per step: walker CSR entries tested and hops taken (0 for LCC steps)
   std::vector<std::pair<uint64_t, uint64_t>> walk_stats;
 

@@ -71,10 +71,16 @@ __device__ __forceinline__ uint64_t find_sorted(const uint32_t* __restrict__ adj
     const uint32_t a = adj[lo], b = adj[hi - 1];
     if (target < a || target > b) return ~uint64_t(0);
     uint64_t mid;
-    if (interp && b > a)
-      mid = lo + static_cast<uint64_t>(target - a) * (hi - 1 - lo) / (b - a);
-    else
+    if (interp && b > a) {
+      // A guess only (any position in [lo, hi) keeps the search exact), so
+      // single precision replaces a 64-bit division.
+      const uint64_t span = hi - 1 - lo;
+      uint64_t step = static_cast<uint64_t>(static_cast<float>(target - a) / static_cast<float>(b - a) *
+                                            static_cast<float>(span));
+      mid = lo + (step < span ? step : span);
+    } else {
       mid = lo + ((hi - lo) >> 1);
+    }
     interp = !interp;
     const uint32_t x = adj[mid];
     if (x == target) return mid;
@@ -96,17 +102,39 @@ __device__ __forceinline__ uint64_t find_sorted(const uint32_t* __restrict__ adj
 // equally many (the reverses of the former are distinct entries of the
 // latter, so equal counts leave none without a reverse; self-loops are
 // their own).  res[0] = 1 when an entry has no reverse; res[1], res[2]
-// count the entries with u < w and u > w.  Warp per vertex, lane per entry.
+// count the entries with u < w and u > w.  Warp per task, lane per entry:
+// the tasks are the segments of the hub plan's multi-segment hubs (so no
+// warp walks a hub's whole list alone; RMAT hubs reach 10^6 entries), then
+// every vertex, skipping those the segments cover.
 __global__ void __launch_bounds__(kThreads) k_check_symmetric(DevGraph g, unsigned long long* res) {
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  const uint64_t seg_entries = uint64_t(1) << g.seg_shift;
   unsigned long long up = 0, down = 0;
-  for (uint64_t u = warp; u < g.V; u += n_warps) {
-    // Another warp found an entry without reverse: stop (warp-uniform read).
-    const unsigned found = lane == 0 ? (*reinterpret_cast<volatile unsigned long long*>(res) != 0) : 0u;
-    if (__shfl_sync(kFull, found, 0)) break;
-    const uint64_t b = g.off[u], e = g.off[u + 1];
+  uint32_t polls = 0;
+  for (uint64_t task = warp; task < g.n_heavy + g.V; task += n_warps) {
+    // Another warp found an entry without reverse: stop (warp-uniform read,
+    // every 16th task).
+    if ((polls++ & 15) == 0) {
+      const unsigned found = lane == 0 ? (*reinterpret_cast<volatile unsigned long long*>(res) != 0) : 0u;
+      if (__shfl_sync(kFull, found, 0)) break;
+    }
+    uint64_t u, b, e;
+    if (task < g.n_heavy) {
+      const uint4 sd = g.seg[task];
+      u = sd.x;
+      const uint64_t a = g.off[u], z = g.off[u + 1];
+      const uint64_t blk = (a >> g.seg_shift) + sd.y;
+      b = sd.y == 0 ? a : blk << g.seg_shift;
+      const uint64_t lim = (blk + 1) << g.seg_shift;
+      e = z < lim ? z : lim;
+    } else {
+      u = task - g.n_heavy;
+      b = g.off[u];
+      e = g.off[u + 1];
+      if (g.n_heavy && e - b > g.hub_degree && e - b > seg_entries) continue;  // in the segments above
+    }
     bool missing = false;
     for (uint64_t x0 = b; x0 < e && !missing; x0 += 32) {
       const uint64_t x = x0 + lane;
