@@ -883,7 +883,7 @@ def main():
     ap.add_argument("--poisson-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--c1-steps", type=int, default=3)
-    ap.add_argument("--cpu-requests", type=int, default=2)
+    ap.add_argument("--cpu-requests", type=int, default=4)
     ap.add_argument("--lcc-roofline", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--walk-table", type=int, default=0, help="--case c4: walker state-memo entries per warp")
