@@ -118,6 +118,7 @@ def c4_config(args, vertices, entries):
             "request": "PruneJuice pruning pipeline (LCC0, LCC fixpoints, CC/PC/TDS); counting: see c1_stream",
             "budget_ms": args.budget_ms, "reference_budget_ms": args.reference_budget_ms,
             "requests_per_step": args.requests_per_step, "slots": args.slots,
+            "walk_table_entries": args.walk_table or "library default",
             "reference_sample": f"requests i % {w['reference_sample_stride']} == 0 of the stream, one per step",
             "l2": "inputs larger than L2 (2.1 GB CSR resident; no flush needed)",
             "parallelism": "replicas (one per GPU)"}
@@ -390,6 +391,8 @@ def run_c4(args, rank, world, pm, T):
     stream = c4_stream(T)
     B = args.requests_per_step
     pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
+    if args.walk_table:
+        pm._check(pm.lib.pm_set_walk_table_entries(args.walk_table))
 
     server = pm.Server(g, slots=args.slots)
     # Warm-up steps serve requests of another seeded stream of the same kind.
@@ -854,8 +857,6 @@ def run_case(args):
     kind, n_labels, s, lseed = C4["labels"]
     g = pm.Graph.rmat(args.scale, 16, seed=1).assign_labels(kind, n_labels, s, lseed).to_device(0)
     pm._check(pm.lib.pm_set_query_budget_ms(args.budget_ms))
-    if args.walk_table:
-        pm._check(pm.lib.pm_set_walk_table_entries(args.walk_table))
     done, t0 = 0, time.perf_counter()
     for p in c4_stream(T)[:args.queries]:
         q = pm.Query(g, pattern=p)
@@ -875,7 +876,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--slots", type=int, default=32)
+    ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--requests-per-step", type=int, default=100)
     ap.add_argument("--budget-ms", type=float, default=250.0, help="per-request budget on the GPU")
     ap.add_argument("--reference-budget-ms", type=float, default=6000.0, help="per-request budget on the CPU")
@@ -886,7 +887,9 @@ def main():
     ap.add_argument("--cpu-requests", type=int, default=4)
     ap.add_argument("--lcc-roofline", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--walk-table", type=int, default=0, help="--case c4: walker state-memo entries per warp")
+    ap.add_argument("--walk-table", type=int, default=2048,
+                    help="served stream: walker state-memo entries per warp (speed knob, the same for every "
+                         "leg; 0 = the library default of 8192)")
     ap.add_argument("--no-label-stream", action="store_true",
                     help="--case lcc: first LCC pass gathers neighbour words instead of reading entry labels")
     ap.add_argument("--no-c1", action="store_true")

@@ -244,14 +244,7 @@ struct LccWarp {
   uint32_t cnt[kHubRanks][32];  // tiles: [rank][owner lane]; segments: [rank][counting lane]
   uint32_t tot[kHubRanks];      // segments: totals per rank
   uint8_t rank_of[64];          // needed slot -> rank, kNoRank otherwise
-  uint8_t code[256];            // first pass, segments: dense label -> kCode* or count rank
 };
-
-// First-pass entry codes of a segment's vertex, by the target's label: a
-// count rank (< kHubRanks), or one of these.
-constexpr uint8_t kCodeKeep = 0xFD;  // a possible neighbour, label not counted
-constexpr uint8_t kCodeElim = 0xFE;  // target holds roles, none a neighbour role: entry eliminated
-constexpr uint8_t kCodeDead = 0xFF;  // target holds no role: live-target bit cleared
 
 // Rank table of `slots` and zeroed counters for its n_slots ranks.
 __device__ __forceinline__ void set_ranks(LccWarp& lw, uint64_t slots, uint32_t n_slots) {
@@ -477,78 +470,6 @@ __device__ void lcc_vertex_warp(const DevGraph& g, const DevState<W>& st, const 
   }
 }
 
-// The first pass after LCC0 over hub segment [beg, end) of a vertex whose
-// roles' neighbour union is ncs: every target word follows from the entry's
-// label byte (label_word), so the warp streams the segment's label bytes,
-// 16 per lane in one 16-byte load (512 entries per warp step), instead of
-// visiting live-target words.  A per-warp table gives each label's code for
-// this vertex; counts go to the lane's column of lw.cnt, and the lane pair
-// of each 32-entry word merges its halves so that one lane clears the
-// word's bits.  Decisions, bit updates and counts are those of the
-// word-driven loop of lcc_segment.  Returns the entries eliminated
-// (warp-uniform).
-template <class W>
-__device__ __forceinline__ uint32_t lcc_segment_first(const DevGraph& g, const DevState<W>& st,
-                                                      const LccTables& t, LccWarp& lw, uint64_t ncs, uint64_t beg,
-                                                      uint64_t end) {
-  const unsigned lane = lane_id();
-  for (uint32_t lb = lane; lb < 256; lb += 32) {
-    const uint64_t cw = t.lab_cand[lb];
-    uint8_t c = kCodeKeep;
-    if (cw == 0) {
-      c = kCodeDead;
-    } else if ((cw & ncs) == 0) {
-      c = kCodeElim;
-    } else {
-      const uint32_t sw = t.lab_slot[lb];
-      if (sw < 64 && lw.rank_of[sw] != kNoRank) c = lw.rank_of[sw];
-    }
-    lw.code[lb] = c;
-  }
-  __syncwarp();
-  uint32_t elim = 0;
-  // Steps start on a 32-entry word: lanes 2i and 2i + 1 cover word i's low
-  // and high halves.  nlab is padded to a multiple of 32 bytes, so a 16-byte
-  // load that starts below `end` stays inside it.
-  for (uint64_t c0 = beg & ~uint64_t(31); c0 < end; c0 += 512) {
-    const uint64_t e0 = c0 + 16 * lane;
-    uint32_t em = 0, dm = 0;
-    if (e0 < end && e0 + 16 > beg) {
-      const uint4 q = *reinterpret_cast<const uint4*>(g.nlab + e0);
-      uint32_t in = (st.lt[e0 >> 5] >> static_cast<uint32_t>(e0 & 31)) & 0xFFFFu;
-      if (beg > e0) in &= 0xFFFFu << static_cast<uint32_t>(beg - e0);
-      if (end < e0 + 16) in &= (1u << static_cast<uint32_t>(end - e0)) - 1u;
-#pragma unroll
-      for (int j4 = 0; j4 < 4; ++j4) {
-        const uint32_t four = j4 == 0 ? q.x : j4 == 1 ? q.y : j4 == 2 ? q.z : q.w;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const int j = 4 * j4 + b;
-          if (!((in >> j) & 1u)) continue;
-          const uint32_t c = lw.code[(four >> (8 * b)) & 0xFFu];
-          if (c < kHubRanks)
-            ++lw.cnt[c][lane];
-          else if (c == kCodeElim)
-            em |= 1u << j;
-          else if (c == kCodeDead)
-            dm |= 1u << j;
-        }
-      }
-    }
-    const uint32_t sh = 16 * (lane & 1);
-    uint32_t kem = em << sh, kill = (em | dm) << sh;
-    kem |= __shfl_xor_sync(kFull, kem, 1);
-    kill |= __shfl_xor_sync(kFull, kill, 1);
-    if (!(lane & 1) && kill) {
-      const uint64_t wi = e0 >> 5;
-      if (kem) atomicAnd(st.eact + wi, ~kem);
-      atomicAnd(st.lt + wi, ~kill);
-    }
-    elim += __popc(em);
-  }
-  return __reduce_add_sync(kFull, elim);
-}
-
 // One live hub segment, streamed by the whole warp.  Lane j holds word j of
 // the segment's live-target bits; the warp then visits only the words with
 // a bit set, kUnroll words per round, loading the CSR entry and gathering
@@ -570,10 +491,9 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
   set_ranks(lw, need, n_slots);
   if (lane == 0) tl.streamed += end - beg;
   uint32_t elim = 0;
-  if (st.first && g.nlab) elim = lcc_segment_first(g, st, t, lw, ncs, beg, end);
   // Windows of 32 words (one per lane); a segment of a multi-segment hub is
   // one window, a single-segment hub's list may take two.
-  for (uint64_t w0 = beg >> 5; !(st.first && g.nlab) && end > beg && w0 <= (end - 1) >> 5; w0 += 32) {
+  for (uint64_t w0 = beg >> 5; end > beg && w0 <= (end - 1) >> 5; w0 += 32) {
     const uint64_t wi = w0 + lane;
     uint32_t word = 0;
     if (wi <= (end - 1) >> 5) {
@@ -582,7 +502,7 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
       if (beg > lo) word &= ~0u << static_cast<uint32_t>(beg - lo);
       if (end < lo + 32) word &= (1u << static_cast<uint32_t>(end - lo)) - 1u;
     }
-    tl.gathered += __popc(word);
+    if (!st.first) tl.gathered += __popc(word);
     for (unsigned nz = __ballot_sync(kFull, word != 0); nz;) {
       uint32_t idx[kUnroll], bits[kUnroll];
 #pragma unroll
@@ -593,12 +513,22 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
         if (idx[u] == 32) bits[u] = 0;
       }
       W ww[kUnroll];
-      uint32_t nb[kUnroll];
+      if (st.first) {
+        uint32_t lb[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
-        nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
+        for (int u = 0; u < kUnroll; ++u)
+          lb[u] = ((bits[u] >> lane) & 1u) ? g.nlab[((w0 + idx[u]) << 5) + lane] : 0u;
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+        for (int u = 0; u < kUnroll; ++u)
+          ww[u] = ((bits[u] >> lane) & 1u) ? label_word<W>(t, lb[u]) : Pack<W>::zero();
+      } else {
+        uint32_t nb[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+          nb[u] = ((bits[u] >> lane) & 1u) ? g.adj[((w0 + idx[u]) << 5) + lane] : 0u;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) ww[u] = ((bits[u] >> lane) & 1u) ? st.vs[nb[u]] : Pack<W>::zero();
+      }
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
         const bool in = (bits[u] >> lane) & 1u;
@@ -748,55 +678,9 @@ __device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTab
     if (e < lo + 32) word &= (1u << static_cast<uint32_t>(e - lo)) - 1u;
     return word;
   };
+  uint32_t word = more ? load_word(w) : 0u;
   uint32_t clr = 0, elm = 0;  // bits of word w to clear in lt / eact
   uint32_t elim = 0, gathered = 0;
-  if (st.first && g.nlab) {
-    // First pass after LCC0: the lane reads its list's label bytes 16 at a
-    // time (one 16-byte load from the 16-aligned group holding entry x;
-    // nlab is padded to whole 32-entry words) and decides every live entry
-    // from its label as the word-driven loop below would.
-    uint64_t x = b & ~uint64_t(15);
-    while (__any_sync(kFull, more)) {
-      if (!more) continue;
-      const uint4 q = *reinterpret_cast<const uint4*>(g.nlab + x);
-      const uint32_t sh = static_cast<uint32_t>(x & 31);
-      uint32_t in = (st.lt[x >> 5] >> sh) & 0xFFFFu;
-      if (b > x) in &= 0xFFFFu << static_cast<uint32_t>(b - x);
-      if (e < x + 16) in &= (1u << static_cast<uint32_t>(e - x)) - 1u;
-#pragma unroll
-      for (int j4 = 0; j4 < 4; ++j4) {
-        const uint32_t four = j4 == 0 ? q.x : j4 == 1 ? q.y : j4 == 2 ? q.z : q.w;
-#pragma unroll
-        for (int bb = 0; bb < 4; ++bb) {
-          const int j = 4 * j4 + bb;
-          if (!((in >> j) & 1u)) continue;
-          const uint32_t lb = (four >> (8 * bb)) & 0xFFu;
-          const uint64_t cw = t.lab_cand[lb];
-          if ((cw & ncs) == 0) {
-            clr |= 1u << (sh + j);
-            if (cw) {
-              elm |= 1u << (sh + j);
-              ++elim;
-            }
-          } else {
-            const uint32_t sw = t.lab_slot[lb];
-            if (sw < 64) {
-              const uint32_t r = lw.rank_of[sw];
-              if (r != kNoRank) ++lw.cnt[r][lane];
-            }
-          }
-        }
-      }
-      x += 16;
-      if ((x & 31) == 0 || x >= e) {
-        if (clr) atomicAnd(st.lt + ((x - 1) >> 5), ~clr);
-        if (elm) atomicAnd(st.eact + ((x - 1) >> 5), ~elm);
-        clr = elm = 0;
-      }
-      if (x >= e) more = false;
-    }
-  }
-  uint32_t word = more ? load_word(w) : 0u;
   while (__any_sync(kFull, more)) {
     // Lanes whose word is used up flush it and move to the next one.
     while (more && word == 0) {
