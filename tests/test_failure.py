@@ -54,10 +54,18 @@ def test_walk_budget_timeout_then_golden(c1):
             q.run()
         assert e.value.code == pm.PM_E_TIMEOUT
         assert "budget" in str(e.value)
+        # The step the deadline cut short: a walker step with no result
+        # row, its device time and the entries its walkers tested.
+        kind, ms, scanned, hops = q.aborted_step()
+        assert pm.STEP_NAMES[kind] in ("CC", "ENUMERATION") and ms > 0 and scanned > 0
         q.close()
     finally:
         assert pm.lib.pm_set_walk_budget_ms(120000.0) == pm.PM_SUCCESS
     _expect_golden(case, g, p)
+    q = pm.Query(g, pattern=p)
+    q.run()
+    assert q.aborted_step() is None
+    q.close()
 
 
 def test_query_budget_timeout_then_golden(c1):
