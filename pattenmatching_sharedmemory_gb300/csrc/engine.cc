@@ -1562,11 +1562,15 @@ void QueryImpl::run_all(int max_iterations) {
   while (!finished && iteration < max_iterations) {
     if (stop_before_enumeration && step == PM_STEP_ENUMERATION) break;
     check_request();
-    if (step == PM_STEP_LCC && g_lcc_graph && active_vertices != 0)
-      run_lcc_loop(max_iterations);
-    else
-      run_step();
+    run_unit(max_iterations);
   }
+}
+
+void QueryImpl::run_unit(int max_iterations) {
+  if (step == PM_STEP_LCC && g_lcc_graph && active_vertices != 0)
+    run_lcc_loop(max_iterations);
+  else
+    run_step();
 }
 
 void QueryImpl::export_state(uint64_t* cand, uint8_t* eact, uint8_t* vact) {

@@ -207,6 +207,9 @@ struct QueryImpl {
   // Runs the current step and advances the machine; returns the row.
   pm_step_record run_step();
   void run_all(int max_iterations = 1000);
+  // One unit of a whole run: the LCC fixpoint as one captured launch when
+  // the schedule is at LCC (and the switch is on), otherwise one step.
+  void run_unit(int max_iterations = 1000);
   // Request checks made before every step of a whole run: cancel flag
   // (PM_E_CANCELLED), deadline (PM_E_TIMEOUT); caps this host thread's
   // walker budget at the time left.

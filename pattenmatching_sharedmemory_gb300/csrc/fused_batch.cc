@@ -60,7 +60,7 @@ void FusedBatch::worker() {
     FusedBatchItem& it = items_[i];
     try {
       it.q->check_request();
-      it.q->run_step();
+      it.q->run_unit();
     } catch (const PmError& e) {
       it.status = e.code;
       it.error = e.message;
@@ -154,9 +154,14 @@ void FusedBatch::run() {
         mark_done(it);
         continue;
       }
+      // Shared launches for LCC0 and the fixpoint right after it (every
+      // vertex scheduled: the passes that read most of the adjacency, which
+      // the queries of one launch share through L2).  Later fixpoints are
+      // short (only vertices next to a change are rescheduled) and run on a
+      // worker as one captured launch, so that no query waits for a group.
       if (q.active_vertices != 0 && q.step == PM_STEP_LCC0)
         at_lcc0.push_back(i);
-      else if (q.active_vertices != 0 && q.step == PM_STEP_LCC)
+      else if (q.active_vertices != 0 && q.step == PM_STEP_LCC && q.lcc_first_pending)
         at_lcc.push_back(i);
       else
         others.push_back(i);

@@ -5,15 +5,17 @@
 // runPatternMatching, multiple_label_cpu.cc:113-184); each query here keeps
 // that schedule (multiple_label_step.cc:30-83) on its own state.  A
 // coordinator thread repeatedly takes the queries that are between steps:
-//   - those whose next step is LCC0, or an LCC fixpoint, run it together:
-//     one multi-query launch (LCC0), or one multi-query launch sequence per
-//     pass over the queries still iterating (LCC), whose blocks of different
-//     queries walk the same CSR ranges at the same time, so one HBM read of
-//     an adjacency range serves every query in the group;
-//   - every other query's next step (CC / PC / TDS / ENUMERATION, or any
-//     step of a query whose graph state is empty) goes to a pool of host
-//     threads and runs on the query's own stream, overlapping the walker
-//     launches of other queries and the shared LCC launches.
+//   - those whose next step is LCC0, or the LCC fixpoint right after LCC0
+//     (every vertex scheduled), run it together: one multi-query launch
+//     (LCC0), or one multi-query launch sequence per pass over the queries
+//     still iterating (LCC), whose blocks of different queries walk the same
+//     CSR ranges at the same time, so one HBM read of an adjacency range
+//     serves every query in the group;
+//   - every other query's next unit (a later LCC fixpoint as one captured
+//     launch, CC / PC / TDS / ENUMERATION, or any step of a query whose
+//     graph state is empty) goes to a pool of host threads and runs on the
+//     query's own stream, overlapping the walker launches of other queries
+//     and the shared LCC launches.
 // No query waits for another's walker step.  Results are those of each query
 // run alone: the same rows (timing columns aside), state and match count.
 #pragma once
