@@ -244,7 +244,14 @@ struct LccWarp {
   uint32_t cnt[kHubRanks][32];  // tiles: [rank][owner lane]; segments: [rank][counting lane]
   uint32_t tot[kHubRanks];      // segments: totals per rank
   uint8_t rank_of[64];          // needed slot -> rank, kNoRank otherwise
+  uint8_t code[256];            // first-pass kernel, segments: dense label -> kCode* or count rank
 };
+
+// First-pass entry codes of a segment's vertex, by the target's label: a
+// count rank (< kHubRanks), or one of these.
+constexpr uint8_t kCodeKeep = 0xFD;  // a possible neighbour, label not counted
+constexpr uint8_t kCodeElim = 0xFE;  // target holds roles, none a neighbour role: entry eliminated
+constexpr uint8_t kCodeDead = 0xFF;  // target holds no role: live-target bit cleared
 
 // Rank table of `slots` and zeroed counters for its n_slots ranks.
 __device__ __forceinline__ void set_ranks(LccWarp& lw, uint64_t slots, uint32_t n_slots) {
@@ -470,11 +477,83 @@ __device__ void lcc_vertex_warp(const DevGraph& g, const DevState<W>& st, const 
   }
 }
 
+// The first pass after LCC0 over hub segment [beg, end) of a vertex whose
+// roles' neighbour union is ncs: every target word follows from the entry's
+// label byte (label_word), so the warp streams the segment's label bytes,
+// 16 per lane in one 16-byte load (512 entries per warp step), instead of
+// visiting live-target words.  A per-warp table gives each label's code for
+// this vertex; counts go to the lane's column of lw.cnt, and the lane pair
+// of each 32-entry word merges its halves so that one lane clears the
+// word's bits.  Decisions, bit updates and counts are those of the
+// word-driven loop of lcc_segment.  Returns the entries eliminated
+// (warp-uniform).
+template <class W>
+__device__ __forceinline__ uint32_t lcc_segment_first(const DevGraph& g, const DevState<W>& st,
+                                                      const LccTables& t, LccWarp& lw, uint64_t ncs, uint64_t beg,
+                                                      uint64_t end) {
+  const unsigned lane = lane_id();
+  for (uint32_t lb = lane; lb < 256; lb += 32) {
+    const uint64_t cw = t.lab_cand[lb];
+    uint8_t c = kCodeKeep;
+    if (cw == 0) {
+      c = kCodeDead;
+    } else if ((cw & ncs) == 0) {
+      c = kCodeElim;
+    } else {
+      const uint32_t sw = t.lab_slot[lb];
+      if (sw < 64 && lw.rank_of[sw] != kNoRank) c = lw.rank_of[sw];
+    }
+    lw.code[lb] = c;
+  }
+  __syncwarp();
+  uint32_t elim = 0;
+  // Steps start on a 32-entry word: lanes 2i and 2i + 1 cover word i's low
+  // and high halves.  nlab is padded to a multiple of 32 bytes, so a 16-byte
+  // load that starts below `end` stays inside it.
+  for (uint64_t c0 = beg & ~uint64_t(31); c0 < end; c0 += 512) {
+    const uint64_t e0 = c0 + 16 * lane;
+    uint32_t em = 0, dm = 0;
+    if (e0 < end && e0 + 16 > beg) {
+      const uint4 q = *reinterpret_cast<const uint4*>(g.nlab + e0);
+      uint32_t in = (st.lt[e0 >> 5] >> static_cast<uint32_t>(e0 & 31)) & 0xFFFFu;
+      if (beg > e0) in &= 0xFFFFu << static_cast<uint32_t>(beg - e0);
+      if (end < e0 + 16) in &= (1u << static_cast<uint32_t>(end - e0)) - 1u;
+#pragma unroll
+      for (int j4 = 0; j4 < 4; ++j4) {
+        const uint32_t four = j4 == 0 ? q.x : j4 == 1 ? q.y : j4 == 2 ? q.z : q.w;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int j = 4 * j4 + b;
+          if (!((in >> j) & 1u)) continue;
+          const uint32_t c = lw.code[(four >> (8 * b)) & 0xFFu];
+          if (c < kHubRanks)
+            ++lw.cnt[c][lane];
+          else if (c == kCodeElim)
+            em |= 1u << j;
+          else if (c == kCodeDead)
+            dm |= 1u << j;
+        }
+      }
+    }
+    const uint32_t sh = 16 * (lane & 1);
+    uint32_t kem = em << sh, kill = (em | dm) << sh;
+    kem |= __shfl_xor_sync(kFull, kem, 1);
+    kill |= __shfl_xor_sync(kFull, kill, 1);
+    if (!(lane & 1) && kill) {
+      const uint64_t wi = e0 >> 5;
+      if (kem) atomicAnd(st.eact + wi, ~kem);
+      atomicAnd(st.lt + wi, ~kill);
+    }
+    elim += __popc(em);
+  }
+  return __reduce_add_sync(kFull, elim);
+}
+
 // One live hub segment, streamed by the whole warp.  Lane j holds word j of
 // the segment's live-target bits; the warp then visits only the words with
 // a bit set, kUnroll words per round, loading the CSR entry and gathering
 // the neighbour word for set bits only.
-template <class W>
+template <class W, bool kFirst>
 __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
                             const uint4 sd, const W wv, const uint64_t beg, const uint64_t end, LccTally& tl) {
   const unsigned lane = lane_id();
@@ -491,9 +570,10 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
   set_ranks(lw, need, n_slots);
   if (lane == 0) tl.streamed += end - beg;
   uint32_t elim = 0;
+  if constexpr (kFirst) elim = lcc_segment_first(g, st, t, lw, ncs, beg, end);
   // Windows of 32 words (one per lane); a segment of a multi-segment hub is
   // one window, a single-segment hub's list may take two.
-  for (uint64_t w0 = beg >> 5; end > beg && w0 <= (end - 1) >> 5; w0 += 32) {
+  for (uint64_t w0 = beg >> 5; !kFirst && end > beg && w0 <= (end - 1) >> 5; w0 += 32) {
     const uint64_t wi = w0 + lane;
     uint32_t word = 0;
     if (wi <= (end - 1) >> 5) {
@@ -596,7 +676,7 @@ __device__ void lcc_segment(const DevGraph& g, const DevState<W>& st, const LccT
 }
 
 // Segment i of a multi-segment hub.
-template <class W>
+template <class W, bool kFirst>
 __device__ void lcc_heavy(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
                           uint64_t i, LccTally& tl) {
   const uint4 sd = g.seg[i];
@@ -607,7 +687,7 @@ __device__ void lcc_heavy(const DevGraph& g, const DevState<W>& st, const LccTab
   uint64_t beg, end;
   segment_range(g, sd, &beg, &end);
   if (!sch || !Pack<W>::cand(wv)) return;
-  lcc_segment(g, st, t, lw, acc, sd, wv, beg, end, tl);
+  lcc_segment<W, kFirst>(g, st, t, lw, acc, sd, wv, beg, end, tl);
 }
 
 template <class W>
@@ -626,7 +706,7 @@ __device__ __forceinline__ W shfl_word(const W& w, int src) {
 
 // 32 single-segment hubs: the lanes test them together (and fetch their
 // ranges), the warp streams the live ones.
-template <class W>
+template <class W, bool kFirst>
 __device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, HubAcc* acc,
                              uint64_t block, LccTally& tl) {
   const unsigned lane = lane_id();
@@ -646,7 +726,7 @@ __device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const Lcc
   for (unsigned m = __ballot_sync(kFull, live); m; m &= m - 1) {
     const int j = __ffs(m) - 1;
     const uint4 s = make_uint4(__shfl_sync(kFull, sd.x, j), 0u, 1u, 0u);
-    lcc_segment(g, st, t, lw, acc, s, shfl_word(wv, j), shfl64(beg, j), shfl64(end, j), tl);
+    lcc_segment<W, kFirst>(g, st, t, lw, acc, s, shfl_word(wv, j), shfl64(beg, j), shfl64(end, j), tl);
   }
 }
 
@@ -655,7 +735,7 @@ __device__ void lcc_segments(const DevGraph& g, const DevState<W>& st, const Lcc
 // of the warp's counters and clearing bits one atomic per word.  Returns
 // false (and does nothing) when the warp's live lanes need more than
 // kHubRanks label slots.
-template <class W>
+template <class W, bool kFirst>
 __device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw, uint32_t v,
                           W wv, uint64_t b, uint64_t e, bool live, LccTally& tl) {
   const unsigned lane = lane_id();
@@ -678,9 +758,55 @@ __device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTab
     if (e < lo + 32) word &= (1u << static_cast<uint32_t>(e - lo)) - 1u;
     return word;
   };
-  uint32_t word = more ? load_word(w) : 0u;
   uint32_t clr = 0, elm = 0;  // bits of word w to clear in lt / eact
   uint32_t elim = 0, gathered = 0;
+  if constexpr (kFirst) {
+    // First pass after LCC0: the lane reads its list's label bytes 16 at a
+    // time (one 16-byte load from the 16-aligned group holding entry x;
+    // nlab is padded to whole 32-entry words) and decides every live entry
+    // from its label as the word-driven loop below would.
+    uint64_t x = b & ~uint64_t(15);
+    while (__any_sync(kFull, more)) {
+      if (!more) continue;
+      const uint4 q = *reinterpret_cast<const uint4*>(g.nlab + x);
+      const uint32_t sh = static_cast<uint32_t>(x & 31);
+      uint32_t in = (st.lt[x >> 5] >> sh) & 0xFFFFu;
+      if (b > x) in &= 0xFFFFu << static_cast<uint32_t>(b - x);
+      if (e < x + 16) in &= (1u << static_cast<uint32_t>(e - x)) - 1u;
+#pragma unroll
+      for (int j4 = 0; j4 < 4; ++j4) {
+        const uint32_t four = j4 == 0 ? q.x : j4 == 1 ? q.y : j4 == 2 ? q.z : q.w;
+#pragma unroll
+        for (int bb = 0; bb < 4; ++bb) {
+          const int j = 4 * j4 + bb;
+          if (!((in >> j) & 1u)) continue;
+          const uint32_t lb = (four >> (8 * bb)) & 0xFFu;
+          const uint64_t cw = t.lab_cand[lb];
+          if ((cw & ncs) == 0) {
+            clr |= 1u << (sh + j);
+            if (cw) {
+              elm |= 1u << (sh + j);
+              ++elim;
+            }
+          } else {
+            const uint32_t sw = t.lab_slot[lb];
+            if (sw < 64) {
+              const uint32_t r = lw.rank_of[sw];
+              if (r != kNoRank) ++lw.cnt[r][lane];
+            }
+          }
+        }
+      }
+      x += 16;
+      if ((x & 31) == 0 || x >= e) {
+        if (clr) atomicAnd(st.lt + ((x - 1) >> 5), ~clr);
+        if (elm) atomicAnd(st.eact + ((x - 1) >> 5), ~elm);
+        clr = elm = 0;
+      }
+      if (x >= e) more = false;
+    }
+  }
+  uint32_t word = more ? load_word(w) : 0u;
   while (__any_sync(kFull, more)) {
     // Lanes whose word is used up flush it and move to the next one.
     while (more && word == 0) {
@@ -748,7 +874,7 @@ __device__ bool lcc_lanes(const DevGraph& g, const DevState<W>& st, const LccTab
 
 // 32 single-segment hubs, one per lane (lcc_lanes); lcc_segments when the
 // batch needs more than kHubRanks slots.
-template <class W>
+template <class W, bool kFirst>
 __device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const LccTables& t, LccWarp& lw,
                                 HubAcc* acc, uint64_t block, LccTally& tl) {
   const uint64_t i = g.n_heavy + block * 32 + lane_id();
@@ -765,7 +891,7 @@ __device__ void lcc_batch_lanes(const DevGraph& g, const DevState<W>& st, const 
     live = sch && Pack<W>::cand(wv) != 0;
   }
   if (!__ballot_sync(kFull, live)) return;
-  if (!lcc_lanes(g, st, t, lw, v, wv, b, e, live, tl)) lcc_segments(g, st, t, lw, acc, block, tl);
+  if (!lcc_lanes<W, kFirst>(g, st, t, lw, v, wv, b, e, live, tl)) lcc_segments<W, kFirst>(g, st, t, lw, acc, block, tl);
 }
 
 // Lane's vertex of a light tile: scheduled, holding a role, not a hub.
@@ -904,7 +1030,7 @@ __device__ __forceinline__ uint64_t grid_warp() {
 }
 __device__ __forceinline__ uint64_t grid_warps() { return (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5; }
 
-template <class W, bool kTiles>
+template <class W, bool kTiles, bool kFirst = false>
 __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState<W>& st,
                                                const QueryTables* __restrict__ qt, HubAcc* hub_acc,
                                                StepCounters* ctr, const uint64_t warp, const uint64_t n_warps) {
@@ -930,9 +1056,9 @@ __device__ __forceinline__ void lcc_check_body(const DevGraph& g, const DevState
         if (__any_sync(kFull, x.work)) lcc_tile(g, st, t, lw, v0, x, tl);
       }
     } else if (task < heavy) {
-      lcc_heavy(g, st, t, lw, hub_acc, task, tl);
+      lcc_heavy<W, kFirst>(g, st, t, lw, hub_acc, task, tl);
     } else {
-      lcc_batch_lanes(g, st, t, lw, hub_acc, task - heavy, tl);
+      lcc_batch_lanes<W, kFirst>(g, st, t, lw, hub_acc, task - heavy, tl);
     }
   }
   const uint32_t ee = __reduce_add_sync(kFull, tl.edge_elim);
@@ -967,6 +1093,8 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check(DevGraph
 template <class W, bool kTiles>
 __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_at(DevGraph g,
                                                                            const QueryDevPtrs* __restrict__ a) {
+  // The first pass after LCC0: k_lcc_first_at did the hubs.
+  if (!kTiles && a->first_pass && g.nlab) return;
   if constexpr (kTiles) {
     // Staged in shared memory: read where used instead of held in
     // registers (no spills at 64 registers; the hub form spills less
@@ -978,6 +1106,27 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_at(DevGr
   } else {
     lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, grid_warp(), grid_warps());
   }
+}
+
+// The hub half of the first LCC pass after LCC0 (DevState::first, with
+// entry labels), as a kernel of its own: the hub paths read each list's
+// label bytes 16 at a time (lcc_segment_first, the first-pass block of
+// lcc_lanes), and keeping that code out of k_lcc_check leaves the gathering
+// passes' register allocation as it is (in one kernel it cost them spills
+// and more time than the first pass saved).
+template <class W>
+__global__ void __launch_bounds__(kThreads, 5) k_lcc_first(DevGraph g, DevState<W> st,
+                                                            const QueryTables* __restrict__ qt, HubAcc* hub_acc,
+                                                            StepCounters* ctr) {
+  lcc_check_body<W, false, true>(g, st, qt, hub_acc, ctr, grid_warp(), grid_warps());
+}
+
+// The same from a query's pointer block; returns at once unless the block
+// marks the first pass (every later pass of a captured fixpoint).
+template <class W>
+__global__ void __launch_bounds__(kThreads, 5) k_lcc_first_at(DevGraph g, const QueryDevPtrs* __restrict__ a) {
+  if (!a->first_pass || !g.nlab) return;
+  lcc_check_body<W, false, true>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, grid_warp(), grid_warps());
 }
 
 // ---- sweep 2 (LCC and NLCC) -------------------------------------------
@@ -2013,8 +2162,13 @@ void launch_lcc_check(const DevGraph& g, const QueryDevPtrs& q, cudaStream_t s) 
   const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
   if (hub_tasks) {
     const int grid = grid_for_tasks(hub_tasks, 5);
-    PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W, false><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables,
-                                                                                   q.hub_acc, q.ctr));
+    if (q.first_pass && g.nlab) {
+      PM_DISPATCH_WORD(q.word_kind, k_lcc_first<W><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables, q.hub_acc,
+                                                                              q.ctr));
+    } else {
+      PM_DISPATCH_WORD(q.word_kind, k_lcc_check<W, false><<<grid, kThreads, 0, s>>>(g, state_of<W>(q), q.tables,
+                                                                                     q.hub_acc, q.ctr));
+    }
   }
   const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4);
   PM_DISPATCH_WORD(q.word_kind,
@@ -2049,6 +2203,7 @@ void launch_lcc_pass_at(const DevGraph& g, int word_kind, const QueryDevPtrs* a,
   const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
   if (hub_tasks) {
     const int grid = grid_for_tasks(hub_tasks, 5);
+    if (g.nlab) PM_DISPATCH_WORD(word_kind, k_lcc_first_at<W><<<grid, kThreads, 0, s>>>(g, a));
     PM_DISPATCH_WORD(word_kind, k_lcc_check_at<W, false><<<grid, kThreads, 0, s>>>(g, a));
   }
   const int grid = grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4);
