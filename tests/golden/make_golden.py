@@ -13,7 +13,16 @@ It writes
                              sha256 of vertex_NNNN / graph_NNNN, match count)
   constraints.json.gz        reference constraint dumps (log.totem) for
                              random templates
-All reference runs use PM_REF_THREADS=1, the canonical sequential order.
+and, on request,
+  --only stream15            stream15_rmat16.json: the RMAT-16 stream's 15
+                             4-cycles (hours of CPU; entries appended as the
+                             reference finishes them)
+  --only article             article_variants.json (needs `make -C oracle
+                             ref-article`)
+  --only order               order_variants.json: the constraint-order
+                             drivers (needs `make -C oracle ref-order`)
+All reference runs use PM_REF_THREADS=1, the canonical sequential order,
+unless an entry records another thread count.
 """
 from __future__ import annotations
 
