@@ -255,6 +255,24 @@ pm_status_t pm_query_step_walk_stats(const pm_query* q, int32_t row, uint64_t* s
  * reference's alreadyMatched shortcut, and of memo-table overflow retries. */
 pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint64_t* overflow_retries);
 
+/* The graph statistics the dynamic constraint order ranks constraints by
+ * (GraphStatCpu::compute, src/patternmatching/algorithms/graph_stat_cpu.tpp:
+ * 42-80), taken on the GPU over the query's current state: active vertices
+ * and the active CSR entries between them, with the vertices split into
+ * `threads` static-schedule blocks whose neighbour-label accumulation is
+ * never reset between a block's vertices.  Labels are the template's
+ * distinct labels in order of first appearance: *n_labels of them (at most
+ * 64) into labels[].  vertex_total[a], edge_total[a * n + b] and
+ * at_least[(a * n + b) * 64 + i] (label-a vertices whose block's running
+ * count of label-b neighbours reached i, for i up to the largest number of
+ * label-b neighbours a label-a template vertex has; 0 elsewhere).  Outputs
+ * may be NULL; arrays sized for 64 labels always suffice.  PM_E_STATISTICS
+ * where the reference's accumulation lookup would throw (an active label
+ * whose template vertices have no neighbours), or while an active vertex
+ * carries no template label (before the first LCC0 or LCC step). */
+pm_status_t pm_query_graph_stat(pm_query* q, int32_t threads, uint32_t* n_labels, uint64_t* labels,
+                                uint64_t* vertex_total, uint64_t* edge_total, uint64_t* at_least);
+
 /* The step that ended a run with PM_E_TIMEOUT because its walkers passed
  * their deadline (it has no result row): its kind, device time, and the CSR
  * entries its walkers tested and hops they took until then (the counters of

@@ -83,6 +83,12 @@ def _load():
                                             ctypes.c_uint32, ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32),
                                             P(ctypes.c_uint64), ctypes.c_uint32, P(ctypes.c_uint64),
                                             P(ctypes.c_uint8), ctypes.c_int64, ctypes.c_int, P(ctypes.c_uint64)]
+        lib.pmo_graph_stat.restype = ctypes.c_int
+        lib.pmo_graph_stat.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64), ctypes.c_uint32,
+                                       ctypes.c_uint64, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
+                                       ctypes.c_uint32, P(ctypes.c_uint64), P(ctypes.c_uint8), ctypes.c_int32,
+                                       P(ctypes.c_uint32), P(ctypes.c_uint64), P(ctypes.c_uint64),
+                                       P(ctypes.c_uint64), P(ctypes.c_uint64)]
         lib.pmo_enumeration_start_role.restype = ctypes.c_int
         lib.pmo_enumeration_start_role.argtypes = [P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint64),
                                                    ctypes.c_uint32]
@@ -195,6 +201,38 @@ def run_ex(offsets, adj, labels, p_offsets, p_adj, p_labels, threads: int = 1, n
     res = OracleResult(rows, cand, eact, vact)
     res.timings = [recs[i].step_ms for i in range(n.value)]
     return res
+
+
+def graph_stat(offsets, adj, labels, p_offsets, p_adj, p_labels, cand, eact, threads: int = 1):
+    """GraphStatCpu::compute over a given state (role mask per vertex, active
+    flag per CSR entry) with `threads` static-schedule blocks: (labels,
+    vertex_total[n], edge_total[n, n], at_least[n, n, 64]) in the layout of
+    the product's pm_query_graph_stat."""
+    lib = _load()
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ad = np.ascontiguousarray(adj, np.uint32)
+    lab = np.ascontiguousarray(labels, np.uint64)
+    po = np.ascontiguousarray(p_offsets, np.uint64)
+    pa = np.ascontiguousarray(p_adj, np.uint32)
+    pl = np.ascontiguousarray(p_labels, np.uint64)
+    c = np.ascontiguousarray(cand, np.uint64)
+    e = np.ascontiguousarray(eact, np.uint8)
+    n = ctypes.c_uint32()
+    labs = np.zeros(64, np.uint64)
+    vt = np.zeros(64, np.uint64)
+    et = np.zeros(64 * 64, np.uint64)
+    al = np.zeros(64 * 64 * 64, np.uint64)
+    st = lib.pmo_graph_stat(_p(off, ctypes.c_uint64), _p(ad, ctypes.c_uint32), _p(lab, ctypes.c_uint64), len(off) - 1,
+                            len(ad), _p(po, ctypes.c_uint64), _p(pa, ctypes.c_uint32), _p(pl, ctypes.c_uint64),
+                            len(po) - 1, _p(c, ctypes.c_uint64), _p(e, ctypes.c_uint8), threads, ctypes.byref(n),
+                            _p(labs, ctypes.c_uint64), _p(vt, ctypes.c_uint64), _p(et, ctypes.c_uint64),
+                            _p(al, ctypes.c_uint64))
+    if st == STATISTICS:
+        raise StatMissing("a graph statistic lookup of the reference would throw")
+    if st != 0:
+        raise RuntimeError(f"oracle failed with status {st}")
+    k = n.value
+    return labs[:k], vt[:k], et[:k * k].reshape(k, k), al[:k * k * 64].reshape(k, k, 64)
 
 
 class StatMissing(RuntimeError):

@@ -1047,6 +1047,50 @@ int pmo_run_ex(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, ui
   }
 }
 
+// GraphStatCpu::compute over a given pruned state (role masks per vertex,
+// one active flag per CSR entry; a vertex is active when it holds a role),
+// `threads` static-schedule blocks, in pm_query_graph_stat's layout.
+int pmo_graph_stat(const uint64_t* off, const uint32_t* adj, const uint64_t* lab, uint32_t V, uint64_t E,
+                   const uint64_t* p_off, const uint32_t* p_adj, const uint64_t* p_lab, uint32_t k,
+                   const uint64_t* cand, const uint8_t* edge_active, int32_t threads, uint32_t* n_labels,
+                   uint64_t* labels, uint64_t* vertex_total, uint64_t* edge_total, uint64_t* at_least) {
+  try {
+    PatternGraph pg;
+    pg.n = k;
+    pg.offsets.assign(p_off, p_off + k + 1);
+    pg.adj.assign(p_adj, p_adj + p_off[k]);
+    pg.labels.assign(p_lab, p_lab + k);
+    State s;
+    s.off = off;
+    s.adj = adj;
+    s.lab = lab;
+    s.V = V;
+    s.E = E;
+    s.k = k;
+    s.active.resize(V);
+    for (uint32_t v = 0; v < V; ++v) s.active[v] = cand[v] != 0;
+    s.edge_active.assign(edge_active, edge_active + E);
+    const AccumulationMaximum am = accumulation_maximum(pg);
+    const GraphStat gs = oracle_graph_stat(s, am, static_cast<uint32_t>(threads > 0 ? threads : 1));
+    const uint32_t n = gs.slots;
+    if (n_labels) *n_labels = n;
+    for (uint32_t a = 0; a < n; ++a) {
+      if (labels) labels[a] = gs.label_of_slot[a];
+      if (vertex_total) vertex_total[a] = gs.vertex_total[a];
+      for (uint32_t b = 0; b < n; ++b) {
+        if (edge_total) edge_total[a * n + b] = gs.edge_total[a * n + b];
+        if (at_least)
+          for (uint32_t i = 0; i < 64; ++i)
+            at_least[(static_cast<size_t>(a) * n + b) * 64 + i] =
+                gs.at_least[(static_cast<size_t>(a) * n + b) * GraphStat::kMaxAtLeast + i];
+      }
+    }
+    return 0;
+  } catch (const PmError& e) {
+    return e.code;
+  }
+}
+
 // The embeddings ENUMERATION counts, listed: the reference's
 // writeEnumeration (multiple_label_enumeration_cpu.tpp:15-35, compiled out
 // there) writes historyIndexVector, the graph vertices bound by the walk's

@@ -185,6 +185,8 @@ def _load_library() -> ctypes.CDLL:
         "pm_query_elapsed_ms": (ctypes.c_int32, [ctypes.c_void_p, P(ctypes.c_double)]),
         "pm_set_walk_budget_ms": (ctypes.c_int32, [ctypes.c_double]),
         "pm_set_order_threads": (ctypes.c_int32, [ctypes.c_int32]),
+        "pm_query_graph_stat": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint32),
+                                                 c_u64p, c_u64p, c_u64p, c_u64p]),
         "pm_query_aborted_step": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
                                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                                    ctypes.POINTER(ctypes.c_uint64)]),
@@ -499,6 +501,19 @@ class Query:
         ms = ctypes.c_double()
         _check(lib.pm_query_elapsed_ms(self._h, ctypes.byref(ms)))
         return ms.value
+
+    def graph_stat(self, threads: int = 1):
+        """pm_query_graph_stat: (labels, vertex_total[n], edge_total[n, n],
+        at_least[n, n, 64]) of the query's current state, taken on the GPU."""
+        n = ctypes.c_uint32()
+        labs = np.zeros(64, np.uint64)
+        vt = np.zeros(64, np.uint64)
+        et = np.zeros(64 * 64, np.uint64)
+        al = np.zeros(64 * 64 * 64, np.uint64)
+        _check(lib.pm_query_graph_stat(self._h, int(threads), ctypes.byref(n), _ptr(labs, ctypes.c_uint64),
+                                       _ptr(vt, ctypes.c_uint64), _ptr(et, ctypes.c_uint64), _ptr(al, ctypes.c_uint64)))
+        k = n.value
+        return labs[:k], vt[:k], et[:k * k].reshape(k, k), al[:k * k * 64].reshape(k, k, 64)
 
     def aborted_step(self):
         """(step kind, device ms, CSR entries tested, hops) of the step that

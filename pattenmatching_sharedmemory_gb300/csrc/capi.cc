@@ -641,6 +641,29 @@ pm_status_t pm_query_stats(const pm_query* q, uint64_t* exact_resolutions, uint6
   return PM_SUCCESS;
 }
 
+pm_status_t pm_query_graph_stat(pm_query* q, int32_t threads, uint32_t* n_labels, uint64_t* labels,
+                                uint64_t* vertex_total, uint64_t* edge_total, uint64_t* at_least) {
+  PM_REQUIRE(q, "null argument");
+  PM_REQUIRE(threads >= 1, "thread count must be at least 1");
+  return guarded([&]() -> pm_status_t {
+    const GraphStat gs = q->impl.graph_stat(threads);
+    const uint32_t n = gs.slots;
+    if (n_labels) *n_labels = n;
+    for (uint32_t a = 0; a < n; ++a) {
+      if (labels) labels[a] = gs.label_of_slot[a];
+      if (vertex_total) vertex_total[a] = gs.vertex_total[a];
+      for (uint32_t b = 0; b < n; ++b) {
+        if (edge_total) edge_total[a * n + b] = gs.edge_total[a * n + b];
+        if (at_least)
+          for (uint32_t i = 0; i < GraphStat::kMaxAtLeast; ++i)
+            at_least[(static_cast<size_t>(a) * n + b) * 64 + i] =
+                gs.at_least[(static_cast<size_t>(a) * n + b) * GraphStat::kMaxAtLeast + i];
+      }
+    }
+    return PM_SUCCESS;
+  });
+}
+
 pm_status_t pm_query_aborted_step(const pm_query* q, int32_t* step, double* step_ms, uint64_t* scanned,
                                   uint64_t* hops) {
   PM_REQUIRE(q, "null argument");

@@ -520,9 +520,10 @@ size_t QueryImpl::cc_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? r
 size_t QueryImpl::pc_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? rem_pc[chosen] : next_pc; }
 size_t QueryImpl::tds_index() const { return (order & PM_ORDER_EFFECTIVENESS) ? rem_tds[chosen] : next_tds; }
 
-GraphStat QueryImpl::graph_stat() {
+GraphStat QueryImpl::graph_stat(int threads) {
+  if (acc_max.slots == 0) acc_max = accumulation_maximum(pattern);
   const uint32_t S = acc_max.slots, S1 = S + 1;
-  const uint32_t T = static_cast<uint32_t>(std::max(order_threads, 1));
+  const uint32_t T = static_cast<uint32_t>(std::max(threads > 0 ? threads : order_threads, 1));
   const uint64_t V = g->host.vertex_count;
   // Host tables: accumulation maxima (column S: 1 for labels without
   // template neighbours, whose accumulation the reference cannot look up)

@@ -177,8 +177,9 @@ struct QueryImpl {
   size_t chosen = 0;
   AccumulationMaximum acc_max;
   DeviceBuffer d_stat, d_stat_tab;
-  // Graph statistics of the active graph on the device (GraphStatCpu).
-  GraphStat graph_stat();
+  // Graph statistics of the active graph on the device (GraphStatCpu), with
+  // the vertices in `threads` static-schedule blocks (0: order_threads).
+  GraphStat graph_stat(int threads = 0);
   bool has_deadline = false;
   std::chrono::steady_clock::time_point deadline{};
   const std::atomic<bool>* cancel = nullptr;

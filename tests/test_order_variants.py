@@ -161,3 +161,62 @@ def test_gpu_dynamic_order_partitions_equal_oracle(case, threads):
     q.close()
     assert rows == ref.rows
     assert np.array_equal(cand, ref.cand) and np.array_equal(eact, ref.eact) and np.array_equal(vact, ref.vact)
+
+
+def test_oracle_graph_stat_accumulation_is_never_reset():
+    """GraphStatCpu::compute (graph_stat_cpu.tpp:46-70) declares its
+    label -> count accumulation outside the vertex loop, so a vertex counts
+    towards "at least i label-b neighbours" with the neighbours of every
+    earlier vertex of its thread's block.  Hand-worked case: vertices
+    0 (label 0), 1 (label 1), 2 (label 0); entries 0->1, 0->2, 1->0, 2->0;
+    template: one edge between labels 0 and 1.  With one thread vertex 2
+    (no label-1 neighbour) inherits vertex 0's count; with three threads
+    (one vertex per block) it does not."""
+    off = np.array([0, 2, 3, 4], np.uint64)
+    adj = np.array([1, 2, 0, 0], np.uint32)
+    lab = np.array([0, 1, 0], np.uint64)
+    p_off, p_adj, p_lab = [0, 1, 2], [1, 0], [0, 1]
+    cand = np.array([1, 2, 1], np.uint64)
+    eact = np.ones(4, np.uint8)
+    labels, vt, et, al = oracle.graph_stat(off, adj, lab, p_off, p_adj, p_lab, cand, eact, threads=1)
+    assert labels.tolist() == [0, 1] and vt.tolist() == [2, 1]
+    assert et.tolist() == [[2, 1], [1, 0]]
+    assert al[0, 1, 1] == 2 and al[1, 0, 1] == 1 and al[0, 0].sum() == 0 and al[1, 1].sum() == 0
+    _, _, _, al3 = oracle.graph_stat(off, adj, lab, p_off, p_adj, p_lab, cand, eact, threads=3)
+    assert al3[0, 1, 1] == 1 and al3[1, 0, 1] == 1
+
+
+STAT_CASES = C.synthetic_cases(include_big=False)[:10]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", STAT_CASES, ids=lambda c: c["name"])
+def test_gpu_graph_stat_equals_oracle(case):
+    """The device statistics (k_stat_counts, k_stat_accum) against the
+    oracle's block-by-block loop on the same states: after LCC0 and one LCC
+    pass, and after the pruning pipeline, for 1, 3 and 17 blocks."""
+    g, p = C.make_graph(case), C.make_pattern(case)
+    off, adj, lab = g.host_csr()
+    g.to_device(0)
+    q = pm.Query(g, pattern=p)
+    q.step()
+    q.step()
+    states = []
+    for phase in ("first pass", "pruned"):
+        if phase == "pruned":
+            q.prune()
+        cand, eact, _ = q.export()
+        for threads in (1, 3, 17):
+            try:
+                ref = oracle.graph_stat(off, adj, lab, p.offsets, p.adj, p.labels, cand, eact, threads=threads)
+            except oracle.StatMissing:
+                with pytest.raises(pm.PmError) as e:
+                    q.graph_stat(threads)
+                assert e.value.code == pm.PM_E_STATISTICS
+                continue
+            got = q.graph_stat(threads)
+            for a, b in zip(got, ref):
+                assert np.array_equal(a, b), (phase, threads)
+            states.append((phase, threads))
+    q.close()
+    assert states
