@@ -1108,19 +1108,19 @@ pm_step_record QueryImpl::run_step() {
   }
   StepResult r;
   try {
-  switch (kind) {
-    case PM_STEP_LCC0: r = step_lcc0(); break;
-    case PM_STEP_LCC: r = step_lcc(); break;
-    case PM_STEP_CC: r = step_nlcc(cycles[cc_index()]); break;
-    case PM_STEP_PC: r = step_nlcc(paths[pc_index()]); break;
-    // The reference's TDS step never advances its constraint iterator
-    // (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and pc :186):
-    // each of the n_template TDS steps checks template constraint 0.
-    // The article drivers' TDS steps do advance (tds_strict_cpu.tpp:192).
-    case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? tds_index() : 0]); break;
-    case PM_STEP_ENUMERATION: r = step_enumeration(); break;
-    default: break;
-  }
+    switch (kind) {
+      case PM_STEP_LCC0: r = step_lcc0(); break;
+      case PM_STEP_LCC: r = step_lcc(); break;
+      case PM_STEP_CC: r = step_nlcc(cycles[cc_index()]); break;
+      case PM_STEP_PC: r = step_nlcc(paths[pc_index()]); break;
+      // The reference's TDS step never advances its constraint iterator
+      // (multiple_label_tds_cpu.tpp:136-244, unlike cc :180 and pc :186):
+      // each of the n_template TDS steps checks template constraint 0.
+      // The article drivers' TDS steps do advance (tds_strict_cpu.tpp:192).
+      case PM_STEP_TDS: r = step_nlcc(templates[nlcc_variant ? tds_index() : 0]); break;
+      case PM_STEP_ENUMERATION: r = step_enumeration(); break;
+      default: break;
+    }
   } catch (const PmError& e) {
     if (e.code == PM_E_TIMEOUT) {
       // The walkers' counters were read when the deadline was seen.
