@@ -1480,6 +1480,8 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_multi(De
                                                                               uint32_t nq) {
   const MultiSlot m = multi_slot(nq);
   const QueryDevPtrs* a = qs + active[m.q];
+  // This query's first pass after LCC0: k_lcc_first_multi did its hubs.
+  if (!kTiles && a->first_pass && g.nlab) return;
   if constexpr (kTiles) {
     __shared__ DevState<W> s_st;
     if (threadIdx.x == 0) s_st = state_at<W>(a);
@@ -1488,6 +1490,17 @@ __global__ void __launch_bounds__(kThreads, kTiles ? 4 : 5) k_lcc_check_multi(De
   } else {
     lcc_check_body<W, kTiles>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, m.warp, m.n_warps);
   }
+}
+
+// k_lcc_first over the queries of a multi-query launch that are at their
+// first pass after LCC0 (the others' blocks return at once).
+template <class W>
+__global__ void __launch_bounds__(kThreads, 5) k_lcc_first_multi(DevGraph g, const QueryDevPtrs* __restrict__ qs,
+                                                                  const uint32_t* __restrict__ active, uint32_t nq) {
+  const MultiSlot m = multi_slot(nq);
+  const QueryDevPtrs* a = qs + active[m.q];
+  if (!a->first_pass || !g.nlab) return;
+  lcc_check_body<W, false, true>(g, state_at<W>(a), a->tables, a->hub_acc, a->ctr, m.warp, m.n_warps);
 }
 
 template <class W>
@@ -2239,6 +2252,7 @@ void launch_lcc_pass_multi(const DevGraph& g, int word_kind, const QueryDevPtrs*
   const uint64_t hub_tasks = g.n_heavy + (static_cast<uint64_t>(g.n_seg - g.n_heavy) + 31) / 32;
   if (hub_tasks) {
     const int grid = multi_grid(grid_for_tasks(hub_tasks, 5), nq);
+    if (g.nlab) PM_DISPATCH_WORD(word_kind, k_lcc_first_multi<W><<<grid, kThreads, 0, s>>>(g, qs, active, nq));
     PM_DISPATCH_WORD(word_kind, k_lcc_check_multi<W, false><<<grid, kThreads, 0, s>>>(g, qs, active, nq));
   }
   const int grid = multi_grid(grid_for_tasks(((static_cast<uint64_t>(g.V) + 31) / 32 + 31) / 32, 4), nq);
