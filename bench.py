@@ -27,7 +27,9 @@ A timed step serves B consecutive requests of the stream (step i: requests
 i*B .. i*B+B-1, so the default 20 steps of 100 serve the whole stream;
 warm-up steps serve another seeded stream), all submitted at once to one
 long-lived server with S slots (continuous batching, admission by device
-memory); the step ends when the last finished.
+memory); the step ends when the last finished.  Every leg of the served
+workload runs with the same speed knobs (walker state memo of --walk-table
+entries per warp, 2048 by default, chosen by a sweep on this stream).
 
 value        : completed requests per second over the timed steps (host
                clock, device synchronised on both sides).
