@@ -77,3 +77,34 @@ def test_sort_vertices_by_degree():
     assert np.array_equal(o2, w_off) and np.array_equal(a2, w_adj)
     assert np.all(np.diff(np.diff(o2.astype(np.int64))) >= 0)  # degrees ascend
     assert np.array_equal(l2[want_map], lab)
+
+
+def test_edges_to_totem_and_vertex_data(tmp_path):
+    """The reference's converter scripts (src/scripts/patternmatching/
+    convert_edges2totem.py, crunch_vertex_data.py): a sorted edge list gains
+    the TOTEM header (vertex count = last line's source + 1, edge count =
+    line count) and loads as the same CSR; vertex label files concatenate
+    into one label file."""
+    from pattenmatching_sharedmemory_gb300 import convert
+
+    _, off, adj, lab = _graph()
+    V = len(off) - 1
+    last = max(u for u in range(V) if off[u + 1] > off[u])
+    src = np.repeat(np.arange(V), np.diff(off.astype(np.int64)))
+    edges = tmp_path / "edges"
+    edges.write_text("".join(f"{u} {w}\n" for u, w in zip(src.tolist(), adj.tolist())))
+    n, m = convert.edges_to_totem(edges, tmp_path / "graph.totem", directed=True)
+    assert (n, m) == (last + 1, len(adj))
+    head = (tmp_path / "graph.totem").read_text().splitlines()[:3]
+    assert head == [f"#Nodes: {last + 1}", f"#Edges: {len(adj)}", "#Directed"]
+    parts = [tmp_path / "a.vertex_data", tmp_path / "b.vertex_data"]
+    half = (last + 1) // 2
+    parts[0].write_text("".join(f"{v} {int(lab[v])}\n" for v in range(half)))
+    parts[1].write_text("".join(f"{v} {int(lab[v])}\n" for v in range(half, last + 1)))
+    convert.concat_vertex_data(parts, tmp_path / "labels")
+    g = pm.Graph.load(tmp_path / "graph.totem", None, tmp_path / "labels", device=-1)
+    o2, a2, l2 = g.host_csr()
+    assert np.array_equal(o2, off[:last + 2]) and np.array_equal(a2, adj)
+    assert np.array_equal(l2, lab[:last + 1])
+    n, _ = convert.edges_to_totem(edges, tmp_path / "u.totem")
+    assert (tmp_path / "u.totem").read_text().splitlines()[2] == "#Undirected"
