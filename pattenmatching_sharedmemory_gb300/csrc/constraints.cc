@@ -256,8 +256,8 @@ bool share_edge(const TemplateConstraint& a, const TemplateConstraint& b) {
 // The reference merges two list entries with
 //     list.erase(it1); list.erase(it2);
 // (generate_constraint_template.cc:33-34, 73-74): it2 is used after the
-// first erase invalidated it.  Under the C++ standard library this build
-// uses, deque::erase shifts the shorter side: when it1 lies in the front half
+// first erase invalidated it.  Under libstdc++ (the GNU C++ standard
+// library), deque::erase shifts the shorter side: when it1 lies in the front half
 // the elements before it move back one slot and it2 still designates the
 // same element; otherwise the elements after it1 move forward one slot, so
 // it2 designates the element that followed it (or end(), in which case the
