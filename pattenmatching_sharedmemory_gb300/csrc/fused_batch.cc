@@ -59,8 +59,17 @@ void FusedBatch::worker() {
     }
     FusedBatchItem& it = items_[i];
     try {
-      it.q->check_request();
-      it.q->run_unit();
+      // The query's units up to its end or its next shared phase (only
+      // LCC0 and the fixpoint right after it are shared, so once a query
+      // is past them its worker runs it to the end, as a server slot does).
+      QueryImpl& q = *it.q;
+      while (true) {
+        q.check_request();
+        q.run_unit();
+        if (q.finished || q.iteration >= 1000 || (prune_only_ && q.step == PM_STEP_ENUMERATION)) break;
+        if (q.active_vertices != 0 && (q.step == PM_STEP_LCC0 || (q.step == PM_STEP_LCC && q.lcc_first_pending)))
+          break;
+      }
     } catch (const PmError& e) {
       it.status = e.code;
       it.error = e.message;

@@ -11,11 +11,11 @@
 //     still iterating (LCC), whose blocks of different queries walk the same
 //     CSR ranges at the same time, so one HBM read of an adjacency range
 //     serves every query in the group;
-//   - every other query's next unit (a later LCC fixpoint as one captured
-//     launch, CC / PC / TDS / ENUMERATION, or any step of a query whose
-//     graph state is empty) goes to a pool of host threads and runs on the
-//     query's own stream, overlapping the walker launches of other queries
-//     and the shared LCC launches.
+//   - every other query goes to a pool of host threads, where a worker runs
+//     its units (later LCC fixpoints as one captured launch each, CC / PC /
+//     TDS / ENUMERATION, any step of a query whose graph state is empty) on
+//     the query's own stream up to its end, overlapping the walker launches
+//     of other queries and the shared LCC launches.
 // No query waits for another's walker step.  Results are those of each query
 // run alone: the same rows (timing columns aside), state and match count.
 #pragma once
