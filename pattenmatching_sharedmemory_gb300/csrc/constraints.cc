@@ -80,27 +80,40 @@ CycleConstraint make_cycle(const std::vector<uint32_t>& hist, const std::vector<
   return c;
 }
 
+// The reference runs one DFS per (start vertex, cycle length) and records
+// the walks that come back to the start after exactly that many steps
+// (generate_constraint_circular.cc:13-56).  A walk that meets the start
+// earlier marks it visited and can no longer close, so the recorded walks of
+// length L are the simple cycles through the start, in the DFS order of
+// their choices.  One DFS per start vertex visits every simple path once and
+// files each closing walk under its length; emitting the lengths in
+// increasing order gives the reference's sequence.
 struct CycleSearch {
   const PatternGraph& p;
   std::vector<CycleConstraint>& out;
   std::vector<uint32_t> hist;
   std::vector<label_t> hist_labels;
   uint64_t visited = 0;
+  std::vector<std::vector<CycleConstraint>> by_length;      // closing walks of the current start
   std::unordered_set<std::vector<uint32_t>, IdsHash> seen;  // ids of out's entries
-  void dfs(uint32_t source, uint32_t cur, size_t remaining) {
-    if (remaining == 0) {
-      if (source != cur) return;
-      CycleConstraint c = make_cycle(hist, hist_labels);
-      if (seen.insert(c.ids).second) out.push_back(std::move(c));
-      return;
-    }
+  void dfs(uint32_t source, uint32_t cur, size_t depth) {
     for (uint64_t e = p.offsets[cur]; e < p.offsets[cur + 1]; ++e) {
       uint32_t w = p.adj[e];
-      if (visited >> w & 1) continue;
+      if (w == source) {
+        if (depth + 1 >= 3) {
+          hist.push_back(w);
+          hist_labels.push_back(p.labels[w]);
+          by_length[depth + 1].push_back(make_cycle(hist, hist_labels));
+          hist.pop_back();
+          hist_labels.pop_back();
+        }
+        continue;
+      }
+      if ((visited >> w & 1) || depth + 1 >= p.n) continue;
       hist.push_back(w);
       hist_labels.push_back(p.labels[w]);
       visited |= uint64_t(1) << w;
-      dfs(source, w, remaining - 1);
+      dfs(source, w, depth + 1);
       visited &= ~(uint64_t(1) << w);
       hist.pop_back();
       hist_labels.pop_back();
@@ -110,16 +123,18 @@ struct CycleSearch {
 
 std::vector<CycleConstraint> gen_cycles(const PatternGraph& p) {
   std::vector<CycleConstraint> out;
-  CycleSearch s{p, out, {}, {}, 0, {}};
+  CycleSearch s{p, out, {}, {}, 0, {}, {}};
   for (uint32_t v = 0; v < p.n; ++v) {
+    s.by_length.assign(p.n + 1, {});
     s.hist.push_back(v);
     s.hist_labels.push_back(p.labels[v]);
-    for (size_t len = 3; len <= p.n; ++len) {
-      s.visited = 0;
-      s.dfs(v, v, len);
-    }
+    s.visited = 0;
+    s.dfs(v, v, 0);
     s.hist.pop_back();
     s.hist_labels.pop_back();
+    for (size_t len = 3; len <= p.n; ++len)
+      for (auto& c : s.by_length[len])
+        if (s.seen.insert(c.ids).second) out.push_back(std::move(c));
   }
   return out;
 }
@@ -172,6 +187,11 @@ std::vector<PathConstraint> gen_paths(const PatternGraph& p) {
   std::vector<PathConstraint> out;
   PathSearch s{p, out, {}, {}, 0, {}};
   for (uint32_t v = 0; v < p.n; ++v) {
+    // A path ends at another vertex with the start's label: without one the
+    // search from v records nothing.
+    bool other = false;
+    for (uint32_t u = 0; u < p.n && !other; ++u) other = u != v && p.labels[u] == p.labels[v];
+    if (!other) continue;
     s.hist.push_back(v);
     s.hist_labels.push_back(p.labels[v]);
     s.visited = uint64_t(1) << v;
