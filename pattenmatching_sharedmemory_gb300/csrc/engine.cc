@@ -209,33 +209,69 @@ void GraphImpl::build_hub_plan(uint32_t degree, uint32_t entries) {
     throw PmError{PM_E_INVALID_ARG, "seg_entries must be a power of two in [32, 1024]"};
   // Light tiles stream at most 32 * hub_degree entries (32-bit stream index).
   if (degree > (1u << 26)) throw PmError{PM_E_INVALID_ARG, "hub_degree above 2^26"};
-  // Segments of multi-segment hubs first (one sweep task each), then the
-  // single-segment hubs (batched 32 to a task).
-  std::vector<uint4> seg, single;
-  uint32_t n_multi = 0;
+  // Segments of multi-segment hubs first (one sweep task each, in vertex
+  // order; the accumulator index is the hub's rank), then the single-segment
+  // hubs (batched 32 to a task) by degree, ties by vertex id, so the 32
+  // lanes of a batch get lists of similar length.  Chunks of vertex ids are
+  // scanned in parallel and concatenated in order; the single-segment hubs
+  // (at most `entries` entries each) are ordered by a stable counting sort
+  // on their degree.
+  struct Part {
+    uint64_t lo = 0;
+    std::vector<uint4> seg;
+    std::vector<uint32_t> single;
+    uint32_t multi = 0;
+  };
+  std::vector<Part> parts;
+  std::mutex parts_mu;
   const uint32_t V = host.vertex_count;
-  for (uint32_t v = 0; v < V; ++v) {
-    const uint64_t deg = host.offsets[v + 1] - host.offsets[v];
-    if (deg <= degree) continue;
-    // Lists longer than `entries` are cut at multiples of it (see
-    // DevGraph::seg); shorter ones are one segment.
-    const uint64_t n = deg <= entries ? 1 : (host.offsets[v + 1] - 1) / entries - host.offsets[v] / entries + 1;
-    if (seg.size() + single.size() + n > 0x7fffffffull) throw PmError{PM_E_INVALID_ARG, "too many hub segments"};
-    if (n == 1) {
-      single.push_back(make_uint4(v, 0, 1, 0xFFFFFFFFu));
-      continue;
+  const uint64_t* off = host.offsets.data();
+  parallel_ranges(V, [&](uint64_t lo, uint64_t hi) {
+    Part pt;
+    pt.lo = lo;
+    for (uint64_t v = lo; v < hi; ++v) {
+      const uint64_t deg = off[v + 1] - off[v];
+      if (deg <= degree) continue;
+      if (deg <= entries) {
+        pt.single.push_back(static_cast<uint32_t>(v));
+        continue;
+      }
+      // Lists longer than `entries` are cut at multiples of it (see
+      // DevGraph::seg).
+      const uint64_t n = (off[v + 1] - 1) / entries - off[v] / entries + 1;
+      for (uint64_t i = 0; i < n; ++i)
+        pt.seg.push_back(make_uint4(static_cast<uint32_t>(v), static_cast<uint32_t>(i), static_cast<uint32_t>(n),
+                                    pt.multi));
+      ++pt.multi;
     }
-    const uint32_t acc = n_multi++;
-    for (uint64_t i = 0; i < n; ++i)
-      seg.push_back(make_uint4(v, static_cast<uint32_t>(i), static_cast<uint32_t>(n), acc));
+    std::lock_guard<std::mutex> lk(parts_mu);
+    parts.push_back(std::move(pt));
+  });
+  std::sort(parts.begin(), parts.end(), [](const Part& x, const Part& y) { return x.lo < y.lo; });
+  size_t n_heavy_seg = 0, n_single = 0;
+  for (const Part& pt : parts) {
+    n_heavy_seg += pt.seg.size();
+    n_single += pt.single.size();
+  }
+  if (n_heavy_seg + n_single > 0x7fffffffull) throw PmError{PM_E_INVALID_ARG, "too many hub segments"};
+  std::vector<uint4> seg;
+  seg.reserve(n_heavy_seg + n_single);
+  uint32_t n_multi = 0;
+  for (const Part& pt : parts) {
+    for (uint4 sd : pt.seg) {
+      sd.w += n_multi;
+      seg.push_back(sd);
+    }
+    n_multi += pt.multi;
   }
   const uint32_t heavy = static_cast<uint32_t>(seg.size());
-  // Single-segment hubs by degree, so the 32 lanes of a batch get lists of
-  // similar length.
-  std::stable_sort(single.begin(), single.end(), [&](const uint4& a, const uint4& b) {
-    return host.offsets[a.x + 1] - host.offsets[a.x] < host.offsets[b.x + 1] - host.offsets[b.x];
-  });
-  seg.insert(seg.end(), single.begin(), single.end());
+  std::vector<uint64_t> pos(static_cast<size_t>(entries) + 2, 0);
+  for (const Part& pt : parts)
+    for (uint32_t v : pt.single) ++pos[off[v + 1] - off[v] + 1];
+  for (size_t d = 1; d < pos.size(); ++d) pos[d] += pos[d - 1];
+  seg.resize(heavy + n_single);
+  for (const Part& pt : parts)
+    for (uint32_t v : pt.single) seg[heavy + pos[off[v + 1] - off[v]]++] = make_uint4(v, 0, 1, 0xFFFFFFFFu);
   d_seg.ensure(sizeof(uint4) * std::max<size_t>(seg.size(), 1));
   if (!seg.empty())
     PM_CUDA(cudaMemcpy(d_seg.ptr, seg.data(), sizeof(uint4) * seg.size(), cudaMemcpyHostToDevice));
