@@ -308,7 +308,7 @@ void merge_pairs(std::deque<TemplateConstraint>& list, Pred overlap) {
         TemplateConstraint m = template_merge(list[i1], list[i2]);
         merged = true;
         erase_pair_as_reference(list, i1, i2);
-        list.push_back(m);
+        list.push_back(std::move(m));
         i1 = 0;
         break;
       }
