@@ -1,4 +1,6 @@
 // Host engine: device residency, step orchestration, output writers.
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.h"
 
 #include <sys/stat.h>
@@ -325,6 +327,22 @@ void WalkPool::ensure(uint32_t n_warps, uint32_t edge_cap, uint32_t hyp_cap, uin
 }
 
 // ---- query ------------------------------------------------------------------
+namespace {
+// NVTX range around a step or a captured LCC fixpoint, so that a profiler's
+// timeline shows the reference's schedule (no-ops when no tool is attached).
+struct StepRange {
+  explicit StepRange(const char* name) { nvtxRangePushA(name); }
+  ~StepRange() { nvtxRangePop(); }
+  StepRange(const StepRange&) = delete;
+  StepRange& operator=(const StepRange&) = delete;
+};
+
+const char* step_label(int kind) {
+  static const char* const kNames[] = {"START", "END", "LCC0", "LCC", "CC", "PC", "TDS", "ENUMERATION"};
+  return kind >= 0 && kind <= PM_STEP_ENUMERATION ? kNames[kind] : "?";
+}
+}  // namespace
+
 std::string step_name(int kind) {
   switch (kind) {
     case PM_STEP_START: return "START";
@@ -1122,6 +1140,7 @@ int QueryImpl::advance(int cur) {
 pm_step_record QueryImpl::run_step() {
   if (finished) return final_record();
   const int kind = step;
+  const StepRange range(step_label(kind));
   // The dynamic order's first iteration runs no step.
   if (kind == PM_STEP_START) {
     append_record(StepResult{}, kind, 0.0, 0, 0);
@@ -1339,6 +1358,7 @@ bool lcc_label_stream() { return g_lcc_label_stream.load(std::memory_order_relax
 void QueryImpl::run_lcc_loop(int max_iterations) {
   const int cap = std::min(max_iterations, 1000) - iteration;
   if (cap <= 0) return;
+  const StepRange range("LCC fixpoint");
   ensure_hub_acc();
   LccLoop& loop = t_lcc_loops.get(*g, word_kind);
   // Arguments and the pass cap in one copy; the head kernel resets the rest.
